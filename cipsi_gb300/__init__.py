@@ -1,0 +1,70 @@
+"""GB300 engine for the CIPSI second-order perturbation / selection step.
+
+Python mirror of the reference's process-level interface: `run_cip` does what
+running cip.exe (variant="cip") or cipsym.exe (variant="cipsym") in a
+calculation directory does, with the perturbation loop on the GPU.  The
+compiled library is built in-tree by `cipsi_gb300.build.build()`; when it is
+missing every entry point raises instead of falling back to a CPU path.
+"""
+from __future__ import annotations
+
+import ctypes
+import json
+import os
+from typing import Optional
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_build", "libcipsi_gb300.so")
+EXE_PATH = os.path.join(_HERE, "_build", "cip_gpu")
+
+_lib = None
+
+EXPORTED = [
+    "cipsi_ctx_create", "cipsi_ctx_destroy", "cipsi_last_error", "cipsi_set_stream",
+    "cipsi_set_integrals", "cipsi_set_integrals_fp64", "cipsi_set_space", "cipsi_set_roots",
+    "cipsi_run_pt2", "cipsi_run_pt2_async", "cipsi_fetch_result", "cipsi_selection_get",
+    "cipsi_cip_main",
+]
+
+
+class CipsiError(RuntimeError):
+    pass
+
+
+def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
+    """Load the engine; raises if it was not built (no silent fallback)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise CipsiError(f"engine library {path} is missing: run cipsi_gb300.build.build()")
+    lib = ctypes.CDLL(path)
+    lib.cipsi_cip_main.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int32, ctypes.c_char_p,
+                                   ctypes.c_void_p, ctypes.c_int32, ctypes.c_char_p, ctypes.c_int32]
+    lib.cipsi_cip_main.restype = ctypes.c_int
+    _lib = lib
+    return lib
+
+
+def run_cip(workdir: str, variant: str = "cipsym", json_path: Optional[str] = None,
+            gen_mask: Optional[np.ndarray] = None, device: int = 0,
+            stdin_path: Optional[str] = None) -> dict:
+    """Run the GPU drop-in in `workdir` (namelists from `stdin_path`, default
+    workdir/cip.in).  Returns the JSON summary (E2 totals, counters)."""
+    lib = load_library()
+    if json_path is None:
+        json_path = os.path.join(workdir, "cip_gpu.json")
+    err = ctypes.create_string_buffer(2048)
+    mask_ptr = None
+    if gen_mask is not None:
+        gen_mask = np.ascontiguousarray(gen_mask, dtype=np.uint8)
+        mask_ptr = gen_mask.ctypes.data_as(ctypes.c_void_p)
+    rc = lib.cipsi_cip_main(workdir.encode(), (stdin_path or os.path.join(workdir, "cip.in")).encode(),
+                            1 if variant == "cipsym" else 0, json_path.encode(), mask_ptr, device,
+                            err, len(err))
+    if rc != 0:
+        raise CipsiError(err.value.decode(errors="replace"))
+    with open(json_path) as fh:
+        return json.load(fh)

@@ -1,0 +1,84 @@
+"""Build the GB300 engine in-tree: libcipsi_gb300.so and the cip_gpu drop-in.
+
+Sources are compiled for sm_103a only, in parallel, and skipped when the
+sources and flags have not changed since the last build.
+"""
+from __future__ import annotations
+
+import hashlib
+import os
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+CSRC = os.path.join(HERE, "csrc")
+OUT = os.path.join(HERE, "_build")
+LIB = os.path.join(OUT, "libcipsi_gb300.so")
+EXE = os.path.join(OUT, "cip_gpu")
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVFLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
+CXXFLAGS = ["-O2", "-std=c++17", "-fPIC", "-Wall"]
+
+SOURCES = ["cipsi_engine.cu", "cip_host.cpp", "cip_gpu_main.cpp"]
+HEADERS = [os.path.join(ROOT, "include", "cipsi_gb300.h")]
+
+
+def _nvcc() -> str:
+    cand = os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"), "bin", "nvcc")
+    return cand if os.path.exists(cand) else "nvcc"
+
+
+def _digest(extra: str = "") -> str:
+    h = hashlib.sha256()
+    for f in [os.path.join(CSRC, s) for s in SOURCES] + HEADERS + [os.path.abspath(__file__)]:
+        with open(f, "rb") as fh:
+            h.update(fh.read())
+    h.update(extra.encode())
+    return h.hexdigest()
+
+
+def _run(cmd):
+    r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("build failed:\n" + " ".join(cmd) + "\n" + r.stdout)
+    return r.stdout
+
+
+def build(force: bool = False, verbose: bool = False) -> str:
+    os.makedirs(OUT, exist_ok=True)
+    nvcc = _nvcc()
+    stamp = os.path.join(OUT, ".stamp")
+    dig = _digest(" ".join(ARCH + NVFLAGS + CXXFLAGS))
+    if not force and os.path.exists(LIB) and os.path.exists(EXE) and os.path.exists(stamp):
+        if open(stamp).read().strip() == dig:
+            return LIB
+    objs = {
+        "engine": os.path.join(OUT, "cipsi_engine.o"),
+        "host": os.path.join(OUT, "cip_host.o"),
+        "main": os.path.join(OUT, "cip_gpu_main.o"),
+    }
+    jobs = [
+        [nvcc] + ARCH + NVFLAGS + ["-Xptxas", "-v", "-c", os.path.join(CSRC, "cipsi_engine.cu"),
+                                   "-o", objs["engine"]],
+        ["g++"] + CXXFLAGS + ["-c", os.path.join(CSRC, "cip_host.cpp"), "-o", objs["host"]],
+        ["g++"] + CXXFLAGS + ["-c", os.path.join(CSRC, "cip_gpu_main.cpp"), "-o", objs["main"]],
+    ]
+    with ThreadPoolExecutor(max_workers=3) as ex:
+        outs = list(ex.map(_run, jobs))
+    if verbose:
+        sys.stdout.write(outs[0])
+    with open(os.path.join(OUT, "ptxas_info.txt"), "w") as fh:
+        fh.write(outs[0])
+    _run([nvcc] + ARCH + ["-shared", "-o", LIB, objs["engine"], objs["host"], "-lcudart"])
+    _run(["g++", "-o", EXE, objs["main"], "-L" + OUT, "-lcipsi_gb300", "-Wl,-rpath,$ORIGIN",
+          "-L" + os.path.join(os.path.dirname(os.path.dirname(nvcc)), "lib64"), "-lcudart"])
+    with open(stamp, "w") as fh:
+        fh.write(dig)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(force="--force" in sys.argv, verbose=True))

@@ -1,0 +1,757 @@
+// cip_host.cpp -- host side of the GPU drop-in for cip.exe / cipsym.exe.
+//
+// Reads what the reference reads (namelists &cipfil and &icinp on standard
+// input; units 40 ijkl, 33 ener, 60 det, 59 bdvec, 4 f04), builds the
+// reference space with its spin-flip partners, computes the zero-order
+// quantities, hands everything to the engine through the C ABI of
+// cipsi_gb300.h, and writes what the reference writes after the perturbation
+// (unit 60 with S and the selected perturbers, unit 33 energy records, the
+// listing lines the Autocip driver parses).
+//
+// Followed sources: cip/cip.f:50-254 and 403-425 (main flow, outputs),
+// cip/openf.f, cip/deter.f:78-251 and 478-567, cip/transf.f, cip/lec60.f,
+// cip/ijkf.f, cip/reijkl.f, cip/rdener.f, cip/ic001.f:44-76, cip/faifoc.f,
+// cip/hmp.f, cip/hdig.f, cip/pie.f, cip/stkener.f and the cipsym variants
+// (cipsym/cip.f:226-254, cipsym/pie.f, cipsym/ic001.f:179).
+//
+// Supported: lecdet 2, 3 (S from unit 60) and 5 (S from unit 60, vectors
+// from unit 59) with ityper >= 0; isz = 0.  Unsupported inputs are rejected
+// with a message (cip stops on them, or they need the S diagonalisation).
+
+#include <algorithm>
+#include <cctype>
+#include <chrono>
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <map>
+#include <set>
+#include <sstream>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/cipsi_gb300.h"
+
+namespace {
+
+struct Error : std::runtime_error {
+  using std::runtime_error::runtime_error;
+};
+
+// ------------------------------------------------ Fortran sequential files
+struct Record {
+  std::vector<unsigned char> b;
+  size_t pos = 0;
+  template <typename T>
+  T get() {
+    if (pos + sizeof(T) > b.size()) throw Error("record too short");
+    T v;
+    std::memcpy(&v, b.data() + pos, sizeof(T));
+    pos += sizeof(T);
+    return v;
+  }
+};
+
+std::vector<Record> read_records(const std::string& path) {
+  std::ifstream f(path, std::ios::binary);
+  if (!f) throw Error("cannot open " + path);
+  std::vector<Record> out;
+  for (;;) {
+    int32_t n1;
+    if (!f.read(reinterpret_cast<char*>(&n1), 4)) break;
+    if (n1 < 0) throw Error("bad record length in " + path);
+    Record r;
+    r.b.resize((size_t)n1);
+    if (n1 && !f.read(reinterpret_cast<char*>(r.b.data()), n1)) throw Error("truncated record in " + path);
+    int32_t n2;
+    if (!f.read(reinterpret_cast<char*>(&n2), 4) || n2 != n1) throw Error("bad record marker in " + path);
+    out.push_back(std::move(r));
+  }
+  return out;
+}
+
+struct RecWriter {
+  std::vector<unsigned char> b;
+  template <typename T>
+  void put(T v) {
+    const unsigned char* p = reinterpret_cast<const unsigned char*>(&v);
+    b.insert(b.end(), p, p + sizeof(T));
+  }
+  void put_bytes(const char* s, size_t n) { b.insert(b.end(), s, s + n); }
+  void flush(std::FILE* f) {
+    const int32_t n = (int32_t)b.size();
+    std::fwrite(&n, 4, 1, f);
+    if (n) std::fwrite(b.data(), 1, b.size(), f);
+    std::fwrite(&n, 4, 1, f);
+    b.clear();
+  }
+};
+
+// ---------------------------------------------------------------- namelists
+struct Namelist {
+  std::map<std::string, std::vector<std::string>> kv;
+  bool found = false;
+  bool has(const std::string& k) const { return kv.count(k) != 0; }
+  const std::vector<std::string>* get(const std::string& k) const {
+    auto it = kv.find(k);
+    return it == kv.end() ? nullptr : &it->second;
+  }
+};
+
+std::string lower(std::string s) {
+  for (auto& c : s) c = (char)std::tolower((unsigned char)c);
+  return s;
+}
+
+Namelist parse_namelist(const std::string& text, const std::string& group) {
+  Namelist nl;
+  const std::string lt = lower(text), key = "&" + lower(group);
+  size_t pos = std::string::npos;
+  for (size_t p = lt.find(key); p != std::string::npos; p = lt.find(key, p + 1)) {
+    const char nx = p + key.size() < lt.size() ? lt[p + key.size()] : ' ';
+    if (!std::isalnum((unsigned char)nx) && nx != '_') {
+      pos = p + key.size();
+      break;
+    }
+  }
+  if (pos == std::string::npos) return nl;
+  nl.found = true;
+  std::string cur;
+  size_t i = pos;
+  const size_t n = text.size();
+  while (i < n) {
+    while (i < n && (std::isspace((unsigned char)text[i]) || text[i] == ',')) ++i;
+    if (i >= n || text[i] == '/' || text[i] == '&') break;
+    std::string tok;
+    if (text[i] == '\'' || text[i] == '"') {
+      const char q = text[i++];
+      while (i < n && text[i] != q) tok += text[i++];
+      if (i < n) ++i;
+    } else {
+      while (i < n && !std::isspace((unsigned char)text[i]) && text[i] != ',' && text[i] != '=' &&
+             text[i] != '/')
+        tok += text[i++];
+    }
+    size_t r = i;
+    while (r < n && std::isspace((unsigned char)text[r])) ++r;
+    if (r < n && text[r] == '=') {
+      cur = lower(tok);
+      nl.kv[cur].clear();  // a repeated key: the last assignment wins
+      i = r + 1;
+      continue;
+    }
+    if (cur.empty()) throw Error("namelist &" + group + ": value without a key");
+    nl.kv[cur].push_back(tok);
+  }
+  return nl;
+}
+
+double to_real(std::string s) {
+  for (auto& c : s)
+    if (c == 'd' || c == 'D') c = 'e';
+  return std::stod(s);
+}
+bool to_logical(const std::string& s) {
+  size_t i = 0;
+  while (i < s.size() && s[i] == '.') ++i;
+  return i < s.size() && (s[i] == 't' || s[i] == 'T');
+}
+
+struct Options {
+  // &icinp (defaults of cip/deter.f:78-226)
+  double test = 0.5, teseff = -1.0, tau = 1.0e-4, tdet = 0.0, coeff = 0.0;
+  int isz = 0, metat = 1, ityper = 1, iselec = 1, lecdet = 1, nclass = 10, maxdet = 500000;
+  int ninact = 0;
+  bool yion = false, ybrd = false, ymoyen = false, ywdeg = true, ytocom = false;
+  double aval[10] = {0.128e-6, 0.64e-6, 0.32e-5, 0.16e-4, 0.8e-4, 0.4e-3, 0.2e-2, 0.1e-1, 0.5e-1, 1.0};
+  std::string title = "                    ";
+  std::vector<double> tocom;
+  // &cipfil
+  std::string f60 = "det", f40 = "ijkl", f04 = "f04", f59 = "bdvec", f33 = "ener";
+};
+
+Options read_options(const std::string& text, const std::string& dir) {
+  Options o;
+  Namelist cf = parse_namelist(text, "cipfil");
+  std::string prefix;
+  if (auto v = cf.get("prefix"); v && !v->empty()) prefix = (*v)[0];
+  auto unit = [&](const char* k, const char* k1, std::string& dst) {
+    if (auto v = cf.get(k1); v && !v->empty() && !(*v)[0].empty()) {
+      dst = (*v)[0];
+    } else {
+      std::string base = dst;
+      if (auto w = cf.get(k); w && !w->empty()) base = (*w)[0];
+      while (!base.empty() && base.back() == ' ') base.pop_back();
+      dst = prefix + base;
+    }
+    if (!dst.empty() && dst[0] != '/') dst = dir + "/" + dst;
+  };
+  unit("det", "det1", o.f60);
+  unit("ijkl", "ijkl1", o.f40);
+  unit("f04", "f041", o.f04);
+  unit("bdvec", "bdvec1", o.f59);
+  unit("ener", "ener1", o.f33);
+  Namelist ic = parse_namelist(text, "icinp");
+  if (!ic.found) throw Error("erreur dans la namelist icinp");
+  auto r1 = [&](const char* k, double& d) { if (auto v = ic.get(k); v && !v->empty()) d = to_real((*v)[0]); };
+  auto i1 = [&](const char* k, int& d) { if (auto v = ic.get(k); v && !v->empty()) d = std::stoi((*v)[0]); };
+  auto l1 = [&](const char* k, bool& d) { if (auto v = ic.get(k); v && !v->empty()) d = to_logical((*v)[0]); };
+  r1("test", o.test); r1("teseff", o.teseff); r1("tau", o.tau); r1("tdet", o.tdet); r1("coeff", o.coeff);
+  i1("isz", o.isz); i1("metat", o.metat); i1("ityper", o.ityper); i1("iselec", o.iselec);
+  i1("lecdet", o.lecdet); i1("nclass", o.nclass); i1("maxdet", o.maxdet); i1("ninact", o.ninact);
+  l1("yion", o.yion); l1("ybrd", o.ybrd); l1("ymoyen", o.ymoyen); l1("ywdeg", o.ywdeg); l1("ytocom", o.ytocom);
+  if (auto v = ic.get("aval"))
+    for (size_t i = 0; i < v->size() && i < 10; ++i) o.aval[i] = to_real((*v)[i]);
+  if (auto v = ic.get("tocom"))
+    for (auto& x : *v) o.tocom.push_back(to_real(x));
+  if (auto v = ic.get("title"); v && !v->empty()) {
+    o.title = (*v)[0];
+    o.title.resize(20, ' ');
+  }
+  if (ic.has("ygen")) throw Error("ygen given in &icinp is not supported");
+  return o;
+}
+
+// ------------------------------------------------------------ the run state
+struct Space {
+  std::vector<int32_t> ne, nd, trou, part;
+  std::vector<uint8_t> ygen, ysaut, yef1;
+  std::vector<int32_t> nesp;
+  std::set<std::vector<int>> keys;  // sorted lists of every determinant (transf.f:76-85)
+  bool insert(int nec, const int* t, const int* p) {
+    std::vector<int> key(t, t + nec);
+    key.insert(key.end(), p, p + nec);
+    return keys.insert(std::move(key)).second;
+  }
+};
+
+struct Run {
+  Options o;
+  int nsym = 1, norb = 0, noc = 0, isym = 0, ncf = 0, metat = 1;
+  bool ydp = true;
+  std::vector<int32_t> itsym, its;  // its column-major nsym x nsym
+  std::vector<double> F, J, K;
+  std::vector<int16_t> ij0;
+  std::vector<int32_t> ntttt;
+  std::vector<float> eri;
+  double escf = 0.0;
+  Space S;
+  std::vector<double> c, e, eb, emp, teste, taum, fmpb, fdiag;
+};
+
+// transf.f: sort, validate, dedup and append one determinant
+void transf(Run& R, int nec, int* nt, int* np) {
+  const int norb = R.norb, mnorb = 2 * norb, noca = R.noc, nocb = R.noc + norb;
+  if (nec == 0) {
+    if (!R.S.insert(0, nullptr, nullptr)) return;
+    R.S.ne.push_back(0);
+    R.S.nd.push_back((int)R.S.trou.size());
+    R.isym = 1;
+    return;
+  }
+  std::sort(nt, nt + nec);
+  std::sort(np, np + nec);
+  int is = 1, ls = 0;
+  auto bad = [&](const char* m) { throw Error(std::string(m)); };
+  if (nt[0] < 1 || np[nec - 1] > mnorb || nt[nec - 1] > nocb || np[nec - 1] <= noca)
+    bad("1 spin orbitale est hors de l espace de base");
+  for (int i = 0; i < nec; ++i) {
+    if (!(nt[i] <= noca) && nt[i] < norb + 1) bad("1 spin orbitale est hors de l espace de base");
+    if (!(np[i] > nocb)) {
+      if (np[i] > norb) bad("1 spin orbitale est hors de l espace de base");
+      if (np[i] <= noca) bad("1 spin orbitale est hors de l espace de base");
+    }
+    const int st = R.itsym[(nt[i] - 1) % norb], sp = R.itsym[(np[i] - 1) % norb];
+    is = R.its[(size_t)(st - 1) * R.nsym + (is - 1)];
+    is = R.its[(size_t)(sp - 1) * R.nsym + (is - 1)];
+    ls += (np[i] > norb) - (nt[i] > norb);
+  }
+  if (R.isym == 0) R.isym = is;
+  if (is != R.isym) bad("dterminant de mauvaise symetrie");
+  if (ls != 0) bad("mauvais spin");
+  if (!R.S.insert(nec, nt, np)) return;
+  R.S.ne.push_back(nec);
+  R.S.nd.push_back((int)R.S.trou.size());
+  for (int j = 0; j < nec; ++j) {
+    R.S.trou.push_back(nt[j]);
+    R.S.part.push_back(np[j]);
+  }
+}
+
+void build_space(Run& R, const std::string& f60) {
+  // lec60.f: determinants of unit 60 with v >= tdet, grouped by degree
+  std::vector<std::vector<std::vector<int>>> byrank(9);
+  bool hf = false;
+  int ndet = 0;
+  for (auto& rec : read_records(f60)) {
+    const int mw = rec.get<int32_t>(), nw = rec.get<int32_t>();
+    std::vector<int32_t> idet(mw), nex(nw);
+    std::vector<double> v(nw);
+    for (auto& x : idet) x = rec.get<int32_t>();
+    for (auto& x : nex) x = rec.get<int32_t>();
+    for (auto& x : v) x = rec.get<double>();
+    int my = 0;
+    for (int l = 0; l < nw; ++l) {
+      const int nec = nex[l];
+      if (nec > 8 || nec < 0) throw Error("erreur degre d excitation depasse les possibilites du programme");
+      if (v[l] < R.o.tdet) {
+        my += 2 * nec;
+        continue;
+      }
+      if (++ndet > R.o.maxdet) {
+        if (R.o.lecdet == 3) goto done;
+        throw Error("trop de determinants selectionnes sur la file60");
+      }
+      std::vector<int> d(2 * nec);
+      for (int s = 0; s < nec; ++s) {
+        d[s] = idet[my++];
+        d[s + nec] = idet[my++];
+      }
+      if (nec == 0)
+        hf = true;
+      else
+        byrank[nec].push_back(std::move(d));
+    }
+  }
+done:
+  // deter.f:478-567: each determinant followed by its spin-flip partner
+  if (hf) transf(R, 0, nullptr, nullptr);
+  R.S.ygen.assign(R.S.ne.size(), 0);
+  R.S.ysaut.assign(R.S.ne.size(), 0);
+  R.S.yef1.assign(R.S.ne.size(), 0);
+  R.S.nesp.assign(R.S.ne.size(), 0);
+  const int norb = R.norb;
+  auto flip = [&](int so) { return so <= norb ? so + norb : so - norb; };
+  for (int nec = 1; nec <= 8; ++nec)
+    for (auto& d : byrank[nec]) {
+      const size_t before = R.S.ne.size();
+      int nt[8], np[8];
+      for (int l = 0; l < nec; ++l) {
+        nt[l] = d[l];
+        np[l] = d[l + nec];
+      }
+      transf(R, nec, nt, np);
+      if (R.S.ne.size() == before) continue;
+      R.S.ygen.push_back(0);
+      R.S.ysaut.push_back(0);
+      R.S.yef1.push_back(0);
+      R.S.nesp.push_back(0);
+      int ft[8], fp[8];
+      for (int l = 0; l < nec; ++l) {
+        ft[l] = flip(nt[l]);
+        fp[l] = flip(np[l]);
+      }
+      transf(R, nec, ft, fp);
+      if (R.S.ne.size() > before + 1) {
+        R.S.ygen.push_back(0);
+        R.S.ysaut.push_back(1);
+        R.S.yef1.push_back(1);
+        R.S.nesp.push_back(0);
+        R.S.yef1[before] = 1;
+        R.S.nesp[before] = 1;
+      }
+    }
+  R.ncf = (int)R.S.ne.size();
+  if (R.ncf == 0) throw Error("erreur dans les donnees: aucun determinant dans le sous espace variationnel");
+}
+
+// hmp / hdig of an S determinant from its excitation lists (cip/hmp.f, hdig.f)
+double hmp_list(const Run& R, int k) {
+  double ac = 0.0;
+  for (int l = 0; l < R.S.ne[k]; ++l) ac = ac + R.fmpb[R.S.part[R.S.nd[k] + l] - 1] - R.fmpb[R.S.trou[R.S.nd[k] + l] - 1];
+  return ac;
+}
+
+double hdig_list(const Run& R, int k) {
+  const int n = R.norb;
+  auto num = [](int i) { return i * (i - 1) / 2; };
+  double ab = 0.0;
+  const int l1 = R.S.nd[k], nei = R.S.ne[k];
+  for (int l = 0; l < nei; ++l) {
+    int n1p = R.S.part[l1 + l], n1t = R.S.trou[l1 + l];
+    ab = ab + R.fdiag[n1p - 1] - R.fdiag[n1t - 1];
+    const int ns1t = n1t > n, ns1p = n1p > n;
+    n1t = (n1t - 1) % n + 1;
+    n1p = (n1p - 1) % n + 1;
+    for (int j = 0; j <= l; ++j) {
+      int n2t = R.S.trou[l1 + j], n2p = R.S.part[l1 + j];
+      const int ns2t = n2t > n, ns2p = n2p > n;
+      n2t = (n2t - 1) % n + 1;
+      n2p = (n2p - 1) % n + 1;
+      const int n12t = n2t > n1t ? num(n2t) + n1t : num(n1t) + n2t;
+      const int n12p = n2p > n1p ? num(n2p) + n1p : num(n1p) + n2p;
+      const int n1tp = num(n2p) + n1t, n2tp = num(n1p) + n2t;
+      double ca = R.J[n12t - 1] + R.J[n12p - 1] - R.J[n1tp - 1] - R.J[n2tp - 1];
+      if (ns1t == ns2t) ca = ca - R.K[n12t - 1];
+      if (ns1p == ns2p) ca = ca - R.K[n12p - 1];
+      if (ns1t == ns2p) ca = ca + R.K[n1tp - 1];
+      if (ns1p == ns2t) ca = ca + R.K[n2tp - 1];
+      if (j == l) ca = 0.5 * ca;
+      ab = ab + ca;
+    }
+  }
+  return ab;
+}
+
+void read_inputs(Run& R, bool sym_variant) {
+  const Options& o = R.o;
+  if (o.yion) throw Error("yion (excitation to infinity) is not supported");
+  if (o.isz != 0) throw Error("only isz = 0 is supported");
+  if (o.ybrd && o.metat > 1) throw Error("ybrd (QDPT effective Hamiltonian) is not supported");
+  if (o.ninact > 0) throw Error("ninact > 0 (restricted perturbation space) is not supported");
+  if (o.ytocom) throw Error("ytocom (occupations from unit 21) is not supported");
+  if (o.ityper < 0) throw Error("ityper < 0 (writing S only) is not supported");
+  if (o.lecdet != 5) throw Error("lecdet must be 5 (vectors of S read from unit 59)");
+  auto recs = read_records(o.f40);
+  if (recs.size() < 9) throw Error("unit 40 too short");
+  {
+    Record& h = recs[0];
+    R.nsym = h.get<int32_t>();
+    R.norb = h.get<int32_t>();
+    R.noc = h.get<int32_t>();
+    const int ntrans = h.get<int32_t>();
+    R.itsym.resize(R.norb);
+    for (auto& x : R.itsym) x = h.get<int32_t>();
+    (void)h.get<int32_t>();
+    R.ydp = h.get<uint8_t>() != 0;
+    if (ntrans != 0) throw Error("degeneracy operations (ntrans > 0) are not supported");
+  }
+  R.its.resize((size_t)R.nsym * R.nsym);
+  for (auto& x : R.its) x = recs[1].get<int32_t>();
+  const size_t nter = (size_t)R.norb * (R.norb + 1) / 2;
+  R.J.resize(nter);
+  R.K.resize(nter);
+  R.F.resize(nter);
+  for (auto& x : R.J) x = recs[3].get<double>();
+  for (auto& x : R.K) x = recs[4].get<double>();
+  for (auto& x : R.F) x = recs[5].get<double>();
+  for (auto& x : R.F)
+    if (std::fabs(x) < 1.0e-10) x = 0.0;  // ijkf.f:34-37
+  R.ij0.resize((size_t)R.norb * R.norb);
+  for (auto& x : R.ij0) x = recs[6].get<int16_t>();
+  const int ninte = recs[7].get<int32_t>();
+  R.ntttt.resize(R.nsym);
+  for (auto& x : R.ntttt) x = recs[7].get<int32_t>();
+  R.eri.assign((size_t)ninte, 0.f);
+  size_t pos = 0;
+  const size_t nbuf = (size_t)ninte / 8192 + 1;
+  if (recs.size() < 8 + nbuf) throw Error("unit 40: missing integral records");
+  for (size_t b = 0; b < nbuf; ++b)
+    for (int i = 0; i < 8192 && pos < (size_t)ninte; ++i, ++pos)
+      R.eri[pos] = R.ydp ? (float)recs[8 + b].get<double>() : recs[8 + b].get<float>();
+  R.fdiag.assign(2 * R.norb, 0.0);
+  for (int i = 1; i <= R.norb; ++i) R.fdiag[i - 1] = R.fdiag[i - 1 + R.norb] = R.F[(size_t)i * (i + 1) / 2 - 1];
+
+  build_space(R, o.f60);
+  // escf (rdener.f)
+  bool found = false;
+  for (auto& r : read_records(o.f33)) {
+    if (r.b.size() >= 48 && std::memcmp(r.b.data(), "energie du determinant de reference     ", 40) == 0) {
+      r.pos = 40;
+      (void)r.get<int32_t>();
+      R.escf = r.get<double>();
+      found = true;
+      break;
+    }
+  }
+  if (!found) throw Error("energie du determinant de reference n'existe pas sur 33");
+  // ic001.f:44-76
+  auto r4 = read_records(o.f04);
+  if (r4.empty()) throw Error("unit 4 is empty");
+  for (int i = 0; i < 4; ++i) (void)r4[0].get<int32_t>();
+  const int mcf = r4[0].get<int32_t>();
+  std::vector<int32_t> iord60;
+  if (!sym_variant) {
+    if (r4.size() < 2) throw Error("unit 4: missing iord60 record");
+    iord60.resize(mcf);
+    for (auto& x : iord60) x = r4[1].get<int32_t>();
+  }
+  auto r59 = read_records(o.f59);
+  if (r59.empty()) throw Error("unit 59 is empty");
+  const int ncf59 = r59[0].get<int32_t>();
+  R.metat = r59[0].get<int32_t>();
+  if (ncf59 != R.ncf) throw Error("files 59 and S incompatibles");
+  if (R.metat < 1 || R.metat > CIPSI_MAX_ROOTS) throw Error("metat outside [1, 8]");
+  R.c.resize((size_t)R.ncf * R.metat);
+  for (auto& x : R.c) x = r59[0].get<double>();
+  R.e.resize(R.metat);
+  for (auto& x : R.e) x = r59[0].get<double>() - R.escf;
+  if (mcf != R.ncf) throw Error("files 4 et 59 incompatibles");
+  if (!sym_variant) {
+    std::vector<double> tmp(R.ncf);
+    for (int m = 0; m < R.metat; ++m) {
+      for (int k = 0; k < R.ncf; ++k) tmp[iord60[k] - 1] = R.c[(size_t)m * R.ncf + k];
+      for (int k = 0; k < R.ncf; ++k) R.c[(size_t)m * R.ncf + k] = tmp[k];
+    }
+  }
+  for (int m = 0; m + 1 < R.metat; ++m)
+    if (std::fabs(R.e[m + 1] - R.e[m]) <= 1.0e-6)
+      throw Error("degenerate roots: the rotation of brdnee.f:299 is not supported");
+  for (int k = 0; k < R.ncf; ++k) {
+    if (sym_variant) {
+      R.S.ygen[k] = 1;
+    } else {
+      for (int m = 0; m < R.metat; ++m)
+        if (std::fabs(R.c[(size_t)m * R.ncf + k]) >= o.coeff) R.S.ygen[k] = 1;
+    }
+  }
+  // faifoc.f with the occupations of cip.f:75-84
+  std::vector<double> tocom(2 * R.norb, 0.0);
+  for (int i = 0; i < R.noc; ++i) tocom[i] = 2.0;
+  for (size_t i = 0; i < o.tocom.size() && i < (size_t)R.norb; ++i) tocom[i] = o.tocom[i];
+  for (int i = 0; i < R.norb; ++i) {
+    if (tocom[i] > 1.0) {
+      tocom[i + R.norb] = tocom[i] - 1.0;
+      tocom[i] = 1.0;
+    } else {
+      tocom[i + R.norb] = 0.0;
+    }
+  }
+  for (int i = 0; i < R.noc; ++i) {
+    tocom[i] -= 1.0;
+    tocom[i + R.norb] -= 1.0;
+  }
+  R.fmpb.assign(2 * R.norb, 0.0);
+  auto num = [](int i) { return i * (i - 1) / 2; };
+  for (int l = 1; l <= R.norb; ++l) {
+    double t = R.fdiag[l - 1];
+    int lj = num(l);
+    for (int j = 1; j <= R.norb; ++j) {
+      lj = lj + 1;
+      if (j > l) lj = num(j) + l;
+      t = t + (tocom[j - 1] + tocom[j - 1 + R.norb]) * R.J[lj - 1];
+    }
+    double tt = t;
+    lj = num(l);
+    for (int j = 1; j <= R.norb; ++j) {
+      lj = lj + 1;
+      if (j > l) lj = num(j) + l;
+      t = t - tocom[j - 1] * R.K[lj - 1];
+      tt = tt - tocom[j - 1 + R.norb] * R.K[lj - 1];
+    }
+    R.fmpb[l - 1] = t;
+    R.fmpb[l - 1 + R.norb] = tt;
+  }
+  for (int i = 0; i < R.norb; ++i) {
+    R.fmpb[i] = (R.fmpb[i] + R.fmpb[i + R.norb]) * 0.5;
+    R.fmpb[i + R.norb] = R.fmpb[i];
+  }
+  // zero order (cip.f:99-135)
+  R.emp.assign(R.metat, 0.0);
+  R.eb.assign(R.metat, 0.0);
+  R.teste.assign(R.metat, o.test);
+  R.taum.assign(R.metat, 1.0);
+  std::vector<double> empdet(R.ncf), hdiag(R.ncf);
+  for (int k = 0; k < R.ncf; ++k) {
+    empdet[k] = hmp_list(R, k);
+    hdiag[k] = hdig_list(R, k);
+  }
+  const bool yselm = o.iselec == 1;
+  for (int m = 0; m < R.metat; ++m) {
+    double t = 0.0;
+    for (int i = 0; i < R.ncf; ++i) {
+      const double ci = R.c[(size_t)m * R.ncf + i];
+      if (!(t > std::fabs(ci))) t = std::fabs(ci);
+      R.emp[m] = R.emp[m] + ci * ci * empdet[i];
+      R.eb[m] = R.eb[m] + (ci * ci * hdiag[i]);
+    }
+    if (yselm) {
+      R.teste[m] = t * o.test;
+      R.taum[m] = 1.0 / t;
+    }
+  }
+}
+
+void write_pie_records(std::FILE* f, const std::vector<int32_t>& nec, const std::vector<int32_t>& h,
+                       const std::vector<int32_t>& p, const std::vector<double>& v,
+                       const std::vector<double>& evp, int metat, bool sym_variant, size_t hstride) {
+  // cip/pie.f (cipsym/pie.f): records of at most lungo = 1000 determinants
+  const size_t n = nec.size();
+  for (size_t s = 0; s < n; s += 1000) {
+    const size_t e = std::min(n, s + 1000);
+    RecWriter w;
+    int32_t m = 0;
+    for (size_t i = s; i < e; ++i) m += 2 * nec[i];
+    w.put<int32_t>(m);
+    w.put<int32_t>((int32_t)(e - s));
+    for (size_t i = s; i < e; ++i)
+      for (int l = 0; l < nec[i]; ++l) {
+        w.put<int32_t>(h[i * hstride + l]);
+        w.put<int32_t>(p[i * hstride + l]);
+      }
+    for (size_t i = s; i < e; ++i) w.put<int32_t>(nec[i]);
+    for (size_t i = s; i < e; ++i) w.put<double>(v[i]);
+    if (sym_variant)
+      for (size_t i = s; i < e; ++i)
+        for (int q = 0; q < metat; ++q) w.put<double>(evp[i * metat + q]);
+    w.flush(f);
+  }
+}
+
+std::string json_array(const double* x, int n) {
+  std::ostringstream s;
+  s.precision(17);
+  s << "[";
+  for (int i = 0; i < n; ++i) s << (i ? ", " : "") << x[i];
+  s << "]";
+  return s.str();
+}
+
+}  // namespace
+
+extern "C" int cipsi_cip_main(const char* workdir, const char* stdin_path, int32_t sym_variant,
+                              const char* json_path, const uint8_t* gen_mask, int32_t device,
+                              char* errbuf, int32_t errlen) {
+  auto seterr = [&](const std::string& m) {
+    if (errbuf && errlen > 0) {
+      std::snprintf(errbuf, (size_t)errlen, "%s", m.c_str());
+    }
+  };
+  cipsi_ctx* ctx = nullptr;
+  try {
+    const std::string dir = workdir ? workdir : ".";
+    std::ifstream in(stdin_path ? std::string(stdin_path) : dir + "/cip.in");
+    if (!in) throw Error("cannot read the namelist input");
+    std::stringstream ss;
+    ss << in.rdbuf();
+    Run R;
+    R.o = read_options(ss.str(), dir);
+    if (R.o.teseff < 0.0) R.o.teseff = 0.05 * R.o.tau;
+    read_inputs(R, sym_variant != 0);
+    const auto t0 = std::chrono::steady_clock::now();
+    cipsi_dims d{R.norb, R.noc, R.nsym, R.isym ? R.isym : 1, 0, R.metat, R.ncf};
+    int rc = cipsi_ctx_create(&ctx, &d, device);
+    auto chk = [&](int code, const char* what) {
+      if (code) throw Error(std::string(what) + ": " + cipsi_last_error(ctx));
+    };
+    chk(rc, "cipsi_ctx_create");
+    chk(cipsi_set_integrals(ctx, R.itsym.data(), R.its.data(), R.F.data(), R.J.data(), R.K.data(),
+                            R.ij0.data(), R.ntttt.data(), R.eri.data(), (int64_t)R.eri.size()),
+        "cipsi_set_integrals");
+    chk(cipsi_set_space(ctx, R.S.ne.data(), R.S.nd.data(), R.S.trou.data(), R.S.part.data(),
+                        (int64_t)R.S.trou.size(), R.S.ygen.data(), R.S.ysaut.data(), R.S.nesp.data(),
+                        R.S.yef1.data()),
+        "cipsi_set_space");
+    chk(cipsi_set_roots(ctx, R.c.data(), R.e.data(), R.eb.data(), R.emp.data(), R.teste.data(),
+                        R.taum.data(), R.fmpb.data()),
+        "cipsi_set_roots");
+    cipsi_opts op{};
+    op.yen = R.o.ityper == 2;
+    op.ysele = R.o.iselec == 3;
+    op.ymoyen = R.o.ymoyen;
+    op.ywdeg = R.o.ywdeg;
+    op.sym_variant = sym_variant != 0;
+    op.nclass = R.o.nclass;
+    op.tau = R.o.tau;
+    op.teseff = R.o.teseff;
+    for (int i = 0; i < 10; ++i) op.aval[i] = R.o.aval[i];
+    op.gen_mask = gen_mask;
+    op.run_pertu = 1;
+    cipsi_result res{};
+    if (R.o.ityper != 0) chk(cipsi_run_pt2(ctx, &op, &res), "cipsi_run_pt2");
+    const auto t1 = std::chrono::steady_clock::now();
+    // unit 60: S (v = 1) then the selected perturbers
+    std::FILE* f60 = std::fopen(R.o.f60.c_str(), "wb");
+    if (!f60) throw Error("cannot rewrite " + R.o.f60);
+    long long ntot = 0;
+    if (R.o.ymoyen) {
+      std::vector<int32_t> nec(R.ncf), h((size_t)R.ncf * 8, 0), p((size_t)R.ncf * 8, 0);
+      std::vector<double> v(R.ncf, 1.0), ev((size_t)R.ncf * R.metat, 0.0);
+      for (int k = 0; k < R.ncf; ++k) {
+        nec[k] = R.S.ne[k];
+        for (int l = 0; l < nec[k]; ++l) {
+          h[(size_t)k * 8 + l] = R.S.trou[R.S.nd[k] + l];
+          p[(size_t)k * 8 + l] = R.S.part[R.S.nd[k] + l];
+        }
+      }
+      write_pie_records(f60, nec, h, p, v, ev, R.metat, sym_variant != 0, 8);
+      ntot += R.ncf;
+      const int64_t ns = res.n_selected;
+      std::vector<int32_t> snec(ns), sh((size_t)ns * 8), sp((size_t)ns * 8), own(ns);
+      std::vector<double> sx(ns), sev((size_t)ns * R.metat);
+      if (ns) chk(cipsi_selection_get(ctx, 0, ns, snec.data(), sh.data(), sp.data(), sx.data(), sev.data(), own.data()),
+                  "cipsi_selection_get");
+      write_pie_records(f60, snec, sh, sp, sx, sev, R.metat, sym_variant != 0, 8);
+      ntot += ns;
+    }
+    std::fclose(f60);
+    // listing lines the Autocip driver reads (cipsym/cip.f:253-254, cip.f:243-247)
+    std::printf("0 ont ete generes:    %10lld  etats efficaces\n", (long long)res.ietat);
+    std::printf(" la contribution du plus grand determinant non ecrit est %8.6f\n", res.dpivot);
+    if (sym_variant) {
+      std::printf("nombre de determinants sur la file 60\n");
+      std::printf("%12lld%12d\n", ntot, R.metat);
+    }
+    std::printf(" energies CIPSI envp\n");
+    for (int m = 0; m < R.metat; ++m)
+      std::printf("  %2d  %14.8f  %14.8f  %14.8f  %14.8f\n", m + 1, R.e[m], res.e2mp[m], res.e2vp[m], res.e2b[m]);
+    std::fflush(stdout);
+    // unit 33 (stkener.f: char*40 then the values, no count)
+    if (std::FILE* f33 = std::fopen(R.o.f33.c_str(), "ab")) {
+      const char* names[4] = {"energies CIPSI var ", "energies CIPSI mpb ", "energies CIPSI envp", "energies CIPSI enb "};
+      std::vector<double> etot(R.metat);
+      for (int m = 0; m < R.metat; ++m) etot[m] = R.e[m] + R.escf;
+      const double* vals[4] = {etot.data(), res.e2mp, res.e2vp, res.e2b};
+      for (int q = 0; q < 4; ++q) {
+        std::string typ = std::string(names[q]) + R.o.title;
+        typ.resize(40, ' ');
+        RecWriter w;
+        w.put_bytes(typ.data(), 40);
+        for (int m = 0; m < R.metat; ++m) w.put<double>(vals[q][m]);
+        w.flush(f33);
+      }
+      std::fclose(f33);
+    }
+    if (json_path) {
+      std::ofstream j(json_path);
+      j.precision(17);
+      const int mt = R.metat;
+      j << "{\n  \"ncf\": " << R.ncf << ", \"metat\": " << mt << ", \"norb\": " << R.norb
+        << ", \"noca\": " << R.noc << ",\n";
+      j << "  \"ietat\": " << res.ietat << ", \"n_processed\": " << res.n_processed
+        << ", \"ntot60\": " << ntot << ",\n";
+      j << "  \"dpivot\": " << res.dpivot << ",\n";
+      j << "  \"e2mp\": " << json_array(res.e2mp, mt) << ",\n";
+      j << "  \"e2vp\": " << json_array(res.e2vp, mt) << ",\n";
+      j << "  \"e2b\": " << json_array(res.e2b, mt) << ",\n";
+      j << "  \"psimp\": " << json_array(res.psimp, mt) << ",\n";
+      j << "  \"psivp\": " << json_array(res.psivp, mt) << ",\n";
+      j << "  \"e\": " << json_array(R.e.data(), mt) << ",\n";
+      j << "  \"emp\": " << json_array(R.emp.data(), mt) << ",\n";
+      j << "  \"eb\": " << json_array(R.eb.data(), mt) << ",\n";
+      j << "  \"nom\": [";
+      for (int i = 0; i < R.o.nclass; ++i) j << (i ? ", " : "") << res.nom[i];
+      j << "],\n  \"nam\": [";
+      for (int m = 0; m < mt; ++m) {
+        j << (m ? ", " : "") << "[";
+        for (int i = 0; i < R.o.nclass; ++i) j << (i ? ", " : "") << res.nam[i * CIPSI_MAX_ROOTS + m];
+        j << "]";
+      }
+      j << "],\n  \"tabmp\": [";
+      for (int m = 0; m < mt; ++m) {
+        j << (m ? ", " : "") << "[";
+        for (int i = 0; i < R.o.nclass; ++i) j << (i ? ", " : "") << res.tabmp[i * CIPSI_MAX_ROOTS + m];
+        j << "]";
+      }
+      j << "],\n  \"tabvp\": [";
+      for (int m = 0; m < mt; ++m) {
+        j << (m ? ", " : "") << "[";
+        for (int i = 0; i < R.o.nclass; ++i) j << (i ? ", " : "") << res.tabvp[i * CIPSI_MAX_ROOTS + m];
+        j << "]";
+      }
+      j << "],\n  \"n_candidates\": " << res.n_candidates << ", \"n_compares\": " << res.n_compares
+        << ", \"n_pairs_1\": " << res.n_pairs_1 << ", \"n_pairs_2\": " << res.n_pairs_2
+        << ", \"alg_bytes\": " << res.alg_bytes << ",\n  \"kernel_ms\": " << res.kernel_ms
+        << ", \"wall_s\": " << std::chrono::duration<double>(t1 - t0).count() << "\n}\n";
+    }
+    cipsi_ctx_destroy(ctx);
+    return 0;
+  } catch (const std::exception& ex) {
+    seterr(ex.what());
+    if (ctx) cipsi_ctx_destroy(ctx);
+    return CIPSI_ERR_ARG;
+  }
+}

@@ -1,0 +1,1555 @@
+// cipsi_engine.cu -- GB300 (sm_103a) engine for the CIPSI second-order
+// perturbation / selection step (the work of cip/pertu.f + cip/diexcit.f).
+//
+// Algorithm (same perturber set, owners and weights as the reference, which
+// walks excitation lists one candidate at a time, cip/igene.f, pert1.f):
+//
+//   * S determinants are alpha/beta occupation bitstrings, W 64-bit words per
+//     spin (W = 1 for norb <= 64, 2 for norb <= 128).
+//   * One CTA owns one generator k at a time (persistent grid, atomic work
+//     queue).  It first gathers nb(k) = { j in S : degree(j,k) <= 4 } with the
+//     mask of k's electrons that j lacks.
+//   * Candidates I = k - R + A are processed in blocks of fixed removed
+//     electrons R (|R| = 1 or 2).  For a block, L_R = { j in nb(k) :
+//     |(k - R) \ j| <= 2 } is compacted into shared memory; it contains every
+//     S determinant that can be within two excitations of any I of the block.
+//     Each thread then takes added spin orbitals A and scans L_R only.
+//   * The reference's loop structure decides which excitations of k are
+//     examined (rank-change classes gated by the content of S,
+//     igene.f:34-35,89-90,199-200,296-298), the owner test (pert1.f:104-118,
+//     diexcit.f:246-259), the scan for interacting S determinants
+//     (pert1.f:129-144, diexcit.f:267-285), the spin-flip weights
+//     (pert1.f:150-164, diexcit.f:304-316), the MP / EN denominators and
+//     selection (pert1.f:171-295, diexcit.f:327-478).  All of that is
+//     restated here per candidate, as set rules on bitstrings.
+//   * Matrix elements use canonical (alpha string, beta string) phases; S
+//     coefficients are converted once on the host from the reference's
+//     excitation-list phase, so <I|H|Psi>^2 is identical.
+//   * (pq|rs) are read as real*4 (as cip stores them, cip/reijkl.f:27) and
+//     widened to double; everything else is double.  E2 sums are Kahan
+//     compensated per thread and reduced in a fixed order (deterministic).
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/cipsi_gb300.h"
+
+namespace {
+
+constexpr int kNClass = CIPSI_NCLASS;
+constexpr int kMaxRoots = CIPSI_MAX_ROOTS;
+constexpr int kThreads = 256;
+constexpr int kMaxSym = 8;
+constexpr int kMaxElec = 64;
+constexpr int kMaxOrb = 128;
+
+// counters[] slots
+enum {
+  C_IETAT = 0,
+  C_NPROC,
+  C_NSEL,
+  C_NCAND,
+  C_NCMP,
+  C_NP1,
+  C_NP2,
+  C_ALGB,
+  C_LRFALLBACK,
+  C_NCOUNTERS
+};
+
+struct Params {
+  int norb, noca, nel, ncf, metat, nsym, isym;
+  int ngen;
+  const int32_t* gens;       // generator indices (0-based); -1 = pertu block
+  const uint8_t* gen_dmask;  // allowed rank changes per generator, bit (D+2)
+  const uint64_t* S;         // ncf x 2W words (alpha words, beta words)
+  const uint8_t* ygen;
+  const int32_t* nesp;
+  const uint8_t* yef;
+  const double* c;           // ncf x metat, canonical phase
+  const float* eri;
+  const int32_t* pairtab;    // norb x norb: pair index | irrep << 24
+  const int32_t* ntttt;     // [irrep 1..nsym] first packed index (1-based)
+  const double* F;           // packed i*(i+1)/2 + j (i >= j, 0-based)
+  const double* J;
+  const double* K;
+  const double* fmpb;        // 2*norb by spin orbital
+  const int8_t* orbsym;      // 0-based irreps
+  int its[kMaxSym][kMaxSym]; // 0-based product table
+  double e[kMaxRoots], eb[kMaxRoots], emp[kMaxRoots], teste[kMaxRoots], taum[kMaxRoots];
+  int yen, ysele, ymoyen, ywdeg, symvar, nclass;
+  double tau, teseff;
+  double aval[kNClass];
+  int pertu_ref, pertu_mono;
+  // scratch
+  int32_t* nb_j;             // per block: ncf entries
+  uint64_t* nb_emask;
+  int32_t* lr_idx;           // per block: ncf entries (fallback path)
+  int lr_cap;                // shared-memory capacity of L_R
+  // outputs
+  double* gen_part;          // ngen x (5 * metat)
+  unsigned long long* counters;
+  unsigned long long* dpivot_bits;
+  unsigned long long* hist_nom;      // nclass
+  unsigned long long* hist_nam;      // nclass x metat
+  double* hist_tab;                  // 2 x nclass x metat (tabmp, tabvp)
+  uint64_t* sel_bits;                // cap x 2W
+  int32_t* sel_owner;
+  double* sel_xam;
+  double* sel_evp;                   // cap x metat
+  long long sel_cap;
+  int* work;                         // work counter
+};
+
+// ------------------------------------------------------------ bit helpers
+template <int W>
+__device__ __forceinline__ int popc_between(const uint64_t* s, int lo, int hi) {
+  // number of set bits strictly between orbital positions lo < hi
+  int cnt = 0;
+#pragma unroll
+  for (int w = 0; w < W; ++w) {
+    const int base = w * 64;
+    const int from = max(lo + 1 - base, 0);
+    const int to = min(hi - base, 64);
+    if (from < to) {
+      const uint64_t hiMask = (to >= 64) ? ~0ull : ((1ull << to) - 1ull);
+      const uint64_t loMask = (1ull << from) - 1ull;
+      cnt += __popcll(s[w] & hiMask & ~loMask);
+    }
+  }
+  return cnt;
+}
+
+template <int W>
+__device__ __forceinline__ int first_bit(const uint64_t* s) {
+#pragma unroll
+  for (int w = 0; w < W; ++w)
+    if (s[w]) return w * 64 + __ffsll((long long)s[w]) - 1;
+  return -1;
+}
+
+template <int W>
+__device__ __forceinline__ int last_bit(const uint64_t* s) {
+#pragma unroll
+  for (int w = W - 1; w >= 0; --w)
+    if (s[w]) return w * 64 + 63 - __clzll((long long)s[w]);
+  return -1;
+}
+
+__device__ __forceinline__ int tri(int i, int j) {
+  return i >= j ? i * (i + 1) / 2 + j : j * (j + 1) / 2 + i;
+}
+
+// (ij|kl) as cip/ai.f looks it up: packed pair indices, zero across irreps
+__device__ __forceinline__ double ai(const Params& p, int i, int j, int k, int l) {
+  const int pij = __ldg(&p.pairtab[i * p.norb + j]);
+  const int pkl = __ldg(&p.pairtab[k * p.norb + l]);
+  const int s1 = pij >> 24, s2 = pkl >> 24;
+  if (s1 != s2) return 0.0;
+  const long long a = pij & 0xFFFFFF, b = pkl & 0xFFFFFF;
+  const long long lo = a < b ? a : b, hi = a < b ? b : a;
+  const long long idx = lo + hi * (hi - 1) / 2 + __ldg(&p.ntttt[s1]) - 2;
+  return (double)__ldg(&p.eri[idx]);
+}
+
+// <I|H|J> for degree 1 or 2, canonical phases.  u = I bits, v = J bits
+// (alpha words then beta words).  rankI / rankJ: excitation degree relative
+// to the reference determinant; the one-difference element sums over the
+// holes and particles of the more excited determinant as cip/hntd.f does.
+template <int W>
+__device__ double hmat(const Params& p, const uint64_t* u, const uint64_t* v, int rankI, int rankJ,
+                       const uint64_t* hf, int& kind) {
+  uint64_t remv[2 * W], addv[2 * W];
+  int nrem[2] = {0, 0};
+#pragma unroll
+  for (int q = 0; q < 2 * W; ++q) {
+    const uint64_t x = u[q] ^ v[q];
+    remv[q] = x & v[q];  // occupied in J only
+    addv[q] = x & u[q];  // occupied in I only
+    nrem[q / W] += __popcll(remv[q]);
+  }
+  const int norb = p.norb;
+  if (nrem[0] + nrem[1] == 1) {
+    kind = 1;
+    const int s = nrem[0] ? 0 : 1;
+    const int pp = first_bit<W>(remv + s * W);
+    const int qq = first_bit<W>(addv + s * W);
+    const int lo = pp < qq ? pp : qq, hi = pp < qq ? qq : pp;
+    const int sign = (popc_between<W>(v + s * W, lo, hi) & 1) ? -1 : 1;
+    double val = __ldg(&p.F[tri(pp, qq)]);
+    const uint64_t* D = (rankI > rankJ) ? u : v;
+    // holes of D (occupied in the reference, empty in D)
+#pragma unroll
+    for (int sp = 0; sp < 2; ++sp) {
+#pragma unroll
+      for (int w = 0; w < W; ++w) {
+        uint64_t h = hf[sp * W + w] & ~D[sp * W + w];
+        while (h) {
+          const int r = w * 64 + __ffsll((long long)h) - 1;
+          h &= h - 1;
+          val -= ai(p, pp, qq, r, r);
+          if (sp == s) val += ai(p, pp, r, qq, r);
+        }
+        uint64_t t = D[sp * W + w] & ~hf[sp * W + w];
+        while (t) {
+          const int r = w * 64 + __ffsll((long long)t) - 1;
+          t &= t - 1;
+          val += ai(p, pp, qq, r, r);
+          if (sp == s) val -= ai(p, pp, r, qq, r);
+        }
+      }
+    }
+    (void)norb;
+    return sign * val;
+  }
+  kind = 2;
+  if (nrem[0] == 1 && nrem[1] == 1) {
+    const int pa = first_bit<W>(remv), qa = first_bit<W>(addv);
+    const int pb = first_bit<W>(remv + W), qb = first_bit<W>(addv + W);
+    const int sa = popc_between<W>(v, min(pa, qa), max(pa, qa));
+    const int sb = popc_between<W>(v + W, min(pb, qb), max(pb, qb));
+    const double val = ai(p, pa, qa, pb, qb);
+    return ((sa + sb) & 1) ? -val : val;
+  }
+  const int s = nrem[0] == 2 ? 0 : 1;
+  const uint64_t* rm = remv + s * W;
+  const uint64_t* ad = addv + s * W;
+  const int p1 = first_bit<W>(rm), p2 = last_bit<W>(rm);
+  const int q1 = first_bit<W>(ad), q2 = last_bit<W>(ad);
+  uint64_t mid[W];
+#pragma unroll
+  for (int w = 0; w < W; ++w) mid[w] = v[s * W + w];
+  const int s1 = popc_between<W>(mid, min(p1, q1), max(p1, q1));
+  mid[p1 >> 6] &= ~(1ull << (p1 & 63));
+  mid[q1 >> 6] |= (1ull << (q1 & 63));
+  const int s2 = popc_between<W>(mid, min(p2, q2), max(p2, q2));
+  const double val = ai(p, p1, q1, p2, q2) - ai(p, p1, q2, p2, q1);
+  return ((s1 + s2) & 1) ? -val : val;
+}
+
+// hmp (cip/hmp.f) and hdig (cip/hdig.f) of I, written over the sets of
+// holes H and particles P of I relative to the reference determinant.
+template <int W>
+__device__ void diag_terms(const Params& p, const uint64_t* u, const uint64_t* hf, double& hmpi,
+                           double& hdigi, bool want_hdig) {
+  int hs[24], ps[24];  // spin orbital codes: orb + spin * norb
+  int nh = 0, np = 0;
+#pragma unroll
+  for (int sp = 0; sp < 2; ++sp) {
+#pragma unroll
+    for (int w = 0; w < W; ++w) {
+      uint64_t h = hf[sp * W + w] & ~u[sp * W + w];
+      while (h && nh < 24) {
+        hs[nh++] = w * 64 + __ffsll((long long)h) - 1 + sp * p.norb;
+        h &= h - 1;
+      }
+      uint64_t t = u[sp * W + w] & ~hf[sp * W + w];
+      while (t && np < 24) {
+        ps[np++] = w * 64 + __ffsll((long long)t) - 1 + sp * p.norb;
+        t &= t - 1;
+      }
+    }
+  }
+  double mp = 0.0;
+  for (int i = 0; i < np; ++i) mp += __ldg(&p.fmpb[ps[i]]);
+  for (int i = 0; i < nh; ++i) mp -= __ldg(&p.fmpb[hs[i]]);
+  hmpi = mp;
+  if (!want_hdig) {
+    hdigi = 0.0;
+    return;
+  }
+  const int n = p.norb;
+  double e = 0.0;
+  for (int i = 0; i < np; ++i) {
+    const int o = ps[i] % n;
+    e += __ldg(&p.F[tri(o, o)]);
+  }
+  for (int i = 0; i < nh; ++i) {
+    const int o = hs[i] % n;
+    e -= __ldg(&p.F[tri(o, o)]);
+  }
+  auto jk = [&](int a, int b) -> double {
+    const int oa = a % n, ob = b % n;
+    const int t = tri(oa, ob);
+    double x = __ldg(&p.J[t]);
+    if ((a / n) == (b / n)) x -= __ldg(&p.K[t]);
+    return x;
+  };
+  // same-position terms of the reference's pair sum, 0.5*(J_tt-K_tt+J_pp-K_pp)
+  for (int i = 0; i < nh; ++i) e += 0.5 * jk(hs[i], hs[i]);
+  for (int i = 0; i < np; ++i) e += 0.5 * jk(ps[i], ps[i]);
+  for (int i = 0; i < nh; ++i)
+    for (int j = i + 1; j < nh; ++j) e += jk(hs[i], hs[j]);
+  for (int i = 0; i < np; ++i)
+    for (int j = i + 1; j < np; ++j) e += jk(ps[i], ps[j]);
+  for (int i = 0; i < nh; ++i)
+    for (int j = 0; j < np; ++j) e -= jk(hs[i], ps[j]);
+  hdigi = e;
+}
+
+__device__ __forceinline__ void kahan_add(double& s, double& c, double x) {
+  const double y = x - c;
+  const double t = s + y;
+  c = (t - s) - y;
+  s = t;
+}
+
+template <int R>
+struct Acc {
+  double e2mp[R], cmp[R], e2vp[R], cvp[R], e2b[R], cb[R], psimp[R], psivp[R];
+  unsigned long long ietat, nproc, nsel, ncand, ncmp, np1, np2, algb;
+  double dpivot;
+  __device__ void zero() {
+#pragma unroll
+    for (int m = 0; m < R; ++m) {
+      e2mp[m] = cmp[m] = e2vp[m] = cvp[m] = e2b[m] = cb[m] = psimp[m] = psivp[m] = 0.0;
+    }
+    ietat = nproc = nsel = ncand = ncmp = np1 = np2 = algb = 0ull;
+    dpivot = 0.0;
+  }
+};
+
+struct SmemHist {
+  unsigned long long nom[kNClass];
+  unsigned long long nam[kNClass * kMaxRoots];
+  double tab[2 * kNClass * kMaxRoots];
+};
+
+__device__ __forceinline__ int hist_class(const Params& p, double val) {
+  const int nc = p.nclass - 1;
+  for (int i = 0; i < nc; ++i)
+    if (val < p.aval[i]) return i;
+  return p.nclass - 1;
+}
+
+// Everything the reference does with one candidate after its interaction
+// scan: denominators, E2, selection, histogram, unit-60 record.
+template <int W, int R>
+__device__ void finish_candidate(const Params& p, const uint64_t* u, const uint64_t* hf,
+                                 const double* bc, int owner1 /*1-based, 0 = pertu*/,
+                                 double fmul, int nmul, bool ybis, bool is_pert1, Acc<R>& acc,
+                                 SmemHist& hist) {
+  double hmpi, hvpi;
+  diag_terms<W>(p, u, hf, hmpi, hvpi, p.yen != 0);
+  double xam = 0.0;
+  bool ydeg = false;
+  double vil[R], semp[R], sevp[R], venvp[R];
+#pragma unroll
+  for (int m = 0; m < R; ++m) {
+    vil[m] = 0.0;
+    semp[m] = sevp[m] = venvp[m] = 0.0;
+    if (m >= p.metat) continue;
+    const double bcalc = bc[m];
+    const double dmp = p.emp[m] - hmpi;
+    const double cimp = bcalc / dmp;
+    const double car = cimp * cimp;
+    const double eimp = bcalc * cimp;
+    kahan_add(acc.e2mp[m], acc.cmp[m], eimp);
+    acc.psimp[m] += car;
+    double xim = p.ysele ? fabs(eimp) : fabs(cimp);
+    double deno = dmp, eim = eimp;
+    double eivp = 0.0, carvp = 0.0, eib = 0.0;
+    if (p.yen) {
+      const double dvp = p.e[m] - hvpi;
+      const double civp = bcalc / dvp;
+      carvp = civp * civp;
+      eivp = bcalc * civp;
+      kahan_add(acc.e2vp[m], acc.cvp[m], eivp);
+      acc.psivp[m] += carvp;
+      xim = p.ysele ? fabs(eivp) : fabs(civp);
+      deno = dvp;
+      eim = eivp;
+      const double db = p.eb[m] - hvpi;
+      const double cib = bcalc / db;
+      eib = bcalc * cib;
+      kahan_add(acc.e2b[m], acc.cb[m], eib);
+    }
+    if (!(fabs(deno) > 0.05) && !(fabs(eim) < 1.0e-6) && p.ywdeg) ydeg = true;
+    if (xim < p.teste[m]) acc.dpivot = fmax(acc.dpivot, xim);
+    if (p.ymoyen) {
+      xim = xim * p.taum[m];
+      vil[m] = xim;
+      xam = fmax(xam, xim);
+    }
+    semp[m] = eimp;
+    sevp[m] = eivp;
+    venvp[m] = eivp * (fmul + 1.0);
+    if (ybis) {
+      kahan_add(acc.e2mp[m], acc.cmp[m], eimp * fmul);
+      acc.psimp[m] += car * fmul;
+      if (p.yen) {
+        kahan_add(acc.e2vp[m], acc.cvp[m], eivp * fmul);
+        kahan_add(acc.e2b[m], acc.cb[m], eib * fmul);
+        acc.psivp[m] += carvp * fmul;
+      }
+    }
+  }
+  acc.ietat += (unsigned long long)(long long)(nmul + 1);
+  acc.nproc += 1;
+  // histogram (cip/isto.f); pert1 calls it always, diexcit only if ymoyen
+  if ((is_pert1 || p.ymoyen) && xam >= p.teseff) {
+    const double fm = fmul + 1.0;
+    const int cls = hist_class(p, xam);
+    atomicAdd(&hist.nom[cls], (unsigned long long)(long long)(1 + nmul));
+#pragma unroll
+    for (int m = 0; m < R; ++m) {
+      if (m >= p.metat || vil[m] < p.teseff) continue;
+      atomicAdd(&hist.tab[cls * kMaxRoots + m], semp[m] * fm);
+      atomicAdd(&hist.tab[kNClass * kMaxRoots + cls * kMaxRoots + m], sevp[m] * fm);
+      const int c2 = hist_class(p, vil[m]);
+      atomicAdd(&hist.nam[c2 * kMaxRoots + m], (unsigned long long)(long long)(nmul + 1));
+    }
+  }
+  if (ydeg) xam = 1.0;
+  if (xam > p.tau && p.ymoyen) {
+    const unsigned long long slot = atomicAdd(&p.counters[C_NSEL], 1ull);
+    if ((long long)slot < p.sel_cap) {
+#pragma unroll
+      for (int q = 0; q < 2 * W; ++q) p.sel_bits[slot * 2 * W + q] = u[q];
+      p.sel_owner[slot] = owner1;
+      p.sel_xam[slot] = xam;
+      for (int m = 0; m < p.metat && m < R; ++m)
+        p.sel_evp[slot * p.metat + m] = p.symvar ? venvp[m] : 0.0;
+    }
+  }
+}
+
+template <int R>
+__device__ void block_flush(const Params& p, Acc<R>& acc, int gslot, double* red) {
+  // reduce 5*metat sums over the block in a fixed order; write gen_part[gslot]
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int nw = blockDim.x >> 5;
+  const int nq = 5 * p.metat;
+  for (int q = 0; q < nq; ++q) {
+    const int m = q % p.metat, which = q / p.metat;
+    double v = 0.0;
+#pragma unroll
+    for (int mm = 0; mm < R; ++mm)
+      if (mm == m) {
+        v = which == 0   ? acc.e2mp[mm] - acc.cmp[mm]
+            : which == 1 ? acc.e2vp[mm] - acc.cvp[mm]
+            : which == 2 ? acc.e2b[mm] - acc.cb[mm]
+            : which == 3 ? acc.psimp[mm]
+                         : acc.psivp[mm];
+      }
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if (lane == 0) red[q * 32 + wid] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < nq) {
+    double s = 0.0, c = 0.0;
+    for (int w = 0; w < nw; ++w) kahan_add(s, c, red[threadIdx.x * 32 + w]);
+    p.gen_part[(long long)gslot * nq + threadIdx.x] = s - c;
+  }
+  __syncthreads();
+#pragma unroll
+  for (int m = 0; m < R; ++m) {
+    acc.e2mp[m] = acc.cmp[m] = acc.e2vp[m] = acc.cvp[m] = acc.e2b[m] = acc.cb[m] = 0.0;
+    acc.psimp[m] = acc.psivp[m] = 0.0;
+  }
+}
+
+// ------------------------------------------------------------------ kernel
+struct BlockShared {
+  uint64_t kbits[2 * 2];
+  int occ[kMaxElec];      // spin orbital code (orb + spin*norb) of k's electrons
+  int vir[2][kMaxOrb];    // virtual orbitals of k per spin
+  int nvir[2];
+  int nel_s[2];
+  int nnb;
+  int nlr;
+  int gen;
+  int kidx;
+  int rank_k;
+};
+
+template <int W, int R>
+__global__ void __launch_bounds__(kThreads) k_pt2(Params p) {
+  extern __shared__ __align__(16) unsigned char dyn[];
+  __shared__ BlockShared sh;
+  __shared__ SmemHist hist;
+  __shared__ double red[5 * kMaxRoots * 32];
+
+  const int tid = threadIdx.x;
+  // shared L_R arrays (fast path)
+  uint64_t* lr_bits = reinterpret_cast<uint64_t*>(dyn);          // cap x 2W
+  int32_t* lr_j = reinterpret_cast<int32_t*>(lr_bits + (size_t)p.lr_cap * 2 * W);
+  int32_t* my_nb_j = p.nb_j + (size_t)blockIdx.x * p.ncf;
+  uint64_t* my_nb_em = p.nb_emask + (size_t)blockIdx.x * p.ncf;
+  int32_t* my_lr_idx = p.lr_idx + (size_t)blockIdx.x * p.ncf;
+
+  for (int i = tid; i < kNClass; i += blockDim.x) hist.nom[i] = 0;
+  for (int i = tid; i < kNClass * kMaxRoots; i += blockDim.x) hist.nam[i] = 0;
+  for (int i = tid; i < 2 * kNClass * kMaxRoots; i += blockDim.x) hist.tab[i] = 0.0;
+
+  uint64_t hf[2 * W];
+#pragma unroll
+  for (int s = 0; s < 2; ++s)
+#pragma unroll
+    for (int w = 0; w < W; ++w) {
+      const int lo = w * 64;
+      const int n = min(max(p.noca - lo, 0), 64);
+      hf[s * W + w] = (n >= 64) ? ~0ull : ((1ull << n) - 1ull);
+    }
+
+  Acc<R> acc;
+  acc.zero();
+  const int ncf = p.ncf;
+
+  for (;;) {
+    __syncthreads();
+    if (tid == 0) sh.gen = atomicAdd(p.work, 1);
+    __syncthreads();
+    const int g = sh.gen;
+    if (g >= p.ngen) break;
+    const int k = p.gens[g];
+
+    if (k < 0) {
+      // ---------------- pertu: reference and its singles, no owner test
+      // candidates: t = 0 -> reference (if pertu_ref), then singles
+      const int no = p.noca, nv = p.norb - p.noca;
+      const int nsing = p.pertu_mono ? 2 * no * nv : 0;
+      const int ntot = nsing + (p.pertu_ref ? 1 : 0);
+      for (int t = tid; t < ntot; t += blockDim.x) {
+        uint64_t u[2 * W];
+#pragma unroll
+        for (int q = 0; q < 2 * W; ++q) u[q] = hf[q];
+        const int tt = p.pertu_ref ? t - 1 : t;  // tt < 0: the reference itself
+        if (tt >= 0) {
+          const int s = tt / (no * nv);
+          const int rem = tt % (no * nv);
+          const int o = rem / nv, vv = no + rem % nv;
+          if (p.its[p.orbsym[o]][p.orbsym[vv]] != p.isym - 1) continue;
+          u[s * W + (o >> 6)] &= ~(1ull << (o & 63));
+          u[s * W + (vv >> 6)] |= (1ull << (vv & 63));
+        }
+        acc.ncand++;
+        {
+          int rankI = 0;
+#pragma unroll
+          for (int q = 0; q < 2 * W; ++q) rankI += __popcll(hf[q] & ~u[q]);
+          double bc[R];
+#pragma unroll
+          for (int m = 0; m < R; ++m) bc[m] = 0.0;
+          int nint = 0;
+          bool drop = false;
+          for (int j = 0; j < ncf; ++j) {
+            const uint64_t* v = p.S + (size_t)j * 2 * W;
+            int x = 0;
+#pragma unroll
+            for (int q = 0; q < 2 * W; ++q) x += __popcll(u[q] ^ __ldg(&v[q]));
+            acc.ncmp++;
+            if (x > 4) continue;
+            if (x == 0) {
+              drop = true;
+              break;
+            }
+            uint64_t vv[2 * W];
+#pragma unroll
+            for (int q = 0; q < 2 * W; ++q) vv[q] = __ldg(&v[q]);
+            int rankJ = 0;
+#pragma unroll
+            for (int q = 0; q < 2 * W; ++q) rankJ += __popcll(hf[q] & ~vv[q]);
+            int kind;
+            const double h = hmat<W>(p, u, vv, rankI, rankJ, hf, kind);
+            if (kind == 1) acc.np1++; else acc.np2++;
+            ++nint;
+#pragma unroll
+            for (int m = 0; m < R; ++m)
+              if (m < p.metat) bc[m] += h * __ldg(&p.c[(size_t)j * p.metat + m]);
+          }
+          if (drop || nint == 0) continue;
+          finish_candidate<W, R>(p, u, hf, bc, 0, 0.0, 0, false, true, acc, hist);
+        }
+      }
+      block_flush<R>(p, acc, g, red);
+      continue;
+    }
+
+    // ---------------- generator k: neighbours within degree 4
+    if (tid == 0) {
+      sh.kidx = k;
+      sh.nnb = 0;
+    }
+    if (tid < 2 * W) sh.kbits[tid] = p.S[(size_t)k * 2 * W + tid];
+    __syncthreads();
+    uint64_t kb[2 * W];
+#pragma unroll
+    for (int q = 0; q < 2 * W; ++q) kb[q] = sh.kbits[q];
+    if (tid == 0) {
+      // electron list and virtual lists of k
+      int ne = 0;
+      for (int s = 0; s < 2; ++s) {
+        int nes = 0, nv = 0;
+        for (int o = 0; o < p.norb; ++o) {
+          if ((kb[s * W + (o >> 6)] >> (o & 63)) & 1ull) {
+            sh.occ[ne++] = o + s * p.norb;
+            ++nes;
+          } else {
+            sh.vir[s][nv++] = o;
+          }
+        }
+        sh.nel_s[s] = nes;
+        sh.nvir[s] = nv;
+      }
+      int rk = 0;
+      for (int q = 0; q < 2 * W; ++q) rk += __popcll(hf[q] & ~kb[q]);
+      sh.rank_k = rk;
+    }
+    __syncthreads();
+    const int nel = sh.nel_s[0] + sh.nel_s[1];
+    for (int j = tid; j < ncf; j += blockDim.x) {
+      const uint64_t* v = p.S + (size_t)j * 2 * W;
+      uint64_t vv[2 * W];
+      int x = 0;
+#pragma unroll
+      for (int q = 0; q < 2 * W; ++q) {
+        vv[q] = __ldg(&v[q]);
+        x += __popcll(kb[q] ^ vv[q]);
+      }
+      if (x > 8) continue;
+      // electrons of k missing in j, as a mask over k's electron indices
+      uint64_t em = 0;
+#pragma unroll
+      for (int q = 0; q < 2 * W; ++q) {
+        uint64_t miss = kb[q] & ~vv[q];
+        while (miss) {
+          const int b = __ffsll((long long)miss) - 1;
+          miss &= miss - 1;
+          // electron index = occupied bits of k before this bit
+          int idx = 0;
+          const int s = q / W, w = q % W;
+          if (s == 1) idx += sh.nel_s[0];
+          for (int w2 = 0; w2 < w; ++w2) idx += __popcll(kb[s * W + w2]);
+          idx += __popcll(kb[q] & ((1ull << b) - 1ull));
+          em |= 1ull << idx;
+        }
+      }
+      const int slot = atomicAdd(&sh.nnb, 1);
+      my_nb_j[slot] = j;
+      my_nb_em[slot] = em;
+    }
+    __syncthreads();
+    const int nnb = sh.nnb;
+    const int rank_k = sh.rank_k;
+    const uint8_t dmask = p.gen_dmask[g];
+    const int k1 = k + 1;  // 1-based owner index
+    const int nespk = p.nesp[k];
+    const bool yefk = p.yef[k] != 0;
+
+    // ---------------- blocks of removed electrons R
+    const int nR = nel + nel * (nel - 1) / 2;
+    for (int r = 0; r < nR; ++r) {
+      int e1, e2 = -1;
+      if (r < nel) {
+        e1 = r;
+      } else {
+        // pair index -> (e1 < e2)
+        int t = r - nel;
+        e1 = 0;
+        while (t >= nel - 1 - e1) {
+          t -= nel - 1 - e1;
+          ++e1;
+        }
+        e2 = e1 + 1 + t;
+      }
+      const int so1 = sh.occ[e1];
+      const int so2 = e2 >= 0 ? sh.occ[e2] : -1;
+      const int sp1 = so1 / p.norb, o1 = so1 % p.norb;
+      const int sp2 = so2 >= 0 ? so2 / p.norb : -1, o2 = so2 >= 0 ? so2 % p.norb : -1;
+      const int nRr = e2 >= 0 ? 2 : 1;
+      const int hfR = (o1 < p.noca ? 1 : 0) + (e2 >= 0 && o2 < p.noca ? 1 : 0);
+      // achievable rank changes D = hfR + aV - |R| (aV = added HF-virtuals)
+      bool any = false;
+      for (int aV = 0; aV <= nRr; ++aV) {
+        const int D = hfR + aV - nRr;
+        if (dmask & (1u << (D + 2))) any = true;
+      }
+      if (!any) continue;
+      const uint64_t rmask = (1ull << e1) | (e2 >= 0 ? (1ull << e2) : 0ull);
+      // L_R
+      if (tid == 0) sh.nlr = 0;
+      __syncthreads();
+      for (int t = tid; t < nnb; t += blockDim.x) {
+        const uint64_t em = my_nb_em[t];
+        const int m = __popcll(em) - __popcll(em & rmask);
+        if (m > 2) continue;
+        const int slot = atomicAdd(&sh.nlr, 1);
+        const int j = my_nb_j[t];
+        if (slot < p.lr_cap) {
+          lr_j[slot] = j;
+          const uint64_t* v = p.S + (size_t)j * 2 * W;
+#pragma unroll
+          for (int q = 0; q < 2 * W; ++q) lr_bits[(size_t)slot * 2 * W + q] = __ldg(&v[q]);
+        }
+        my_lr_idx[slot] = j;
+      }
+      __syncthreads();
+      const int nlr = sh.nlr;
+      const bool fast = nlr <= p.lr_cap;
+      if (!fast && tid == 0) atomicAdd(&p.counters[C_LRFALLBACK], 1ull);
+      // K' = k - R
+      uint64_t kp[2 * W];
+#pragma unroll
+      for (int q = 0; q < 2 * W; ++q) kp[q] = kb[q];
+      kp[sp1 * W + (o1 >> 6)] &= ~(1ull << (o1 & 63));
+      if (e2 >= 0) kp[sp2 * W + (o2 >> 6)] &= ~(1ull << (o2 & 63));
+      const int symR = e2 >= 0 ? p.its[p.orbsym[o1]][p.orbsym[o2]] : p.orbsym[o1];
+      // added-orbital space
+      int nA;
+      const int nv1 = sh.nvir[sp1];
+      if (nRr == 1) {
+        nA = nv1;
+      } else if (sp1 == sp2) {
+        nA = nv1 * (nv1 - 1) / 2;
+      } else {
+        nA = sh.nvir[0] * sh.nvir[1];
+      }
+      for (int t = tid; t < nA; t += blockDim.x) {
+        int a1, a2 = -1, sa1 = sp1, sa2 = sp2;
+        if (nRr == 1) {
+          a1 = sh.vir[sp1][t];
+        } else if (sp1 == sp2) {
+          // t -> (x < y) over nv1 virtuals
+          int x = 0, tt = t;
+          while (tt >= nv1 - 1 - x) {
+            tt -= nv1 - 1 - x;
+            ++x;
+          }
+          a1 = sh.vir[sp1][x];
+          a2 = sh.vir[sp1][x + 1 + tt];
+        } else {
+          a1 = sh.vir[0][t / sh.nvir[1]];
+          a2 = sh.vir[1][t % sh.nvir[1]];
+          sa1 = 0;
+          sa2 = 1;
+        }
+        const int aV = (a1 >= p.noca ? 1 : 0) + (a2 >= 0 && a2 >= p.noca ? 1 : 0);
+        const int D = hfR + aV - nRr;
+        if (!(dmask & (1u << (D + 2)))) continue;
+        const int symA = a2 >= 0 ? p.its[p.orbsym[a1]][p.orbsym[a2]] : p.orbsym[a1];
+        if (p.its[symR][symA] != 0) continue;
+        // diexcit spin patterns for generators without a flip partner
+        bool ysyspi = true;
+        if (D == 2) {
+          if (sp1 != sp2) {
+            // alpha hole orbital a, beta hole b, alpha particle c, beta particle d
+            const int ha = o1, hb = o2, pc = a1, pd = a2;  // sp1 = alpha, sp2 = beta
+            ysyspi = !(ha == hb && pc == pd);
+            const bool unflipped = (ha < hb) || (ha == hb && pc <= pd);
+            if (!yefk && !unflipped) continue;
+          } else {
+            if (!yefk && sp1 == 1) continue;
+          }
+        }
+        acc.ncand++;
+        uint64_t u[2 * W];
+#pragma unroll
+        for (int q = 0; q < 2 * W; ++q) u[q] = kp[q];
+        u[sa1 * W + (a1 >> 6)] |= (1ull << (a1 & 63));
+        if (a2 >= 0) u[sa2 * W + (a2 >> 6)] |= (1ull << (a2 & 63));
+        const int rankI = rank_k + D;
+        double bc[R];
+#pragma unroll
+        for (int m = 0; m < R; ++m) bc[m] = 0.0;
+        int nint = 0, nnz = 0, lesp = 0;
+        bool drop = false;
+        for (int i = 0; i < nlr; ++i) {
+          uint64_t vv[2 * W];
+          int j = 0;
+          if (fast) {
+#pragma unroll
+            for (int q = 0; q < 2 * W; ++q) vv[q] = lr_bits[(size_t)i * 2 * W + q];
+          } else {
+            j = my_lr_idx[i];
+#pragma unroll
+            for (int q = 0; q < 2 * W; ++q) vv[q] = __ldg(&p.S[(size_t)j * 2 * W + q]);
+          }
+          int x = 0;
+#pragma unroll
+          for (int q = 0; q < 2 * W; ++q) x += __popcll(u[q] ^ vv[q]);
+          if (x > 4) continue;
+          if (fast) j = lr_j[i];
+          if (j < k) {
+            if (p.ygen[j]) {
+              drop = true;
+              break;
+            }
+            continue;
+          }
+          if (x == 0) {
+            drop = true;
+            break;
+          }
+          int rankJ = 0;
+#pragma unroll
+          for (int q = 0; q < 2 * W; ++q) rankJ += __popcll(hf[q] & ~vv[q]);
+          int kind;
+          const double h = hmat<W>(p, u, vv, rankI, rankJ, hf, kind);
+          if (kind == 1) acc.np1++; else acc.np2++;
+          ++nint;
+          if (h != 0.0) ++nnz;
+          if (j > k && j <= k + nespk) ++lesp;
+#pragma unroll
+          for (int m = 0; m < R; ++m)
+            if (m < p.metat) bc[m] += h * __ldg(&p.c[(size_t)j * p.metat + m]);
+        }
+        acc.ncmp += (unsigned long long)nlr;
+        if (drop || nint == 0) continue;
+        const bool is_pert1 = (D != 2);
+        if (!is_pert1 && nnz == 0) continue;
+        double fmul;
+        int nmul;
+        bool ybis;
+        if (is_pert1) {
+          if (nespk != 0) {
+            ybis = true;
+            fmul = (1.0 / (double)(lesp + 1)) * (double)(nespk + 1) - 1.0;
+            nmul = (int)fmul;
+          } else {
+            ybis = false;
+            fmul = 0.0;
+            nmul = 0;
+          }
+        } else {
+          int nespf = nespk;
+          ybis = nespf > 0;
+          if (yefk || ysyspi) {
+            ybis = true;
+            if (!yefk) nespf = nespf + nespf + 1;
+          }
+          fmul = (1.0 / (double)(lesp + 1)) * (double)(nespf + 1) - 1.0;
+          nmul = (int)fmul;
+        }
+        finish_candidate<W, R>(p, u, hf, bc, k1, fmul, nmul, ybis, is_pert1, acc, hist);
+      }
+      __syncthreads();
+    }
+    block_flush<R>(p, acc, g, red);
+  }
+
+  // block totals of the integer counters and the histogram
+  __syncthreads();
+  {
+    unsigned long long v[8] = {acc.ietat, acc.nproc, 0ull, acc.ncand, acc.ncmp, acc.np1, acc.np2, 0ull};
+    for (int q = 0; q < 8; ++q) {
+      unsigned long long x = v[q];
+      for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+      if ((tid & 31) == 0 && x) atomicAdd(&p.counters[q], x);
+    }
+    unsigned long long db = __double_as_longlong(acc.dpivot);
+    for (int o = 16; o > 0; o >>= 1) {
+      const unsigned long long y = __shfl_down_sync(0xffffffffu, db, o);
+      db = y > db ? y : db;
+    }
+    if ((tid & 31) == 0) atomicMax(p.dpivot_bits, db);
+  }
+  for (int i = tid; i < p.nclass; i += blockDim.x)
+    if (hist.nom[i]) atomicAdd(&p.hist_nom[i], hist.nom[i]);
+  for (int i = tid; i < p.nclass * kMaxRoots; i += blockDim.x) {
+    const int c = i / kMaxRoots, m = i % kMaxRoots;
+    if (m >= p.metat) continue;
+    if (hist.nam[i]) atomicAdd(&p.hist_nam[c * p.metat + m], hist.nam[i]);
+    if (hist.tab[i] != 0.0) atomicAdd(&p.hist_tab[c * p.metat + m], hist.tab[i]);
+    const double tv = hist.tab[kNClass * kMaxRoots + i];
+    if (tv != 0.0) atomicAdd(&p.hist_tab[p.nclass * p.metat + c * p.metat + m], tv);
+  }
+}
+
+// fixed-order Kahan reduction of the per-generator partial sums
+__global__ void k_reduce(const double* part, int ngen, int nq, double* out) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= nq) return;
+  double s = 0.0, c = 0.0;
+  for (int g = 0; g < ngen; ++g) kahan_add(s, c, part[(long long)g * nq + q]);
+  out[q] = s - c;
+}
+
+}  // namespace
+
+// =================================================================== host
+
+struct cipsi_ctx {
+  cipsi_dims d{};
+  int device = 0;
+  int W = 1;
+  std::string err;
+  cudaStream_t own_stream = nullptr;
+  cudaStream_t stream = nullptr;
+  bool have_int = false, have_space = false, have_roots = false;
+  // host copies needed for set-up
+  std::vector<int32_t> itsym, its;
+  std::vector<int32_t> rank;
+  std::vector<uint64_t> Sbits;
+  std::vector<uint8_t> ygen, ysaut, yef1;
+  std::vector<int32_t> nesp;
+  std::vector<double> sigma;
+  std::vector<double> croot;  // metat*ncf reference phase (column-major)
+  double e[kMaxRoots]{}, eb[kMaxRoots]{}, emp[kMaxRoots]{}, teste[kMaxRoots]{}, taum[kMaxRoots]{};
+  // device buffers
+  uint64_t* dS = nullptr;
+  uint8_t *dygen = nullptr, *dyef = nullptr;
+  int32_t* dnesp = nullptr;
+  double* dc = nullptr;
+  float* deri = nullptr;
+  int32_t* dpairtab = nullptr;
+  int32_t* dntttt = nullptr;
+  double *dF = nullptr, *dJ = nullptr, *dK = nullptr, *dfmpb = nullptr;
+  int8_t* dorbsym = nullptr;
+  int64_t ninte = 0;
+  // per-run buffers
+  int32_t* dgens = nullptr;
+  uint8_t* dgmask = nullptr;
+  int gens_cap = 0;
+  int32_t* dnb_j = nullptr;
+  uint64_t* dnb_em = nullptr;
+  int32_t* dlr_idx = nullptr;
+  size_t scratch_blocks = 0;
+  double* dgen_part = nullptr;
+  size_t gen_part_cap = 0;
+  unsigned long long* dcounters = nullptr;  // counters + dpivot + hist
+  double* dhist_tab = nullptr;
+  double* dred = nullptr;
+  int* dwork = nullptr;
+  uint64_t* dsel_bits = nullptr;
+  int32_t* dsel_owner = nullptr;
+  double *dsel_xam = nullptr, *dsel_evp = nullptr;
+  long long sel_cap = 0;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  // pending run
+  int ngen = 0;
+  int nclass = kNClass;
+  bool pending = false;
+  cipsi_opts last_opts{};
+  // fetched selection (sorted)
+  std::vector<int32_t> sel_nec, sel_h, sel_p, sel_owner;
+  std::vector<double> sel_xam, sel_evp;
+};
+
+namespace {
+
+int fail(cipsi_ctx* c, int code, const std::string& msg) {
+  if (c) c->err = msg;
+  return code;
+}
+
+#define CK(call)                                                                        \
+  do {                                                                                  \
+    cudaError_t e_ = (call);                                                            \
+    if (e_ != cudaSuccess)                                                              \
+      return fail(ctx, CIPSI_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+template <typename T>
+int upload(cipsi_ctx* ctx, T** dptr, const T* h, size_t n) {
+  if (*dptr) cudaFree(*dptr);
+  *dptr = nullptr;
+  CK(cudaMalloc((void**)dptr, std::max<size_t>(n, 1) * sizeof(T)));
+  if (n) CK(cudaMemcpyAsync(*dptr, h, n * sizeof(T), cudaMemcpyHostToDevice, ctx->stream));
+  return 0;
+}
+
+template <typename T>
+void dfree(T*& p) {
+  if (p) cudaFree(p);
+  p = nullptr;
+}
+
+}  // namespace
+
+extern "C" {
+
+int cipsi_ctx_create(cipsi_ctx** out, const cipsi_dims* dims, int32_t device) {
+  if (!out || !dims) return CIPSI_ERR_ARG;
+  *out = nullptr;
+  cipsi_ctx* ctx = new cipsi_ctx();
+  ctx->d = *dims;
+  ctx->device = device;
+  const cipsi_dims& d = *dims;
+  if (d.norb < 2 || d.norb > kMaxOrb) {
+    *out = ctx;
+    return fail(ctx, CIPSI_ERR_ARG, "norb must be in [2, 128]");
+  }
+  if (d.noca < 1 || d.noca >= d.norb || 2 * d.noca > kMaxElec) {
+    *out = ctx;
+    return fail(ctx, CIPSI_ERR_ARG, "noca must be in [1, min(norb-1, 32)]");
+  }
+  if (d.nsym < 1 || d.nsym > kMaxSym || d.isym < 1 || d.isym > d.nsym) {
+    *out = ctx;
+    return fail(ctx, CIPSI_ERR_ARG, "nsym must be in [1, 8] and isym in [1, nsym]");
+  }
+  if (d.isz != 0) {
+    *out = ctx;
+    return fail(ctx, CIPSI_ERR_ARG, "only isz = 0 (Ms = 0) is supported");
+  }
+  if (d.metat < 1 || d.metat > kMaxRoots) {
+    *out = ctx;
+    return fail(ctx, CIPSI_ERR_ARG, "metat must be in [1, 8]");
+  }
+  if (d.ncf < 1) {
+    *out = ctx;
+    return fail(ctx, CIPSI_ERR_ARG, "ncf must be positive");
+  }
+  ctx->W = d.norb <= 64 ? 1 : 2;
+  *out = ctx;
+  CK(cudaSetDevice(device));
+  CK(cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking));
+  ctx->stream = ctx->own_stream;
+  CK(cudaEventCreate(&ctx->ev0));
+  CK(cudaEventCreate(&ctx->ev1));
+  return CIPSI_OK;
+}
+
+void cipsi_ctx_destroy(cipsi_ctx* ctx) {
+  if (!ctx) return;
+  cudaSetDevice(ctx->device);
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  dfree(ctx->dS); dfree(ctx->dygen); dfree(ctx->dyef); dfree(ctx->dnesp); dfree(ctx->dc);
+  dfree(ctx->deri); dfree(ctx->dpairtab); dfree(ctx->dntttt); dfree(ctx->dF); dfree(ctx->dJ);
+  dfree(ctx->dK); dfree(ctx->dfmpb); dfree(ctx->dorbsym); dfree(ctx->dgens); dfree(ctx->dgmask);
+  dfree(ctx->dnb_j); dfree(ctx->dnb_em); dfree(ctx->dlr_idx); dfree(ctx->dgen_part);
+  dfree(ctx->dcounters); dfree(ctx->dhist_tab); dfree(ctx->dred); dfree(ctx->dwork);
+  dfree(ctx->dsel_bits); dfree(ctx->dsel_owner); dfree(ctx->dsel_xam); dfree(ctx->dsel_evp);
+  if (ctx->ev0) cudaEventDestroy(ctx->ev0);
+  if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+  if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
+  delete ctx;
+}
+
+const char* cipsi_last_error(const cipsi_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+int cipsi_set_stream(cipsi_ctx* ctx, void* stream) {
+  if (!ctx) return CIPSI_ERR_ARG;
+  ctx->stream = stream ? (cudaStream_t)stream : ctx->own_stream;
+  return CIPSI_OK;
+}
+
+static int set_integrals_common(cipsi_ctx* ctx, const int32_t* itsym, const int32_t* its,
+                                const double* f, const double* aj, const double* ak,
+                                const int16_t* ij0, const int32_t* ntttt, int64_t ninte) {
+  const int n = ctx->d.norb, ns = ctx->d.nsym;
+  if (!itsym || !its || !f || !aj || !ak || !ij0 || !ntttt || ninte < 1)
+    return fail(ctx, CIPSI_ERR_ARG, "set_integrals: null array or empty integral list");
+  CK(cudaSetDevice(ctx->device));
+  ctx->itsym.assign(itsym, itsym + n);
+  ctx->its.assign(its, its + ns * ns);
+  std::vector<int8_t> orbsym(n);
+  for (int i = 0; i < n; ++i) {
+    if (itsym[i] < 1 || itsym[i] > ns) return fail(ctx, CIPSI_ERR_ARG, "itsym out of range");
+    orbsym[i] = (int8_t)(itsym[i] - 1);
+  }
+  for (int i = 0; i < ns * ns; ++i)
+    if (its[i] < 1 || its[i] > ns) return fail(ctx, CIPSI_ERR_ARG, "its out of range");
+  // pair table: pair index (1-based) | irrep (1-based) << 24, as cip/ai.f reads ij0
+  std::vector<int32_t> pt((size_t)n * n);
+  auto IJ0 = [&](int i, int j) -> int { return ij0[(size_t)(j - 1) * n + (i - 1)]; };
+  for (int i = 1; i <= n; ++i)
+    for (int j = 1; j <= n; ++j) {
+      const int mi = std::min(i, j), ma = std::max(i, j);
+      const int pidx = IJ0(mi, ma);
+      const int irr = (mi == ma) ? 1 : IJ0(ma, mi);
+      if (pidx < 1 || irr < 1 || irr > ns)
+        return fail(ctx, CIPSI_ERR_ARG, "ij0 holds an invalid pair index or irrep");
+      pt[(size_t)(i - 1) * n + (j - 1)] = pidx | (irr << 24);
+    }
+  std::vector<int32_t> nt(ns + 1, 0);
+  for (int s = 0; s < ns; ++s) nt[s + 1] = ntttt[s];
+  const size_t nter = (size_t)n * (n + 1) / 2;
+  std::vector<double> F(f, f + nter);
+  // cip/ijkf.f:34-37 zeroes |F| < 1e-10
+  for (auto& x : F)
+    if (std::fabs(x) < 1.0e-10) x = 0.0;
+  int rc;
+  if ((rc = upload(ctx, &ctx->dorbsym, orbsym.data(), orbsym.size()))) return rc;
+  if ((rc = upload(ctx, &ctx->dpairtab, pt.data(), pt.size()))) return rc;
+  if ((rc = upload(ctx, &ctx->dntttt, nt.data(), nt.size()))) return rc;
+  if ((rc = upload(ctx, &ctx->dF, F.data(), F.size()))) return rc;
+  if ((rc = upload(ctx, &ctx->dJ, aj, nter))) return rc;
+  if ((rc = upload(ctx, &ctx->dK, ak, nter))) return rc;
+  ctx->ninte = ninte;
+  return CIPSI_OK;
+}
+
+int cipsi_set_integrals(cipsi_ctx* ctx, const int32_t* itsym, const int32_t* its, const double* f,
+                        const double* aj, const double* ak, const int16_t* ij0,
+                        const int32_t* ntttt, const float* bijkl, int64_t ninte) {
+  if (!ctx) return CIPSI_ERR_ARG;
+  int rc = set_integrals_common(ctx, itsym, its, f, aj, ak, ij0, ntttt, ninte);
+  if (rc) return rc;
+  if (!bijkl) return fail(ctx, CIPSI_ERR_ARG, "bijkl is null");
+  if ((rc = upload(ctx, &ctx->deri, bijkl, (size_t)ninte))) return rc;
+  CK(cudaStreamSynchronize(ctx->stream));
+  ctx->have_int = true;
+  return CIPSI_OK;
+}
+
+int cipsi_set_integrals_fp64(cipsi_ctx* ctx, const int32_t* itsym, const int32_t* its,
+                             const double* f, const double* aj, const double* ak,
+                             const int16_t* ij0, const int32_t* ntttt, const double* pqrs,
+                             int64_t ninte) {
+  if (!ctx) return CIPSI_ERR_ARG;
+  if (!pqrs) return fail(ctx, CIPSI_ERR_ARG, "pqrs is null");
+  std::vector<float> b((size_t)ninte);
+  for (int64_t i = 0; i < ninte; ++i) b[i] = (float)pqrs[i];  // real*8 -> real*4 (RN)
+  return cipsi_set_integrals(ctx, itsym, its, f, aj, ak, ij0, ntttt, b.data(), ninte);
+}
+
+int cipsi_set_space(cipsi_ctx* ctx, const int32_t* ne, const int32_t* nd, const int32_t* trou,
+                    const int32_t* part, int64_t ntp, const uint8_t* ygen, const uint8_t* ysaut,
+                    const int32_t* nesp, const uint8_t* yef1) {
+  if (!ctx) return CIPSI_ERR_ARG;
+  if (!ne || !nd || !trou || !part || !ygen || !ysaut || !nesp || !yef1)
+    return fail(ctx, CIPSI_ERR_ARG, "set_space: null array");
+  const int ncf = ctx->d.ncf, n = ctx->d.norb, W = ctx->W, noca = ctx->d.noca;
+  CK(cudaSetDevice(ctx->device));
+  ctx->Sbits.assign((size_t)ncf * 2 * W, 0ull);
+  ctx->rank.assign(ncf, 0);
+  ctx->sigma.assign(ncf, 1.0);
+  for (int k = 0; k < ncf; ++k) {
+    const int nec = ne[k];
+    if (nec < 0 || nec > 16 || (nec > 0 && (nd[k] < 0 || nd[k] + nec > ntp)))
+      return fail(ctx, CIPSI_ERR_ARG, "set_space: bad ne/nd at determinant " + std::to_string(k + 1));
+    // reference determinant bits over 2*norb spin orbitals
+    std::vector<uint64_t> full(4, 0ull);  // spin orbital so (0-based) -> bit so
+    auto setb = [&](int so, bool on) {
+      if (on) full[so >> 6] |= 1ull << (so & 63);
+      else full[so >> 6] &= ~(1ull << (so & 63));
+    };
+    auto getb = [&](int so) { return (full[so >> 6] >> (so & 63)) & 1ull; };
+    for (int o = 0; o < noca; ++o) {
+      setb(o, true);
+      setb(o + n, true);
+    }
+    int sign = 1;
+    for (int i = 0; i < nec; ++i) {
+      const int h = trou[nd[k] + i], pp = part[nd[k] + i];
+      if (h < 1 || h > 2 * n || pp < 1 || pp > 2 * n)
+        return fail(ctx, CIPSI_ERR_ARG, "set_space: spin orbital out of range");
+      const int h0 = h - 1, p0 = pp - 1;
+      if (!getb(h0) || getb(p0))
+        return fail(ctx, CIPSI_ERR_ARG, "set_space: invalid excitation list at determinant " +
+                                            std::to_string(k + 1));
+      // phase of a+_p a_h on the canonical string (reference pair convention)
+      const int lo = std::min(h0, p0), hi = std::max(h0, p0);
+      int cnt = 0;
+      for (int so = lo + 1; so < hi; ++so) cnt += (int)getb(so);
+      if (cnt & 1) sign = -sign;
+      setb(h0, false);
+      setb(p0, true);
+    }
+    ctx->sigma[k] = sign;
+    ctx->rank[k] = nec;
+    int nal = 0, nbe = 0;
+    for (int o = 0; o < n; ++o) {
+      if (getb(o)) {
+        ctx->Sbits[(size_t)k * 2 * W + (o >> 6)] |= 1ull << (o & 63);
+        ++nal;
+      }
+      if (getb(o + n)) {
+        ctx->Sbits[(size_t)k * 2 * W + W + (o >> 6)] |= 1ull << (o & 63);
+        ++nbe;
+      }
+    }
+    if (nal != noca || nbe != noca)
+      return fail(ctx, CIPSI_ERR_ARG, "set_space: determinant with Ms != 0");
+  }
+  ctx->ygen.assign(ygen, ygen + ncf);
+  ctx->ysaut.assign(ysaut, ysaut + ncf);
+  ctx->yef1.assign(yef1, yef1 + ncf);
+  ctx->nesp.assign(nesp, nesp + ncf);
+  for (int k = 0; k < ncf; ++k) {
+    ctx->ygen[k] = ctx->ygen[k] ? 1 : 0;
+    ctx->ysaut[k] = ctx->ysaut[k] ? 1 : 0;
+    ctx->yef1[k] = ctx->yef1[k] ? 1 : 0;
+  }
+  int rc;
+  if ((rc = upload(ctx, &ctx->dS, ctx->Sbits.data(), ctx->Sbits.size()))) return rc;
+  if ((rc = upload(ctx, &ctx->dygen, ctx->ygen.data(), ctx->ygen.size()))) return rc;
+  if ((rc = upload(ctx, &ctx->dyef, ctx->yef1.data(), ctx->yef1.size()))) return rc;
+  if ((rc = upload(ctx, &ctx->dnesp, ctx->nesp.data(), ctx->nesp.size()))) return rc;
+  CK(cudaStreamSynchronize(ctx->stream));
+  ctx->have_space = true;
+  ctx->have_roots = false;  // coefficients need the phases of this space
+  return CIPSI_OK;
+}
+
+int cipsi_set_roots(cipsi_ctx* ctx, const double* c, const double* e, const double* eb,
+                    const double* emp, const double* teste, const double* taum,
+                    const double* fmpb) {
+  if (!ctx) return CIPSI_ERR_ARG;
+  if (!ctx->have_space) return fail(ctx, CIPSI_ERR_STATE, "set_roots before set_space");
+  if (!c || !e || !eb || !emp || !teste || !taum || !fmpb)
+    return fail(ctx, CIPSI_ERR_ARG, "set_roots: null array");
+  const int ncf = ctx->d.ncf, mt = ctx->d.metat, n = ctx->d.norb;
+  CK(cudaSetDevice(ctx->device));
+  std::vector<double> cc((size_t)ncf * mt);
+  for (int k = 0; k < ncf; ++k)
+    for (int m = 0; m < mt; ++m) cc[(size_t)k * mt + m] = ctx->sigma[k] * c[(size_t)m * ncf + k];
+  for (int m = 0; m < mt; ++m) {
+    ctx->e[m] = e[m];
+    ctx->eb[m] = eb[m];
+    ctx->emp[m] = emp[m];
+    ctx->teste[m] = teste[m];
+    ctx->taum[m] = taum[m];
+  }
+  int rc;
+  if ((rc = upload(ctx, &ctx->dc, cc.data(), cc.size()))) return rc;
+  if ((rc = upload(ctx, &ctx->dfmpb, fmpb, (size_t)2 * n))) return rc;
+  CK(cudaStreamSynchronize(ctx->stream));
+  ctx->have_roots = true;
+  return CIPSI_OK;
+}
+
+}  // extern "C"
+
+template <int W, int R>
+static cudaError_t launch_pt2(const Params& p, int grid, size_t smem, cudaStream_t st) {
+  cudaError_t e = cudaFuncSetAttribute(k_pt2<W, R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       160 * 1024);
+  if (e != cudaSuccess) return e;
+  k_pt2<W, R><<<grid, kThreads, smem, st>>>(p);
+  return cudaGetLastError();
+}
+
+extern "C" {
+
+int cipsi_run_pt2_async(cipsi_ctx* ctx, const cipsi_opts* o) {
+  if (!ctx || !o) return CIPSI_ERR_ARG;
+  if (!ctx->have_int || !ctx->have_space || !ctx->have_roots)
+    return fail(ctx, CIPSI_ERR_STATE, "run before set_integrals / set_space / set_roots");
+  if (o->nclass < 2 || o->nclass > kNClass) return fail(ctx, CIPSI_ERR_ARG, "nclass must be in [2, 10]");
+  CK(cudaSetDevice(ctx->device));
+  const int ncf = ctx->d.ncf, W = ctx->W, mt = ctx->d.metat;
+  // flags on the content of S (pertu.f:52-61)
+  bool yd = false, ym = false, yf = false;
+  for (int k = 0; k < ncf; ++k) {
+    if (ctx->rank[k] == 1) ym = true;
+    if (ctx->rank[k] == 0) yd = true;
+    if (ctx->rank[k] == 2) yf = true;
+  }
+  if (ym) yf = true;
+  std::vector<int32_t> gens;
+  std::vector<uint8_t> gmask;
+  const bool pertu_ref = yf && !yd && ctx->d.isym == 1;  // isz == 0, !yion
+  const bool pertu_mono = yf && ym;
+  if (o->run_pertu && (pertu_ref || pertu_mono)) {
+    gens.push_back(-1);
+    gmask.push_back(0);
+  }
+  for (int k = 0; k < ncf; ++k) {
+    if (!ctx->ygen[k] || ctx->ysaut[k]) continue;
+    if (o->gen_mask && !o->gen_mask[k]) continue;
+    const int nec = ctx->rank[k];
+    // allowed rank changes, bit (D + 2); D = +2 (diexcit) always
+    uint8_t m = 1u << 4;
+    if (!((nec == 0 && ym) || (nec == 1 && yd))) {
+      m |= 1u << 3;  // +1
+      const bool stop1 = nec < 1 || (ym && nec == 1) || (nec == 2 && yd);
+      if (!stop1) {
+        m |= 1u << 2;  // 0
+        if (!((nec == 3 && yd) || (nec == 2 && ym))) {
+          m |= 1u << 1;  // -1
+          if (!((nec == 2 && (yd || yf)) || (nec == 3 && ym) || (nec == 4 && yd))) m |= 1u << 0;
+        }
+      }
+    }
+    gens.push_back(k);
+    gmask.push_back(m);
+  }
+  const int ngen = (int)gens.size();
+  ctx->ngen = ngen;
+  int dev_sms = 0;
+  CK(cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, ctx->device));
+  // shared L_R capacity: enough for every neighbour list when it fits
+  const size_t per_entry = (size_t)2 * W * 8 + 4;
+  const size_t smem_budget = 150 * 1024;
+  int lr_cap = (int)std::min<size_t>((size_t)ncf, smem_budget / per_entry);
+  const size_t smem = (size_t)lr_cap * per_entry + 16;
+  const int blocks_per_sm = smem <= 70 * 1024 ? 2 : 1;
+  int grid = std::max(1, std::min(ngen, dev_sms * blocks_per_sm));
+  if (ngen == 0) grid = 1;
+  // buffers
+  if ((size_t)grid > ctx->scratch_blocks || !ctx->dnb_j) {
+    dfree(ctx->dnb_j); dfree(ctx->dnb_em); dfree(ctx->dlr_idx);
+    CK(cudaMalloc(&ctx->dnb_j, (size_t)grid * ncf * sizeof(int32_t)));
+    CK(cudaMalloc(&ctx->dnb_em, (size_t)grid * ncf * sizeof(uint64_t)));
+    CK(cudaMalloc(&ctx->dlr_idx, (size_t)grid * ncf * sizeof(int32_t)));
+    ctx->scratch_blocks = grid;
+  }
+  if (ngen > ctx->gens_cap) {
+    dfree(ctx->dgens); dfree(ctx->dgmask);
+    CK(cudaMalloc(&ctx->dgens, (size_t)std::max(ngen, 1) * sizeof(int32_t)));
+    CK(cudaMalloc(&ctx->dgmask, (size_t)std::max(ngen, 1)));
+    ctx->gens_cap = ngen;
+  }
+  if (ngen) {
+    CK(cudaMemcpyAsync(ctx->dgens, gens.data(), ngen * sizeof(int32_t), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(ctx->dgmask, gmask.data(), ngen, cudaMemcpyHostToDevice, ctx->stream));
+  }
+  const size_t nq = (size_t)5 * mt;
+  if ((size_t)std::max(ngen, 1) * nq > ctx->gen_part_cap) {
+    dfree(ctx->dgen_part);
+    ctx->gen_part_cap = (size_t)std::max(ngen, 1) * nq;
+    CK(cudaMalloc(&ctx->dgen_part, ctx->gen_part_cap * sizeof(double)));
+  }
+  // counters [C_NCOUNTERS] + dpivot + nom[10] + nam[10*8]
+  const size_t ncount = C_NCOUNTERS + 1 + kNClass + kNClass * kMaxRoots;
+  if (!ctx->dcounters) {
+    CK(cudaMalloc(&ctx->dcounters, ncount * sizeof(unsigned long long)));
+    CK(cudaMalloc(&ctx->dhist_tab, 2 * kNClass * kMaxRoots * sizeof(double)));
+    CK(cudaMalloc(&ctx->dred, 5 * kMaxRoots * sizeof(double)));
+    CK(cudaMalloc(&ctx->dwork, sizeof(int)));
+  }
+  if (ctx->sel_cap == 0) {
+    ctx->sel_cap = 1 << 20;
+    CK(cudaMalloc(&ctx->dsel_bits, (size_t)ctx->sel_cap * 2 * W * sizeof(uint64_t)));
+    CK(cudaMalloc(&ctx->dsel_owner, (size_t)ctx->sel_cap * sizeof(int32_t)));
+    CK(cudaMalloc(&ctx->dsel_xam, (size_t)ctx->sel_cap * sizeof(double)));
+    CK(cudaMalloc(&ctx->dsel_evp, (size_t)ctx->sel_cap * mt * sizeof(double)));
+  }
+  CK(cudaMemsetAsync(ctx->dcounters, 0, ncount * sizeof(unsigned long long), ctx->stream));
+  CK(cudaMemsetAsync(ctx->dhist_tab, 0, 2 * kNClass * kMaxRoots * sizeof(double), ctx->stream));
+  CK(cudaMemsetAsync(ctx->dwork, 0, sizeof(int), ctx->stream));
+  CK(cudaMemsetAsync(ctx->dgen_part, 0, (size_t)std::max(ngen, 1) * nq * sizeof(double), ctx->stream));
+
+  Params p{};
+  p.norb = ctx->d.norb;
+  p.noca = ctx->d.noca;
+  p.nel = 2 * ctx->d.noca;
+  p.ncf = ncf;
+  p.metat = mt;
+  p.nsym = ctx->d.nsym;
+  p.isym = ctx->d.isym;
+  p.ngen = ngen;
+  p.gens = ctx->dgens;
+  p.gen_dmask = ctx->dgmask;
+  p.S = ctx->dS;
+  p.ygen = ctx->dygen;
+  p.nesp = ctx->dnesp;
+  p.yef = ctx->dyef;
+  p.c = ctx->dc;
+  p.eri = ctx->deri;
+  p.pairtab = ctx->dpairtab;
+  p.ntttt = ctx->dntttt;
+  p.F = ctx->dF;
+  p.J = ctx->dJ;
+  p.K = ctx->dK;
+  p.fmpb = ctx->dfmpb;
+  p.orbsym = ctx->dorbsym;
+  for (int i = 0; i < ctx->d.nsym; ++i)
+    for (int j = 0; j < ctx->d.nsym; ++j) p.its[i][j] = ctx->its[(size_t)j * ctx->d.nsym + i] - 1;
+  for (int m = 0; m < mt; ++m) {
+    p.e[m] = ctx->e[m];
+    p.eb[m] = ctx->eb[m];
+    p.emp[m] = ctx->emp[m];
+    p.teste[m] = ctx->teste[m];
+    p.taum[m] = ctx->taum[m];
+  }
+  p.yen = o->yen;
+  p.ysele = o->ysele;
+  p.ymoyen = o->ymoyen;
+  p.ywdeg = o->ywdeg;
+  p.symvar = o->sym_variant;
+  p.nclass = o->nclass;
+  p.tau = o->tau;
+  p.teseff = o->teseff;
+  for (int i = 0; i < kNClass; ++i) p.aval[i] = o->aval[i];
+  p.pertu_ref = pertu_ref ? 1 : 0;
+  p.pertu_mono = pertu_mono ? 1 : 0;
+  p.nb_j = ctx->dnb_j;
+  p.nb_emask = ctx->dnb_em;
+  p.lr_idx = ctx->dlr_idx;
+  p.lr_cap = lr_cap;
+  p.gen_part = ctx->dgen_part;
+  p.counters = ctx->dcounters;
+  p.dpivot_bits = ctx->dcounters + C_NCOUNTERS;
+  p.hist_nom = ctx->dcounters + C_NCOUNTERS + 1;
+  p.hist_nam = ctx->dcounters + C_NCOUNTERS + 1 + kNClass;
+  p.hist_tab = ctx->dhist_tab;
+  p.sel_bits = ctx->dsel_bits;
+  p.sel_owner = ctx->dsel_owner;
+  p.sel_xam = ctx->dsel_xam;
+  p.sel_evp = ctx->dsel_evp;
+  p.sel_cap = ctx->sel_cap;
+  p.work = ctx->dwork;
+
+  CK(cudaEventRecord(ctx->ev0, ctx->stream));
+  if (ngen > 0) {
+    cudaError_t e;
+    const int R = mt <= 1 ? 1 : mt <= 2 ? 2 : mt <= 4 ? 4 : 8;
+    if (W == 1) {
+      e = R == 1 ? launch_pt2<1, 1>(p, grid, smem, ctx->stream)
+        : R == 2 ? launch_pt2<1, 2>(p, grid, smem, ctx->stream)
+        : R == 4 ? launch_pt2<1, 4>(p, grid, smem, ctx->stream)
+                 : launch_pt2<1, 8>(p, grid, smem, ctx->stream);
+    } else {
+      e = R == 1 ? launch_pt2<2, 1>(p, grid, smem, ctx->stream)
+        : R == 2 ? launch_pt2<2, 2>(p, grid, smem, ctx->stream)
+        : R == 4 ? launch_pt2<2, 4>(p, grid, smem, ctx->stream)
+                 : launch_pt2<2, 8>(p, grid, smem, ctx->stream);
+    }
+    if (e != cudaSuccess) return fail(ctx, CIPSI_ERR_CUDA, std::string("k_pt2 launch: ") + cudaGetErrorString(e));
+    k_reduce<<<1, 64, 0, ctx->stream>>>(ctx->dgen_part, ngen, (int)nq, ctx->dred);
+    CK(cudaGetLastError());
+  } else {
+    CK(cudaMemsetAsync(ctx->dred, 0, nq * sizeof(double), ctx->stream));
+  }
+  CK(cudaEventRecord(ctx->ev1, ctx->stream));
+  ctx->nclass = o->nclass;
+  ctx->pending = true;
+  ctx->last_opts = *o;
+  return CIPSI_OK;
+}
+
+int cipsi_fetch_result(cipsi_ctx* ctx, cipsi_result* r) {
+  if (!ctx || !r) return CIPSI_ERR_ARG;
+  if (!ctx->pending) return fail(ctx, CIPSI_ERR_STATE, "fetch_result without a run");
+  CK(cudaSetDevice(ctx->device));
+  CK(cudaStreamSynchronize(ctx->stream));
+  ctx->pending = false;
+  const int mt = ctx->d.metat, W = ctx->W;
+  memset(r, 0, sizeof(*r));
+  std::vector<double> red(5 * mt);
+  CK(cudaMemcpy(red.data(), ctx->dred, red.size() * sizeof(double), cudaMemcpyDeviceToHost));
+  for (int m = 0; m < mt; ++m) {
+    r->e2mp[m] = red[0 * mt + m];
+    r->e2vp[m] = red[1 * mt + m];
+    r->e2b[m] = red[2 * mt + m];
+    r->psimp[m] = red[3 * mt + m];
+    r->psivp[m] = red[4 * mt + m];
+  }
+  const size_t ncount = C_NCOUNTERS + 1 + kNClass + kNClass * kMaxRoots;
+  std::vector<unsigned long long> cnt(ncount);
+  CK(cudaMemcpy(cnt.data(), ctx->dcounters, ncount * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
+  std::vector<double> tab(2 * kNClass * kMaxRoots);
+  CK(cudaMemcpy(tab.data(), ctx->dhist_tab, tab.size() * sizeof(double), cudaMemcpyDeviceToHost));
+  r->ietat = (int64_t)cnt[C_IETAT];
+  r->n_processed = (int64_t)cnt[C_NPROC];
+  r->n_candidates = (int64_t)cnt[C_NCAND];
+  r->n_compares = (int64_t)cnt[C_NCMP];
+  r->n_pairs_1 = (int64_t)cnt[C_NP1];
+  r->n_pairs_2 = (int64_t)cnt[C_NP2];
+  {
+    unsigned long long b = cnt[C_NCOUNTERS];
+    double dp;
+    memcpy(&dp, &b, 8);
+    r->dpivot = dp;
+  }
+  const int nc = ctx->nclass;
+  for (int i = 0; i < nc; ++i) r->nom[i] = (int64_t)cnt[C_NCOUNTERS + 1 + i];
+  for (int c = 0; c < nc; ++c)
+    for (int m = 0; m < mt; ++m) {
+      r->nam[c * kMaxRoots + m] = (int64_t)cnt[C_NCOUNTERS + 1 + kNClass + c * mt + m];
+      r->tabmp[c * kMaxRoots + m] = tab[c * mt + m];
+      r->tabvp[c * kMaxRoots + m] = tab[nc * mt + c * mt + m];
+    }
+  // algorithmic bytes of the E2 loop (per interacting pair: metat coefficients
+  // + integrals as stored; per perturber: diagonal terms), see the docs
+  const double avg_rank = 4.0;
+  r->alg_bytes = (int64_t)(cnt[C_NP2] * (8.0 * mt + 2 * 4.0 + 8.0) +
+                           cnt[C_NP1] * (8.0 * mt + 8.0 + 2.0 * avg_rank * 2 * 4.0) +
+                           cnt[C_NPROC] * (8.0 * avg_rank + 8.0 * (avg_rank + avg_rank * avg_rank) + 8.0 * mt));
+  float ms = 0.f;
+  CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+  r->kernel_ms = ms;
+  // selection
+  long long nsel = (long long)cnt[C_NSEL];
+  if (nsel > ctx->sel_cap)
+    return fail(ctx, CIPSI_ERR_OVERFLOW,
+                "selection buffer overflow: " + std::to_string(nsel) + " records > capacity " +
+                    std::to_string(ctx->sel_cap) + " (raise tau or rerun; the capacity grows)");
+  std::vector<uint64_t> bits((size_t)nsel * 2 * W);
+  std::vector<int32_t> own(nsel);
+  std::vector<double> xam(nsel), evp((size_t)nsel * mt);
+  if (nsel) {
+    CK(cudaMemcpy(bits.data(), ctx->dsel_bits, bits.size() * 8, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(own.data(), ctx->dsel_owner, own.size() * 4, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(xam.data(), ctx->dsel_xam, xam.size() * 8, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(evp.data(), ctx->dsel_evp, evp.size() * 8, cudaMemcpyDeviceToHost));
+  }
+  std::vector<long long> order(nsel);
+  for (long long i = 0; i < nsel; ++i) order[i] = i;
+  std::sort(order.begin(), order.end(), [&](long long a, long long b) {
+    if (own[a] != own[b]) return own[a] < own[b];
+    for (int q = 0; q < 2 * W; ++q) {
+      const uint64_t x = bits[(size_t)a * 2 * W + q], y = bits[(size_t)b * 2 * W + q];
+      if (x != y) return x < y;
+    }
+    return false;
+  });
+  const int n = ctx->d.norb, noca = ctx->d.noca;
+  ctx->sel_nec.assign(nsel, 0);
+  ctx->sel_h.assign((size_t)nsel * 8, 0);
+  ctx->sel_p.assign((size_t)nsel * 8, 0);
+  ctx->sel_owner.assign(nsel, 0);
+  ctx->sel_xam.assign(nsel, 0.0);
+  ctx->sel_evp.assign((size_t)nsel * mt, 0.0);
+  for (long long ii = 0; ii < nsel; ++ii) {
+    const long long i = order[ii];
+    int nh = 0, np = 0;
+    for (int s = 0; s < 2; ++s)
+      for (int o = 0; o < n; ++o) {
+        const bool occ = (bits[(size_t)i * 2 * W + s * W + (o >> 6)] >> (o & 63)) & 1ull;
+        const bool inhf = o < noca;
+        if (inhf && !occ && nh < 8) ctx->sel_h[(size_t)ii * 8 + nh++] = o + 1 + s * n;
+        if (!inhf && occ && np < 8) ctx->sel_p[(size_t)ii * 8 + np++] = o + 1 + s * n;
+      }
+    ctx->sel_nec[ii] = nh;
+    ctx->sel_owner[ii] = own[i];
+    ctx->sel_xam[ii] = xam[i];
+    for (int m = 0; m < mt; ++m) ctx->sel_evp[(size_t)ii * mt + m] = evp[(size_t)i * mt + m];
+  }
+  r->n_selected = nsel;
+  return CIPSI_OK;
+}
+
+int cipsi_run_pt2(cipsi_ctx* ctx, const cipsi_opts* opts, cipsi_result* res) {
+  for (int attempt = 0; attempt < 4; ++attempt) {
+    int rc = cipsi_run_pt2_async(ctx, opts);
+    if (rc) return rc;
+    rc = cipsi_fetch_result(ctx, res);
+    if (rc != CIPSI_ERR_OVERFLOW) return rc;
+    // grow the selection buffer to what the run needed and redo
+    unsigned long long nsel = 0;
+    CK(cudaMemcpy(&nsel, ctx->dcounters + C_NSEL, 8, cudaMemcpyDeviceToHost));
+    dfree(ctx->dsel_bits); dfree(ctx->dsel_owner); dfree(ctx->dsel_xam); dfree(ctx->dsel_evp);
+    ctx->sel_cap = (long long)(nsel + nsel / 8 + 1024);
+    const int W = ctx->W, mt = ctx->d.metat;
+    CK(cudaMalloc(&ctx->dsel_bits, (size_t)ctx->sel_cap * 2 * W * sizeof(uint64_t)));
+    CK(cudaMalloc(&ctx->dsel_owner, (size_t)ctx->sel_cap * sizeof(int32_t)));
+    CK(cudaMalloc(&ctx->dsel_xam, (size_t)ctx->sel_cap * sizeof(double)));
+    CK(cudaMalloc(&ctx->dsel_evp, (size_t)ctx->sel_cap * mt * sizeof(double)));
+  }
+  return fail(ctx, CIPSI_ERR_OVERFLOW, "selection buffer could not be grown");
+}
+
+int cipsi_selection_get(cipsi_ctx* ctx, int64_t first, int64_t count, int32_t* nec, int32_t* holes,
+                        int32_t* parts, double* xam, double* evp, int32_t* owner) {
+  if (!ctx) return CIPSI_ERR_ARG;
+  const int64_t n = (int64_t)ctx->sel_nec.size();
+  if (first < 0 || count < 0 || first + count > n)
+    return fail(ctx, CIPSI_ERR_ARG, "selection_get: range outside the selection");
+  const int mt = ctx->d.metat;
+  for (int64_t i = 0; i < count; ++i) {
+    const int64_t s = first + i;
+    if (nec) nec[i] = ctx->sel_nec[s];
+    for (int q = 0; q < 8; ++q) {
+      if (holes) holes[i * 8 + q] = ctx->sel_h[s * 8 + q];
+      if (parts) parts[i * 8 + q] = ctx->sel_p[s * 8 + q];
+    }
+    if (xam) xam[i] = ctx->sel_xam[s];
+    if (evp)
+      for (int m = 0; m < mt; ++m) evp[i * mt + m] = ctx->sel_evp[s * mt + m];
+    if (owner) owner[i] = ctx->sel_owner[s];
+  }
+  return CIPSI_OK;
+}
+
+}  // extern "C"

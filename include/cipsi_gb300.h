@@ -1,0 +1,183 @@
+/*
+ * cipsi_gb300.h -- C ABI of the GB300 engine for the CIPSI second-order
+ * perturbation and selection step (the `cip` / `cipsym` hot path).
+ *
+ * The engine replaces, in one call, the two subroutine calls that do all the
+ * work of the reference program after its set-up:
+ *
+ *     if(ypertu) call pertu        CIPSI_sources/cip/cip.f:238
+ *     if(ypertu) call diexcit      CIPSI_sources/cip/cip.f:241
+ *     (CIPSI_sources/cipsym/cip.f:248,251 in the symmetric variant)
+ *
+ * Those subroutines take no arguments; they read and write COMMON blocks.
+ * Each setter below takes the arrays of one group of COMMON variables, with
+ * the reference's own layout and meaning, so that a patched cip.f can pass
+ * its COMMON storage directly (see the Fortran ISO_C_BINDING interface in
+ * INTEGRATION.md).  All arrays are owned by the caller and copied by the
+ * call; nothing is retained.  Indices stored in arrays (spin orbitals,
+ * offsets) keep the reference's 1-based values.
+ *
+ * Return codes: 0 = success, negative = error (cipsi_last_error(ctx) gives a
+ * message).  The library never exits the process.  One context drives one
+ * GPU; contexts are independent (one per Autocip process / geometry).
+ */
+#ifndef CIPSI_GB300_H
+#define CIPSI_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CIPSI_OK 0
+#define CIPSI_ERR_ARG (-1)      /* invalid argument or unsupported input */
+#define CIPSI_ERR_CUDA (-2)     /* CUDA runtime error                    */
+#define CIPSI_ERR_STATE (-3)    /* call order (setters before run)       */
+#define CIPSI_ERR_OVERFLOW (-4) /* internal buffer overflow              */
+
+#define CIPSI_MAX_ROOTS 8
+#define CIPSI_NCLASS 10
+
+typedef struct cipsi_ctx cipsi_ctx;
+
+/* Sizes: COMMON /cipsi/ (CIPSI_sources/cip/cip.f:36-39). */
+typedef struct {
+  int32_t norb;  /* number of orbitals (norb)                               */
+  int32_t noca;  /* doubly occupied orbitals of the reference det (noca)    */
+  int32_t nsym;  /* number of irreducible representations (nsym)            */
+  int32_t isym;  /* symmetry of the treated states (isym, 1-based)          */
+  int32_t isz;   /* 2*Sz (isz); only 0 is supported                          */
+  int32_t metat; /* number of roots (metat), 1..CIPSI_MAX_ROOTS            */
+  int32_t ncf;   /* determinants of S including spin-flip partners (ncf)    */
+} cipsi_dims;
+
+/* Options: COMMON /cipsi/, /tome/, /hist/ flags used by pertu/diexcit. */
+typedef struct {
+  int32_t yen;        /* Epstein-Nesbet partitions (ityper = 2)              */
+  int32_t ysele;      /* select on energy contributions (iselec = 3)         */
+  int32_t ymoyen;     /* histogram + unit-60 selection (ymoyen)              */
+  int32_t ywdeg;      /* near-degenerate perturbers are selected (ywdeg)     */
+  int32_t sym_variant;/* 1: cipsym (ENvp per root in the selection records)  */
+  int32_t nclass;     /* histogram classes (nclass <= 10)                     */
+  double tau;         /* unit-60 selection threshold (tau)                    */
+  double teseff;      /* histogram threshold (teseff)                         */
+  double aval[CIPSI_NCLASS]; /* class upper bounds (aval)                     */
+  const uint8_t* gen_mask; /* optional, ncf bytes: 0 = do not run this det as
+                              a generator (generator-range sharding); NULL =
+                              all.  Owner tests still see every determinant. */
+  int32_t run_pertu;  /* 1: include pertu's reference-only and reference-
+                         single perturbers (pertu.f:62-108)                   */
+} cipsi_opts;
+
+/* Results: the accumulators of COMMON /ic/ and /hist/ after pertu+diexcit. */
+typedef struct {
+  double e2mp[CIPSI_MAX_ROOTS];  /* MP barycentric E2 (e2mp)                 */
+  double e2vp[CIPSI_MAX_ROOTS];  /* EN eigenvalue E2 (e2vp)                  */
+  double e2b[CIPSI_MAX_ROOTS];   /* EN barycentric E2 (e2b)                  */
+  double psimp[CIPSI_MAX_ROOTS]; /* norm of the first-order function, MP     */
+  double psivp[CIPSI_MAX_ROOTS]; /* norm of the first-order function, EN     */
+  double dpivot;                 /* largest non-listed contribution (dpivot) */
+  int64_t ietat;                 /* effective states generated (ietat)       */
+  int64_t n_processed;           /* perturbers that reached the E2 loop      */
+  int64_t n_selected;            /* records available through selection_get  */
+  int64_t nom[CIPSI_NCLASS];     /* histogram totals (nom)                   */
+  int64_t nam[CIPSI_NCLASS * CIPSI_MAX_ROOTS];     /* nam(class, root)       */
+  double tabmp[CIPSI_NCLASS * CIPSI_MAX_ROOTS];    /* tabmp(class, root)     */
+  double tabvp[CIPSI_NCLASS * CIPSI_MAX_ROOTS];    /* tabvp(class, root)     */
+  /* work counters (not in the reference; for throughput and roofline)      */
+  int64_t n_candidates;   /* excitations examined                           */
+  int64_t n_compares;     /* candidate-vs-S determinant comparisons          */
+  int64_t n_pairs_1;      /* interacting (I,K) pairs differing by 1 spin orb */
+  int64_t n_pairs_2;      /* interacting (I,K) pairs differing by 2          */
+  int64_t alg_bytes;      /* algorithmic bytes (integrals, coefficients,     */
+                          /* diagonal terms) read by the E2 loop             */
+  double kernel_ms;       /* device time of the perturbation kernels         */
+} cipsi_result;
+
+/* Create a context on CUDA device `device`.
+   Replaces the static sizing of pshf.prm (ndetz, doa, metz, kget). */
+int cipsi_ctx_create(cipsi_ctx** ctx, const cipsi_dims* dims, int32_t device);
+void cipsi_ctx_destroy(cipsi_ctx* ctx);
+const char* cipsi_last_error(const cipsi_ctx* ctx);
+
+/* Run the engine's kernels on this CUDA stream (cudaStream_t; NULL = the
+   context's own stream). */
+int cipsi_set_stream(cipsi_ctx* ctx, void* stream);
+
+/* Integrals: COMMON /jkf/ (f, aj, ak), /ij1/ (ij0, ntttt), /bij/ (bijkl) and
+   the symmetry tables itsym, its of /spo/ (cip/ijkf.f:26-43,
+   cip/reijkl.f:12-36, cip/ai.f:1-42).
+     itsym[norb]        irrep of each orbital (1-based values)
+     its[nsym*nsym]     product table, column-major its(i,j)
+     f, aj, ak          packed lower triangles ((x(i,j),j=1,i),i=1,norb)
+     ij0[norb*norb]     int16 pair map, column-major ij0(i,j)
+     ntttt[nsym]        first packed index of each irrep block (1-based)
+     bijkl[ninte]       (pq|rs) as stored by cip: real*4                     */
+int cipsi_set_integrals(cipsi_ctx* ctx, const int32_t* itsym, const int32_t* its,
+                        const double* f, const double* aj, const double* ak,
+                        const int16_t* ij0, const int32_t* ntttt, const float* bijkl,
+                        int64_t ninte);
+/* Same, from the real*8 values of the unit-40 file: rounded to real*4 exactly
+   as cip/reijkl.f:27 does. */
+int cipsi_set_integrals_fp64(cipsi_ctx* ctx, const int32_t* itsym, const int32_t* its,
+                             const double* f, const double* aj, const double* ak,
+                             const int16_t* ij0, const int32_t* ntttt, const double* pqrs,
+                             int64_t ninte);
+
+/* Reference space S: COMMON /spo/ (ne, nd, trou, part, ygen) and /degene/
+   (ysaut, nesp, yef(.,1)) as built by cip/deter.f:478-567.
+     ne[ncf], nd[ncf]   excitation degree and offset: the holes of det k are
+                        trou[nd[k]] .. trou[nd[k]+ne[k]-1] (C indexing of
+                        trou(nd(k)+1..nd(k)+ne(k)))
+     trou[], part[]     hole / particle spin orbitals (1..2*norb)
+     ygen, ysaut        generator and spin-flip-partner flags (bytes)
+     nesp               number of partners following a determinant
+     yef1               yef(k,1): det has a distinct spin-flip partner in S */
+int cipsi_set_space(cipsi_ctx* ctx, const int32_t* ne, const int32_t* nd, const int32_t* trou,
+                    const int32_t* part, int64_t ntp, const uint8_t* ygen, const uint8_t* ysaut,
+                    const int32_t* nesp, const uint8_t* yef1);
+
+/* Zero-order quantities: COMMON /ic/ and /tome/ (cip/cip.f:75-135).
+     c[ncf*metat]   S coefficients, column-major per root (reference phase)
+     e, eb, emp, teste, taum [metat]   e relative to escf
+     fmpb[2*norb]   barycentric MP one-electron energies                    */
+int cipsi_set_roots(cipsi_ctx* ctx, const double* c, const double* e, const double* eb,
+                    const double* emp, const double* teste, const double* taum,
+                    const double* fmpb);
+
+/* pertu + diexcit on the GPU (cip.f:238-241).  Blocks until done. */
+int cipsi_run_pt2(cipsi_ctx* ctx, const cipsi_opts* opts, cipsi_result* res);
+
+/* Enqueue the same work on the context stream without waiting; the result is
+   collected by cipsi_fetch_result.  Used to time the kernels alone. */
+int cipsi_run_pt2_async(cipsi_ctx* ctx, const cipsi_opts* opts);
+int cipsi_fetch_result(cipsi_ctx* ctx, cipsi_result* res);
+
+/* Selected perturbers (what pie.f writes to unit 60), sorted by owner
+   generator then by determinant: records [first, first+count).
+     nec[count]           excitation degree
+     holes/parts[8*count] sorted spin orbitals (1-based), zero padded
+     xam[count]           selection value written as v(n)
+     evp[metat*count]     ENvp contribution per root (cipsym), else zeros
+     owner[count]         generator index (1-based; 0 = pertu)             */
+int cipsi_selection_get(cipsi_ctx* ctx, int64_t first, int64_t count, int32_t* nec,
+                        int32_t* holes, int32_t* parts, double* xam, double* evp,
+                        int32_t* owner);
+
+/* Process-level drop-in for cip.exe (sym_variant = 0) and cipsym.exe
+   (sym_variant = 1): reads the &cipfil/&icinp namelists from `stdin_path`
+   and the unit files of `workdir` exactly as CIPSI_sources/cip/cip.f:50-242
+   does, runs the engine in place of pertu + diexcit, and writes unit 60,
+   unit 33 and the listing lines of cip.f:243-254 / cipsym/cip.f:253-254.
+   `json_path` (optional) receives the E2 totals and counters; `gen_mask`
+   (optional, one byte per determinant of S) limits the generators.  On
+   error returns a negative code and copies the message into errbuf. */
+int cipsi_cip_main(const char* workdir, const char* stdin_path, int32_t sym_variant,
+                   const char* json_path, const uint8_t* gen_mask, int32_t device, char* errbuf,
+                   int32_t errlen);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CIPSI_GB300_H */

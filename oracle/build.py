@@ -1,0 +1,51 @@
+"""Build recipe for the CPU oracle (test infrastructure; never linked into
+the product).  Compiles oracle/cipsi_ref.c with gcc into oracle/_build/."""
+from __future__ import annotations
+
+import os
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+OUT = os.path.join(HERE, "_build")
+EXE = os.path.join(OUT, "cipsi_ref")
+
+
+def build(force: bool = False) -> str:
+    os.makedirs(OUT, exist_ok=True)
+    src = os.path.join(HERE, "cipsi_ref.c")
+    if not force and os.path.exists(EXE) and os.path.getmtime(EXE) >= os.path.getmtime(src):
+        return EXE
+    cmd = ["gcc", "-O2", "-std=c11", "-Wall", "-o", EXE, src, "-lm"]
+    r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("oracle build failed:\n" + r.stdout)
+    return EXE
+
+
+def run(workdir: str, variant: str = "cipsym", json_name: str = "cipsi_ref.json",
+        candlog: str | None = None, genmask: str | None = None, no_pertu_ref: bool = False,
+        timeout: float | None = None) -> str:
+    """Run the oracle in `workdir` (it rewrites unit 60 and appends to unit 33,
+    as cip does).  Returns the JSON path."""
+    exe = build()
+    args = [exe]
+    if variant == "cipsym":
+        args.append("--sym")
+    args += ["--json", json_name]
+    if candlog:
+        args += ["--candlog", candlog]
+    if genmask:
+        args += ["--genmask", genmask]
+    if no_pertu_ref:
+        args.append("--no-pertu-ref")
+    with open(os.path.join(workdir, "cip.in")) as fin:
+        r = subprocess.run(args, cwd=workdir, stdin=fin, stdout=subprocess.PIPE, stderr=subprocess.PIPE,
+                           text=True, timeout=timeout)
+    if r.returncode != 0:
+        raise RuntimeError("oracle failed: " + r.stderr)
+    return os.path.join(workdir, json_name)
+
+
+if __name__ == "__main__":
+    print(build(force="--force" in sys.argv))

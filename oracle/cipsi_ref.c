@@ -206,7 +206,7 @@ static int nl_parse(const char* group, nlgroup_t* g) {
   return 1;
 }
 static nlitem_t* nl_get(nlgroup_t* g, const char* key) {
-  for (int i = 0; i < g->n; i++)
+  for (int i = g->n - 1; i >= 0; i--) /* a repeated key: the last one wins */
     if (strcasecmp(g->it[i].key, key) == 0) return &g->it[i];
   return NULL;
 }
