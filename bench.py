@@ -1,0 +1,335 @@
+#!/usr/bin/env python3
+"""Benchmark of the CIPSI perturbation / selection step on GB300.
+
+Workload ("medium"): 60 orbitals, 20 electrons (Ms = 0), S = 2000
+determinants (reference + singles/doubles/triples, spin-flip closed), 3 roots,
+MP + EN partitions, selection threshold 0.01; seeded synthetic integrals.
+
+A step is one full pass of the hot path (the work of pertu + diexcit) over
+the workload.  Metric: perturber contributions per second, one contribution
+being one (perturber that reaches the E2 loop, root) term.
+
+  value   device time of the engine's kernels, inputs resident in HBM, L2
+          flushed (256 MiB write) before every step;
+  e2e     the same through the C ABI from host buffers: every step uploads
+          the inputs (cipsi_inputs_upload), runs, fetches the result and the
+          selected determinants;
+  cpu_baseline  the CPU oracle (a restatement of the reference's loop nest)
+          on one core, on a sample of the generators.
+
+--impl reference times that CPU restatement on all host cores (one process
+per core, disjoint generator samples); the reference's Fortran cannot be
+built here (no Fortran compiler).
+
+For --gpus N (torchrun), every rank runs its own instance of the workload
+(seed + rank: independent geometries, as the batch driver runs them), so
+per-GPU work is fixed (weak scaling); value = all contributions / max time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import shutil
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+CONFIG = "medium"
+METRIC = "perturber contributions/s"
+UNIT = "contributions/s"
+
+
+def workload_desc():
+    return {"workload": "medium: 60 MOs, 20 e-, Ms=0, S=2000 dets (ref+S/D/T, spin-flip closed), "
+                        "3 roots, MP+EN, tau=0.01",
+            "norb": 60, "electrons": 20, "ncf": 2000, "roots": 3, "tau": 0.01,
+            "l2": "flushed before each step (256 MiB write)"}
+
+
+def make_workload(seed_offset: int, base: str):
+    from cipsi_gb300 import synth
+    import dataclasses
+    cfg = dataclasses.replace(synth.CONFIGS[CONFIG])
+    cfg.seed = cfg.seed + seed_offset
+    wd = os.path.join(base, f"{CONFIG}_s{cfg.seed}")
+    if not os.path.exists(os.path.join(wd, "cip.in")):
+        synth.generate(cfg, wd)
+    return wd
+
+
+# ------------------------------------------------------------ clocks sampler
+class Clocks:
+    def __init__(self, index: int):
+        self.index = index
+        self.samples = []
+        self.proc = None
+
+    def start(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.samples.append([x.strip() for x in line.split(",")])
+
+    def stop(self):
+        if self.proc:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        sm = [float(s[1]) for s in self.samples if len(s) > 2 and s[1].replace(".", "").isdigit()]
+        mx = [float(s[2]) for s in self.samples if len(s) > 2 and s[2].replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for s in self.samples:
+            for i, n in enumerate(names):
+                if len(s) > 5 + i and s[5 + i].lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.samples)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+# ------------------------------------------------------------ CPU baseline
+def oracle_sample(wd: str, every: int, offset: int, run_pertu: bool, tmpbase: str):
+    """Run the CPU oracle on generators k with (k % every == offset)."""
+    import numpy as np
+    from oracle import build as ob
+    run = tempfile.mkdtemp(dir=tmpbase)
+    shutil.rmtree(run)
+    shutil.copytree(wd, run)
+    info = json.load(open(os.path.join(wd, "..", "info_" + os.path.basename(wd) + ".json")))
+    m = np.zeros(info["ncf"], dtype=np.uint8)
+    m[offset::every] = 1
+    mp = os.path.join(run, "mask.bin")
+    m.tofile(mp)
+    t0 = time.perf_counter()
+    j = json.load(open(ob.run(run, genmask=mp, no_pertu_ref=not run_pertu)))
+    dt = time.perf_counter() - t0
+    shutil.rmtree(run, ignore_errors=True)
+    return j["n_processed"] * j["metat"], dt
+
+
+def write_info(wd: str):
+    from cipsi_gb300 import engine
+    inp = engine.Inputs(wd)
+    info = {"ncf": inp.dims.ncf, "metat": inp.dims.metat}
+    with open(os.path.join(wd, "..", "info_" + os.path.basename(wd) + ".json"), "w") as fh:
+        json.dump(info, fh)
+    return info
+
+
+def run_reference(args, rank: int, world: int):
+    """CPU restatement on all host cores; rank 0 only."""
+    if rank != 0:
+        return
+    from oracle import build as ob
+    from concurrent.futures import ProcessPoolExecutor
+    import multiprocessing as mpm
+    ob.build()
+    base = tempfile.mkdtemp(prefix="cipsi_ref_bench_")
+    wd = make_workload(0, base)
+    write_info(wd)
+    ncores = os.cpu_count() or 1
+    every = 240  # about 4 generators per process per step
+    steps_t, contribs = [], []
+    ctx = mpm.get_context("spawn")
+    with ProcessPoolExecutor(max_workers=ncores, mp_context=ctx) as ex:
+        for it in range(args.warmup + args.steps):
+            t0 = time.perf_counter()
+            futs = [ex.submit(oracle_sample, wd, every * ncores, (it * ncores + c) % (every * ncores),
+                              c == 0 and it == 0, base) for c in range(ncores)]
+            res = [f.result() for f in futs]
+            dt = time.perf_counter() - t0
+            if it >= args.warmup:
+                steps_t.append(dt)
+                contribs.append(sum(r[0] for r in res))
+    shutil.rmtree(base, ignore_errors=True)
+    tot_t = sum(steps_t)
+    val = sum(contribs) / tot_t
+    line = {"impl": "reference", "metric": METRIC, "value": val, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot_t / len(steps_t),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded integrals and reference space)", "config": workload_desc(),
+            "cpu_baseline": {"value": val, "unit": UNIT, "cores": ncores, "kind": "port",
+                             "sample": f"each step: {ncores} processes, each on a disjoint 1/{every * ncores} "
+                                       "sample of the generators of S (all of diexcit's per-double set-up)"},
+            "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------ GPU arm
+def run_gpu(args, rank: int, world: int, local_rank: int):
+    import numpy as np
+    import torch
+    from cipsi_gb300 import build, engine
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
+    torch.cuda.set_device(local_rank)
+    build.build()
+    base = tempfile.mkdtemp(prefix=f"cipsi_bench_r{rank}_")
+    wd = make_workload(rank, base)
+    info = write_info(wd)
+    inp = engine.Inputs(wd)
+    ctx = engine.Context(inp.dims, device=local_rank)
+    stream = torch.cuda.Stream()
+    ctx.set_stream(stream.cuda_stream)
+    ctx.upload(inp)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    for _ in range(args.warmup):
+        ctx.run_async(inp.opts)
+        res = ctx.fetch()
+    contrib_per_step = res["n_processed"] * inp.dims.metat
+    clocks = Clocks(local_rank)
+    clocks.start()
+    # ---- device-resident timing
+    barrier()
+    torch.cuda.synchronize()
+    step_ms, kern_ms = [], []
+    launches = 0
+    for _ in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        ctx.run_async(inp.opts)
+        e1.record(stream)
+        r = ctx.fetch()
+        assert r["n_processed"] * inp.dims.metat == contrib_per_step
+        step_ms.append(e0.elapsed_time(e1))
+        kern_ms.append(r["kernel_ms"])
+        launches += 2  # k_pt2 + k_reduce
+    torch.cuda.synchronize()
+    barrier()
+    # ---- end-to-end through the C ABI from host buffers
+    e2e_ms = []
+    nsel = r["n_selected"]
+    for _ in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ctx.upload(inp)
+        ctx.run_async(inp.opts)
+        r2 = ctx.fetch()
+        sel = ctx.selection(r2["n_selected"])
+        e2e_ms.append(1e3 * (time.perf_counter() - t0))
+    clk = clocks.stop()
+    tot_ms = sum(step_ms)
+    tot_e2e = sum(e2e_ms)
+    if world > 1:
+        t = torch.tensor([tot_ms, tot_e2e, float(contrib_per_step)], dtype=torch.float64, device="cuda")
+        mx = t.clone()
+        torch.distributed.all_reduce(mx[:2], op=torch.distributed.ReduceOp.MAX)
+        sm = t.clone()
+        torch.distributed.all_reduce(sm[2:], op=torch.distributed.ReduceOp.SUM)
+        tot_ms, tot_e2e, all_contrib = float(mx[0]), float(mx[1]), float(sm[2])
+    else:
+        all_contrib = float(contrib_per_step)
+    value = all_contrib * args.steps / (tot_ms / 1e3)
+    e2e_value = all_contrib * args.steps / (tot_e2e / 1e3)
+    # bytes copied per e2e step
+    n, nint = inp.dims.norb, None
+    ninte = os.path.getsize(os.path.join(wd, "ijkl"))  # upper bound source; exact below
+    from cipsi_gb300 import synth
+    recs = synth.read_records(os.path.join(wd, "ijkl"))
+    import struct
+    nint = struct.unpack_from("<i", recs[7], 0)[0]
+    ncf, mt = inp.dims.ncf, inp.dims.metat
+    W = 1 if n <= 64 else 2
+    nter = n * (n + 1) // 2
+    h2d = (nint * 4 + 3 * nter * 8 + n * n * 4 + (nsym := inp.dims.nsym) * 4 + n + ncf * 2 * W * 8
+           + ncf * (1 + 1 + 4) + ncf * mt * 8 + 2 * n * 8)
+    d2h = (5 * mt * 8 + 8 * (10 + 1 + 10 + 10 * 8) + 2 * 10 * 8 * 8
+           + nsel * (2 * W * 8 + 4 + 8 + mt * 8))
+    peak, peak_kind = measured_peaks()
+    kms = statistics.mean(kern_ms)
+    achieved = r["alg_bytes"] / (kms / 1e3) / 1e9
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": tot_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded integrals and reference space)",
+            "config": dict(workload_desc(), parallelism=f"replicas x{world}" if world > 1 else "single GPU"),
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(d2h), "ms_per_step": tot_e2e / args.steps},
+            "gpu_launches": launches,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": None, "kernel": "k_pt2",
+                         "peak_source": peak_kind,
+                         "note": "algorithmic bytes of the E2 loop per launch / mean k_pt2+k_reduce time; "
+                                 "the kernel is integer-issue bound (bit compares), see profiles/"},
+            "clocks": clk,
+            "work": {"perturbers": r["n_processed"], "candidates": r["n_candidates"],
+                     "compares": r["n_compares"], "pairs_1": r["n_pairs_1"], "pairs_2": r["n_pairs_2"],
+                     "selected": r["n_selected"], "ietat": r["ietat"], "e2vp": r["e2vp"]}}
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        from oracle import build as ob
+        ob.build()
+        every = 400
+        contrib, dt = oracle_sample(wd, every, 0, False, base)
+        line["cpu_baseline"] = {"value": contrib / dt, "unit": UNIT, "cores": 1, "kind": "port",
+                                "sample": f"generators k = 0 mod {every} of S (1/{every} of the "
+                                          f"generators), {dt:.1f} s on one core"}
+    ctx.close()
+    shutil.rmtree(base, ignore_errors=True)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser(description="CIPSI E2/selection benchmark")
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+    run_gpu(args, rank, world, local_rank)
+
+
+if __name__ == "__main__":
+    main()

@@ -25,7 +25,8 @@ EXPORTED = [
     "cipsi_ctx_create", "cipsi_ctx_destroy", "cipsi_last_error", "cipsi_set_stream",
     "cipsi_set_integrals", "cipsi_set_integrals_fp64", "cipsi_set_space", "cipsi_set_roots",
     "cipsi_run_pt2", "cipsi_run_pt2_async", "cipsi_fetch_result", "cipsi_selection_get",
-    "cipsi_cip_main",
+    "cipsi_cip_main", "cipsi_inputs_read", "cipsi_inputs_dims", "cipsi_inputs_upload",
+    "cipsi_inputs_free",
 ]
 
 

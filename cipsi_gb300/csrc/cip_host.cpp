@@ -602,54 +602,107 @@ std::string json_array(const double* x, int n) {
 
 }  // namespace
 
-extern "C" int cipsi_cip_main(const char* workdir, const char* stdin_path, int32_t sym_variant,
-                              const char* json_path, const uint8_t* gen_mask, int32_t device,
-                              char* errbuf, int32_t errlen) {
-  auto seterr = [&](const std::string& m) {
-    if (errbuf && errlen > 0) {
-      std::snprintf(errbuf, (size_t)errlen, "%s", m.c_str());
-    }
-  };
-  cipsi_ctx* ctx = nullptr;
+struct cipsi_inputs {
+  Run R;
+  int sym_variant = 1;
+};
+
+namespace {
+
+cipsi_opts opts_of(const Run& R, int sym_variant) {
+  cipsi_opts op{};
+  op.yen = R.o.ityper == 2;
+  op.ysele = R.o.iselec == 3;
+  op.ymoyen = R.o.ymoyen;
+  op.ywdeg = R.o.ywdeg;
+  op.sym_variant = sym_variant != 0;
+  op.nclass = R.o.nclass;
+  op.tau = R.o.tau;
+  op.teseff = R.o.teseff;
+  for (int i = 0; i < 10; ++i) op.aval[i] = R.o.aval[i];
+  op.gen_mask = nullptr;
+  op.run_pertu = 1;
+  return op;
+}
+
+void seterr(char* errbuf, int32_t errlen, const std::string& m) {
+  if (errbuf && errlen > 0) std::snprintf(errbuf, (size_t)errlen, "%s", m.c_str());
+}
+
+}  // namespace
+
+extern "C" int cipsi_inputs_read(cipsi_inputs** out, const char* workdir, const char* stdin_path,
+                                 int32_t sym_variant, char* errbuf, int32_t errlen) {
+  if (!out) return CIPSI_ERR_ARG;
+  *out = nullptr;
   try {
     const std::string dir = workdir ? workdir : ".";
     std::ifstream in(stdin_path ? std::string(stdin_path) : dir + "/cip.in");
     if (!in) throw Error("cannot read the namelist input");
     std::stringstream ss;
     ss << in.rdbuf();
-    Run R;
-    R.o = read_options(ss.str(), dir);
-    if (R.o.teseff < 0.0) R.o.teseff = 0.05 * R.o.tau;
-    read_inputs(R, sym_variant != 0);
+    auto* h = new cipsi_inputs();
+    h->sym_variant = sym_variant != 0;
+    try {
+      h->R.o = read_options(ss.str(), dir);
+      if (h->R.o.teseff < 0.0) h->R.o.teseff = 0.05 * h->R.o.tau;
+      read_inputs(h->R, sym_variant != 0);
+    } catch (...) {
+      delete h;
+      throw;
+    }
+    *out = h;
+    return CIPSI_OK;
+  } catch (const std::exception& ex) {
+    seterr(errbuf, errlen, ex.what());
+    return CIPSI_ERR_ARG;
+  }
+}
+
+extern "C" void cipsi_inputs_free(cipsi_inputs* in) { delete in; }
+
+extern "C" int cipsi_inputs_dims(const cipsi_inputs* in, cipsi_dims* dims, cipsi_opts* opts) {
+  if (!in) return CIPSI_ERR_ARG;
+  const Run& R = in->R;
+  if (dims) *dims = cipsi_dims{R.norb, R.noc, R.nsym, R.isym ? R.isym : 1, 0, R.metat, R.ncf};
+  if (opts) *opts = opts_of(R, in->sym_variant);
+  return CIPSI_OK;
+}
+
+extern "C" int cipsi_inputs_upload(const cipsi_inputs* in, cipsi_ctx* ctx) {
+  if (!in || !ctx) return CIPSI_ERR_ARG;
+  const Run& R = in->R;
+  int rc = cipsi_set_integrals(ctx, R.itsym.data(), R.its.data(), R.F.data(), R.J.data(), R.K.data(),
+                               R.ij0.data(), R.ntttt.data(), R.eri.data(), (int64_t)R.eri.size());
+  if (rc) return rc;
+  rc = cipsi_set_space(ctx, R.S.ne.data(), R.S.nd.data(), R.S.trou.data(), R.S.part.data(),
+                       (int64_t)R.S.trou.size(), R.S.ygen.data(), R.S.ysaut.data(), R.S.nesp.data(),
+                       R.S.yef1.data());
+  if (rc) return rc;
+  return cipsi_set_roots(ctx, R.c.data(), R.e.data(), R.eb.data(), R.emp.data(), R.teste.data(),
+                         R.taum.data(), R.fmpb.data());
+}
+
+extern "C" int cipsi_cip_main(const char* workdir, const char* stdin_path, int32_t sym_variant,
+                              const char* json_path, const uint8_t* gen_mask, int32_t device,
+                              char* errbuf, int32_t errlen) {
+  cipsi_ctx* ctx = nullptr;
+  cipsi_inputs* in = nullptr;
+  try {
+    int rc = cipsi_inputs_read(&in, workdir, stdin_path, sym_variant, errbuf, errlen);
+    if (rc) return rc;
+    const Run& R = in->R;
     const auto t0 = std::chrono::steady_clock::now();
-    cipsi_dims d{R.norb, R.noc, R.nsym, R.isym ? R.isym : 1, 0, R.metat, R.ncf};
-    int rc = cipsi_ctx_create(&ctx, &d, device);
+    cipsi_dims d{};
+    cipsi_opts op{};
+    cipsi_inputs_dims(in, &d, &op);
+    op.gen_mask = gen_mask;
+    rc = cipsi_ctx_create(&ctx, &d, device);
     auto chk = [&](int code, const char* what) {
       if (code) throw Error(std::string(what) + ": " + cipsi_last_error(ctx));
     };
     chk(rc, "cipsi_ctx_create");
-    chk(cipsi_set_integrals(ctx, R.itsym.data(), R.its.data(), R.F.data(), R.J.data(), R.K.data(),
-                            R.ij0.data(), R.ntttt.data(), R.eri.data(), (int64_t)R.eri.size()),
-        "cipsi_set_integrals");
-    chk(cipsi_set_space(ctx, R.S.ne.data(), R.S.nd.data(), R.S.trou.data(), R.S.part.data(),
-                        (int64_t)R.S.trou.size(), R.S.ygen.data(), R.S.ysaut.data(), R.S.nesp.data(),
-                        R.S.yef1.data()),
-        "cipsi_set_space");
-    chk(cipsi_set_roots(ctx, R.c.data(), R.e.data(), R.eb.data(), R.emp.data(), R.teste.data(),
-                        R.taum.data(), R.fmpb.data()),
-        "cipsi_set_roots");
-    cipsi_opts op{};
-    op.yen = R.o.ityper == 2;
-    op.ysele = R.o.iselec == 3;
-    op.ymoyen = R.o.ymoyen;
-    op.ywdeg = R.o.ywdeg;
-    op.sym_variant = sym_variant != 0;
-    op.nclass = R.o.nclass;
-    op.tau = R.o.tau;
-    op.teseff = R.o.teseff;
-    for (int i = 0; i < 10; ++i) op.aval[i] = R.o.aval[i];
-    op.gen_mask = gen_mask;
-    op.run_pertu = 1;
+    chk(cipsi_inputs_upload(in, ctx), "cipsi_inputs_upload");
     cipsi_result res{};
     if (R.o.ityper != 0) chk(cipsi_run_pt2(ctx, &op, &res), "cipsi_run_pt2");
     const auto t1 = std::chrono::steady_clock::now();
@@ -672,8 +725,9 @@ extern "C" int cipsi_cip_main(const char* workdir, const char* stdin_path, int32
       const int64_t ns = res.n_selected;
       std::vector<int32_t> snec(ns), sh((size_t)ns * 8), sp((size_t)ns * 8), own(ns);
       std::vector<double> sx(ns), sev((size_t)ns * R.metat);
-      if (ns) chk(cipsi_selection_get(ctx, 0, ns, snec.data(), sh.data(), sp.data(), sx.data(), sev.data(), own.data()),
-                  "cipsi_selection_get");
+      if (ns)
+        chk(cipsi_selection_get(ctx, 0, ns, snec.data(), sh.data(), sp.data(), sx.data(), sev.data(), own.data()),
+            "cipsi_selection_get");
       write_pie_records(f60, snec, sh, sp, sx, sev, R.metat, sym_variant != 0, 8);
       ntot += ns;
     }
@@ -748,10 +802,12 @@ extern "C" int cipsi_cip_main(const char* workdir, const char* stdin_path, int32
         << ", \"wall_s\": " << std::chrono::duration<double>(t1 - t0).count() << "\n}\n";
     }
     cipsi_ctx_destroy(ctx);
+    cipsi_inputs_free(in);
     return 0;
   } catch (const std::exception& ex) {
-    seterr(ex.what());
+    seterr(errbuf, errlen, ex.what());
     if (ctx) cipsi_ctx_destroy(ctx);
+    if (in) cipsi_inputs_free(in);
     return CIPSI_ERR_ARG;
   }
 }

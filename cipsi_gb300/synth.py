@@ -87,6 +87,7 @@ class SynthConfig:
     iselec: int = 1
     variant: str = "cipsym"  # or "cip"
     extra_icinp: str = ""
+    virt_shift: float = 0.0  # added to h_aa of virtual orbitals (0 = the plain recipe)
 
 
 CONFIGS: Dict[str, SynthConfig] = {
@@ -120,6 +121,10 @@ def make_integrals(cfg: SynthConfig, rng: np.random.Generator):
     off = off + off.T
     same = irrep[:, None] == irrep[None, :]
     h = h + off * same
+    if cfg.virt_shift:
+        # a gap between occupied and virtual orbital energies keeps every
+        # perturbation denominator away from zero (well-conditioned E2)
+        h[np.arange(cfg.nocc, n), np.arange(cfg.nocc, n)] += cfg.virt_shift
     L = np.zeros((cfg.ncholesky, n, n))
     for K in range(cfg.ncholesky):
         a = rng.normal(0.0, 0.3 * 0.85 ** K, size=(n, n))

@@ -165,6 +165,20 @@ int cipsi_selection_get(cipsi_ctx* ctx, int64_t first, int64_t count, int32_t* n
                         int32_t* holes, int32_t* parts, double* xam, double* evp,
                         int32_t* owner);
 
+/* Host-side inputs of one cip/cipsym run, read from a calculation directory
+   exactly as CIPSI_sources/cip/cip.f:50-135 does (namelists, units 40, 33,
+   60, 59, 4; S with its spin-flip partners, deter.f:478-567; zero order,
+   faifoc.f and cip.f:99-135).  Host memory only: no device work. */
+typedef struct cipsi_inputs cipsi_inputs;
+int cipsi_inputs_read(cipsi_inputs** in, const char* workdir, const char* stdin_path,
+                      int32_t sym_variant, char* errbuf, int32_t errlen);
+/* Sizes and namelist options of the run (either pointer may be NULL). */
+int cipsi_inputs_dims(const cipsi_inputs* in, cipsi_dims* dims, cipsi_opts* opts);
+/* Copy the inputs into a context: cipsi_set_integrals + cipsi_set_space +
+   cipsi_set_roots from the host arrays (host-to-device copies). */
+int cipsi_inputs_upload(const cipsi_inputs* in, cipsi_ctx* ctx);
+void cipsi_inputs_free(cipsi_inputs* in);
+
 /* Process-level drop-in for cip.exe (sym_variant = 0) and cipsym.exe
    (sym_variant = 1): reads the &cipfil/&icinp namelists from `stdin_path`
    and the unit files of `workdir` exactly as CIPSI_sources/cip/cip.f:50-242

@@ -278,6 +278,11 @@ static double e[64], eb[64], e2b[64], emp[64], teste[64], e2mp[64], e2vp[64], ps
     psivp[64], taum[64];
 static double dpivot;
 static long long ietat;
+/* first-order rounding-propagation bound of each E2 sum (not in cip): the
+   sum over perturbers of |term| * (2*kb + kd), kb = 16u*sum|H c|/|b|,
+   kd = 16u*(|E0| + sum of |diagonal terms|)/|denominator| */
+static double cond_mp[64], cond_vp[64], cond_b[64];
+#define U16 (16.0 * 1.1102230246251565e-16)
 static double* fmpb;
 /* /hist/ */
 static long long nom[11], nam[11][64];
@@ -385,6 +390,29 @@ static double hdig(int iii) {
       if (ns1p == ns2t) ca = ca + ak[n2tp];
       if (j == l) ca = 0.5 * ca;
       ab = ab + ca;
+    }
+  }
+  return ab;
+}
+
+/* sums of |terms| of hmp and hdig (for the rounding bound only) */
+static double hmp_abs(int iiii) {
+  double ac = 0.0;
+  for (int l = nd[iiii] + 1; l <= nd[iiii] + ne[iiii]; l++) ac += fabs(fmpb[part[l]]) + fabs(fmpb[trou[l]]);
+  return ac;
+}
+static double hdig_abs(int iii) {
+  double ab = 0.0;
+  int l1 = nd[iii] + 1, l2 = nd[iii] + ne[iii];
+  for (int l = l1; l <= l2; l++) {
+    ab += fabs(fdiag[part[l]]) + fabs(fdiag[trou[l]]);
+    int n1t = iorb[trou[l]], n1p = iorb[part[l]];
+    for (int j = l1; j <= l; j++) {
+      int n2t = iorb[trou[j]], n2p = iorb[part[j]];
+      int n12t = n2t > n1t ? num(n2t) + n1t : num(n1t) + n2t;
+      int n12p = n2p > n1p ? num(n2p) + n1p : num(n1p) + n2p;
+      ab += fabs(aj[n12t]) + fabs(aj[n12p]) + fabs(aj[num(n2p) + n1t]) + fabs(aj[num(n1p) + n2t]);
+      ab += fabs(ak[n12t]) + fabs(ak[n12p]) + fabs(ak[num(n2p) + n1t]) + fabs(ak[num(n1p) + n2t]);
     }
   }
   return ab;
@@ -665,13 +693,27 @@ static void pert1(int kkmod, int nf) {
     int ydeg = 0;
     double hmpi = hmp(nf), hvpi = 0.0;
     if (yen) hvpi = hdig(nf);
+    double hmpa = hmp_abs(nf), hvpa = yen ? hdig_abs(nf) : 0.0;
     double eimp = 0, car = 0, eivp = 0, carvp = 0, eib = 0;
     for (int m = 1; m <= metat; m++) {
       double bcalc = 0.0;
       int mncf = (m - 1) * ncf;
+      double babs = 0.0;
       for (int j = 1; j <= ijune; j++) bcalc = bcalc + (stok_buf[j] * c[mncf + ikk_buf[j]]);
+      for (int j = 1; j <= ijune; j++) babs += fabs(stok_buf[j] * c[mncf + ikk_buf[j]]);
       him[m] = bcalc;
       dmp[m] = emp[m] - hmpi;
+      {
+        double w = 1.0 + (ybis ? fabs(fmul) : 0.0);
+        double kb = bcalc != 0.0 ? U16 * babs / fabs(bcalc) : 0.0;
+        double t = fabs(bcalc * bcalc / dmp[m]);
+        cond_mp[m] += w * t * (2.0 * kb + U16 * (fabs(emp[m]) + hmpa) / fabs(dmp[m]));
+        if (yen) {
+          double dv = e[m] - hvpi, dbb = eb[m] - hvpi;
+          cond_vp[m] += w * fabs(bcalc * bcalc / dv) * (2.0 * kb + U16 * (fabs(e[m]) + hvpa) / fabs(dv));
+          cond_b[m] += w * fabs(bcalc * bcalc / dbb) * (2.0 * kb + U16 * (fabs(eb[m]) + hvpa) / fabs(dbb));
+        }
+      }
       double cimp = bcalc / dmp[m];
       car = cimp * cimp;
       psimp[m] = psimp[m] + car;
@@ -1257,12 +1299,24 @@ static void diexcit_one(int ii, int jj, int kk, int ll, int nspin, int yijkl, do
         int ydeg = 0;
         double hmpi = hmp(nf), hvpi = 0.0;
         if (yen) hvpi = hdig(nf);
+        double hmpa = hmp_abs(nf), hvpa = yen ? hdig_abs(nf) : 0.0;
         for (int m = 1; m <= metat; m++) {
-          double bcalc = 0.0;
+          double bcalc = 0.0, babs = 0.0;
           int mncf = (m - 1) * ncf;
           for (int j = 1; j <= ijune; j++) bcalc = bcalc + (stok_buf[j] * c[mncf + ikk_buf[j]]);
+          for (int j = 1; j <= ijune; j++) babs += fabs(stok_buf[j] * c[mncf + ikk_buf[j]]);
           him[m] = bcalc;
           double dmpm = emp[m] - hmpi;
+          {
+            double w = 1.0 + (ybis ? fabs(fmul) : 0.0);
+            double kb = bcalc != 0.0 ? U16 * babs / fabs(bcalc) : 0.0;
+            cond_mp[m] += w * fabs(bcalc * bcalc / dmpm) * (2.0 * kb + U16 * (fabs(emp[m]) + hmpa) / fabs(dmpm));
+            if (yen) {
+              double dv = e[m] - hvpi, dbb = eb[m] - hvpi;
+              cond_vp[m] += w * fabs(bcalc * bcalc / dv) * (2.0 * kb + U16 * (fabs(e[m]) + hvpa) / fabs(dv));
+              cond_b[m] += w * fabs(bcalc * bcalc / dbb) * (2.0 * kb + U16 * (fabs(eb[m]) + hvpa) / fabs(dbb));
+            }
+          }
           double cimp = bcalc / dmpm;
           double car = cimp * cimp;
           psimp[m] = psimp[m] + car;
@@ -2146,9 +2200,9 @@ int main(int argc, char** argv) {
     fprintf(fj, "  \"ietat\": %lld, \"n_processed\": %lld, \"ntot60\": %lld,\n", ietat, n_processed,
             det_ntot);
     fprintf(fj, "  \"dpivot\": %.17g,\n", dpivot);
-    const char* nm[5] = {"e2mp", "e2vp", "e2b", "psimp", "psivp"};
-    double* ar[5] = {e2mp, e2vp, e2b, psimp, psivp};
-    for (int q = 0; q < 5; q++) {
+    const char* nm[8] = {"e2mp", "e2vp", "e2b", "psimp", "psivp", "cond_e2mp", "cond_e2vp", "cond_e2b"};
+    double* ar[8] = {e2mp, e2vp, e2b, psimp, psivp, cond_mp, cond_vp, cond_b};
+    for (int q = 0; q < 8; q++) {
       fprintf(fj, "  \"%s\": [", nm[q]);
       for (int m = 1; m <= metat; m++) fprintf(fj, "%s%.17g", m > 1 ? ", " : "", ar[q][m]);
       fprintf(fj, "],\n");

@@ -1,0 +1,146 @@
+"""GPU engine (through the C ABI / the cipsym drop-in) against the CPU oracle
+on the same input files.
+
+Bit-exact: the processed perturber set (counts, ietat), the histogram counts,
+the set of determinants written to unit 60.  Floating point: E2 within
+1e-10 Eh on well-conditioned inputs; on inputs whose EN/MP denominators come
+close to zero the tolerance adds the oracle's first-order rounding bound
+(cond_e2*), since there a 1-ulp change of a diagonal energy moves E2 by far
+more than 1e-10.  Selection values xam agree to 1e-9 relative."""
+import collections
+import dataclasses
+import json
+import os
+import struct
+
+import numpy as np
+import pytest
+
+import cipsi_gb300 as cg
+from cases import small_cases
+from cipsi_gb300 import synth
+from conftest import copy_dir
+from oracle import build as ob
+
+pytestmark = pytest.mark.gpu
+
+
+def read60(path, metat, sym):
+    out = []
+    for r in synth.read_records(path):
+        m, n = struct.unpack_from("<ii", r, 0)
+        idet = struct.unpack_from(f"<{m}i", r, 8)
+        nex = struct.unpack_from(f"<{n}i", r, 8 + 4 * m)
+        v = struct.unpack_from(f"<{n}d", r, 8 + 4 * m + 4 * n)
+        ev = struct.unpack_from(f"<{n * metat}d", r, 8 + 4 * m + 12 * n) if sym else (0.0,) * (n * metat)
+        pos = 0
+        for i, nec in enumerate(nex):
+            h = tuple(sorted(idet[pos + 2 * q] for q in range(nec)))
+            p = tuple(sorted(idet[pos + 2 * q + 1] for q in range(nec)))
+            pos += 2 * nec
+            out.append(((h, p), v[i], ev[i * metat:(i + 1) * metat]))
+    return out
+
+
+def run_both(tmp_path, cfg, variant="cipsym", mask_every=None):
+    wd = str(tmp_path / "in")
+    info = synth.generate(cfg, wd)
+    wo = copy_dir(wd, str(tmp_path / "ora"))
+    wg = copy_dir(wd, str(tmp_path / "gpu"))
+    mask = None
+    mpath = None
+    if mask_every:
+        mask = np.zeros(info["ncf"], dtype=np.uint8)
+        mask[::mask_every] = 1
+        mpath = os.path.join(wo, "mask.bin")
+        mask.tofile(mpath)
+    jo = json.load(open(ob.run(wo, variant=variant, genmask=mpath)))
+    jg = cg.run_cip(wg, variant=variant, gen_mask=mask)
+    return jo, jg, wo, wg
+
+
+def check(jo, jg, wo, wg, variant, strict=False):
+    for k in ("ncf", "ietat", "n_processed", "ntot60", "nom", "nam"):
+        assert jo[k] == jg[k], k
+    assert jo["dpivot"] == pytest.approx(jg["dpivot"], rel=1e-12, abs=1e-15)
+    for k in ("e2mp", "e2vp", "e2b"):
+        a, b = np.array(jo[k]), np.array(jg[k])
+        tol = 1e-10 + (0.0 if strict else np.array(jo["cond_" + k]))
+        assert np.all(np.abs(a - b) <= tol), (k, a, b, np.abs(a - b), tol)
+    mt = jo["metat"]
+    so = read60(os.path.join(wo, "det"), mt, variant == "cipsym")
+    sg = read60(os.path.join(wg, "det"), mt, variant == "cipsym")
+    assert collections.Counter(x[0] for x in so) == collections.Counter(x[0] for x in sg)
+    dg = {x[0]: x for x in sg}
+    for key, v, ev in so:
+        assert v == pytest.approx(dg[key][1], rel=1e-9, abs=1e-12)
+
+
+@pytest.mark.parametrize("name,cfg", small_cases(), ids=[c[0] for c in small_cases()])
+def test_parity_small(tmp_path, oracle_exe, engine_lib, name, cfg):
+    jo, jg, wo, wg = run_both(tmp_path, cfg)
+    check(jo, jg, wo, wg, "cipsym")
+
+
+def test_parity_cip_variant(tmp_path, oracle_exe, engine_lib):
+    jo, jg, wo, wg = run_both(tmp_path, synth.CONFIGS["small"], variant="cip")
+    check(jo, jg, wo, wg, "cip")
+
+
+@pytest.mark.parametrize("seed,ranks,nsym", [(31, (2,), 1), (32, (1, 2, 3), 1), (33, (1, 2), 2)])
+def test_parity_well_conditioned_strict(tmp_path, oracle_exe, engine_lib, seed, ranks, nsym):
+    cfg = synth.SynthConfig("gap", norb=16, nocc=4, ncholesky=16, ncf=60, metat=2, tau=0.01, ranks=ranks,
+                            coef_mode="gauss005", seed=seed, nsym=nsym, virt_shift=3.0)
+    jo, jg, wo, wg = run_both(tmp_path, cfg)
+    check(jo, jg, wo, wg, "cipsym", strict=True)
+
+
+def test_parity_two_word_bitstrings(tmp_path, oracle_exe, engine_lib):
+    cfg = synth.SynthConfig("w2", norb=70, nocc=6, ncholesky=16, ncf=100, metat=2, tau=0.02,
+                            ranks=(1, 2, 3), coef_mode="decay09", seed=11)
+    jo, jg, wo, wg = run_both(tmp_path, cfg)
+    check(jo, jg, wo, wg, "cipsym")
+
+
+def test_parity_medium_generator_sample(tmp_path, oracle_exe, engine_lib):
+    """The benchmark workload (60 orbitals, S = 2000, 3 roots) on a sample of
+    its generators (every 199th determinant of S as generator)."""
+    jo, jg, wo, wg = run_both(tmp_path, synth.CONFIGS["medium"], mask_every=199)
+    check(jo, jg, wo, wg, "cipsym")
+
+
+def test_deterministic(tmp_path, engine_lib):
+    from cipsi_gb300 import engine
+    wd = str(tmp_path / "in")
+    synth.generate(synth.CONFIGS["small"], wd)
+    inp = engine.Inputs(wd)
+    with engine.Context(inp.dims) as ctx:
+        ctx.upload(inp)
+        r1 = ctx.run(inp.opts)
+        s1 = ctx.selection(r1["n_selected"])
+        r2 = ctx.run(inp.opts)
+        s2 = ctx.selection(r2["n_selected"])
+    for k in ("e2mp", "e2vp", "e2b", "psimp", "psivp", "ietat", "n_processed", "dpivot"):
+        assert r1[k] == r2[k], k
+    for k in s1:
+        assert np.array_equal(s1[k], s2[k]), k
+
+
+def test_generator_shards_add_up(tmp_path, engine_lib):
+    """Two disjoint generator masks (rank 0 also runs pertu's reference
+    candidates) give the full run's sums: the multi-GPU sharding rule."""
+    from cipsi_gb300 import engine, shard
+    wd = str(tmp_path / "in")
+    synth.generate(dataclasses.replace(synth.CONFIGS["small"], seed=5), wd)
+    inp = engine.Inputs(wd)
+    with engine.Context(inp.dims) as ctx:
+        ctx.upload(inp)
+        full = ctx.run(inp.opts)
+        parts = [ctx.run(inp.opts, gen_mask=shard.generator_mask(inp.dims.ncf, r, 2), run_pertu=(r == 0))
+                 for r in range(2)]
+    comb = shard.combine(parts)
+    for k in ("ietat", "n_processed", "n_selected"):
+        assert comb[k] == full[k], k
+    assert comb["nom"] == full["nom"]
+    for k in ("e2mp", "e2vp", "e2b"):
+        np.testing.assert_allclose(comb[k], full[k], rtol=1e-12, atol=1e-9)
