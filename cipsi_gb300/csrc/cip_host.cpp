@@ -723,12 +723,16 @@ extern "C" int cipsi_cip_main(const char* workdir, const char* stdin_path, int32
       write_pie_records(f60, nec, h, p, v, ev, R.metat, sym_variant != 0, 8);
       ntot += R.ncf;
       const int64_t ns = res.n_selected;
-      std::vector<int32_t> snec(ns), sh((size_t)ns * 8), sp((size_t)ns * 8), own(ns);
-      std::vector<double> sx(ns), sev((size_t)ns * R.metat);
-      if (ns)
-        chk(cipsi_selection_get(ctx, 0, ns, snec.data(), sh.data(), sp.data(), sx.data(), sev.data(), own.data()),
+      const int64_t chunk = 1 << 20;  // records converted per call (a multiple of lungo)
+      for (int64_t first = 0; first < ns; first += chunk) {
+        const int64_t cnt = std::min(chunk, ns - first);
+        std::vector<int32_t> snec(cnt), sh((size_t)cnt * 8), sp((size_t)cnt * 8), own(cnt);
+        std::vector<double> sx(cnt), sev((size_t)cnt * R.metat);
+        chk(cipsi_selection_get(ctx, first, cnt, snec.data(), sh.data(), sp.data(), sx.data(), sev.data(),
+                                own.data()),
             "cipsi_selection_get");
-      write_pie_records(f60, snec, sh, sp, sx, sev, R.metat, sym_variant != 0, 8);
+        write_pie_records(f60, snec, sh, sp, sx, sev, R.metat, sym_variant != 0, 8);
+      }
       ntot += ns;
     }
     std::fclose(f60);

@@ -301,6 +301,37 @@ __device__ __forceinline__ void kahan_add(double& s, double& c, double x) {
   s = t;
 }
 
+// Block-wide order-preserving compaction: calls emit(slot, i) for every i in
+// [0, n) with pred(i), slots dense and increasing with i (deterministic).
+// Must be called by every thread of the block.
+template <typename Pred, typename Emit>
+__device__ int ordered_compact(int n, Pred pred, Emit emit, int* warp_tmp /* >= 33 ints */) {
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5, nw = blockDim.x >> 5;
+  int total = 0;
+  for (int base = 0; base < n; base += blockDim.x) {
+    const int i = base + tid;
+    const bool keep = i < n && pred(i);
+    const unsigned m = __ballot_sync(0xffffffffu, keep);
+    if (lane == 0) warp_tmp[wid] = __popc(m);
+    __syncthreads();
+    if (wid == 0) {
+      const int v = lane < nw ? warp_tmp[lane] : 0;
+      int x = v;
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+      }
+      if (lane < nw) warp_tmp[lane] = x - v;  // exclusive prefix
+      if (lane == 31) warp_tmp[32] = x;       // round total
+    }
+    __syncthreads();
+    if (keep) emit(total + warp_tmp[wid] + __popc(m & ((1u << lane) - 1u)), i);
+    total += warp_tmp[32];
+    __syncthreads();
+  }
+  return total;
+}
+
 template <int R>
 struct Acc {
   double e2mp[R], cmp[R], e2vp[R], cvp[R], e2b[R], cb[R], psimp[R], psivp[R];
@@ -332,12 +363,10 @@ __device__ __forceinline__ int hist_class(const Params& p, double val) {
 // Everything the reference does with one candidate after its interaction
 // scan: denominators, E2, selection, histogram, unit-60 record.
 template <int W, int R>
-__device__ void finish_candidate(const Params& p, const uint64_t* u, const uint64_t* hf,
+__device__ void finish_candidate(const Params& p, const uint64_t* u, double hmpi, double hvpi,
                                  const double* bc, int owner1 /*1-based, 0 = pertu*/,
                                  double fmul, int nmul, bool ybis, bool is_pert1, Acc<R>& acc,
                                  SmemHist& hist) {
-  double hmpi, hvpi;
-  diag_terms<W>(p, u, hf, hmpi, hvpi, p.yen != 0);
   double xam = 0.0;
   bool ydeg = false;
   double vil[R], semp[R], sevp[R], venvp[R];
@@ -408,8 +437,16 @@ __device__ void finish_candidate(const Params& p, const uint64_t* u, const uint6
     }
   }
   if (ydeg) xam = 1.0;
-  if (xam > p.tau && p.ymoyen) {
-    const unsigned long long slot = atomicAdd(&p.counters[C_NSEL], 1ull);
+  const bool sel = xam > p.tau && p.ymoyen;
+  const unsigned am = __activemask();
+  const unsigned sm = __ballot_sync(am, sel);
+  if (sel) {
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(sm) - 1;
+    unsigned long long base = 0;
+    if (lane == leader) base = atomicAdd(&p.counters[C_NSEL], (unsigned long long)__popc(sm));
+    base = __shfl_sync(sm, base, leader);
+    const unsigned long long slot = base + __popc(sm & ((1u << lane) - 1u));
     if ((long long)slot < p.sel_cap) {
 #pragma unroll
       for (int q = 0; q < 2 * W; ++q) p.sel_bits[slot * 2 * W + q] = u[q];
@@ -458,6 +495,11 @@ __device__ void block_flush(const Params& p, Acc<R>& acc, int gslot, double* red
 
 // ------------------------------------------------------------------ kernel
 struct BlockShared {
+  double vdg[2 * kMaxOrb];  // hdig(K'+a) - hdig(K') without the pair term
+  double hK, mK;            // hdig(K'), hmp(K')
+  int dn_so[48];            // spin orbitals where K' differs from the reference
+  int dn_sg[48];            // +1 (occupied virtual) / -1 (empty reference orbital)
+  int ndn;
   uint64_t kbits[2 * 2];
   int occ[kMaxElec];      // spin orbital code (orb + spin*norb) of k's electrons
   int vir[2][kMaxOrb];    // virtual orbitals of k per spin
@@ -476,6 +518,7 @@ __global__ void __launch_bounds__(kThreads) k_pt2(Params p) {
   __shared__ BlockShared sh;
   __shared__ SmemHist hist;
   __shared__ double red[5 * kMaxRoots * 32];
+  __shared__ int ctmp[33];
 
   const int tid = threadIdx.x;
   // shared L_R arrays (fast path)
@@ -566,7 +609,9 @@ __global__ void __launch_bounds__(kThreads) k_pt2(Params p) {
               if (m < p.metat) bc[m] += h * __ldg(&p.c[(size_t)j * p.metat + m]);
           }
           if (drop || nint == 0) continue;
-          finish_candidate<W, R>(p, u, hf, bc, 0, 0.0, 0, false, true, acc, hist);
+          double hmpi, hvpi;
+          diag_terms<W>(p, u, hf, hmpi, hvpi, p.yen != 0);
+          finish_candidate<W, R>(p, u, hmpi, hvpi, bc, 0, 0.0, 0, false, true, acc, hist);
         }
       }
       block_flush<R>(p, acc, g, red);
@@ -605,39 +650,36 @@ __global__ void __launch_bounds__(kThreads) k_pt2(Params p) {
     }
     __syncthreads();
     const int nel = sh.nel_s[0] + sh.nel_s[1];
-    for (int j = tid; j < ncf; j += blockDim.x) {
-      const uint64_t* v = p.S + (size_t)j * 2 * W;
-      uint64_t vv[2 * W];
-      int x = 0;
+    const int nnb = ordered_compact(
+        ncf,
+        [&](int j) {
+          int x = 0;
 #pragma unroll
-      for (int q = 0; q < 2 * W; ++q) {
-        vv[q] = __ldg(&v[q]);
-        x += __popcll(kb[q] ^ vv[q]);
-      }
-      if (x > 8) continue;
-      // electrons of k missing in j, as a mask over k's electron indices
-      uint64_t em = 0;
+          for (int q = 0; q < 2 * W; ++q) x += __popcll(kb[q] ^ __ldg(&p.S[(size_t)j * 2 * W + q]));
+          return x <= 8;
+        },
+        [&](int slot, int j) {
+          // electrons of k missing in j, as a mask over k's electron indices
+          uint64_t em = 0;
 #pragma unroll
-      for (int q = 0; q < 2 * W; ++q) {
-        uint64_t miss = kb[q] & ~vv[q];
-        while (miss) {
-          const int b = __ffsll((long long)miss) - 1;
-          miss &= miss - 1;
-          // electron index = occupied bits of k before this bit
-          int idx = 0;
-          const int s = q / W, w = q % W;
-          if (s == 1) idx += sh.nel_s[0];
-          for (int w2 = 0; w2 < w; ++w2) idx += __popcll(kb[s * W + w2]);
-          idx += __popcll(kb[q] & ((1ull << b) - 1ull));
-          em |= 1ull << idx;
-        }
-      }
-      const int slot = atomicAdd(&sh.nnb, 1);
-      my_nb_j[slot] = j;
-      my_nb_em[slot] = em;
-    }
-    __syncthreads();
-    const int nnb = sh.nnb;
+          for (int q = 0; q < 2 * W; ++q) {
+            uint64_t miss = kb[q] & ~__ldg(&p.S[(size_t)j * 2 * W + q]);
+            while (miss) {
+              const int b = __ffsll((long long)miss) - 1;
+              miss &= miss - 1;
+              // electron index = occupied bits of k before this bit
+              int idx = 0;
+              const int s = q / W, w = q % W;
+              if (s == 1) idx += sh.nel_s[0];
+              for (int w2 = 0; w2 < w; ++w2) idx += __popcll(kb[s * W + w2]);
+              idx += __popcll(kb[q] & ((1ull << b) - 1ull));
+              em |= 1ull << idx;
+            }
+          }
+          my_nb_j[slot] = j;
+          my_nb_em[slot] = em;
+        },
+        ctmp);
     const int rank_k = sh.rank_k;
     const uint8_t dmask = p.gen_dmask[g];
     const int k1 = k + 1;  // 1-based owner index
@@ -674,25 +716,25 @@ __global__ void __launch_bounds__(kThreads) k_pt2(Params p) {
       }
       if (!any) continue;
       const uint64_t rmask = (1ull << e1) | (e2 >= 0 ? (1ull << e2) : 0ull);
-      // L_R
-      if (tid == 0) sh.nlr = 0;
-      __syncthreads();
-      for (int t = tid; t < nnb; t += blockDim.x) {
-        const uint64_t em = my_nb_em[t];
-        const int m = __popcll(em) - __popcll(em & rmask);
-        if (m > 2) continue;
-        const int slot = atomicAdd(&sh.nlr, 1);
-        const int j = my_nb_j[t];
-        if (slot < p.lr_cap) {
-          lr_j[slot] = j;
-          const uint64_t* v = p.S + (size_t)j * 2 * W;
+      // L_R (ascending j: the sums over interacting determinants run in a
+      // fixed order, so results are bitwise reproducible)
+      const int nlr = ordered_compact(
+          nnb,
+          [&](int t) {
+            const uint64_t em = my_nb_em[t];
+            return __popcll(em) - __popcll(em & rmask) <= 2;
+          },
+          [&](int slot, int t) {
+            const int j = my_nb_j[t];
+            if (slot < p.lr_cap) {
+              lr_j[slot] = j;
+              const uint64_t* v = p.S + (size_t)j * 2 * W;
 #pragma unroll
-          for (int q = 0; q < 2 * W; ++q) lr_bits[(size_t)slot * 2 * W + q] = __ldg(&v[q]);
-        }
-        my_lr_idx[slot] = j;
-      }
-      __syncthreads();
-      const int nlr = sh.nlr;
+              for (int q = 0; q < 2 * W; ++q) lr_bits[(size_t)slot * 2 * W + q] = __ldg(&v[q]);
+            }
+            my_lr_idx[slot] = j;
+          },
+          ctmp);
       const bool fast = nlr <= p.lr_cap;
       if (!fast && tid == 0) atomicAdd(&p.counters[C_LRFALLBACK], 1ull);
       // K' = k - R
@@ -701,6 +743,66 @@ __global__ void __launch_bounds__(kThreads) k_pt2(Params p) {
       for (int q = 0; q < 2 * W; ++q) kp[q] = kb[q];
       kp[sp1 * W + (o1 >> 6)] &= ~(1ull << (o1 & 63));
       if (e2 >= 0) kp[sp2 * W + (o2 >> 6)] &= ~(1ull << (o2 & 63));
+      // diagonal energies of I = K' + A from those of K' (cip/hdig.f, hmp.f
+      // written over occupation changes dn relative to the reference):
+      //   hdig = sum_r dn_r F_rr + 1/2 sum_rs dn_r dn_s (J_rs - [same spin] K_rs)
+      //   hmp  = sum_r dn_r fmpb_r
+      if (tid == 0) {
+        int nd = 0;
+        for (int sp = 0; sp < 2; ++sp)
+          for (int w = 0; w < W; ++w) {
+            uint64_t h = hf[sp * W + w] & ~kp[sp * W + w];
+            while (h) {
+              const int b = __ffsll((long long)h) - 1;
+              h &= h - 1;
+              sh.dn_so[nd] = w * 64 + b + sp * p.norb;
+              sh.dn_sg[nd++] = -1;
+            }
+            uint64_t t2 = kp[sp * W + w] & ~hf[sp * W + w];
+            while (t2) {
+              const int b = __ffsll((long long)t2) - 1;
+              t2 &= t2 - 1;
+              sh.dn_so[nd] = w * 64 + b + sp * p.norb;
+              sh.dn_sg[nd++] = 1;
+            }
+          }
+        sh.ndn = nd;
+      }
+      __syncthreads();
+      {
+        const int ndn = sh.ndn, n = p.norb;
+        for (int a = tid; a < 2 * n; a += blockDim.x) {
+          const int oa = a % n, sa = a / n;
+          double g = 0.0;
+          for (int i = 0; i < ndn; ++i) {
+            const int r = sh.dn_so[i];
+            const int t = tri(oa, r % n);
+            double x = __ldg(&p.J[t]);
+            if (sa == r / n) x -= __ldg(&p.K[t]);
+            g += sh.dn_sg[i] * x;
+          }
+          const int ta = tri(oa, oa);
+          sh.vdg[a] = __ldg(&p.F[ta]) + g + 0.5 * (__ldg(&p.J[ta]) - __ldg(&p.K[ta]));
+        }
+        if (tid == 32) {
+          double e = 0.0, mp = 0.0;
+          for (int i = 0; i < ndn; ++i) {
+            const int r = sh.dn_so[i], orr = r % n;
+            e += sh.dn_sg[i] * __ldg(&p.F[tri(orr, orr)]);
+            mp += sh.dn_sg[i] * __ldg(&p.fmpb[r]);
+            for (int j = 0; j < ndn; ++j) {
+              const int q = sh.dn_so[j];
+              const int t = tri(orr, q % n);
+              double x = __ldg(&p.J[t]);
+              if (r / n == q / n) x -= __ldg(&p.K[t]);
+              e += 0.5 * sh.dn_sg[i] * sh.dn_sg[j] * x;
+            }
+          }
+          sh.hK = e;
+          sh.mK = mp;
+        }
+      }
+      __syncthreads();
       const int symR = e2 >= 0 ? p.its[p.orbsym[o1]][p.orbsym[o2]] : p.orbsym[o1];
       // added-orbital space
       int nA;
@@ -828,7 +930,16 @@ __global__ void __launch_bounds__(kThreads) k_pt2(Params p) {
           fmul = (1.0 / (double)(lesp + 1)) * (double)(nespf + 1) - 1.0;
           nmul = (int)fmul;
         }
-        finish_candidate<W, R>(p, u, hf, bc, k1, fmul, nmul, ybis, is_pert1, acc, hist);
+        double hmpi = sh.mK + __ldg(&p.fmpb[a1 + sa1 * p.norb]);
+        double hvpi = sh.hK + sh.vdg[a1 + sa1 * p.norb];
+        if (a2 >= 0) {
+          hmpi += __ldg(&p.fmpb[a2 + sa2 * p.norb]);
+          const int t = tri(a1, a2);
+          double g = __ldg(&p.J[t]);
+          if (sa1 == sa2) g -= __ldg(&p.K[t]);
+          hvpi += sh.vdg[a2 + sa2 * p.norb] + g;
+        }
+        finish_candidate<W, R>(p, u, hmpi, hvpi, bc, k1, fmul, nmul, ybis, is_pert1, acc, hist);
       }
       __syncthreads();
     }
@@ -928,9 +1039,7 @@ struct cipsi_ctx {
   int nclass = kNClass;
   bool pending = false;
   cipsi_opts last_opts{};
-  // fetched selection (sorted)
-  std::vector<int32_t> sel_nec, sel_h, sel_p, sel_owner;
-  std::vector<double> sel_xam, sel_evp;
+  long long nsel = 0;  // records of the last fetched run
 };
 
 namespace {
@@ -1459,53 +1568,13 @@ int cipsi_fetch_result(cipsi_ctx* ctx, cipsi_result* r) {
   float ms = 0.f;
   CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
   r->kernel_ms = ms;
-  // selection
-  long long nsel = (long long)cnt[C_NSEL];
+  // selection: records stay on the device until cipsi_selection_get/raw
+  const long long nsel = (long long)cnt[C_NSEL];
   if (nsel > ctx->sel_cap)
     return fail(ctx, CIPSI_ERR_OVERFLOW,
                 "selection buffer overflow: " + std::to_string(nsel) + " records > capacity " +
-                    std::to_string(ctx->sel_cap) + " (raise tau or rerun; the capacity grows)");
-  std::vector<uint64_t> bits((size_t)nsel * 2 * W);
-  std::vector<int32_t> own(nsel);
-  std::vector<double> xam(nsel), evp((size_t)nsel * mt);
-  if (nsel) {
-    CK(cudaMemcpy(bits.data(), ctx->dsel_bits, bits.size() * 8, cudaMemcpyDeviceToHost));
-    CK(cudaMemcpy(own.data(), ctx->dsel_owner, own.size() * 4, cudaMemcpyDeviceToHost));
-    CK(cudaMemcpy(xam.data(), ctx->dsel_xam, xam.size() * 8, cudaMemcpyDeviceToHost));
-    CK(cudaMemcpy(evp.data(), ctx->dsel_evp, evp.size() * 8, cudaMemcpyDeviceToHost));
-  }
-  std::vector<long long> order(nsel);
-  for (long long i = 0; i < nsel; ++i) order[i] = i;
-  std::sort(order.begin(), order.end(), [&](long long a, long long b) {
-    if (own[a] != own[b]) return own[a] < own[b];
-    for (int q = 0; q < 2 * W; ++q) {
-      const uint64_t x = bits[(size_t)a * 2 * W + q], y = bits[(size_t)b * 2 * W + q];
-      if (x != y) return x < y;
-    }
-    return false;
-  });
-  const int n = ctx->d.norb, noca = ctx->d.noca;
-  ctx->sel_nec.assign(nsel, 0);
-  ctx->sel_h.assign((size_t)nsel * 8, 0);
-  ctx->sel_p.assign((size_t)nsel * 8, 0);
-  ctx->sel_owner.assign(nsel, 0);
-  ctx->sel_xam.assign(nsel, 0.0);
-  ctx->sel_evp.assign((size_t)nsel * mt, 0.0);
-  for (long long ii = 0; ii < nsel; ++ii) {
-    const long long i = order[ii];
-    int nh = 0, np = 0;
-    for (int s = 0; s < 2; ++s)
-      for (int o = 0; o < n; ++o) {
-        const bool occ = (bits[(size_t)i * 2 * W + s * W + (o >> 6)] >> (o & 63)) & 1ull;
-        const bool inhf = o < noca;
-        if (inhf && !occ && nh < 8) ctx->sel_h[(size_t)ii * 8 + nh++] = o + 1 + s * n;
-        if (!inhf && occ && np < 8) ctx->sel_p[(size_t)ii * 8 + np++] = o + 1 + s * n;
-      }
-    ctx->sel_nec[ii] = nh;
-    ctx->sel_owner[ii] = own[i];
-    ctx->sel_xam[ii] = xam[i];
-    for (int m = 0; m < mt; ++m) ctx->sel_evp[(size_t)ii * mt + m] = evp[(size_t)i * mt + m];
-  }
+                    std::to_string(ctx->sel_cap) + " (cipsi_run_pt2 grows the buffer and reruns)");
+  ctx->nsel = nsel;
   r->n_selected = nsel;
   return CIPSI_OK;
 }
@@ -1530,24 +1599,64 @@ int cipsi_run_pt2(cipsi_ctx* ctx, const cipsi_opts* opts, cipsi_result* res) {
   return fail(ctx, CIPSI_ERR_OVERFLOW, "selection buffer could not be grown");
 }
 
+int cipsi_selection_raw(cipsi_ctx* ctx, int64_t first, int64_t count, uint64_t* bits,
+                        int32_t* owner, double* xam, double* evp) {
+  if (!ctx) return CIPSI_ERR_ARG;
+  if (first < 0 || count < 0 || first + count > ctx->nsel)
+    return fail(ctx, CIPSI_ERR_ARG, "selection: range outside the selection");
+  if (count == 0) return CIPSI_OK;
+  CK(cudaSetDevice(ctx->device));
+  const int W = ctx->W, mt = ctx->d.metat;
+  if (bits)
+    CK(cudaMemcpyAsync(bits, ctx->dsel_bits + (size_t)first * 2 * W, (size_t)count * 2 * W * 8,
+                       cudaMemcpyDeviceToHost, ctx->stream));
+  if (owner)
+    CK(cudaMemcpyAsync(owner, ctx->dsel_owner + first, (size_t)count * 4, cudaMemcpyDeviceToHost, ctx->stream));
+  if (xam) CK(cudaMemcpyAsync(xam, ctx->dsel_xam + first, (size_t)count * 8, cudaMemcpyDeviceToHost, ctx->stream));
+  if (evp)
+    CK(cudaMemcpyAsync(evp, ctx->dsel_evp + (size_t)first * mt, (size_t)count * mt * 8,
+                       cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return CIPSI_OK;
+}
+
 int cipsi_selection_get(cipsi_ctx* ctx, int64_t first, int64_t count, int32_t* nec, int32_t* holes,
                         int32_t* parts, double* xam, double* evp, int32_t* owner) {
   if (!ctx) return CIPSI_ERR_ARG;
-  const int64_t n = (int64_t)ctx->sel_nec.size();
-  if (first < 0 || count < 0 || first + count > n)
-    return fail(ctx, CIPSI_ERR_ARG, "selection_get: range outside the selection");
-  const int mt = ctx->d.metat;
+  const int W = ctx->W, n = ctx->d.norb, noca = ctx->d.noca;
+  std::vector<uint64_t> bits((size_t)std::max<int64_t>(count, 0) * 2 * W);
+  int rc = cipsi_selection_raw(ctx, first, count, bits.data(), owner, xam, evp);
+  if (rc) return rc;
   for (int64_t i = 0; i < count; ++i) {
-    const int64_t s = first + i;
-    if (nec) nec[i] = ctx->sel_nec[s];
+    int nh = 0, np = 0;
+    int32_t* h = holes ? holes + i * 8 : nullptr;
+    int32_t* pp = parts ? parts + i * 8 : nullptr;
     for (int q = 0; q < 8; ++q) {
-      if (holes) holes[i * 8 + q] = ctx->sel_h[s * 8 + q];
-      if (parts) parts[i * 8 + q] = ctx->sel_p[s * 8 + q];
+      if (h) h[q] = 0;
+      if (pp) pp[q] = 0;
     }
-    if (xam) xam[i] = ctx->sel_xam[s];
-    if (evp)
-      for (int m = 0; m < mt; ++m) evp[i * mt + m] = ctx->sel_evp[s * mt + m];
-    if (owner) owner[i] = ctx->sel_owner[s];
+    for (int s = 0; s < 2; ++s)
+      for (int w = 0; w < W; ++w) {
+        const uint64_t word = bits[(size_t)i * 2 * W + s * W + w];
+        const int lo = w * 64;
+        const int nref = std::min(std::max(noca - lo, 0), 64);
+        const uint64_t ref = nref >= 64 ? ~0ull : ((1ull << nref) - 1ull);
+        uint64_t hm = ref & ~word, pm = word & ~ref;
+        while (hm) {
+          const int b = __builtin_ctzll(hm);
+          hm &= hm - 1;
+          if (h && nh < 8) h[nh] = lo + b + 1 + s * n;
+          ++nh;
+        }
+        while (pm) {
+          const int b = __builtin_ctzll(pm);
+          pm &= pm - 1;
+          if (pp && np < 8) pp[np] = lo + b + 1 + s * n;
+          ++np;
+        }
+      }
+    if (nh > 8) return fail(ctx, CIPSI_ERR_OVERFLOW, "selected determinant with excitation degree > 8");
+    if (nec) nec[i] = nh;
   }
   return CIPSI_OK;
 }

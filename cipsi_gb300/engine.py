@@ -67,6 +67,7 @@ def _lib():
         "cipsi_run_pt2_async": ([P, ctypes.POINTER(Opts)], ctypes.c_int),
         "cipsi_fetch_result": ([P, ctypes.POINTER(Result)], ctypes.c_int),
         "cipsi_selection_get": ([P, ctypes.c_int64, ctypes.c_int64, P, P, P, P, P, P], ctypes.c_int),
+        "cipsi_selection_raw": ([P, ctypes.c_int64, ctypes.c_int64, P, P, P, P], ctypes.c_int),
         "cipsi_inputs_read": ([ctypes.POINTER(P), ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int32,
                                ctypes.c_char_p, ctypes.c_int32], ctypes.c_int),
         "cipsi_inputs_dims": ([P, ctypes.POINTER(Dims), ctypes.POINTER(Opts)], ctypes.c_int),
@@ -186,6 +187,20 @@ class Context:
                 self._c, 0, count, nec.ctypes.data, h.ctypes.data, p.ctypes.data, xam.ctypes.data,
                 evp.ctypes.data, own.ctypes.data), "selection_get")
         return {"nec": nec, "holes": h, "parts": p, "xam": xam, "evp": evp, "owner": own}
+
+    def selection_raw(self, count: int, out: Optional[dict] = None) -> dict:
+        """Selected records as bitstrings (no conversion): bits[count, 2W],
+        owner, xam, evp.  `out` may supply preallocated (pinned) arrays."""
+        mt = self.dims.metat
+        W = 1 if self.dims.norb <= 64 else 2
+        if out is None:
+            out = {"bits": np.zeros((count, 2 * W), np.uint64), "owner": np.zeros(count, np.int32),
+                   "xam": np.zeros(count, np.float64), "evp": np.zeros((count, mt), np.float64)}
+        if count:
+            self._check(self.lib.cipsi_selection_raw(
+                self._c, 0, count, out["bits"].ctypes.data, out["owner"].ctypes.data,
+                out["xam"].ctypes.data, out["evp"].ctypes.data), "selection_raw")
+        return out
 
     def close(self):
         if self._c:

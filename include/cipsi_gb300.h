@@ -154,8 +154,9 @@ int cipsi_run_pt2(cipsi_ctx* ctx, const cipsi_opts* opts, cipsi_result* res);
 int cipsi_run_pt2_async(cipsi_ctx* ctx, const cipsi_opts* opts);
 int cipsi_fetch_result(cipsi_ctx* ctx, cipsi_result* res);
 
-/* Selected perturbers (what pie.f writes to unit 60), sorted by owner
-   generator then by determinant: records [first, first+count).
+/* Selected perturbers (what pie.f writes to unit 60), records
+   [first, first+count) of the last run in the engine's emission order (the
+   set of records is deterministic; their order is not).
      nec[count]           excitation degree
      holes/parts[8*count] sorted spin orbitals (1-based), zero padded
      xam[count]           selection value written as v(n)
@@ -190,6 +191,13 @@ void cipsi_inputs_free(cipsi_inputs* in);
 int cipsi_cip_main(const char* workdir, const char* stdin_path, int32_t sym_variant,
                    const char* json_path, const uint8_t* gen_mask, int32_t device, char* errbuf,
                    int32_t errlen);
+
+/* The same records without conversion: occupation bitstrings, 2*W 64-bit
+   words per record (W = 1 if norb <= 64 else 2; alpha words then beta
+   words, bit o of word o/64 = orbital o+1), owner, xam, evp[metat].  Any
+   output pointer may be NULL. */
+int cipsi_selection_raw(cipsi_ctx* ctx, int64_t first, int64_t count, uint64_t* bits,
+                        int32_t* owner, double* xam, double* evp);
 
 #ifdef __cplusplus
 }

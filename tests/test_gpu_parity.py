@@ -120,10 +120,13 @@ def test_deterministic(tmp_path, engine_lib):
         s1 = ctx.selection(r1["n_selected"])
         r2 = ctx.run(inp.opts)
         s2 = ctx.selection(r2["n_selected"])
-    for k in ("e2mp", "e2vp", "e2b", "psimp", "psivp", "ietat", "n_processed", "dpivot"):
+    for k in ("e2mp", "e2vp", "e2b", "psimp", "psivp", "ietat", "n_processed", "dpivot", "nom", "nam"):
         assert r1[k] == r2[k], k
-    for k in s1:
-        assert np.array_equal(s1[k], s2[k]), k
+    # the set of selected records is reproducible (their order is not)
+    def rows(s):
+        return sorted(zip(s["owner"].tolist(), map(tuple, s["holes"].tolist()), map(tuple, s["parts"].tolist()),
+                          s["xam"].tolist(), map(tuple, s["evp"].tolist())))
+    assert rows(s1) == rows(s2)
 
 
 def test_generator_shards_add_up(tmp_path, engine_lib):
