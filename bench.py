@@ -209,8 +209,12 @@ def run_gpu(args, rank: int, world: int, local_rank: int):
         if world > 1:
             torch.distributed.barrier()
 
+    gmask = None
+    if args.gen_every > 1:
+        gmask = np.zeros(inp.dims.ncf, dtype=np.uint8)
+        gmask[::args.gen_every] = 1
     for _ in range(args.warmup):
-        res = ctx.run(inp.opts)  # grows the selection buffer to what the workload needs
+        res = ctx.run(inp.opts, gen_mask=gmask)  # grows the selection buffer as needed
     contrib_per_step = res["n_processed"] * inp.dims.metat
     clocks = Clocks(local_rank)
     clocks.start()
@@ -225,7 +229,7 @@ def run_gpu(args, rank: int, world: int, local_rank: int):
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        ctx.run_async(inp.opts)
+        ctx.run_async(inp.opts, gen_mask=gmask)
         e1.record(stream)
         r = ctx.fetch()
         assert r["n_processed"] * inp.dims.metat == contrib_per_step
@@ -248,7 +252,7 @@ def run_gpu(args, rank: int, world: int, local_rank: int):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         ctx.upload(inp)
-        ctx.run_async(inp.opts)
+        ctx.run_async(inp.opts, gen_mask=gmask)
         r2 = ctx.fetch()
         ctx.selection_raw(r2["n_selected"], out=pinned)
         e2e_ms.append(1e3 * (time.perf_counter() - t0))
@@ -286,7 +290,9 @@ def run_gpu(args, rank: int, world: int, local_rank: int):
             "warmup": args.warmup, "ms_per_step": tot_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded integrals and reference space)",
-            "config": dict(workload_desc(), parallelism=f"replicas x{world}" if world > 1 else "single GPU"),
+            "config": dict(workload_desc(), parallelism=f"replicas x{world}" if world > 1 else "single GPU",
+                           **({"generator_sample": f"1/{args.gen_every} (profiling run)"}
+                              if args.gen_every > 1 else {})),
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h), "ms_per_step": tot_e2e / args.steps},
             "gpu_launches": launches,
@@ -322,6 +328,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--gen-every", type=int, default=1,
+                    help="profiling aid: run only every n-th determinant of S as a generator")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
