@@ -69,6 +69,10 @@ struct Params {
   int ngen;
   const int32_t* gens;       // generator indices (0-based); -1 = pertu block
   const uint8_t* gen_dmask;  // allowed rank changes per generator, bit (D+2)
+  int nunits;                // work units: (generator slot, range of R blocks
+  const int32_t* unit_g;     //   or, for the pertu block, of candidates)
+  const int32_t* unit_r0;
+  const int32_t* unit_r1;
   const uint64_t* S;         // ncf x 2W words (alpha words, beta words)
   const uint8_t* ygen;
   const int32_t* nesp;
@@ -513,7 +517,7 @@ struct BlockShared {
 };
 
 template <int W, int R>
-__global__ void __launch_bounds__(kThreads) k_pt2(Params p) {
+__global__ void __launch_bounds__(kThreads, 2) k_pt2(Params p) {
   extern __shared__ __align__(16) unsigned char dyn[];
   __shared__ BlockShared sh;
   __shared__ SmemHist hist;
@@ -550,17 +554,17 @@ __global__ void __launch_bounds__(kThreads) k_pt2(Params p) {
     __syncthreads();
     if (tid == 0) sh.gen = atomicAdd(p.work, 1);
     __syncthreads();
-    const int g = sh.gen;
-    if (g >= p.ngen) break;
+    const int unit = sh.gen;
+    if (unit >= p.nunits) break;
+    const int g = p.unit_g[unit];
+    const int ur0 = p.unit_r0[unit], ur1 = p.unit_r1[unit];
     const int k = p.gens[g];
 
     if (k < 0) {
       // ---------------- pertu: reference and its singles, no owner test
       // candidates: t = 0 -> reference (if pertu_ref), then singles
       const int no = p.noca, nv = p.norb - p.noca;
-      const int nsing = p.pertu_mono ? 2 * no * nv : 0;
-      const int ntot = nsing + (p.pertu_ref ? 1 : 0);
-      for (int t = tid; t < ntot; t += blockDim.x) {
+      for (int t = ur0 + tid; t < ur1; t += blockDim.x) {
         uint64_t u[2 * W];
 #pragma unroll
         for (int q = 0; q < 2 * W; ++q) u[q] = hf[q];
@@ -614,7 +618,7 @@ __global__ void __launch_bounds__(kThreads) k_pt2(Params p) {
           finish_candidate<W, R>(p, u, hmpi, hvpi, bc, 0, 0.0, 0, false, true, acc, hist);
         }
       }
-      block_flush<R>(p, acc, g, red);
+      block_flush<R>(p, acc, unit, red);
       continue;
     }
 
@@ -686,9 +690,8 @@ __global__ void __launch_bounds__(kThreads) k_pt2(Params p) {
     const int nespk = p.nesp[k];
     const bool yefk = p.yef[k] != 0;
 
-    // ---------------- blocks of removed electrons R
-    const int nR = nel + nel * (nel - 1) / 2;
-    for (int r = 0; r < nR; ++r) {
+    // ---------------- blocks of removed electrons R (this unit's range)
+    for (int r = ur0; r < ur1; ++r) {
       int e1, e2 = -1;
       if (r < nel) {
         e1 = r;
@@ -863,10 +866,36 @@ __global__ void __launch_bounds__(kThreads) k_pt2(Params p) {
         for (int m = 0; m < R; ++m) bc[m] = 0.0;
         int nint = 0, nnz = 0, lesp = 0;
         bool drop = false;
-        for (int i = 0; i < nlr; ++i) {
+        for (int i0 = 0; i0 < nlr && !drop; i0 += 4) {
+          // four independent compares per step (latency of the shared loads overlaps)
+          int xs[4];
+#pragma unroll
+          for (int g4 = 0; g4 < 4; ++g4) {
+            const int i = i0 + g4;
+            int x = 99;
+            if (i < nlr) {
+              x = 0;
+              if (fast) {
+#pragma unroll
+                for (int q = 0; q < 2 * W; ++q) x += __popcll(u[q] ^ lr_bits[(size_t)i * 2 * W + q]);
+              } else {
+                const int jj = my_lr_idx[i];
+#pragma unroll
+                for (int q = 0; q < 2 * W; ++q) x += __popcll(u[q] ^ __ldg(&p.S[(size_t)jj * 2 * W + q]));
+              }
+            }
+            xs[g4] = x;
+          }
+          if (xs[0] > 4 && xs[1] > 4 && xs[2] > 4 && xs[3] > 4) continue;
+#pragma unroll 1
+          for (int g4 = 0; g4 < 4; ++g4) {
+          const int i = i0 + g4;
+          const int x = xs[g4];
+          if (x > 4) continue;
           uint64_t vv[2 * W];
-          int j = 0;
+          int j;
           if (fast) {
+            j = lr_j[i];
 #pragma unroll
             for (int q = 0; q < 2 * W; ++q) vv[q] = lr_bits[(size_t)i * 2 * W + q];
           } else {
@@ -874,11 +903,6 @@ __global__ void __launch_bounds__(kThreads) k_pt2(Params p) {
 #pragma unroll
             for (int q = 0; q < 2 * W; ++q) vv[q] = __ldg(&p.S[(size_t)j * 2 * W + q]);
           }
-          int x = 0;
-#pragma unroll
-          for (int q = 0; q < 2 * W; ++q) x += __popcll(u[q] ^ vv[q]);
-          if (x > 4) continue;
-          if (fast) j = lr_j[i];
           if (j < k) {
             if (p.ygen[j]) {
               drop = true;
@@ -902,6 +926,7 @@ __global__ void __launch_bounds__(kThreads) k_pt2(Params p) {
 #pragma unroll
           for (int m = 0; m < R; ++m)
             if (m < p.metat) bc[m] += h * __ldg(&p.c[(size_t)j * p.metat + m]);
+          }
         }
         acc.ncmp += (unsigned long long)nlr;
         if (drop || nint == 0) continue;
@@ -943,7 +968,7 @@ __global__ void __launch_bounds__(kThreads) k_pt2(Params p) {
       }
       __syncthreads();
     }
-    block_flush<R>(p, acc, g, red);
+    block_flush<R>(p, acc, unit, red);
   }
 
   // block totals of the integer counters and the histogram
@@ -1016,6 +1041,10 @@ struct cipsi_ctx {
   int8_t* dorbsym = nullptr;
   int64_t ninte = 0;
   // per-run buffers
+  int32_t* dunits = nullptr;
+  int units_cap = 0;
+  int nunits = 0;
+  std::vector<int32_t> hunits;
   int32_t* dgens = nullptr;
   uint8_t* dgmask = nullptr;
   int gens_cap = 0;
@@ -1123,6 +1152,7 @@ void cipsi_ctx_destroy(cipsi_ctx* ctx) {
   dfree(ctx->dS); dfree(ctx->dygen); dfree(ctx->dyef); dfree(ctx->dnesp); dfree(ctx->dc);
   dfree(ctx->deri); dfree(ctx->dpairtab); dfree(ctx->dntttt); dfree(ctx->dF); dfree(ctx->dJ);
   dfree(ctx->dK); dfree(ctx->dfmpb); dfree(ctx->dorbsym); dfree(ctx->dgens); dfree(ctx->dgmask);
+  dfree(ctx->dunits);
   dfree(ctx->dnb_j); dfree(ctx->dnb_em); dfree(ctx->dlr_idx); dfree(ctx->dgen_part);
   dfree(ctx->dcounters); dfree(ctx->dhist_tab); dfree(ctx->dred); dfree(ctx->dwork);
   dfree(ctx->dsel_bits); dfree(ctx->dsel_owner); dfree(ctx->dsel_xam); dfree(ctx->dsel_evp);
@@ -1374,6 +1404,80 @@ int cipsi_run_pt2_async(cipsi_ctx* ctx, const cipsi_opts* o) {
   }
   const int ngen = (int)gens.size();
   ctx->ngen = ngen;
+  // work units: a generator's R blocks are split into chunks of at most
+  // kRChunk blocks that have an allowed rank-change class, so one heavy
+  // generator does not serialise on one SM; low-rank generators (which meet
+  // most of S) are queued first.
+  constexpr int kRChunk = 6;
+  constexpr int kPertuChunk = 128;
+  std::vector<int32_t> ug, ur0, ur1;
+  {
+    const int n = ctx->d.norb, noca = ctx->d.noca, nel = 2 * noca;
+    const int nR = nel + nel * (nel - 1) / 2;
+    std::vector<int> order(ngen);
+    for (int g = 0; g < ngen; ++g) order[g] = g;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+      const int ra = gens[a] < 0 ? -1 : ctx->rank[gens[a]];
+      const int rb = gens[b] < 0 ? -1 : ctx->rank[gens[b]];
+      return ra < rb;
+    });
+    std::vector<int> hfe(nel);
+    for (int g : order) {
+      const int k = gens[g];
+      if (k < 0) {
+        const int ntot = (pertu_ref ? 1 : 0) + (pertu_mono ? 2 * noca * (n - noca) : 0);
+        for (int t = 0; t < ntot; t += kPertuChunk) {
+          ug.push_back(g);
+          ur0.push_back(t);
+          ur1.push_back(std::min(ntot, t + kPertuChunk));
+        }
+        continue;
+      }
+      // electrons of k: alpha orbitals ascending, then beta; HF-occupied?
+      int ne = 0;
+      for (int sp = 0; sp < 2; ++sp)
+        for (int o = 0; o < n; ++o)
+          if ((ctx->Sbits[(size_t)k * 2 * W + sp * W + (o >> 6)] >> (o & 63)) & 1ull) hfe[ne++] = o < noca;
+      const uint8_t m = gmask[g];
+      auto allowed = [&](int r) {
+        int hfR, nRr;
+        if (r < nel) {
+          hfR = hfe[r];
+          nRr = 1;
+        } else {
+          int t = r - nel, e1 = 0;
+          while (t >= nel - 1 - e1) {
+            t -= nel - 1 - e1;
+            ++e1;
+          }
+          hfR = hfe[e1] + hfe[e1 + 1 + t];
+          nRr = 2;
+        }
+        for (int aV = 0; aV <= nRr; ++aV)
+          if (m & (1u << (hfR + aV - nRr + 2))) return true;
+        return false;
+      };
+      int cnt = 0, start = -1;
+      for (int r = 0; r < nR; ++r) {
+        if (!allowed(r)) continue;
+        if (start < 0) start = r;
+        if (++cnt == kRChunk) {
+          ug.push_back(g);
+          ur0.push_back(start);
+          ur1.push_back(r + 1);
+          cnt = 0;
+          start = -1;
+        }
+      }
+      if (start >= 0) {
+        ug.push_back(g);
+        ur0.push_back(start);
+        ur1.push_back(nR);
+      }
+    }
+  }
+  const int nunits = (int)ug.size();
+  ctx->nunits = nunits;
   int dev_sms = 0;
   CK(cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, ctx->device));
   // shared L_R capacity: enough for every neighbour list when it fits
@@ -1381,9 +1485,8 @@ int cipsi_run_pt2_async(cipsi_ctx* ctx, const cipsi_opts* o) {
   const size_t smem_budget = 150 * 1024;
   int lr_cap = (int)std::min<size_t>((size_t)ncf, smem_budget / per_entry);
   const size_t smem = (size_t)lr_cap * per_entry + 16;
-  const int blocks_per_sm = smem <= 70 * 1024 ? 2 : 1;
-  int grid = std::max(1, std::min(ngen, dev_sms * blocks_per_sm));
-  if (ngen == 0) grid = 1;
+  const int blocks_per_sm = smem <= 90 * 1024 ? 2 : 1;
+  int grid = std::max(1, std::min(nunits, dev_sms * blocks_per_sm));
   // buffers
   if ((size_t)grid > ctx->scratch_blocks || !ctx->dnb_j) {
     dfree(ctx->dnb_j); dfree(ctx->dnb_em); dfree(ctx->dlr_idx);
@@ -1398,14 +1501,27 @@ int cipsi_run_pt2_async(cipsi_ctx* ctx, const cipsi_opts* o) {
     CK(cudaMalloc(&ctx->dgmask, (size_t)std::max(ngen, 1)));
     ctx->gens_cap = ngen;
   }
+  if (nunits > ctx->units_cap) {
+    dfree(ctx->dunits);
+    CK(cudaMalloc(&ctx->dunits, (size_t)std::max(nunits, 1) * 3 * sizeof(int32_t)));
+    ctx->units_cap = nunits;
+  }
   if (ngen) {
     CK(cudaMemcpyAsync(ctx->dgens, gens.data(), ngen * sizeof(int32_t), cudaMemcpyHostToDevice, ctx->stream));
     CK(cudaMemcpyAsync(ctx->dgmask, gmask.data(), ngen, cudaMemcpyHostToDevice, ctx->stream));
   }
+  if (nunits) {
+    ctx->hunits.resize((size_t)3 * nunits);
+    std::copy(ug.begin(), ug.end(), ctx->hunits.begin());
+    std::copy(ur0.begin(), ur0.end(), ctx->hunits.begin() + nunits);
+    std::copy(ur1.begin(), ur1.end(), ctx->hunits.begin() + 2 * nunits);
+    CK(cudaMemcpyAsync(ctx->dunits, ctx->hunits.data(), (size_t)3 * nunits * sizeof(int32_t),
+                       cudaMemcpyHostToDevice, ctx->stream));
+  }
   const size_t nq = (size_t)5 * mt;
-  if ((size_t)std::max(ngen, 1) * nq > ctx->gen_part_cap) {
+  if ((size_t)std::max(nunits, 1) * nq > ctx->gen_part_cap) {
     dfree(ctx->dgen_part);
-    ctx->gen_part_cap = (size_t)std::max(ngen, 1) * nq;
+    ctx->gen_part_cap = (size_t)std::max(nunits, 1) * nq;
     CK(cudaMalloc(&ctx->dgen_part, ctx->gen_part_cap * sizeof(double)));
   }
   // counters [C_NCOUNTERS] + dpivot + nom[10] + nam[10*8]
@@ -1426,7 +1542,7 @@ int cipsi_run_pt2_async(cipsi_ctx* ctx, const cipsi_opts* o) {
   CK(cudaMemsetAsync(ctx->dcounters, 0, ncount * sizeof(unsigned long long), ctx->stream));
   CK(cudaMemsetAsync(ctx->dhist_tab, 0, 2 * kNClass * kMaxRoots * sizeof(double), ctx->stream));
   CK(cudaMemsetAsync(ctx->dwork, 0, sizeof(int), ctx->stream));
-  CK(cudaMemsetAsync(ctx->dgen_part, 0, (size_t)std::max(ngen, 1) * nq * sizeof(double), ctx->stream));
+  CK(cudaMemsetAsync(ctx->dgen_part, 0, (size_t)std::max(nunits, 1) * nq * sizeof(double), ctx->stream));
 
   Params p{};
   p.norb = ctx->d.norb;
@@ -1439,6 +1555,10 @@ int cipsi_run_pt2_async(cipsi_ctx* ctx, const cipsi_opts* o) {
   p.ngen = ngen;
   p.gens = ctx->dgens;
   p.gen_dmask = ctx->dgmask;
+  p.nunits = nunits;
+  p.unit_g = ctx->dunits;
+  p.unit_r0 = ctx->dunits + nunits;
+  p.unit_r1 = ctx->dunits + 2 * nunits;
   p.S = ctx->dS;
   p.ygen = ctx->dygen;
   p.nesp = ctx->dnesp;
@@ -1490,7 +1610,7 @@ int cipsi_run_pt2_async(cipsi_ctx* ctx, const cipsi_opts* o) {
   p.work = ctx->dwork;
 
   CK(cudaEventRecord(ctx->ev0, ctx->stream));
-  if (ngen > 0) {
+  if (nunits > 0) {
     cudaError_t e;
     const int R = mt <= 1 ? 1 : mt <= 2 ? 2 : mt <= 4 ? 4 : 8;
     if (W == 1) {
@@ -1505,7 +1625,7 @@ int cipsi_run_pt2_async(cipsi_ctx* ctx, const cipsi_opts* o) {
                  : launch_pt2<2, 8>(p, grid, smem, ctx->stream);
     }
     if (e != cudaSuccess) return fail(ctx, CIPSI_ERR_CUDA, std::string("k_pt2 launch: ") + cudaGetErrorString(e));
-    k_reduce<<<1, 64, 0, ctx->stream>>>(ctx->dgen_part, ngen, (int)nq, ctx->dred);
+    k_reduce<<<1, 64, 0, ctx->stream>>>(ctx->dgen_part, nunits, (int)nq, ctx->dred);
     CK(cudaGetLastError());
   } else {
     CK(cudaMemsetAsync(ctx->dred, 0, nq * sizeof(double), ctx->stream));
