@@ -523,11 +523,19 @@ __global__ void __launch_bounds__(kThreads, 2) k_pt2(Params p) {
   __shared__ SmemHist hist;
   __shared__ double red[5 * kMaxRoots * 32];
   __shared__ int ctmp[33];
+  __shared__ int bcnt[2][2 * kMaxOrb], boff[2][2 * kMaxOrb + 1], bfill[2][2 * kMaxOrb];
+  __shared__ int s_nl0;
 
   const int tid = threadIdx.x;
   // shared L_R arrays (fast path)
   uint64_t* lr_bits = reinterpret_cast<uint64_t*>(dyn);          // cap x 2W
   int32_t* lr_j = reinterpret_cast<int32_t*>(lr_bits + (size_t)p.lr_cap * 2 * W);
+  // index of L_R for double-excitation blocks: entries with |K' \ j| = 0, and
+  // buckets (per virtual spin orbital v of k) of entries with |K' \ j| = 1, 2
+  // that occupy v
+  int16_t* l0 = reinterpret_cast<int16_t*>(lr_j + p.lr_cap);
+  int16_t* bkt1 = l0 + p.lr_cap;       // <= 3 per entry
+  int16_t* bkt2 = bkt1 + 3 * p.lr_cap; // <= 4 per entry
   int32_t* my_nb_j = p.nb_j + (size_t)blockIdx.x * p.ncf;
   uint64_t* my_nb_em = p.nb_emask + (size_t)blockIdx.x * p.ncf;
   int32_t* my_lr_idx = p.lr_idx + (size_t)blockIdx.x * p.ncf;
@@ -806,6 +814,86 @@ __global__ void __launch_bounds__(kThreads, 2) k_pt2(Params p) {
         }
       }
       __syncthreads();
+      const bool indexed = fast && nRr == 2;
+      if (indexed) {
+        const int nb2 = 2 * p.norb;
+        for (int i = tid; i < 2 * nb2; i += blockDim.x) {
+          bcnt[i / nb2][i % nb2] = 0;
+          bfill[i / nb2][i % nb2] = 0;
+        }
+        __syncthreads();
+        for (int t = tid; t < nlr; t += blockDim.x) {
+          const uint64_t* v = lr_bits + (size_t)t * 2 * W;
+          int m = 0;
+#pragma unroll
+          for (int q = 0; q < 2 * W; ++q) m += __popcll(kp[q] & ~v[q]);
+          if (m == 0) continue;
+#pragma unroll
+          for (int q = 0; q < 2 * W; ++q) {
+            uint64_t ext = v[q] & ~kb[q];
+            while (ext) {
+              const int b = __ffsll((long long)ext) - 1;
+              ext &= ext - 1;
+              atomicAdd(&bcnt[m - 1][(q / W) * p.norb + (q % W) * 64 + b], 1);
+            }
+          }
+        }
+        __syncthreads();
+        if (tid < 2) {
+          int acc0 = 0;
+          for (int b = 0; b < nb2; ++b) {
+            boff[tid][b] = acc0;
+            acc0 += bcnt[tid][b];
+          }
+          boff[tid][nb2] = acc0;
+        }
+        __syncthreads();
+        for (int t = tid; t < nlr; t += blockDim.x) {
+          const uint64_t* v = lr_bits + (size_t)t * 2 * W;
+          int m = 0;
+#pragma unroll
+          for (int q = 0; q < 2 * W; ++q) m += __popcll(kp[q] & ~v[q]);
+          if (m == 0) continue;
+          int16_t* dst = m == 1 ? bkt1 : bkt2;
+#pragma unroll
+          for (int q = 0; q < 2 * W; ++q) {
+            uint64_t ext = v[q] & ~kb[q];
+            while (ext) {
+              const int b = __ffsll((long long)ext) - 1;
+              ext &= ext - 1;
+              const int so = (q / W) * p.norb + (q % W) * 64 + b;
+              dst[boff[m - 1][so] + atomicAdd(&bfill[m - 1][so], 1)] = (int16_t)t;
+            }
+          }
+        }
+        __syncthreads();
+        // sort each bucket by entry index: fixed summation order (deterministic)
+        for (int i = tid; i < 2 * nb2; i += blockDim.x) {
+          const int mm = i / nb2, b = i % nb2;
+          int16_t* d = (mm == 0 ? bkt1 : bkt2) + boff[mm][b];
+          const int n = boff[mm][b + 1] - boff[mm][b];
+          for (int x = 1; x < n; ++x) {
+            const int16_t key = d[x];
+            int y = x - 1;
+            while (y >= 0 && d[y] > key) {
+              d[y + 1] = d[y];
+              --y;
+            }
+            d[y + 1] = key;
+          }
+        }
+        const int nl0 = ordered_compact(
+            nlr,
+            [&](int t) {
+              int m = 0;
+#pragma unroll
+              for (int q = 0; q < 2 * W; ++q) m += __popcll(kp[q] & ~lr_bits[(size_t)t * 2 * W + q]);
+              return m == 0;
+            },
+            [&](int slot, int t) { l0[slot] = (int16_t)t; }, ctmp);
+        if (tid == 0) s_nl0 = nl0;
+        __syncthreads();
+      }
       const int symR = e2 >= 0 ? p.its[p.orbsym[o1]][p.orbsym[o2]] : p.orbsym[o1];
       // added-orbital space
       int nA;
@@ -866,32 +954,9 @@ __global__ void __launch_bounds__(kThreads, 2) k_pt2(Params p) {
         for (int m = 0; m < R; ++m) bc[m] = 0.0;
         int nint = 0, nnz = 0, lesp = 0;
         bool drop = false;
-        for (int i0 = 0; i0 < nlr && !drop; i0 += 4) {
-          // four independent compares per step (latency of the shared loads overlaps)
-          int xs[4];
-#pragma unroll
-          for (int g4 = 0; g4 < 4; ++g4) {
-            const int i = i0 + g4;
-            int x = 99;
-            if (i < nlr) {
-              x = 0;
-              if (fast) {
-#pragma unroll
-                for (int q = 0; q < 2 * W; ++q) x += __popcll(u[q] ^ lr_bits[(size_t)i * 2 * W + q]);
-              } else {
-                const int jj = my_lr_idx[i];
-#pragma unroll
-                for (int q = 0; q < 2 * W; ++q) x += __popcll(u[q] ^ __ldg(&p.S[(size_t)jj * 2 * W + q]));
-              }
-            }
-            xs[g4] = x;
-          }
-          if (xs[0] > 4 && xs[1] > 4 && xs[2] > 4 && xs[3] > 4) continue;
-#pragma unroll 1
-          for (int g4 = 0; g4 < 4; ++g4) {
-          const int i = i0 + g4;
-          const int x = xs[g4];
-          if (x > 4) continue;
+        // one S determinant of L_R against I: owner test, already-in-S test,
+        // <I|H|j> accumulation; returns true when I is dropped
+        auto visit = [&](int i, int x) -> bool {
           uint64_t vv[2 * W];
           int j;
           if (fast) {
@@ -903,17 +968,14 @@ __global__ void __launch_bounds__(kThreads, 2) k_pt2(Params p) {
 #pragma unroll
             for (int q = 0; q < 2 * W; ++q) vv[q] = __ldg(&p.S[(size_t)j * 2 * W + q]);
           }
-          if (j < k) {
-            if (p.ygen[j]) {
-              drop = true;
-              break;
-            }
-            continue;
+          if (x < 0) {
+            x = 0;
+#pragma unroll
+            for (int q = 0; q < 2 * W; ++q) x += __popcll(u[q] ^ vv[q]);
           }
-          if (x == 0) {
-            drop = true;
-            break;
-          }
+          if (x > 4) return false;
+          if (j < k) return p.ygen[j] != 0;
+          if (x == 0) return true;
           int rankJ = 0;
 #pragma unroll
           for (int q = 0; q < 2 * W; ++q) rankJ += __popcll(hf[q] & ~vv[q]);
@@ -926,9 +988,56 @@ __global__ void __launch_bounds__(kThreads, 2) k_pt2(Params p) {
 #pragma unroll
           for (int m = 0; m < R; ++m)
             if (m < p.metat) bc[m] += h * __ldg(&p.c[(size_t)j * p.metat + m]);
+          return false;
+        };
+        if (indexed) {
+          // only the determinants that can be within two excitations of I
+          const int so1 = a1 + sa1 * p.norb, so2 = a2 + sa2 * p.norb;
+          const int w1 = sa1 * W + (a1 >> 6), w2 = sa2 * W + (a2 >> 6);
+          const uint64_t b1 = 1ull << (a1 & 63), b2 = 1ull << (a2 & 63);
+          int nvis = s_nl0;
+          for (int q = 0; q < s_nl0 && !drop; ++q) drop = visit(l0[q], -1);
+          for (int q = boff[0][so1]; q < boff[0][so1 + 1] && !drop; ++q) drop = visit(bkt1[q], -1);
+          nvis += boff[0][so1 + 1] - boff[0][so1];
+          for (int q = boff[0][so2]; q < boff[0][so2 + 1] && !drop; ++q) {
+            const int i = bkt1[q];
+            if (!(lr_bits[(size_t)i * 2 * W + w1] & b1)) drop = visit(i, -1);
           }
+          nvis += boff[0][so2 + 1] - boff[0][so2];
+          for (int q = boff[1][so1]; q < boff[1][so1 + 1] && !drop; ++q) {
+            const int i = bkt2[q];
+            if (lr_bits[(size_t)i * 2 * W + w2] & b2) drop = visit(i, -1);
+          }
+          nvis += boff[1][so1 + 1] - boff[1][so1];
+          acc.ncmp += (unsigned long long)nvis;
+        } else {
+          for (int i0 = 0; i0 < nlr && !drop; i0 += 4) {
+            // four independent compares per step (latency of the loads overlaps)
+            int xs[4];
+#pragma unroll
+            for (int g4 = 0; g4 < 4; ++g4) {
+              const int i = i0 + g4;
+              int x = 99;
+              if (i < nlr) {
+                x = 0;
+                if (fast) {
+#pragma unroll
+                  for (int q = 0; q < 2 * W; ++q) x += __popcll(u[q] ^ lr_bits[(size_t)i * 2 * W + q]);
+                } else {
+                  const int jj = my_lr_idx[i];
+#pragma unroll
+                  for (int q = 0; q < 2 * W; ++q) x += __popcll(u[q] ^ __ldg(&p.S[(size_t)jj * 2 * W + q]));
+                }
+              }
+              xs[g4] = x;
+            }
+            if (xs[0] > 4 && xs[1] > 4 && xs[2] > 4 && xs[3] > 4) continue;
+#pragma unroll 1
+            for (int g4 = 0; g4 < 4 && !drop; ++g4)
+              if (xs[g4] <= 4) drop = visit(i0 + g4, xs[g4]);
+          }
+          acc.ncmp += (unsigned long long)nlr;
         }
-        acc.ncmp += (unsigned long long)nlr;
         if (drop || nint == 0) continue;
         const bool is_pert1 = (D != 2);
         if (!is_pert1 && nnz == 0) continue;
@@ -1481,7 +1590,7 @@ int cipsi_run_pt2_async(cipsi_ctx* ctx, const cipsi_opts* o) {
   int dev_sms = 0;
   CK(cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, ctx->device));
   // shared L_R capacity: enough for every neighbour list when it fits
-  const size_t per_entry = (size_t)2 * W * 8 + 4;
+  const size_t per_entry = (size_t)2 * W * 8 + 4 + 2 * (1 + 3 + 4);
   const size_t smem_budget = 150 * 1024;
   int lr_cap = (int)std::min<size_t>((size_t)ncf, smem_budget / per_entry);
   const size_t smem = (size_t)lr_cap * per_entry + 16;
