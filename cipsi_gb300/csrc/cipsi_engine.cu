@@ -956,7 +956,9 @@ __global__ void __launch_bounds__(kThreads, 2) k_pt2(Params p) {
         bool drop = false;
         // one S determinant of L_R against I: owner test, already-in-S test,
         // <I|H|j> accumulation; returns true when I is dropped
-        auto visit = [&](int i, int x) -> bool {
+        // mode 0: tests and matrix element; 1: owner / already-in-S tests only;
+        // 2: matrix element only (tests done by a mode-1 pass)
+        auto visit = [&](int i, int x, int mode) -> bool {
           uint64_t vv[2 * W];
           int j;
           if (fast) {
@@ -974,8 +976,9 @@ __global__ void __launch_bounds__(kThreads, 2) k_pt2(Params p) {
             for (int q = 0; q < 2 * W; ++q) x += __popcll(u[q] ^ vv[q]);
           }
           if (x > 4) return false;
-          if (j < k) return p.ygen[j] != 0;
-          if (x == 0) return true;
+          if (j < k) return mode != 2 && p.ygen[j] != 0;
+          if (x == 0) return mode != 2;
+          if (mode == 1) return false;
           int rankJ = 0;
 #pragma unroll
           for (int q = 0; q < 2 * W; ++q) rankJ += __popcll(hf[q] & ~vv[q]);
@@ -995,20 +998,22 @@ __global__ void __launch_bounds__(kThreads, 2) k_pt2(Params p) {
           const int so1 = a1 + sa1 * p.norb, so2 = a2 + sa2 * p.norb;
           const int w1 = sa1 * W + (a1 >> 6), w2 = sa2 * W + (a2 >> 6);
           const uint64_t b1 = 1ull << (a1 & 63), b2 = 1ull << (a2 & 63);
-          int nvis = s_nl0;
-          for (int q = 0; q < s_nl0 && !drop; ++q) drop = visit(l0[q], -1);
-          for (int q = boff[0][so1]; q < boff[0][so1 + 1] && !drop; ++q) drop = visit(bkt1[q], -1);
-          nvis += boff[0][so1 + 1] - boff[0][so1];
-          for (int q = boff[0][so2]; q < boff[0][so2 + 1] && !drop; ++q) {
-            const int i = bkt1[q];
-            if (!(lr_bits[(size_t)i * 2 * W + w1] & b1)) drop = visit(i, -1);
+          const int nvis = s_nl0 + (boff[0][so1 + 1] - boff[0][so1]) + (boff[0][so2 + 1] - boff[0][so2]) +
+                           (boff[1][so1 + 1] - boff[1][so1]);
+          // pass 0: owner and already-in-S tests; pass 1: matrix elements
+          for (int pass = 0; pass < 2 && !drop; ++pass) {
+            const int chk = pass == 0 ? 1 : 2;
+            for (int q = 0; q < s_nl0 && !drop; ++q) drop = visit(l0[q], -1, chk);
+            for (int q = boff[0][so1]; q < boff[0][so1 + 1] && !drop; ++q) drop = visit(bkt1[q], -1, chk);
+            for (int q = boff[0][so2]; q < boff[0][so2 + 1] && !drop; ++q) {
+              const int i = bkt1[q];
+              if (!(lr_bits[(size_t)i * 2 * W + w1] & b1)) drop = visit(i, -1, chk);
+            }
+            for (int q = boff[1][so1]; q < boff[1][so1 + 1] && !drop; ++q) {
+              const int i = bkt2[q];
+              if (lr_bits[(size_t)i * 2 * W + w2] & b2) drop = visit(i, -1, chk);
+            }
           }
-          nvis += boff[0][so2 + 1] - boff[0][so2];
-          for (int q = boff[1][so1]; q < boff[1][so1 + 1] && !drop; ++q) {
-            const int i = bkt2[q];
-            if (lr_bits[(size_t)i * 2 * W + w2] & b2) drop = visit(i, -1);
-          }
-          nvis += boff[1][so1 + 1] - boff[1][so1];
           acc.ncmp += (unsigned long long)nvis;
         } else {
           for (int i0 = 0; i0 < nlr && !drop; i0 += 4) {
@@ -1034,7 +1039,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_pt2(Params p) {
             if (xs[0] > 4 && xs[1] > 4 && xs[2] > 4 && xs[3] > 4) continue;
 #pragma unroll 1
             for (int g4 = 0; g4 < 4 && !drop; ++g4)
-              if (xs[g4] <= 4) drop = visit(i0 + g4, xs[g4]);
+              if (xs[g4] <= 4) drop = visit(i0 + g4, xs[g4], 0);
           }
           acc.ncmp += (unsigned long long)nlr;
         }
