@@ -373,36 +373,37 @@ __device__ void finish_candidate(const Params& p, const uint64_t* u, double hmpi
                                  SmemHist& hist) {
   double xam = 0.0;
   bool ydeg = false;
-  double vil[R], semp[R], sevp[R], venvp[R];
+  double vil[R], semp[R], sevp[R];
+  // the reference adds each term and then term*fmul (spin-flip weight,
+  // pert1.f:280-287); one compensated add of term*(1+fmul) is used here
+  const double wgt = ybis ? 1.0 + fmul : 1.0;
 #pragma unroll
   for (int m = 0; m < R; ++m) {
     vil[m] = 0.0;
-    semp[m] = sevp[m] = venvp[m] = 0.0;
+    semp[m] = sevp[m] = 0.0;
     if (m >= p.metat) continue;
     const double bcalc = bc[m];
     const double dmp = p.emp[m] - hmpi;
     const double cimp = bcalc / dmp;
     const double car = cimp * cimp;
     const double eimp = bcalc * cimp;
-    kahan_add(acc.e2mp[m], acc.cmp[m], eimp);
-    acc.psimp[m] += car;
+    kahan_add(acc.e2mp[m], acc.cmp[m], eimp * wgt);
+    acc.psimp[m] += car * wgt;
     double xim = p.ysele ? fabs(eimp) : fabs(cimp);
     double deno = dmp, eim = eimp;
-    double eivp = 0.0, carvp = 0.0, eib = 0.0;
+    double eivp = 0.0;
     if (p.yen) {
       const double dvp = p.e[m] - hvpi;
       const double civp = bcalc / dvp;
-      carvp = civp * civp;
       eivp = bcalc * civp;
-      kahan_add(acc.e2vp[m], acc.cvp[m], eivp);
-      acc.psivp[m] += carvp;
+      kahan_add(acc.e2vp[m], acc.cvp[m], eivp * wgt);
+      acc.psivp[m] += (civp * civp) * wgt;
       xim = p.ysele ? fabs(eivp) : fabs(civp);
       deno = dvp;
       eim = eivp;
       const double db = p.eb[m] - hvpi;
-      const double cib = bcalc / db;
-      eib = bcalc * cib;
-      kahan_add(acc.e2b[m], acc.cb[m], eib);
+      const double eib = bcalc * (bcalc / db);
+      kahan_add(acc.e2b[m], acc.cb[m], eib * wgt);
     }
     if (!(fabs(deno) > 0.05) && !(fabs(eim) < 1.0e-6) && p.ywdeg) ydeg = true;
     if (xim < p.teste[m]) acc.dpivot = fmax(acc.dpivot, xim);
@@ -413,16 +414,6 @@ __device__ void finish_candidate(const Params& p, const uint64_t* u, double hmpi
     }
     semp[m] = eimp;
     sevp[m] = eivp;
-    venvp[m] = eivp * (fmul + 1.0);
-    if (ybis) {
-      kahan_add(acc.e2mp[m], acc.cmp[m], eimp * fmul);
-      acc.psimp[m] += car * fmul;
-      if (p.yen) {
-        kahan_add(acc.e2vp[m], acc.cvp[m], eivp * fmul);
-        kahan_add(acc.e2b[m], acc.cb[m], eib * fmul);
-        acc.psivp[m] += carvp * fmul;
-      }
-    }
   }
   acc.ietat += (unsigned long long)(long long)(nmul + 1);
   acc.nproc += 1;
@@ -456,8 +447,10 @@ __device__ void finish_candidate(const Params& p, const uint64_t* u, double hmpi
       for (int q = 0; q < 2 * W; ++q) p.sel_bits[slot * 2 * W + q] = u[q];
       p.sel_owner[slot] = owner1;
       p.sel_xam[slot] = xam;
-      for (int m = 0; m < p.metat && m < R; ++m)
-        p.sel_evp[slot * p.metat + m] = p.symvar ? venvp[m] : 0.0;
+      // ENvp per root written by cipsym (cipsym/pert1.f:244): eivp*(fmul+1)
+#pragma unroll
+      for (int m = 0; m < R; ++m)
+        if (m < p.metat) p.sel_evp[slot * p.metat + m] = p.symvar ? sevp[m] * (fmul + 1.0) : 0.0;
     }
   }
 }
