@@ -365,12 +365,15 @@ __device__ __forceinline__ int hist_class(const Params& p, double val) {
 }
 
 // Everything the reference does with one candidate after its interaction
-// scan: denominators, E2, selection, histogram, unit-60 record.
+// scan: denominators, E2, selection, histogram, unit-60 record.  Called by
+// all 32 lanes of a warp; `live` marks the lanes holding a perturber.
 template <int W, int R>
-__device__ void finish_candidate(const Params& p, const uint64_t* u, double hmpi, double hvpi,
-                                 const double* bc, int owner1 /*1-based, 0 = pertu*/,
+__device__ void finish_candidate(const Params& p, bool live, const uint64_t* u, double hmpi,
+                                 double hvpi, const double* bc, int owner1 /*1-based, 0 = pertu*/,
                                  double fmul, int nmul, bool ybis, bool is_pert1, Acc<R>& acc,
                                  SmemHist& hist) {
+  constexpr unsigned kFull = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
   double xam = 0.0;
   bool ydeg = false;
   double vil[R], semp[R], sevp[R];
@@ -381,7 +384,7 @@ __device__ void finish_candidate(const Params& p, const uint64_t* u, double hmpi
   for (int m = 0; m < R; ++m) {
     vil[m] = 0.0;
     semp[m] = sevp[m] = 0.0;
-    if (m >= p.metat) continue;
+    if (!live || m >= p.metat) continue;
     const double bcalc = bc[m];
     const double dmp = p.emp[m] - hmpi;
     const double cimp = bcalc / dmp;
@@ -415,42 +418,69 @@ __device__ void finish_candidate(const Params& p, const uint64_t* u, double hmpi
     semp[m] = eimp;
     sevp[m] = eivp;
   }
-  acc.ietat += (unsigned long long)(long long)(nmul + 1);
-  acc.nproc += 1;
-  // histogram (cip/isto.f); pert1 calls it always, diexcit only if ymoyen
-  if ((is_pert1 || p.ymoyen) && xam >= p.teseff) {
-    const double fm = fmul + 1.0;
-    const int cls = hist_class(p, xam);
-    atomicAdd(&hist.nom[cls], (unsigned long long)(long long)(1 + nmul));
+  if (live) {
+    acc.ietat += (unsigned long long)(long long)(nmul + 1);
+    acc.nproc += 1;
+  }
+  // histogram (cip/isto.f; pert1 calls it always, diexcit only if ymoyen),
+  // reduced over the warp first: one shared-memory atomic per class present
+  const bool in_hist = live && (is_pert1 || p.ymoyen) && xam >= p.teseff;
+  const int cls = in_hist ? hist_class(p, xam) : -1;
+  const double fm = fmul + 1.0;
+  unsigned present = __reduce_or_sync(kFull, in_hist ? (1u << cls) : 0u);
+  while (present) {
+    const int c = __ffs(present) - 1;
+    present &= present - 1;
+    const bool in = cls == c;
+    const unsigned cnt = __reduce_add_sync(kFull, in ? (unsigned)(1 + nmul) : 0u);
+    if (lane == 0) atomicAdd(&hist.nom[c], (unsigned long long)cnt);
 #pragma unroll
     for (int m = 0; m < R; ++m) {
-      if (m >= p.metat || vil[m] < p.teseff) continue;
-      atomicAdd(&hist.tab[cls * kMaxRoots + m], semp[m] * fm);
-      atomicAdd(&hist.tab[kNClass * kMaxRoots + cls * kMaxRoots + m], sevp[m] * fm);
-      const int c2 = hist_class(p, vil[m]);
-      atomicAdd(&hist.nam[c2 * kMaxRoots + m], (unsigned long long)(long long)(nmul + 1));
+      if (m >= p.metat) break;
+      const bool inm = in && vil[m] >= p.teseff;
+      double v1 = inm ? semp[m] * fm : 0.0, v2 = inm ? sevp[m] * fm : 0.0;
+      for (int o = 16; o > 0; o >>= 1) {
+        v1 += __shfl_xor_sync(kFull, v1, o);
+        v2 += __shfl_xor_sync(kFull, v2, o);
+      }
+      if (lane == 0) {
+        if (v1 != 0.0) atomicAdd(&hist.tab[c * kMaxRoots + m], v1);
+        if (v2 != 0.0) atomicAdd(&hist.tab[kNClass * kMaxRoots + c * kMaxRoots + m], v2);
+      }
+    }
+  }
+#pragma unroll
+  for (int m = 0; m < R; ++m) {
+    if (m >= p.metat) break;
+    const int c2 = (in_hist && vil[m] >= p.teseff) ? hist_class(p, vil[m]) : -1;
+    unsigned pr = __reduce_or_sync(kFull, c2 >= 0 ? (1u << c2) : 0u);
+    while (pr) {
+      const int c = __ffs(pr) - 1;
+      pr &= pr - 1;
+      const unsigned cnt = __reduce_add_sync(kFull, c2 == c ? (unsigned)(1 + nmul) : 0u);
+      if (lane == 0) atomicAdd(&hist.nam[c * kMaxRoots + m], (unsigned long long)cnt);
     }
   }
   if (ydeg) xam = 1.0;
-  const bool sel = xam > p.tau && p.ymoyen;
-  const unsigned am = __activemask();
-  const unsigned sm = __ballot_sync(am, sel);
-  if (sel) {
-    const int lane = threadIdx.x & 31;
-    const int leader = __ffs(sm) - 1;
+  // unit-60 record (pie.f): one slot reservation per warp
+  const bool sel = live && xam > p.tau && p.ymoyen;
+  const unsigned sm = __ballot_sync(kFull, sel);
+  if (sm) {
     unsigned long long base = 0;
-    if (lane == leader) base = atomicAdd(&p.counters[C_NSEL], (unsigned long long)__popc(sm));
-    base = __shfl_sync(sm, base, leader);
-    const unsigned long long slot = base + __popc(sm & ((1u << lane) - 1u));
-    if ((long long)slot < p.sel_cap) {
+    if (lane == 0) base = atomicAdd(&p.counters[C_NSEL], (unsigned long long)__popc(sm));
+    base = __shfl_sync(kFull, base, 0);
+    if (sel) {
+      const unsigned long long slot = base + __popc(sm & ((1u << lane) - 1u));
+      if ((long long)slot < p.sel_cap) {
 #pragma unroll
-      for (int q = 0; q < 2 * W; ++q) p.sel_bits[slot * 2 * W + q] = u[q];
-      p.sel_owner[slot] = owner1;
-      p.sel_xam[slot] = xam;
-      // ENvp per root written by cipsym (cipsym/pert1.f:244): eivp*(fmul+1)
+        for (int q = 0; q < 2 * W; ++q) p.sel_bits[slot * 2 * W + q] = u[q];
+        p.sel_owner[slot] = owner1;
+        p.sel_xam[slot] = xam;
+        // ENvp per root written by cipsym (cipsym/pert1.f:244): eivp*(fmul+1)
 #pragma unroll
-      for (int m = 0; m < R; ++m)
-        if (m < p.metat) p.sel_evp[slot * p.metat + m] = p.symvar ? sevp[m] * (fmul + 1.0) : 0.0;
+        for (int m = 0; m < R; ++m)
+          if (m < p.metat) p.sel_evp[slot * p.metat + m] = p.symvar ? sevp[m] * (fmul + 1.0) : 0.0;
+      }
     }
   }
 }
@@ -516,19 +546,11 @@ __global__ void __launch_bounds__(kThreads, 2) k_pt2(Params p) {
   __shared__ SmemHist hist;
   __shared__ double red[5 * kMaxRoots * 32];
   __shared__ int ctmp[33];
-  __shared__ int bcnt[2][2 * kMaxOrb], boff[2][2 * kMaxOrb + 1], bfill[2][2 * kMaxOrb];
-  __shared__ int s_nl0;
 
   const int tid = threadIdx.x;
   // shared L_R arrays (fast path)
   uint64_t* lr_bits = reinterpret_cast<uint64_t*>(dyn);          // cap x 2W
   int32_t* lr_j = reinterpret_cast<int32_t*>(lr_bits + (size_t)p.lr_cap * 2 * W);
-  // index of L_R for double-excitation blocks: entries with |K' \ j| = 0, and
-  // buckets (per virtual spin orbital v of k) of entries with |K' \ j| = 1, 2
-  // that occupy v
-  int16_t* l0 = reinterpret_cast<int16_t*>(lr_j + p.lr_cap);
-  int16_t* bkt1 = l0 + p.lr_cap;       // <= 3 per entry
-  int16_t* bkt2 = bkt1 + 3 * p.lr_cap; // <= 4 per entry
   int32_t* my_nb_j = p.nb_j + (size_t)blockIdx.x * p.ncf;
   uint64_t* my_nb_em = p.nb_emask + (size_t)blockIdx.x * p.ncf;
   int32_t* my_lr_idx = p.lr_idx + (size_t)blockIdx.x * p.ncf;
@@ -565,27 +587,30 @@ __global__ void __launch_bounds__(kThreads, 2) k_pt2(Params p) {
       // ---------------- pertu: reference and its singles, no owner test
       // candidates: t = 0 -> reference (if pertu_ref), then singles
       const int no = p.noca, nv = p.norb - p.noca;
-      for (int t = ur0 + tid; t < ur1; t += blockDim.x) {
+      for (int t0 = ur0; t0 < ur1; t0 += blockDim.x) {
+        const int t = t0 + tid;
+        bool live = t < ur1;
         uint64_t u[2 * W];
 #pragma unroll
         for (int q = 0; q < 2 * W; ++q) u[q] = hf[q];
         const int tt = p.pertu_ref ? t - 1 : t;  // tt < 0: the reference itself
-        if (tt >= 0) {
+        if (live && tt >= 0) {
           const int s = tt / (no * nv);
           const int rem = tt % (no * nv);
           const int o = rem / nv, vv = no + rem % nv;
-          if (p.its[p.orbsym[o]][p.orbsym[vv]] != p.isym - 1) continue;
+          if (p.its[p.orbsym[o]][p.orbsym[vv]] != p.isym - 1) live = false;
           u[s * W + (o >> 6)] &= ~(1ull << (o & 63));
           u[s * W + (vv >> 6)] |= (1ull << (vv & 63));
         }
-        acc.ncand++;
-        {
+        double bc[R];
+#pragma unroll
+        for (int m = 0; m < R; ++m) bc[m] = 0.0;
+        double hmpi = 0.0, hvpi = 0.0;
+        if (live) {
+          acc.ncand++;
           int rankI = 0;
 #pragma unroll
           for (int q = 0; q < 2 * W; ++q) rankI += __popcll(hf[q] & ~u[q]);
-          double bc[R];
-#pragma unroll
-          for (int m = 0; m < R; ++m) bc[m] = 0.0;
           int nint = 0;
           bool drop = false;
           for (int j = 0; j < ncf; ++j) {
@@ -613,11 +638,10 @@ __global__ void __launch_bounds__(kThreads, 2) k_pt2(Params p) {
             for (int m = 0; m < R; ++m)
               if (m < p.metat) bc[m] += h * __ldg(&p.c[(size_t)j * p.metat + m]);
           }
-          if (drop || nint == 0) continue;
-          double hmpi, hvpi;
-          diag_terms<W>(p, u, hf, hmpi, hvpi, p.yen != 0);
-          finish_candidate<W, R>(p, u, hmpi, hvpi, bc, 0, 0.0, 0, false, true, acc, hist);
+          if (drop || nint == 0) live = false;
+          if (live) diag_terms<W>(p, u, hf, hmpi, hvpi, p.yen != 0);
         }
+        finish_candidate<W, R>(p, live, u, hmpi, hvpi, bc, 0, 0.0, 0, false, true, acc, hist);
       }
       block_flush<R>(p, acc, unit, red);
       continue;
@@ -807,86 +831,6 @@ __global__ void __launch_bounds__(kThreads, 2) k_pt2(Params p) {
         }
       }
       __syncthreads();
-      const bool indexed = fast && nRr == 2;
-      if (indexed) {
-        const int nb2 = 2 * p.norb;
-        for (int i = tid; i < 2 * nb2; i += blockDim.x) {
-          bcnt[i / nb2][i % nb2] = 0;
-          bfill[i / nb2][i % nb2] = 0;
-        }
-        __syncthreads();
-        for (int t = tid; t < nlr; t += blockDim.x) {
-          const uint64_t* v = lr_bits + (size_t)t * 2 * W;
-          int m = 0;
-#pragma unroll
-          for (int q = 0; q < 2 * W; ++q) m += __popcll(kp[q] & ~v[q]);
-          if (m == 0) continue;
-#pragma unroll
-          for (int q = 0; q < 2 * W; ++q) {
-            uint64_t ext = v[q] & ~kb[q];
-            while (ext) {
-              const int b = __ffsll((long long)ext) - 1;
-              ext &= ext - 1;
-              atomicAdd(&bcnt[m - 1][(q / W) * p.norb + (q % W) * 64 + b], 1);
-            }
-          }
-        }
-        __syncthreads();
-        if (tid < 2) {
-          int acc0 = 0;
-          for (int b = 0; b < nb2; ++b) {
-            boff[tid][b] = acc0;
-            acc0 += bcnt[tid][b];
-          }
-          boff[tid][nb2] = acc0;
-        }
-        __syncthreads();
-        for (int t = tid; t < nlr; t += blockDim.x) {
-          const uint64_t* v = lr_bits + (size_t)t * 2 * W;
-          int m = 0;
-#pragma unroll
-          for (int q = 0; q < 2 * W; ++q) m += __popcll(kp[q] & ~v[q]);
-          if (m == 0) continue;
-          int16_t* dst = m == 1 ? bkt1 : bkt2;
-#pragma unroll
-          for (int q = 0; q < 2 * W; ++q) {
-            uint64_t ext = v[q] & ~kb[q];
-            while (ext) {
-              const int b = __ffsll((long long)ext) - 1;
-              ext &= ext - 1;
-              const int so = (q / W) * p.norb + (q % W) * 64 + b;
-              dst[boff[m - 1][so] + atomicAdd(&bfill[m - 1][so], 1)] = (int16_t)t;
-            }
-          }
-        }
-        __syncthreads();
-        // sort each bucket by entry index: fixed summation order (deterministic)
-        for (int i = tid; i < 2 * nb2; i += blockDim.x) {
-          const int mm = i / nb2, b = i % nb2;
-          int16_t* d = (mm == 0 ? bkt1 : bkt2) + boff[mm][b];
-          const int n = boff[mm][b + 1] - boff[mm][b];
-          for (int x = 1; x < n; ++x) {
-            const int16_t key = d[x];
-            int y = x - 1;
-            while (y >= 0 && d[y] > key) {
-              d[y + 1] = d[y];
-              --y;
-            }
-            d[y + 1] = key;
-          }
-        }
-        const int nl0 = ordered_compact(
-            nlr,
-            [&](int t) {
-              int m = 0;
-#pragma unroll
-              for (int q = 0; q < 2 * W; ++q) m += __popcll(kp[q] & ~lr_bits[(size_t)t * 2 * W + q]);
-              return m == 0;
-            },
-            [&](int slot, int t) { l0[slot] = (int16_t)t; }, ctmp);
-        if (tid == 0) s_nl0 = nl0;
-        __syncthreads();
-      }
       const int symR = e2 >= 0 ? p.its[p.orbsym[o1]][p.orbsym[o2]] : p.orbsym[o1];
       // added-orbital space
       int nA;
@@ -898,117 +842,89 @@ __global__ void __launch_bounds__(kThreads, 2) k_pt2(Params p) {
       } else {
         nA = sh.nvir[0] * sh.nvir[1];
       }
-      for (int t = tid; t < nA; t += blockDim.x) {
-        int a1, a2 = -1, sa1 = sp1, sa2 = sp2;
-        if (nRr == 1) {
-          a1 = sh.vir[sp1][t];
-        } else if (sp1 == sp2) {
-          // t -> (x < y) over nv1 virtuals
-          int x = 0, tt = t;
-          while (tt >= nv1 - 1 - x) {
-            tt -= nv1 - 1 - x;
-            ++x;
-          }
-          a1 = sh.vir[sp1][x];
-          a2 = sh.vir[sp1][x + 1 + tt];
-        } else {
-          a1 = sh.vir[0][t / sh.nvir[1]];
-          a2 = sh.vir[1][t % sh.nvir[1]];
-          sa1 = 0;
-          sa2 = 1;
-        }
-        const int aV = (a1 >= p.noca ? 1 : 0) + (a2 >= 0 && a2 >= p.noca ? 1 : 0);
-        const int D = hfR + aV - nRr;
-        if (!(dmask & (1u << (D + 2)))) continue;
-        const int symA = a2 >= 0 ? p.its[p.orbsym[a1]][p.orbsym[a2]] : p.orbsym[a1];
-        if (p.its[symR][symA] != 0) continue;
-        // diexcit spin patterns for generators without a flip partner
+      for (int t0 = 0; t0 < nA; t0 += blockDim.x) {
+        const int t = t0 + tid;
+        bool live = t < nA;
+        int a1 = 0, a2 = -1, sa1 = sp1, sa2 = sp2, D = 0;
         bool ysyspi = true;
-        if (D == 2) {
-          if (sp1 != sp2) {
-            // alpha hole orbital a, beta hole b, alpha particle c, beta particle d
-            const int ha = o1, hb = o2, pc = a1, pd = a2;  // sp1 = alpha, sp2 = beta
-            ysyspi = !(ha == hb && pc == pd);
-            const bool unflipped = (ha < hb) || (ha == hb && pc <= pd);
-            if (!yefk && !unflipped) continue;
+        if (live) {
+          if (nRr == 1) {
+            a1 = sh.vir[sp1][t];
+          } else if (sp1 == sp2) {
+            // t -> (x < y) over nv1 virtuals
+            int x = 0, tt = t;
+            while (tt >= nv1 - 1 - x) {
+              tt -= nv1 - 1 - x;
+              ++x;
+            }
+            a1 = sh.vir[sp1][x];
+            a2 = sh.vir[sp1][x + 1 + tt];
           } else {
-            if (!yefk && sp1 == 1) continue;
+            a1 = sh.vir[0][t / sh.nvir[1]];
+            a2 = sh.vir[1][t % sh.nvir[1]];
+            sa1 = 0;
+            sa2 = 1;
+          }
+          const int aV = (a1 >= p.noca ? 1 : 0) + (a2 >= 0 && a2 >= p.noca ? 1 : 0);
+          D = hfR + aV - nRr;
+          if (!(dmask & (1u << (D + 2)))) live = false;
+          const int symA = a2 >= 0 ? p.its[p.orbsym[a1]][p.orbsym[a2]] : p.orbsym[a1];
+          if (p.its[symR][symA] != 0) live = false;
+          // diexcit spin patterns for generators without a flip partner
+          if (live && D == 2) {
+            if (sp1 != sp2) {
+              // alpha hole orbital o1, beta hole o2, alpha particle a1, beta particle a2
+              ysyspi = !(o1 == o2 && a1 == a2);
+              const bool unflipped = (o1 < o2) || (o1 == o2 && a1 <= a2);
+              if (!yefk && !unflipped) live = false;
+            } else if (!yefk && sp1 == 1) {
+              live = false;
+            }
           }
         }
-        acc.ncand++;
         uint64_t u[2 * W];
 #pragma unroll
         for (int q = 0; q < 2 * W; ++q) u[q] = kp[q];
-        u[sa1 * W + (a1 >> 6)] |= (1ull << (a1 & 63));
-        if (a2 >= 0) u[sa2 * W + (a2 >> 6)] |= (1ull << (a2 & 63));
-        const int rankI = rank_k + D;
         double bc[R];
 #pragma unroll
         for (int m = 0; m < R; ++m) bc[m] = 0.0;
         int nint = 0, nnz = 0, lesp = 0;
-        bool drop = false;
-        // one S determinant of L_R against I: owner test, already-in-S test,
-        // <I|H|j> accumulation; returns true when I is dropped
-        // mode 0: tests and matrix element; 1: owner / already-in-S tests only;
-        // 2: matrix element only (tests done by a mode-1 pass)
-        auto visit = [&](int i, int x, int mode) -> bool {
-          uint64_t vv[2 * W];
-          int j;
-          if (fast) {
-            j = lr_j[i];
+        if (live) {
+          acc.ncand++;
+          u[sa1 * W + (a1 >> 6)] |= (1ull << (a1 & 63));
+          if (a2 >= 0) u[sa2 * W + (a2 >> 6)] |= (1ull << (a2 & 63));
+          const int rankI = rank_k + D;
+          bool drop = false;
+          // one S determinant of L_R against I: owner test, already-in-S
+          // test, <I|H|j> accumulation; returns true when I is dropped
+          auto visit = [&](int i, int x) -> bool {
+            uint64_t vv[2 * W];
+            int j;
+            if (fast) {
+              j = lr_j[i];
 #pragma unroll
-            for (int q = 0; q < 2 * W; ++q) vv[q] = lr_bits[(size_t)i * 2 * W + q];
-          } else {
-            j = my_lr_idx[i];
+              for (int q = 0; q < 2 * W; ++q) vv[q] = lr_bits[(size_t)i * 2 * W + q];
+            } else {
+              j = my_lr_idx[i];
 #pragma unroll
-            for (int q = 0; q < 2 * W; ++q) vv[q] = __ldg(&p.S[(size_t)j * 2 * W + q]);
-          }
-          if (x < 0) {
-            x = 0;
-#pragma unroll
-            for (int q = 0; q < 2 * W; ++q) x += __popcll(u[q] ^ vv[q]);
-          }
-          if (x > 4) return false;
-          if (j < k) return mode != 2 && p.ygen[j] != 0;
-          if (x == 0) return mode != 2;
-          if (mode == 1) return false;
-          int rankJ = 0;
-#pragma unroll
-          for (int q = 0; q < 2 * W; ++q) rankJ += __popcll(hf[q] & ~vv[q]);
-          int kind;
-          const double h = hmat<W>(p, u, vv, rankI, rankJ, hf, kind);
-          if (kind == 1) acc.np1++; else acc.np2++;
-          ++nint;
-          if (h != 0.0) ++nnz;
-          if (j > k && j <= k + nespk) ++lesp;
-#pragma unroll
-          for (int m = 0; m < R; ++m)
-            if (m < p.metat) bc[m] += h * __ldg(&p.c[(size_t)j * p.metat + m]);
-          return false;
-        };
-        if (indexed) {
-          // only the determinants that can be within two excitations of I
-          const int so1 = a1 + sa1 * p.norb, so2 = a2 + sa2 * p.norb;
-          const int w1 = sa1 * W + (a1 >> 6), w2 = sa2 * W + (a2 >> 6);
-          const uint64_t b1 = 1ull << (a1 & 63), b2 = 1ull << (a2 & 63);
-          const int nvis = s_nl0 + (boff[0][so1 + 1] - boff[0][so1]) + (boff[0][so2 + 1] - boff[0][so2]) +
-                           (boff[1][so1 + 1] - boff[1][so1]);
-          // pass 0: owner and already-in-S tests; pass 1: matrix elements
-          for (int pass = 0; pass < 2 && !drop; ++pass) {
-            const int chk = pass == 0 ? 1 : 2;
-            for (int q = 0; q < s_nl0 && !drop; ++q) drop = visit(l0[q], -1, chk);
-            for (int q = boff[0][so1]; q < boff[0][so1 + 1] && !drop; ++q) drop = visit(bkt1[q], -1, chk);
-            for (int q = boff[0][so2]; q < boff[0][so2 + 1] && !drop; ++q) {
-              const int i = bkt1[q];
-              if (!(lr_bits[(size_t)i * 2 * W + w1] & b1)) drop = visit(i, -1, chk);
+              for (int q = 0; q < 2 * W; ++q) vv[q] = __ldg(&p.S[(size_t)j * 2 * W + q]);
             }
-            for (int q = boff[1][so1]; q < boff[1][so1 + 1] && !drop; ++q) {
-              const int i = bkt2[q];
-              if (lr_bits[(size_t)i * 2 * W + w2] & b2) drop = visit(i, -1, chk);
-            }
-          }
-          acc.ncmp += (unsigned long long)nvis;
-        } else {
+            if (j < k) return p.ygen[j] != 0;
+            if (x == 0) return true;
+            int rankJ = 0;
+#pragma unroll
+            for (int q = 0; q < 2 * W; ++q) rankJ += __popcll(hf[q] & ~vv[q]);
+            int kind;
+            const double h = hmat<W>(p, u, vv, rankI, rankJ, hf, kind);
+            if (kind == 1) acc.np1++; else acc.np2++;
+            ++nint;
+            if (h != 0.0) ++nnz;
+            if (j > k && j <= k + nespk) ++lesp;
+#pragma unroll
+            for (int m = 0; m < R; ++m)
+              if (m < p.metat) bc[m] += h * __ldg(&p.c[(size_t)j * p.metat + m]);
+            return false;
+          };
           for (int i0 = 0; i0 < nlr && !drop; i0 += 4) {
             // four independent compares per step (latency of the loads overlaps)
             int xs[4];
@@ -1032,46 +948,44 @@ __global__ void __launch_bounds__(kThreads, 2) k_pt2(Params p) {
             if (xs[0] > 4 && xs[1] > 4 && xs[2] > 4 && xs[3] > 4) continue;
 #pragma unroll 1
             for (int g4 = 0; g4 < 4 && !drop; ++g4)
-              if (xs[g4] <= 4) drop = visit(i0 + g4, xs[g4], 0);
+              if (xs[g4] <= 4) drop = visit(i0 + g4, xs[g4]);
           }
           acc.ncmp += (unsigned long long)nlr;
+          if (drop || nint == 0) live = false;
+          if (live && D == 2 && nnz == 0) live = false;  // diexcit drops zero couplings
         }
-        if (drop || nint == 0) continue;
         const bool is_pert1 = (D != 2);
-        if (!is_pert1 && nnz == 0) continue;
-        double fmul;
-        int nmul;
-        bool ybis;
-        if (is_pert1) {
-          if (nespk != 0) {
-            ybis = true;
-            fmul = (1.0 / (double)(lesp + 1)) * (double)(nespk + 1) - 1.0;
-            nmul = (int)fmul;
+        double fmul = 0.0, hmpi = 0.0, hvpi = 0.0;
+        int nmul = 0;
+        bool ybis = false;
+        if (live) {
+          if (is_pert1) {
+            if (nespk != 0) {
+              ybis = true;
+              fmul = (1.0 / (double)(lesp + 1)) * (double)(nespk + 1) - 1.0;
+              nmul = (int)fmul;
+            }
           } else {
-            ybis = false;
-            fmul = 0.0;
-            nmul = 0;
+            int nespf = nespk;
+            ybis = nespf > 0;
+            if (yefk || ysyspi) {
+              ybis = true;
+              if (!yefk) nespf = nespf + nespf + 1;
+            }
+            fmul = (1.0 / (double)(lesp + 1)) * (double)(nespf + 1) - 1.0;
+            nmul = (int)fmul;
           }
-        } else {
-          int nespf = nespk;
-          ybis = nespf > 0;
-          if (yefk || ysyspi) {
-            ybis = true;
-            if (!yefk) nespf = nespf + nespf + 1;
+          hmpi = sh.mK + __ldg(&p.fmpb[a1 + sa1 * p.norb]);
+          hvpi = sh.hK + sh.vdg[a1 + sa1 * p.norb];
+          if (a2 >= 0) {
+            hmpi += __ldg(&p.fmpb[a2 + sa2 * p.norb]);
+            const int tq = tri(a1, a2);
+            double gq = __ldg(&p.J[tq]);
+            if (sa1 == sa2) gq -= __ldg(&p.K[tq]);
+            hvpi += sh.vdg[a2 + sa2 * p.norb] + gq;
           }
-          fmul = (1.0 / (double)(lesp + 1)) * (double)(nespf + 1) - 1.0;
-          nmul = (int)fmul;
         }
-        double hmpi = sh.mK + __ldg(&p.fmpb[a1 + sa1 * p.norb]);
-        double hvpi = sh.hK + sh.vdg[a1 + sa1 * p.norb];
-        if (a2 >= 0) {
-          hmpi += __ldg(&p.fmpb[a2 + sa2 * p.norb]);
-          const int t = tri(a1, a2);
-          double g = __ldg(&p.J[t]);
-          if (sa1 == sa2) g -= __ldg(&p.K[t]);
-          hvpi += sh.vdg[a2 + sa2 * p.norb] + g;
-        }
-        finish_candidate<W, R>(p, u, hmpi, hvpi, bc, k1, fmul, nmul, ybis, is_pert1, acc, hist);
+        finish_candidate<W, R>(p, live, u, hmpi, hvpi, bc, k1, fmul, nmul, ybis, is_pert1, acc, hist);
       }
       __syncthreads();
     }
@@ -1588,7 +1502,7 @@ int cipsi_run_pt2_async(cipsi_ctx* ctx, const cipsi_opts* o) {
   int dev_sms = 0;
   CK(cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, ctx->device));
   // shared L_R capacity: enough for every neighbour list when it fits
-  const size_t per_entry = (size_t)2 * W * 8 + 4 + 2 * (1 + 3 + 4);
+  const size_t per_entry = (size_t)2 * W * 8 + 4;
   const size_t smem_budget = 150 * 1024;
   int lr_cap = (int)std::min<size_t>((size_t)ncf, smem_budget / per_entry);
   const size_t smem = (size_t)lr_cap * per_entry + 16;
@@ -1750,7 +1664,7 @@ int cipsi_fetch_result(cipsi_ctx* ctx, cipsi_result* r) {
   CK(cudaSetDevice(ctx->device));
   CK(cudaStreamSynchronize(ctx->stream));
   ctx->pending = false;
-  const int mt = ctx->d.metat, W = ctx->W;
+  const int mt = ctx->d.metat;
   memset(r, 0, sizeof(*r));
   std::vector<double> red(5 * mt);
   CK(cudaMemcpy(red.data(), ctx->dred, red.size() * sizeof(double), cudaMemcpyDeviceToHost));
