@@ -49,6 +49,7 @@ constexpr int kThreads = 256;
 constexpr int kMaxSym = 8;
 constexpr int kMaxElec = 64;
 constexpr int kMaxOrb = 128;
+constexpr int kRowCap = 128;  // per-warp list of |K' \ j| = 2 entries holding a1
 
 // counters[] slots
 enum {
@@ -91,6 +92,7 @@ struct Params {
   int yen, ysele, ymoyen, ywdeg, symvar, nclass;
   double tau, teseff;
   double aval[kNClass];
+  long long aval_bits[kNClass];  // bit patterns of aval (non-negative, ascending)
   int pertu_ref, pertu_mono;
   // scratch
   int32_t* nb_j;             // per block: ncf entries
@@ -357,11 +359,15 @@ struct SmemHist {
   double tab[2 * kNClass * kMaxRoots];
 };
 
+// histogram class of a non-negative value (cip/isto.f: first i with
+// val < aval(i)); compared as IEEE bit patterns, which order non-negative
+// doubles exactly as the values (integer pipe instead of FP64 compares)
 __device__ __forceinline__ int hist_class(const Params& p, double val) {
+  const long long v = __double_as_longlong(val);
   const int nc = p.nclass - 1;
-  for (int i = 0; i < nc; ++i)
-    if (val < p.aval[i]) return i;
-  return p.nclass - 1;
+  int c = 0;
+  for (int i = 0; i < nc; ++i) c += (v >= p.aval_bits[i]) ? 1 : 0;
+  return c;
 }
 
 // Everything the reference does with one candidate after its interaction
@@ -546,6 +552,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_pt2(Params p) {
   __shared__ SmemHist hist;
   __shared__ double red[5 * kMaxRoots * 32];
   __shared__ int ctmp[33];
+  __shared__ int16_t wrow[(kThreads / 32) * kRowCap];
 
   const int tid = threadIdx.x;
   // shared L_R arrays (fast path)
@@ -744,25 +751,28 @@ __global__ void __launch_bounds__(kThreads, 2) k_pt2(Params p) {
       }
       if (!any) continue;
       const uint64_t rmask = (1ull << e1) | (e2 >= 0 ? (1ull << e2) : 0ull);
-      // L_R (ascending j: the sums over interacting determinants run in a
-      // fixed order, so results are bitwise reproducible)
-      const int nlr = ordered_compact(
-          nnb,
-          [&](int t) {
-            const uint64_t em = my_nb_em[t];
-            return __popcll(em) - __popcll(em & rmask) <= 2;
-          },
-          [&](int slot, int t) {
-            const int j = my_nb_j[t];
-            if (slot < p.lr_cap) {
-              lr_j[slot] = j;
-              const uint64_t* v = p.S + (size_t)j * 2 * W;
+      // L_R, partitioned: entries with |K' \ j| <= 1 first, then those with
+      // |K' \ j| = 2; each part in ascending j, so every sum over interacting
+      // determinants runs in a fixed order (bitwise reproducible results)
+      auto lr_store = [&](int slot, int t) {
+        const int j = my_nb_j[t];
+        if (slot < p.lr_cap) {
+          lr_j[slot] = j;
+          const uint64_t* v = p.S + (size_t)j * 2 * W;
 #pragma unroll
-              for (int q = 0; q < 2 * W; ++q) lr_bits[(size_t)slot * 2 * W + q] = __ldg(&v[q]);
-            }
-            my_lr_idx[slot] = j;
-          },
+          for (int q = 0; q < 2 * W; ++q) lr_bits[(size_t)slot * 2 * W + q] = __ldg(&v[q]);
+        }
+        my_lr_idx[slot] = j;
+      };
+      auto lr_m = [&](int t) {
+        const uint64_t em = my_nb_em[t];
+        return __popcll(em) - __popcll(em & rmask);
+      };
+      const int n01 = ordered_compact(nnb, [&](int t) { return lr_m(t) <= 1; }, lr_store, ctmp);
+      const int n2 = ordered_compact(
+          nnb, [&](int t) { return lr_m(t) == 2; }, [&](int slot, int t) { lr_store(n01 + slot, t); },
           ctmp);
+      const int nlr = n01 + n2;
       const bool fast = nlr <= p.lr_cap;
       if (!fast && tid == 0) atomicAdd(&p.counters[C_LRFALLBACK], 1ull);
       // K' = k - R
@@ -833,8 +843,8 @@ __global__ void __launch_bounds__(kThreads, 2) k_pt2(Params p) {
       __syncthreads();
       const int symR = e2 >= 0 ? p.its[p.orbsym[o1]][p.orbsym[o2]] : p.orbsym[o1];
       // added-orbital space
-      int nA;
       const int nv1 = sh.nvir[sp1];
+      int nA;
       if (nRr == 1) {
         nA = nv1;
       } else if (sp1 == sp2) {
@@ -842,29 +852,15 @@ __global__ void __launch_bounds__(kThreads, 2) k_pt2(Params p) {
       } else {
         nA = sh.nvir[0] * sh.nvir[1];
       }
-      for (int t0 = 0; t0 < nA; t0 += blockDim.x) {
-        const int t = t0 + tid;
-        bool live = t < nA;
-        int a1 = 0, a2 = -1, sa1 = sp1, sa2 = sp2, D = 0;
+      // One candidate I = K' + {a1[, a2]}: rank-change class, symmetry and
+      // spin-pattern rules, then a scan of L_R entries [0, nscan) plus the
+      // listed entries rb[0..nrb) (owner test, already in S, <I|H|j>), then
+      // the E2 / selection epilogue.  Called by whole warps.
+      auto candidate = [&](bool live, int a1, int a2, int sa1, int sa2, int nscan, const int16_t* rb,
+                           int nrb) {
+        int D = 0;
         bool ysyspi = true;
         if (live) {
-          if (nRr == 1) {
-            a1 = sh.vir[sp1][t];
-          } else if (sp1 == sp2) {
-            // t -> (x < y) over nv1 virtuals
-            int x = 0, tt = t;
-            while (tt >= nv1 - 1 - x) {
-              tt -= nv1 - 1 - x;
-              ++x;
-            }
-            a1 = sh.vir[sp1][x];
-            a2 = sh.vir[sp1][x + 1 + tt];
-          } else {
-            a1 = sh.vir[0][t / sh.nvir[1]];
-            a2 = sh.vir[1][t % sh.nvir[1]];
-            sa1 = 0;
-            sa2 = 1;
-          }
           const int aV = (a1 >= p.noca ? 1 : 0) + (a2 >= 0 && a2 >= p.noca ? 1 : 0);
           D = hfR + aV - nRr;
           if (!(dmask & (1u << (D + 2)))) live = false;
@@ -925,14 +921,14 @@ __global__ void __launch_bounds__(kThreads, 2) k_pt2(Params p) {
               if (m < p.metat) bc[m] += h * __ldg(&p.c[(size_t)j * p.metat + m]);
             return false;
           };
-          for (int i0 = 0; i0 < nlr && !drop; i0 += 4) {
+          for (int i0 = 0; i0 < nscan && !drop; i0 += 4) {
             // four independent compares per step (latency of the loads overlaps)
             int xs[4];
 #pragma unroll
             for (int g4 = 0; g4 < 4; ++g4) {
               const int i = i0 + g4;
               int x = 99;
-              if (i < nlr) {
+              if (i < nscan) {
                 x = 0;
                 if (fast) {
 #pragma unroll
@@ -950,7 +946,14 @@ __global__ void __launch_bounds__(kThreads, 2) k_pt2(Params p) {
             for (int g4 = 0; g4 < 4 && !drop; ++g4)
               if (xs[g4] <= 4) drop = visit(i0 + g4, xs[g4]);
           }
-          acc.ncmp += (unsigned long long)nlr;
+          for (int q2 = 0; q2 < nrb && !drop; ++q2) {
+            const int i = rb[q2];
+            int x = 0;
+#pragma unroll
+            for (int q = 0; q < 2 * W; ++q) x += __popcll(u[q] ^ lr_bits[(size_t)i * 2 * W + q]);
+            if (x <= 4) drop = visit(i, x);
+          }
+          acc.ncmp += (unsigned long long)(nscan + nrb);
           if (drop || nint == 0) live = false;
           if (live && D == 2 && nnz == 0) live = false;  // diexcit drops zero couplings
         }
@@ -986,6 +989,73 @@ __global__ void __launch_bounds__(kThreads, 2) k_pt2(Params p) {
           }
         }
         finish_candidate<W, R>(p, live, u, hmpi, hvpi, bc, k1, fmul, nmul, ybis, is_pert1, acc, hist);
+      };
+      if (nRr == 1 || !fast) {
+        // flat: threads take candidates, every candidate scans all of L_R
+        for (int t0 = 0; t0 < nA; t0 += blockDim.x) {
+          const int t = t0 + tid;
+          const bool live = t < nA;
+          int a1 = 0, a2 = -1, sa1 = sp1, sa2 = sp2;
+          if (live) {
+            if (nRr == 1) {
+              a1 = sh.vir[sp1][t];
+            } else if (sp1 == sp2) {
+              // t -> (x < y) over nv1 virtuals
+              int x = 0, tt = t;
+              while (tt >= nv1 - 1 - x) {
+                tt -= nv1 - 1 - x;
+                ++x;
+              }
+              a1 = sh.vir[sp1][x];
+              a2 = sh.vir[sp1][x + 1 + tt];
+            } else {
+              a1 = sh.vir[0][t / sh.nvir[1]];
+              a2 = sh.vir[1][t % sh.nvir[1]];
+              sa1 = 0;
+              sa2 = 1;
+            }
+          }
+          candidate(live, a1, a2, sa1, sa2, nlr, nullptr, 0);
+        }
+      } else {
+        // rows: one warp per first added orbital a1; an entry with
+        // |K' \ j| = 2 interacts only if it occupies both added orbitals, so
+        // the warp lists the ones that occupy a1 and its lanes (columns a2)
+        // scan the |K' \ j| <= 1 part plus that short list
+        const int lane = tid & 31, wid = tid >> 5, nwarps = blockDim.x >> 5;
+        const bool same = sp1 == sp2;
+        const int sr = same ? sp1 : 0, sc = same ? sp1 : 1;
+        const int nrows = same ? nv1 - 1 : sh.nvir[0];
+        int16_t* rowbuf = wrow + wid * kRowCap;
+        for (int row = wid; row < nrows; row += nwarps) {
+          const int a1 = sh.vir[sr][row];
+          const int w1 = sr * W + (a1 >> 6);
+          const uint64_t b1 = 1ull << (a1 & 63);
+          int nrb = 0;
+          for (int i0 = n01; i0 < nlr; i0 += 32) {
+            const int i = i0 + lane;
+            const bool has = i < nlr && (lr_bits[(size_t)i * 2 * W + w1] & b1);
+            const unsigned bm = __ballot_sync(0xffffffffu, has);
+            if (has) {
+              const int pos = nrb + __popc(bm & ((1u << lane) - 1u));
+              if (pos < kRowCap) rowbuf[pos] = (int16_t)i;
+            }
+            nrb += __popc(bm);
+          }
+          __syncwarp();
+          const bool overflow = nrb > kRowCap;
+          const int ncols = same ? nv1 - 1 - row : sh.nvir[1];
+          for (int c0 = 0; c0 < ncols; c0 += 32) {
+            const int c = c0 + lane;
+            const bool live = c < ncols;
+            const int a2 = live ? (same ? sh.vir[sc][row + 1 + c] : sh.vir[sc][c]) : 0;
+            if (!overflow)
+              candidate(live, a1, a2, sr, sc, n01, rowbuf, nrb);
+            else
+              candidate(live, a1, a2, sr, sc, nlr, nullptr, 0);
+          }
+          __syncwarp();
+        }
       }
       __syncthreads();
     }
@@ -1610,7 +1680,13 @@ int cipsi_run_pt2_async(cipsi_ctx* ctx, const cipsi_opts* o) {
   p.nclass = o->nclass;
   p.tau = o->tau;
   p.teseff = o->teseff;
-  for (int i = 0; i < kNClass; ++i) p.aval[i] = o->aval[i];
+  for (int i = 0; i < kNClass; ++i) {
+    p.aval[i] = o->aval[i];
+    std::memcpy(&p.aval_bits[i], &o->aval[i], 8);
+  }
+  for (int i = 0; i + 1 < o->nclass; ++i)
+    if (!(o->aval[i] >= 0.0) || (i > 0 && !(o->aval[i] > o->aval[i - 1])))
+      return fail(ctx, CIPSI_ERR_ARG, "aval must be non-negative and increasing");
   p.pertu_ref = pertu_ref ? 1 : 0;
   p.pertu_mono = pertu_mono ? 1 : 0;
   p.nb_j = ctx->dnb_j;
