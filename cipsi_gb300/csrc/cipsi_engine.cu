@@ -353,6 +353,25 @@ struct Acc {
   }
 };
 
+// One thread's histogram (cip/isto.f): class sums and counts, indexed by
+// class at run time, so it lives in local memory (L1-resident); one FP64 add
+// per contribution, no atomics; merged into the block's at kernel end.
+template <int R>
+struct HistPriv {
+  double tab[kNClass][2][R];
+  unsigned long long nom[kNClass];
+  unsigned long long nam[kNClass][R];
+  __device__ void zero() {
+    for (int c = 0; c < kNClass; ++c) {
+      nom[c] = 0ull;
+      for (int m = 0; m < R; ++m) {
+        tab[c][0][m] = tab[c][1][m] = 0.0;
+        nam[c][m] = 0ull;
+      }
+    }
+  }
+};
+
 struct SmemHist {
   unsigned long long nom[kNClass];
   unsigned long long nam[kNClass * kMaxRoots];
@@ -377,7 +396,7 @@ template <int W, int R>
 __device__ void finish_candidate(const Params& p, bool live, const uint64_t* u, double hmpi,
                                  double hvpi, const double* bc, int owner1 /*1-based, 0 = pertu*/,
                                  double fmul, int nmul, bool ybis, bool is_pert1, Acc<R>& acc,
-                                 SmemHist& hist) {
+                                 HistPriv<R>& hp) {
   constexpr unsigned kFull = 0xffffffffu;
   const int lane = threadIdx.x & 31;
   double xam = 0.0;
@@ -428,43 +447,17 @@ __device__ void finish_candidate(const Params& p, bool live, const uint64_t* u, 
     acc.ietat += (unsigned long long)(long long)(nmul + 1);
     acc.nproc += 1;
   }
-  // histogram (cip/isto.f; pert1 calls it always, diexcit only if ymoyen),
-  // reduced over the warp first: one shared-memory atomic per class present
-  const bool in_hist = live && (is_pert1 || p.ymoyen) && xam >= p.teseff;
-  const int cls = in_hist ? hist_class(p, xam) : -1;
-  const double fm = fmul + 1.0;
-  unsigned present = __reduce_or_sync(kFull, in_hist ? (1u << cls) : 0u);
-  while (present) {
-    const int c = __ffs(present) - 1;
-    present &= present - 1;
-    const bool in = cls == c;
-    const unsigned cnt = __reduce_add_sync(kFull, in ? (unsigned)(1 + nmul) : 0u);
-    if (lane == 0) atomicAdd(&hist.nom[c], (unsigned long long)cnt);
+  // histogram (cip/isto.f; pert1 calls it always, diexcit only if ymoyen)
+  if (live && (is_pert1 || p.ymoyen) && xam >= p.teseff) {
+    const double fm = fmul + 1.0;
+    const int cls = hist_class(p, xam);
+    hp.nom[cls] += (unsigned long long)(1 + nmul);
 #pragma unroll
     for (int m = 0; m < R; ++m) {
-      if (m >= p.metat) break;
-      const bool inm = in && vil[m] >= p.teseff;
-      double v1 = inm ? semp[m] * fm : 0.0, v2 = inm ? sevp[m] * fm : 0.0;
-      for (int o = 16; o > 0; o >>= 1) {
-        v1 += __shfl_xor_sync(kFull, v1, o);
-        v2 += __shfl_xor_sync(kFull, v2, o);
-      }
-      if (lane == 0) {
-        if (v1 != 0.0) atomicAdd(&hist.tab[c * kMaxRoots + m], v1);
-        if (v2 != 0.0) atomicAdd(&hist.tab[kNClass * kMaxRoots + c * kMaxRoots + m], v2);
-      }
-    }
-  }
-#pragma unroll
-  for (int m = 0; m < R; ++m) {
-    if (m >= p.metat) break;
-    const int c2 = (in_hist && vil[m] >= p.teseff) ? hist_class(p, vil[m]) : -1;
-    unsigned pr = __reduce_or_sync(kFull, c2 >= 0 ? (1u << c2) : 0u);
-    while (pr) {
-      const int c = __ffs(pr) - 1;
-      pr &= pr - 1;
-      const unsigned cnt = __reduce_add_sync(kFull, c2 == c ? (unsigned)(1 + nmul) : 0u);
-      if (lane == 0) atomicAdd(&hist.nam[c * kMaxRoots + m], (unsigned long long)cnt);
+      if (m >= p.metat || vil[m] < p.teseff) continue;
+      hp.tab[cls][0][m] += semp[m] * fm;
+      hp.tab[cls][1][m] += sevp[m] * fm;
+      hp.nam[hist_class(p, vil[m])][m] += (unsigned long long)(1 + nmul);
     }
   }
   if (ydeg) xam = 1.0;
@@ -578,6 +571,8 @@ __global__ void __launch_bounds__(kThreads, 2) k_pt2(Params p) {
 
   Acc<R> acc;
   acc.zero();
+  HistPriv<R> hp;
+  hp.zero();
   const int ncf = p.ncf;
 
   for (;;) {
@@ -648,7 +643,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_pt2(Params p) {
           if (drop || nint == 0) live = false;
           if (live) diag_terms<W>(p, u, hf, hmpi, hvpi, p.yen != 0);
         }
-        finish_candidate<W, R>(p, live, u, hmpi, hvpi, bc, 0, 0.0, 0, false, true, acc, hist);
+        finish_candidate<W, R>(p, live, u, hmpi, hvpi, bc, 0, 0.0, 0, false, true, acc, hp);
       }
       block_flush<R>(p, acc, unit, red);
       continue;
@@ -988,7 +983,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_pt2(Params p) {
             hvpi += sh.vdg[a2 + sa2 * p.norb] + gq;
           }
         }
-        finish_candidate<W, R>(p, live, u, hmpi, hvpi, bc, k1, fmul, nmul, ybis, is_pert1, acc, hist);
+        finish_candidate<W, R>(p, live, u, hmpi, hvpi, bc, k1, fmul, nmul, ybis, is_pert1, acc, hp);
       };
       if (nRr == 1 || !fast) {
         // flat: threads take candidates, every candidate scans all of L_R
@@ -1078,6 +1073,17 @@ __global__ void __launch_bounds__(kThreads, 2) k_pt2(Params p) {
     }
     if ((tid & 31) == 0) atomicMax(p.dpivot_bits, db);
   }
+  // this thread's histogram into the block's
+  for (int c = 0; c < p.nclass; ++c) {
+    if (hp.nom[c]) atomicAdd(&hist.nom[c], hp.nom[c]);
+    for (int m = 0; m < R && m < p.metat; ++m) {
+      if (hp.tab[c][0][m] != 0.0) atomicAdd(&hist.tab[c * kMaxRoots + m], hp.tab[c][0][m]);
+      if (hp.tab[c][1][m] != 0.0)
+        atomicAdd(&hist.tab[kNClass * kMaxRoots + c * kMaxRoots + m], hp.tab[c][1][m]);
+      if (hp.nam[c][m]) atomicAdd(&hist.nam[c * kMaxRoots + m], hp.nam[c][m]);
+    }
+  }
+  __syncthreads();
   for (int i = tid; i < p.nclass; i += blockDim.x)
     if (hist.nom[i]) atomicAdd(&p.hist_nom[i], hist.nom[i]);
   for (int i = tid; i < p.nclass * kMaxRoots; i += blockDim.x) {
