@@ -412,26 +412,42 @@ __device__ void finish_candidate(const Params& p, bool live, const uint64_t* u, 
     if (!live || m >= p.metat) continue;
     const double bcalc = bc[m];
     const double dmp = p.emp[m] - hmpi;
-    const double cimp = bcalc / dmp;
-    const double car = cimp * cimp;
-    const double eimp = bcalc * cimp;
-    kahan_add(acc.e2mp[m], acc.cmp[m], eimp * wgt);
-    acc.psimp[m] += car * wgt;
-    double xim = p.ysele ? fabs(eimp) : fabs(cimp);
-    double deno = dmp, eim = eimp;
-    double eivp = 0.0;
+    double eivp = 0.0, cimp, xim, deno, eim;
     if (p.yen) {
+      // the three denominators share one FP64 division (GB300's FP64 rate is
+      // 1/64 of FP32): r = 1/(dmp*dvp*db), 1/dmp = dvp*db*r, etc.
       const double dvp = p.e[m] - hvpi;
-      const double civp = bcalc / dvp;
+      const double db = p.eb[m] - hvpi;
+      const double pvb = dvp * db;
+      const double prod = dmp * pvb;
+      double civp, cib;
+      if (fabs(prod) > 1.0e-280 && fabs(prod) < 1.0e280) {
+        const double r = 1.0 / prod;
+        cimp = bcalc * (pvb * r);
+        civp = bcalc * ((dmp * db) * r);
+        cib = bcalc * ((dmp * dvp) * r);
+      } else {  // a denominator at (or near) zero or huge: divide one by one
+        cimp = bcalc / dmp;
+        civp = bcalc / dvp;
+        cib = bcalc / db;
+      }
       eivp = bcalc * civp;
       kahan_add(acc.e2vp[m], acc.cvp[m], eivp * wgt);
-      acc.psivp[m] += (civp * civp) * wgt;
+      acc.psivp[m] = fma(civp * civp, wgt, acc.psivp[m]);
+      kahan_add(acc.e2b[m], acc.cb[m], (bcalc * cib) * wgt);
       xim = p.ysele ? fabs(eivp) : fabs(civp);
       deno = dvp;
       eim = eivp;
-      const double db = p.eb[m] - hvpi;
-      const double eib = bcalc * (bcalc / db);
-      kahan_add(acc.e2b[m], acc.cb[m], eib * wgt);
+    } else {
+      cimp = bcalc / dmp;
+    }
+    const double eimp = bcalc * cimp;
+    kahan_add(acc.e2mp[m], acc.cmp[m], eimp * wgt);
+    acc.psimp[m] = fma(cimp * cimp, wgt, acc.psimp[m]);
+    if (!p.yen) {
+      xim = p.ysele ? fabs(eimp) : fabs(cimp);
+      deno = dmp;
+      eim = eimp;
     }
     if (!(fabs(deno) > 0.05) && !(fabs(eim) < 1.0e-6) && p.ywdeg) ydeg = true;
     if (xim < p.teste[m]) acc.dpivot = fmax(acc.dpivot, xim);
