@@ -300,6 +300,22 @@ __device__ void diag_terms(const Params& p, const uint64_t* u, const uint64_t* h
   hdigi = e;
 }
 
+// bit patterns of 0.05, 1e-6 and +inf
+constexpr long long kBits005 = 0x3fa999999999999all;
+constexpr long long kBits1em6 = 0x3eb0c6f7a0b5ed8dll;
+constexpr long long kBitsInf = 0x7ff0000000000000ll;
+// a < b for a >= 0 (a may be NaN: false), b >= 0
+__device__ __forceinline__ bool lt_nonneg(double a, double b) {
+  const long long x = __double_as_longlong(a), y = __double_as_longlong(b);
+  return x < y && x <= kBitsInf;
+}
+// max of a >= 0 (not NaN) and b >= 0 (may be NaN: fmax ignores it)
+__device__ __forceinline__ double max_nonneg(double a, double b) {
+  const long long x = __double_as_longlong(a), y = __double_as_longlong(b);
+  if (y > kBitsInf) return a;
+  return __longlong_as_double(x > y ? x : y);
+}
+
 __device__ __forceinline__ void kahan_add(double& s, double& c, double x) {
   const double y = x - c;
   const double t = s + y;
@@ -449,12 +465,16 @@ __device__ void finish_candidate(const Params& p, bool live, const uint64_t* u, 
       deno = dmp;
       eim = eimp;
     }
-    if (!(fabs(deno) > 0.05) && !(fabs(eim) < 1.0e-6) && p.ywdeg) ydeg = true;
-    if (xim < p.teste[m]) acc.dpivot = fmax(acc.dpivot, xim);
+    // comparisons of magnitudes on their IEEE bit patterns (exact for
+    // non-negative doubles; NaN compares as in the reference: never below)
+    const long long bdeno = __double_as_longlong(deno) & 0x7fffffffffffffffll;
+    const long long beim = __double_as_longlong(eim) & 0x7fffffffffffffffll;
+    if (!(bdeno > kBits005 && bdeno <= kBitsInf) && !(beim < kBits1em6) && p.ywdeg) ydeg = true;
+    if (lt_nonneg(xim, p.teste[m])) acc.dpivot = max_nonneg(acc.dpivot, xim);
     if (p.ymoyen) {
       xim = xim * p.taum[m];
       vil[m] = xim;
-      xam = fmax(xam, xim);
+      xam = max_nonneg(xam, xim);
     }
     semp[m] = eimp;
     sevp[m] = eivp;
@@ -535,6 +555,76 @@ __device__ void block_flush(const Params& p, Acc<R>& acc, int gslot, double* red
   }
 }
 
+// Per-warp queue of perturbers that survived the interaction scan.  The
+// FP64 epilogue (denominators, E2, selection) then runs on full warps: the
+// FP64 pipe of GB300 is narrow, and a warp instruction costs the same with
+// 32 lanes or with the few that would be live at the candidate level.
+constexpr int kQCap = 64;
+template <int W, int R>
+struct WarpQueue {
+  uint64_t u[2 * W][kQCap];
+  double bc[R][kQCap];
+  double hmp[kQCap], hvp[kQCap], fmul[kQCap];
+  int nmul[kQCap], owner[kQCap];
+  unsigned char flags[kQCap];  // bit 0 ybis, bit 1 is_pert1
+};
+
+// Enqueue the live lanes' perturbers (called by a whole warp); runs the
+// epilogue on every full batch of 32.
+template <int W, int R>
+__device__ void enqueue_candidate(const Params& p, WarpQueue<W, R>& q, int& qn, bool live,
+                                  const uint64_t* u, double hmpi, double hvpi, const double* bc,
+                                  int owner1, double fmul, int nmul, bool ybis, bool is_pert1,
+                                  Acc<R>& acc, HistPriv<R>& hp);
+
+template <int W, int R>
+__device__ void drain_queue(const Params& p, WarpQueue<W, R>& q, int& qn, bool all, Acc<R>& acc,
+                            HistPriv<R>& hp) {
+  const int lane = threadIdx.x & 31;
+  while (qn >= 32 || (all && qn > 0)) {
+    const int base = qn >= 32 ? qn - 32 : 0;
+    const int cnt = qn >= 32 ? 32 : qn;
+    const bool live = lane < cnt;
+    const int e = base + (live ? lane : 0);
+    uint64_t u[2 * W];
+#pragma unroll
+    for (int w = 0; w < 2 * W; ++w) u[w] = q.u[w][e];
+    double bc[R];
+#pragma unroll
+    for (int m = 0; m < R; ++m) bc[m] = q.bc[m][e];
+    const unsigned char f = q.flags[e];
+    finish_candidate<W, R>(p, live, u, q.hmp[e], q.hvp[e], bc, q.owner[e], q.fmul[e], q.nmul[e],
+                           (f & 1) != 0, (f & 2) != 0, acc, hp);
+    __syncwarp();
+    qn = base;
+  }
+}
+
+template <int W, int R>
+__device__ void enqueue_candidate(const Params& p, WarpQueue<W, R>& q, int& qn, bool live,
+                                  const uint64_t* u, double hmpi, double hvpi, const double* bc,
+                                  int owner1, double fmul, int nmul, bool ybis, bool is_pert1,
+                                  Acc<R>& acc, HistPriv<R>& hp) {
+  const int lane = threadIdx.x & 31;
+  const unsigned lm = __ballot_sync(0xffffffffu, live);
+  if (live) {
+    const int e = qn + __popc(lm & ((1u << lane) - 1u));
+#pragma unroll
+    for (int w = 0; w < 2 * W; ++w) q.u[w][e] = u[w];
+#pragma unroll
+    for (int m = 0; m < R; ++m) q.bc[m][e] = bc[m];
+    q.hmp[e] = hmpi;
+    q.hvp[e] = hvpi;
+    q.fmul[e] = fmul;
+    q.nmul[e] = nmul;
+    q.owner[e] = owner1;
+    q.flags[e] = (unsigned char)((ybis ? 1 : 0) | (is_pert1 ? 2 : 0));
+  }
+  qn += __popc(lm);
+  __syncwarp();
+  drain_queue<W, R>(p, q, qn, false, acc, hp);
+}
+
 // ------------------------------------------------------------------ kernel
 struct BlockShared {
   double vdg[2 * kMaxOrb];  // hdig(K'+a) - hdig(K') without the pair term
@@ -567,6 +657,10 @@ __global__ void __launch_bounds__(kThreads, 2) k_pt2(Params p) {
   // shared L_R arrays (fast path)
   uint64_t* lr_bits = reinterpret_cast<uint64_t*>(dyn);          // cap x 2W
   int32_t* lr_j = reinterpret_cast<int32_t*>(lr_bits + (size_t)p.lr_cap * 2 * W);
+  // per-warp epilogue queues, 16-byte aligned after the L_R arrays
+  const size_t qoff = (((size_t)p.lr_cap * (2 * W * 8 + 4)) + 15) & ~(size_t)15;
+  WarpQueue<W, R>& wq = reinterpret_cast<WarpQueue<W, R>*>(dyn + qoff)[threadIdx.x >> 5];
+  int qn = 0;
   int32_t* my_nb_j = p.nb_j + (size_t)blockIdx.x * p.ncf;
   uint64_t* my_nb_em = p.nb_emask + (size_t)blockIdx.x * p.ncf;
   int32_t* my_lr_idx = p.lr_idx + (size_t)blockIdx.x * p.ncf;
@@ -659,8 +753,9 @@ __global__ void __launch_bounds__(kThreads, 2) k_pt2(Params p) {
           if (drop || nint == 0) live = false;
           if (live) diag_terms<W>(p, u, hf, hmpi, hvpi, p.yen != 0);
         }
-        finish_candidate<W, R>(p, live, u, hmpi, hvpi, bc, 0, 0.0, 0, false, true, acc, hp);
+        enqueue_candidate<W, R>(p, wq, qn, live, u, hmpi, hvpi, bc, 0, 0.0, 0, false, true, acc, hp);
       }
+      drain_queue<W, R>(p, wq, qn, true, acc, hp);
       block_flush<R>(p, acc, unit, red);
       continue;
     }
@@ -999,7 +1094,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_pt2(Params p) {
             hvpi += sh.vdg[a2 + sa2 * p.norb] + gq;
           }
         }
-        finish_candidate<W, R>(p, live, u, hmpi, hvpi, bc, k1, fmul, nmul, ybis, is_pert1, acc, hp);
+        enqueue_candidate<W, R>(p, wq, qn, live, u, hmpi, hvpi, bc, k1, fmul, nmul, ybis, is_pert1, acc, hp);
       };
       if (nRr == 1 || !fast) {
         // flat: threads take candidates, every candidate scans all of L_R
@@ -1070,6 +1165,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_pt2(Params p) {
       }
       __syncthreads();
     }
+    drain_queue<W, R>(p, wq, qn, true, acc, hp);
     block_flush<R>(p, acc, unit, red);
   }
 
@@ -1461,10 +1557,23 @@ int cipsi_set_roots(cipsi_ctx* ctx, const double* c, const double* e, const doub
 
 }  // extern "C"
 
+static size_t queue_bytes(int W, int R) {
+  switch (W * 16 + R) {
+    case 16 + 1: return sizeof(WarpQueue<1, 1>);
+    case 16 + 2: return sizeof(WarpQueue<1, 2>);
+    case 16 + 4: return sizeof(WarpQueue<1, 4>);
+    case 16 + 8: return sizeof(WarpQueue<1, 8>);
+    case 32 + 1: return sizeof(WarpQueue<2, 1>);
+    case 32 + 2: return sizeof(WarpQueue<2, 2>);
+    case 32 + 4: return sizeof(WarpQueue<2, 4>);
+    default: return sizeof(WarpQueue<2, 8>);
+  }
+}
+
 template <int W, int R>
 static cudaError_t launch_pt2(const Params& p, int grid, size_t smem, cudaStream_t st) {
   cudaError_t e = cudaFuncSetAttribute(k_pt2<W, R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       160 * 1024);
+                                       (int)smem);
   if (e != cudaSuccess) return e;
   k_pt2<W, R><<<grid, kThreads, smem, st>>>(p);
   return cudaGetLastError();
@@ -1595,10 +1704,11 @@ int cipsi_run_pt2_async(cipsi_ctx* ctx, const cipsi_opts* o) {
   CK(cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, ctx->device));
   // shared L_R capacity: enough for every neighbour list when it fits
   const size_t per_entry = (size_t)2 * W * 8 + 4;
-  const size_t smem_budget = 150 * 1024;
+  const size_t qbytes = (size_t)(kThreads / 32) * queue_bytes(W, mt <= 1 ? 1 : mt <= 2 ? 2 : mt <= 4 ? 4 : 8);
+  const size_t smem_budget = (size_t)200 * 1024 - qbytes;  // L_R share of the dynamic smem
   int lr_cap = (int)std::min<size_t>((size_t)ncf, smem_budget / per_entry);
-  const size_t smem = (size_t)lr_cap * per_entry + 16;
-  const int blocks_per_sm = smem <= 90 * 1024 ? 2 : 1;
+  const size_t smem = (((size_t)lr_cap * per_entry + 15) & ~(size_t)15) + qbytes + 16;
+  const int blocks_per_sm = smem <= 95 * 1024 ? 2 : 1;
   int grid = std::max(1, std::min(nunits, dev_sms * blocks_per_sm));
   // buffers
   if ((size_t)grid > ctx->scratch_blocks || !ctx->dnb_j) {
