@@ -578,7 +578,7 @@ __device__ void enqueue_candidate(const Params& p, WarpQueue<W, R>& q, int& qn, 
                                   Acc<R>& acc, HistPriv<R>& hp);
 
 template <int W, int R>
-__device__ void drain_queue(const Params& p, WarpQueue<W, R>& q, int& qn, bool all, Acc<R>& acc,
+__device__ __noinline__ void drain_queue(const Params& p, WarpQueue<W, R>& q, int& qn, bool all, Acc<R>& acc,
                             HistPriv<R>& hp) {
   const int lane = threadIdx.x & 31;
   while (qn >= 32 || (all && qn > 0)) {
