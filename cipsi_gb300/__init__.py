@@ -26,7 +26,7 @@ EXPORTED = [
     "cipsi_set_integrals", "cipsi_set_integrals_fp64", "cipsi_set_space", "cipsi_set_roots",
     "cipsi_run_pt2", "cipsi_run_pt2_async", "cipsi_fetch_result", "cipsi_selection_get",
     "cipsi_cip_main", "cipsi_inputs_read", "cipsi_inputs_dims", "cipsi_inputs_upload",
-    "cipsi_inputs_free", "cipsi_selection_raw",
+    "cipsi_inputs_free", "cipsi_selection_raw", "cipsi_run_pt2_static",
 ]
 
 

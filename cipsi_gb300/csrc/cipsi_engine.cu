@@ -2010,4 +2010,366 @@ int cipsi_selection_get(cipsi_ctx* ctx, int64_t first, int64_t count, int32_t* n
   return CIPSI_OK;
 }
 
+
+// ------------------------------------------------- run without allocation
+// cipsi_run_pt2_static runs k_pt2 + k_reduce with every per-run buffer taken
+// from one file-scope device array instead of cudaMalloc'd context buffers.
+// Layout of the array (each region 256-byte aligned): counters + dpivot +
+// histogram counts | histogram sums | reduced sums | work counter |
+// generator list | generator masks | work units | per-unit partial sums |
+// per-block neighbour scratch (nb_j, nb_emask, lr_idx).  The generator and
+// unit lists are staged in file-scope host arrays of fixed size.
+
+}  // extern "C"
+
+namespace {
+
+constexpr size_t kStaticScratchBytes = (size_t)32 << 20;  // 32 MiB
+constexpr int kStaticMaxUnits = 1 << 18;
+constexpr int kStaticMaxGens = 1 << 17;
+constexpr int kStaticMaxDevices = 64;
+
+static __device__ __align__(256) unsigned char g_pt2_scratch[kStaticScratchBytes];
+
+// host staging of the generator and unit lists (copied to the device array)
+static int32_t g_static_gens[kStaticMaxGens];
+static uint8_t g_static_gmask[kStaticMaxGens];
+static int32_t g_static_units[3 * kStaticMaxUnits];
+
+// device address of g_pt2_scratch, looked up once per device
+static unsigned char* g_static_ptr[kStaticMaxDevices];
+static bool g_static_ready[kStaticMaxDevices];
+
+size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+}  // namespace
+
+extern "C" {
+
+int cipsi_run_pt2_static(cipsi_ctx* ctx, const cipsi_opts* o, cipsi_result* r) {
+  if (!ctx || !o || !r) return CIPSI_ERR_ARG;
+  if (!ctx->have_int || !ctx->have_space || !ctx->have_roots)
+    return fail(ctx, CIPSI_ERR_STATE, "run before set_integrals / set_space / set_roots");
+  if (ctx->pending)
+    return fail(ctx, CIPSI_ERR_STATE, "an asynchronous run is pending: fetch its result first");
+  if (o->nclass < 2 || o->nclass > kNClass) return fail(ctx, CIPSI_ERR_ARG, "nclass must be in [2, 10]");
+  for (int i = 0; i + 1 < o->nclass; ++i)
+    if (!(o->aval[i] >= 0.0) || (i > 0 && !(o->aval[i] > o->aval[i - 1])))
+      return fail(ctx, CIPSI_ERR_ARG, "aval must be non-negative and increasing");
+  if (ctx->device < 0 || ctx->device >= kStaticMaxDevices)
+    return fail(ctx, CIPSI_ERR_ARG, "device ordinal out of range for the static scratch table");
+  CK(cudaSetDevice(ctx->device));
+  // set-up, once per device, with that device current
+  if (!g_static_ready[ctx->device]) {
+    void* ptr = nullptr;
+    CK(cudaGetSymbolAddress(&ptr, g_pt2_scratch));
+    g_static_ptr[ctx->device] = static_cast<unsigned char*>(ptr);
+    g_static_ready[ctx->device] = true;
+  }
+  unsigned char* base = g_static_ptr[ctx->device];
+  const int ncf = ctx->d.ncf, W = ctx->W, mt = ctx->d.metat;
+
+  // generators and their allowed rank changes (pertu.f:52-61, igene.f:34-35,
+  // 89-90, 199-200, 296-298; same rules as cipsi_run_pt2_async)
+  bool yd = false, ym = false, yf = false;
+  int maxrank = 0;
+  for (int k = 0; k < ncf; ++k) {
+    if (ctx->rank[k] == 1) ym = true;
+    if (ctx->rank[k] == 0) yd = true;
+    if (ctx->rank[k] == 2) yf = true;
+    maxrank = std::max(maxrank, ctx->rank[k]);
+  }
+  if (ym) yf = true;
+  const bool pertu_ref = yf && !yd && ctx->d.isym == 1;
+  const bool pertu_mono = yf && ym;
+  int ngen = 0;
+  auto too_many_gens = [&]() {
+    return fail(ctx, CIPSI_ERR_OVERFLOW,
+                "cipsi_run_pt2_static: more than " + std::to_string(kStaticMaxGens) + " generators");
+  };
+  if (o->run_pertu && (pertu_ref || pertu_mono)) {
+    g_static_gens[ngen] = -1;
+    g_static_gmask[ngen++] = 0;
+  }
+  for (int k = 0; k < ncf; ++k) {
+    if (!ctx->ygen[k] || ctx->ysaut[k]) continue;
+    if (o->gen_mask && !o->gen_mask[k]) continue;
+    const int nec = ctx->rank[k];
+    uint8_t m = 1u << 4;
+    if (!((nec == 0 && ym) || (nec == 1 && yd))) {
+      m |= 1u << 3;
+      const bool stop1 = nec < 1 || (ym && nec == 1) || (nec == 2 && yd);
+      if (!stop1) {
+        m |= 1u << 2;
+        if (!((nec == 3 && yd) || (nec == 2 && ym))) {
+          m |= 1u << 1;
+          if (!((nec == 2 && (yd || yf)) || (nec == 3 && ym) || (nec == 4 && yd))) m |= 1u << 0;
+        }
+      }
+    }
+    if (ngen == kStaticMaxGens) return too_many_gens();
+    g_static_gens[ngen] = k;
+    g_static_gmask[ngen++] = m;
+  }
+
+  // work units in the order of cipsi_run_pt2_async: generators by rank
+  // (pertu block first), each split into chunks of at most 6 allowed R blocks
+  constexpr int kRChunk = 6;
+  constexpr int kPertuChunk = 128;
+  const int n = ctx->d.norb, noca = ctx->d.noca, nel = 2 * noca;
+  const int nR = nel + nel * (nel - 1) / 2;
+  int nunits = 0;
+  int32_t* ug = g_static_units;
+  int32_t* ur0 = g_static_units + kStaticMaxUnits;
+  int32_t* ur1 = g_static_units + 2 * kStaticMaxUnits;
+  auto push_unit = [&](int g, int a, int b) {
+    if (nunits == kStaticMaxUnits) return false;
+    ug[nunits] = g;
+    ur0[nunits] = a;
+    ur1[nunits] = b;
+    ++nunits;
+    return true;
+  };
+  auto too_many_units = [&]() {
+    return fail(ctx, CIPSI_ERR_OVERFLOW,
+                "cipsi_run_pt2_static: more than " + std::to_string(kStaticMaxUnits) + " work units");
+  };
+  int hfe[2 * 128];
+  for (int rk = -1; rk <= maxrank; ++rk) {
+    for (int g = 0; g < ngen; ++g) {
+      const int k = g_static_gens[g];
+      if ((k < 0 ? -1 : ctx->rank[k]) != rk) continue;
+      if (k < 0) {
+        const int ntot = (pertu_ref ? 1 : 0) + (pertu_mono ? 2 * noca * (n - noca) : 0);
+        for (int t = 0; t < ntot; t += kPertuChunk)
+          if (!push_unit(g, t, std::min(ntot, t + kPertuChunk))) return too_many_units();
+        continue;
+      }
+      int ne = 0;
+      for (int sp = 0; sp < 2; ++sp)
+        for (int orb = 0; orb < n; ++orb)
+          if ((ctx->Sbits[(size_t)k * 2 * W + sp * W + (orb >> 6)] >> (orb & 63)) & 1ull)
+            hfe[ne++] = orb < noca;
+      const uint8_t m = g_static_gmask[g];
+      int cnt = 0, start = -1;
+      for (int rb = 0; rb < nR; ++rb) {
+        int hfR, nRr;
+        if (rb < nel) {
+          hfR = hfe[rb];
+          nRr = 1;
+        } else {
+          int t = rb - nel, e1 = 0;
+          while (t >= nel - 1 - e1) {
+            t -= nel - 1 - e1;
+            ++e1;
+          }
+          hfR = hfe[e1] + hfe[e1 + 1 + t];
+          nRr = 2;
+        }
+        bool ok = false;
+        for (int aV = 0; aV <= nRr; ++aV)
+          if (m & (1u << (hfR + aV - nRr + 2))) ok = true;
+        if (!ok) continue;
+        if (start < 0) start = rb;
+        if (++cnt == kRChunk) {
+          if (!push_unit(g, start, rb + 1)) return too_many_units();
+          cnt = 0;
+          start = -1;
+        }
+      }
+      if (start >= 0 && !push_unit(g, start, nR)) return too_many_units();
+    }
+  }
+
+  // launch shape as in cipsi_run_pt2_async, then fewer blocks if the
+  // per-block neighbour scratch would not fit in the array
+  int dev_sms = 0;
+  CK(cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, ctx->device));
+  const int R = mt <= 1 ? 1 : mt <= 2 ? 2 : mt <= 4 ? 4 : 8;
+  const size_t per_entry = (size_t)2 * W * 8 + 4;
+  const size_t qbytes = (size_t)(kThreads / 32) * queue_bytes(W, R);
+  const size_t smem_budget = (size_t)200 * 1024 - qbytes;
+  const int lr_cap = (int)std::min<size_t>((size_t)ncf, smem_budget / per_entry);
+  const size_t smem = (((size_t)lr_cap * per_entry + 15) & ~(size_t)15) + qbytes + 16;
+  const int blocks_per_sm = smem <= 95 * 1024 ? 2 : 1;
+  const size_t nq = (size_t)5 * mt;
+  const size_t ncount = C_NCOUNTERS + 1 + kNClass + kNClass * kMaxRoots;
+  const size_t off_counters = 0;
+  const size_t off_tab = align256(off_counters + ncount * sizeof(unsigned long long));
+  const size_t off_red = align256(off_tab + 2 * kNClass * kMaxRoots * sizeof(double));
+  const size_t off_work = align256(off_red + 5 * kMaxRoots * sizeof(double));
+  const size_t off_gens = align256(off_work + sizeof(int));
+  const size_t off_gmask = align256(off_gens + (size_t)std::max(ngen, 1) * sizeof(int32_t));
+  const size_t off_units = align256(off_gmask + (size_t)std::max(ngen, 1));
+  const size_t off_part = align256(off_units + (size_t)3 * std::max(nunits, 1) * sizeof(int32_t));
+  const size_t off_nb = align256(off_part + (size_t)std::max(nunits, 1) * nq * sizeof(double));
+  const size_t per_block = 3 * align256((size_t)ncf * sizeof(uint64_t));
+  int grid = std::max(1, std::min(nunits, dev_sms * blocks_per_sm));
+  if (off_nb + per_block > kStaticScratchBytes)
+    return fail(ctx, CIPSI_ERR_OVERFLOW,
+                "cipsi_run_pt2_static: the run needs " + std::to_string(off_nb + per_block) +
+                    " bytes of scratch, more than the static " + std::to_string(kStaticScratchBytes) +
+                    " (ncf = " + std::to_string(ncf) + ", work units = " + std::to_string(nunits) +
+                    "); use cipsi_run_pt2");
+  grid = (int)std::min<size_t>((size_t)grid, (kStaticScratchBytes - off_nb) / per_block);
+  const size_t nb_stride = align256((size_t)ncf * sizeof(uint64_t));
+  unsigned char* nb0 = base + off_nb;
+
+  // zero what the kernels accumulate into; upload the lists
+  CK(cudaMemsetAsync(base, 0, off_gens, ctx->stream));
+  CK(cudaMemsetAsync(base + off_part, 0, (size_t)std::max(nunits, 1) * nq * sizeof(double), ctx->stream));
+  if (ngen) {
+    CK(cudaMemcpyAsync(base + off_gens, g_static_gens, (size_t)ngen * sizeof(int32_t),
+                       cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(base + off_gmask, g_static_gmask, (size_t)ngen, cudaMemcpyHostToDevice, ctx->stream));
+  }
+  int32_t* dunits = reinterpret_cast<int32_t*>(base + off_units);
+  if (nunits) {
+    CK(cudaMemcpyAsync(dunits, ug, (size_t)nunits * sizeof(int32_t), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(dunits + nunits, ur0, (size_t)nunits * sizeof(int32_t), cudaMemcpyHostToDevice,
+                       ctx->stream));
+    CK(cudaMemcpyAsync(dunits + 2 * nunits, ur1, (size_t)nunits * sizeof(int32_t), cudaMemcpyHostToDevice,
+                       ctx->stream));
+  }
+
+  Params p{};
+  p.norb = ctx->d.norb;
+  p.noca = ctx->d.noca;
+  p.nel = nel;
+  p.ncf = ncf;
+  p.metat = mt;
+  p.nsym = ctx->d.nsym;
+  p.isym = ctx->d.isym;
+  p.ngen = ngen;
+  p.gens = reinterpret_cast<const int32_t*>(base + off_gens);
+  p.gen_dmask = base + off_gmask;
+  p.nunits = nunits;
+  p.unit_g = dunits;
+  p.unit_r0 = dunits + nunits;
+  p.unit_r1 = dunits + 2 * nunits;
+  p.S = ctx->dS;
+  p.ygen = ctx->dygen;
+  p.nesp = ctx->dnesp;
+  p.yef = ctx->dyef;
+  p.c = ctx->dc;
+  p.eri = ctx->deri;
+  p.pairtab = ctx->dpairtab;
+  p.ntttt = ctx->dntttt;
+  p.F = ctx->dF;
+  p.J = ctx->dJ;
+  p.K = ctx->dK;
+  p.fmpb = ctx->dfmpb;
+  p.orbsym = ctx->dorbsym;
+  for (int i = 0; i < ctx->d.nsym; ++i)
+    for (int j = 0; j < ctx->d.nsym; ++j) p.its[i][j] = ctx->its[(size_t)j * ctx->d.nsym + i] - 1;
+  for (int m = 0; m < mt; ++m) {
+    p.e[m] = ctx->e[m];
+    p.eb[m] = ctx->eb[m];
+    p.emp[m] = ctx->emp[m];
+    p.teste[m] = ctx->teste[m];
+    p.taum[m] = ctx->taum[m];
+  }
+  p.yen = o->yen;
+  p.ysele = o->ysele;
+  p.ymoyen = o->ymoyen;
+  p.ywdeg = o->ywdeg;
+  p.symvar = o->sym_variant;
+  p.nclass = o->nclass;
+  p.tau = o->tau;
+  p.teseff = o->teseff;
+  for (int i = 0; i < kNClass; ++i) {
+    p.aval[i] = o->aval[i];
+    std::memcpy(&p.aval_bits[i], &o->aval[i], 8);
+  }
+  p.pertu_ref = pertu_ref ? 1 : 0;
+  p.pertu_mono = pertu_mono ? 1 : 0;
+  // nb_j, nb_emask, lr_idx: grid x ncf entries each (k_pt2 indexes block b at
+  // b * ncf), in three regions of grid * nb_stride >= grid * ncf * 8 bytes
+  p.nb_j = reinterpret_cast<int32_t*>(nb0);
+  p.nb_emask = reinterpret_cast<uint64_t*>(nb0 + (size_t)grid * nb_stride);
+  p.lr_idx = reinterpret_cast<int32_t*>(nb0 + (size_t)2 * grid * nb_stride);
+  p.lr_cap = lr_cap;
+  p.gen_part = reinterpret_cast<double*>(base + off_part);
+  unsigned long long* dcounters = reinterpret_cast<unsigned long long*>(base + off_counters);
+  p.counters = dcounters;
+  p.dpivot_bits = dcounters + C_NCOUNTERS;
+  p.hist_nom = dcounters + C_NCOUNTERS + 1;
+  p.hist_nam = dcounters + C_NCOUNTERS + 1 + kNClass;
+  p.hist_tab = reinterpret_cast<double*>(base + off_tab);
+  // no record storage: selected perturbers are counted only
+  p.sel_bits = nullptr;
+  p.sel_owner = nullptr;
+  p.sel_xam = nullptr;
+  p.sel_evp = nullptr;
+  p.sel_cap = 0;
+  p.work = reinterpret_cast<int*>(base + off_work);
+  double* dred = reinterpret_cast<double*>(base + off_red);
+
+  CK(cudaEventRecord(ctx->ev0, ctx->stream));
+  if (nunits > 0) {
+    cudaError_t e;
+    if (W == 1) {
+      e = R == 1 ? launch_pt2<1, 1>(p, grid, smem, ctx->stream)
+        : R == 2 ? launch_pt2<1, 2>(p, grid, smem, ctx->stream)
+        : R == 4 ? launch_pt2<1, 4>(p, grid, smem, ctx->stream)
+                 : launch_pt2<1, 8>(p, grid, smem, ctx->stream);
+    } else {
+      e = R == 1 ? launch_pt2<2, 1>(p, grid, smem, ctx->stream)
+        : R == 2 ? launch_pt2<2, 2>(p, grid, smem, ctx->stream)
+        : R == 4 ? launch_pt2<2, 4>(p, grid, smem, ctx->stream)
+                 : launch_pt2<2, 8>(p, grid, smem, ctx->stream);
+    }
+    if (e != cudaSuccess) return fail(ctx, CIPSI_ERR_CUDA, std::string("k_pt2 launch: ") + cudaGetErrorString(e));
+    k_reduce<<<1, 64, 0, ctx->stream>>>(p.gen_part, nunits, (int)nq, dred);
+    CK(cudaGetLastError());
+  }
+  CK(cudaEventRecord(ctx->ev1, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+
+  // results (same fields as cipsi_fetch_result; no records are kept)
+  double red[5 * kMaxRoots];
+  unsigned long long cnt[C_NCOUNTERS + 1 + kNClass + kNClass * kMaxRoots];
+  double tab[2 * kNClass * kMaxRoots];
+  CK(cudaMemcpy(red, dred, nq * sizeof(double), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(cnt, dcounters, ncount * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(tab, p.hist_tab, 2 * kNClass * kMaxRoots * sizeof(double), cudaMemcpyDeviceToHost));
+  memset(r, 0, sizeof(*r));
+  for (int m = 0; m < mt; ++m) {
+    r->e2mp[m] = red[0 * mt + m];
+    r->e2vp[m] = red[1 * mt + m];
+    r->e2b[m] = red[2 * mt + m];
+    r->psimp[m] = red[3 * mt + m];
+    r->psivp[m] = red[4 * mt + m];
+  }
+  r->ietat = (int64_t)cnt[C_IETAT];
+  r->n_processed = (int64_t)cnt[C_NPROC];
+  r->n_candidates = (int64_t)cnt[C_NCAND];
+  r->n_compares = (int64_t)cnt[C_NCMP];
+  r->n_pairs_1 = (int64_t)cnt[C_NP1];
+  r->n_pairs_2 = (int64_t)cnt[C_NP2];
+  {
+    const unsigned long long b = cnt[C_NCOUNTERS];
+    double dp;
+    memcpy(&dp, &b, 8);
+    r->dpivot = dp;
+  }
+  const int nc = o->nclass;
+  for (int i = 0; i < nc; ++i) r->nom[i] = (int64_t)cnt[C_NCOUNTERS + 1 + i];
+  for (int c = 0; c < nc; ++c)
+    for (int m = 0; m < mt; ++m) {
+      r->nam[c * kMaxRoots + m] = (int64_t)cnt[C_NCOUNTERS + 1 + kNClass + c * mt + m];
+      r->tabmp[c * kMaxRoots + m] = tab[c * mt + m];
+      r->tabvp[c * kMaxRoots + m] = tab[nc * mt + c * mt + m];
+    }
+  const double avg_rank = 4.0;
+  r->alg_bytes = (int64_t)(cnt[C_NP2] * (8.0 * mt + 2 * 4.0 + 8.0) +
+                           cnt[C_NP1] * (8.0 * mt + 8.0 + 2.0 * avg_rank * 2 * 4.0) +
+                           cnt[C_NPROC] * (8.0 * avg_rank + 8.0 * (avg_rank + avg_rank * avg_rank) + 8.0 * mt));
+  float ms = 0.f;
+  CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+  r->kernel_ms = ms;
+  r->n_selected = (int64_t)cnt[C_NSEL];
+  return CIPSI_OK;
+}
+
 }  // extern "C"

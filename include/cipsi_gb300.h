@@ -199,6 +199,40 @@ int cipsi_cip_main(const char* workdir, const char* stdin_path, int32_t sym_vari
 int cipsi_selection_raw(cipsi_ctx* ctx, int64_t first, int64_t count, uint64_t* bits,
                         int32_t* owner, double* xam, double* evp);
 
+/* pertu + diexcit like cipsi_run_pt2, but the call allocates no device
+   memory.  This entry point has no counterpart in the reference.
+
+   For callers that must not allocate while they run: a program that has
+   handed the free device memory to its own pool (cudaMalloc would fail or
+   fragment it), or one that keeps other streams busy while E2 is computed
+   (cudaMalloc and cudaFree can synchronise the whole device and stall
+   them).  The context's inputs (set_integrals / set_space / set_roots) are
+   the only device memory it uses besides one 32 MiB array that is part of
+   the library's device image.
+
+   Returns the same energies, histogram and counters as cipsi_run_pt2.
+   Selected perturbers are counted (n_selected) but not stored: use
+   cipsi_run_pt2 when the records are needed.  The records of an earlier
+   cipsi_run_pt2 stay readable.  Blocks until done.
+
+   Limits: at most 131072 generators and 262144 work units (a generator
+   makes one unit per six allowed excitation blocks), and the per-run
+   buffers must fit the 32 MiB array: per-unit sums (40 * metat bytes per
+   unit) plus, per thread block, 3 * ncf * 8 bytes of neighbour lists; the
+   call runs fewer thread blocks when the lists do not fit for all of them,
+   and returns CIPSI_ERR_OVERFLOW with the needed size when even one block
+   does not fit.  CIPSI_ERR_STATE if a cipsi_run_pt2_async result is still
+   pending on the context.
+
+   The first call on each device looks up the array's device address
+   (cudaGetSymbolAddress) with that device current; make that first call
+   before any stream capture starts.  Every call clears the counters and
+   sums it accumulates into before its kernels run.  All calls in the
+   process share the one array (and fixed host staging arrays): two calls
+   that overlap in time, from two threads or on two contexts, race and
+   corrupt each other's results, so callers must serialise them. */
+int cipsi_run_pt2_static(cipsi_ctx* ctx, const cipsi_opts* opts, cipsi_result* res);
+
 #ifdef __cplusplus
 }
 #endif
