@@ -185,6 +185,169 @@ def run_reference(args, rank: int, world: int):
     print(json.dumps(line), flush=True)
 
 
+# ------------------------------------------------------------ batched form
+def run_batched(args, rank: int, world: int, local_rank: int):
+    """Potential-curve batch: `--geometries` seeded geometries (norb 40..100,
+    |S| 500..5000, 1 root) run (a) one after another through the plain form
+    and (b) as one batch (one persistent launch per class, CUDA graph, tuning
+    picked by the autotuner on a sub-batch).  Metric: geometries per second."""
+    import numpy as np
+    import torch
+    from cipsi_gb300 import batch, build, engine, synth
+    torch.cuda.set_device(local_rank)
+    build.build()
+    cfgs = synth.curve_geometries(args.geometries, seed=100 + rank)
+    t0 = time.perf_counter()
+    opts, ctxs = batch.load_geometries(cfgs, device=local_rank)
+    t_load = time.perf_counter() - t0
+    ng = len(ctxs)
+    clocks = Clocks(local_rank)
+    # plain form, serially (first pass sizes the buffers, second is timed)
+    batch.run_serial(ctxs, opts)
+    torch.cuda.synchronize()
+    clocks.start()
+    t_serial, res_serial = batch.run_serial(ctxs, opts)
+    serial_kernel_ms = sum(r["kernel_ms"] for r in res_serial)
+    # autotuner on a sub-batch, then the batch with the chosen tuning
+    best, tune_ms = batch.autotune(ctxs, opts, sample=16)
+    b = engine.Batch(ctxs, opts, r_chunk=best[0], ctas_per_sm=best[1])
+    for _ in range(args.batch_warmup):
+        b.run()
+        b.wait()
+        b.fetch_all()
+    dev_ms, wall = [], []
+    for _ in range(args.batch_steps):
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        b.run()
+        dev_ms.append(b.wait())
+        res_b = b.fetch_all()
+        wall.append(time.perf_counter() - t1)
+    clk = clocks.stop()
+    ok = all(rb["n_processed"] == rs["n_processed"] and rb["ietat"] == rs["ietat"]
+             for rb, rs in zip(res_b, res_serial))
+    b.close()
+    line = {"metric": "geometries/s (batched form)", "value": ng / (statistics.mean(dev_ms) / 1e3),
+            "unit": "geometries/s", "n_gpus": world, "steps": args.batch_steps, "warmup": args.batch_warmup,
+            "ms_per_step": statistics.mean(dev_ms), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded potential-curve geometries)",
+            "config": {"workload": f"{ng} geometries, R uniform [2,12] bohr, norb uniform 40..100, "
+                                   "|S| uniform 500..5000, 20 e-, 1 root, tau 0.01",
+                       "geometries": ng, "perturbers": int(sum(r["n_processed"] for r in res_b))},
+            "batched": {"device_ms": statistics.mean(dev_ms), "wall_ms": 1e3 * statistics.mean(wall),
+                        "geometries_per_s_wall": ng / statistics.mean(wall), "tuning": list(best),
+                        "autotune_ms": {f"{k[0]},{k[1]}": v for k, v in tune_ms.items()}},
+            "plain_serial": {"wall_ms": 1e3 * t_serial, "kernel_ms_sum": serial_kernel_ms,
+                             "geometries_per_s": ng / t_serial},
+            "speedup_wall": t_serial / statistics.mean(wall),
+            "same_counts_as_plain": ok, "load_s": t_load, "clocks": clk}
+    for c in ctxs:
+        c.close()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------ adjoint form
+def run_adjoint_form(args, rank: int, world: int, local_rank: int):
+    """The medium system plus a seeded symmetric dipole matrix mu ~ N(0, 0.5):
+    dE2/dh and dE2/d(pq|rs) from one backward pass, checked against central
+    differences (step 1e-5) on `--fd-elements` random integrals and the
+    dipole sum mu_pq dE2/dh_pq against finite-field runs at F = +-1e-4
+    (integrals in FP64 on the device)."""
+    import dataclasses
+    import numpy as np
+    import torch
+    from cipsi_gb300 import adjoint, build, synth
+    torch.cuda.set_device(local_rank)
+    build.build()
+    cfg = synth.CONFIGS[CONFIG]
+    base = tempfile.mkdtemp(prefix="cipsi_adj_")
+    wd = os.path.join(base, "sys")
+    synth.generate(cfg, wd)
+    h, L, _ = synth.make_integrals(cfg, np.random.default_rng(cfg.seed))
+    S = adjoint.System(wd, device=local_rank)
+    eri = S.pk.pack_from_cholesky(L, S.ninte)
+    n, mt = cfg.norb, S.dims.metat
+    ti, tj = np.tril_indices(n)
+    h_tri = np.zeros(n * (n + 1) // 2)
+    h_tri[adjoint._tri(ti, tj)] = h[ti, tj]
+    rng = np.random.default_rng(12345)
+    mu = rng.normal(0.0, 0.5, size=(n, n))
+    mu = 0.5 * (mu + mu.T)
+    seed = np.zeros((3, mt))
+    seed[1, 0] = 1.0  # e2vp of the first root
+    args_e = [x.numpy().copy() for x in S.engine_inputs(torch.as_tensor(h_tri), torch.as_tensor(eri))]
+    eng = [args_e[0], args_e[1], args_e[2], eri.copy(), args_e[3], args_e[4], args_e[5], args_e[6]]
+    S.run_engine(*[torch.as_tensor(x) for x in eng])  # warm-up (sizes the buffers)
+    fwd_ms, adj_ms = [], []
+    for _ in range(args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        S.run_engine(*[torch.as_tensor(x) for x in eng])
+        fwd_ms.append(1e3 * (time.perf_counter() - t0))
+        t0 = time.perf_counter()
+        g = S.ctx.adjoint(S.opts, seed)  # at the inputs the forward above loaded
+        adj_ms.append(1e3 * (time.perf_counter() - t0))
+    # finite differences on random integrals the sums depend on
+    nz = np.nonzero(g["eri"])[0]
+    picks = rng.choice(nz, min(args.fd_elements, len(nz)), replace=False)
+    step, worst = 1e-5, 0.0
+    for i in picks:
+        v = []
+        for sgn in (1.0, -1.0):
+            a = [x.copy() for x in eng]
+            a[3][i] += sgn * step
+            v.append(float((S.run_engine(*[torch.as_tensor(x) for x in a]) * seed).sum()))
+        fd = (v[0] - v[1]) / (2 * step)
+        worst = max(worst, abs(g["eri"][i] - fd) / max(1.0, abs(fd)))
+    # dipole: one backward pass against two finite-field runs
+    def dipole_check(system, h_t, eri_t):
+        t0 = time.perf_counter()
+        d_adj = adjoint.dipole(system, h_t, eri_t, mu, seed)
+        t_dip = time.perf_counter() - t0
+        mu_tri = np.zeros_like(h_t)
+        mu_tri[adjoint._tri(ti, tj)] = mu[ti, tj]
+        ff = {}
+        t0 = time.perf_counter()
+        for field in (1e-4, 1e-5):
+            e = []
+            for sgn in (1.0, -1.0):
+                with torch.no_grad():
+                    E = system.e2(torch.as_tensor(h_t + sgn * field * mu_tri), torch.as_tensor(eri_t))
+                e.append(float((E.numpy() * seed).sum()))
+            ff[f"{field:g}"] = (e[0] - e[1]) / (2 * field)
+        t_ff = (time.perf_counter() - t0) / 2
+        return {"adjoint": d_adj, "finite_field": ff, "abs_diff_1e-4": abs(d_adj - ff["0.0001"]),
+                "adjoint_s": t_dip, "finite_field_s": t_ff}
+
+    dip = dipole_check(S, h_tri, eri)
+    S.close()
+    # the same system with a 3 Eh occupied/virtual gap (denominators away from
+    # zero): there the finite-field difference converges and checks the dipole
+    cfg_w = dataclasses.replace(cfg, name="medium_gap", virt_shift=3.0)
+    wd_w = os.path.join(base, "gap")
+    synth.generate(cfg_w, wd_w)
+    h_w, L_w, _ = synth.make_integrals(cfg_w, np.random.default_rng(cfg_w.seed))
+    S = adjoint.System(wd_w, device=local_rank)
+    eri_w = S.pk.pack_from_cholesky(L_w, S.ninte)
+    h_tri_w = np.zeros(n * (n + 1) // 2)
+    h_tri_w[adjoint._tri(ti, tj)] = h_w[ti, tj]
+    dip_w = dipole_check(S, h_tri_w, eri_w)
+    S.close()
+    shutil.rmtree(base, ignore_errors=True)
+    line = {"metric": "adjoint dE2/d(h, (pq|rs)): backward / forward time", "value": statistics.mean(adj_ms)
+            / statistics.mean(fwd_ms), "unit": "ratio", "n_gpus": 1, "steps": args.steps, "warmup": 1,
+            "higher_is_better": False, "dtype": "f64", "data": "synthetic (seeded medium system + dipole)",
+            "config": {"workload": "medium (60 MOs, S = 2000, 3 roots), integrals in FP64, seed on e2vp[0]"},
+            "forward_ms": statistics.mean(fwd_ms), "adjoint_ms": statistics.mean(adj_ms),
+            "fd_check": {"elements": len(picks), "step": step, "max_rel_err": worst},
+            "dipole_medium": dip, "dipole_medium_gap3": dip_w,
+            "note": "the medium recipe has EN denominators near zero, so its finite-field differences do not "
+                    "converge with the field; the gap-3 variant is the dipole check"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 # ------------------------------------------------------------ GPU arm
 def run_gpu(args, rank: int, world: int, local_rank: int):
     import numpy as np
@@ -328,6 +491,13 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--form", choices=["plain", "batched", "adjoint"], default="plain",
+                    help="batched: the potential-curve batch (geometries/s, batched vs plain); "
+                         "adjoint: dE2/d integrals on the medium system with checks")
+    ap.add_argument("--fd-elements", type=int, default=200)
+    ap.add_argument("--geometries", type=int, default=256)
+    ap.add_argument("--batch-steps", type=int, default=2)
+    ap.add_argument("--batch-warmup", type=int, default=1)
     ap.add_argument("--gen-every", type=int, default=1,
                     help="profiling aid: run only every n-th determinant of S as a generator")
     args = ap.parse_args()
@@ -338,6 +508,12 @@ def main():
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
     if args.impl == "reference":
         run_reference(args, rank, world)
+        return
+    if args.form == "batched":
+        run_batched(args, rank, world, local_rank)
+        return
+    if args.form == "adjoint":
+        run_adjoint_form(args, rank, world, local_rank)
         return
     run_gpu(args, rank, world, local_rank)
 

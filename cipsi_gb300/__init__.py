@@ -27,6 +27,9 @@ EXPORTED = [
     "cipsi_run_pt2", "cipsi_run_pt2_async", "cipsi_fetch_result", "cipsi_selection_get",
     "cipsi_cip_main", "cipsi_inputs_read", "cipsi_inputs_dims", "cipsi_inputs_upload",
     "cipsi_inputs_free", "cipsi_selection_raw", "cipsi_run_pt2_static",
+    "cipsi_set_tuning", "cipsi_batch_create", "cipsi_batch_run", "cipsi_batch_wait",
+    "cipsi_batch_last_error", "cipsi_batch_destroy", "cipsi_inputs_array", "cipsi_set_integrals_f64store",
+    "cipsi_run_pt2_adjoint",
 ]
 
 

@@ -1,0 +1,98 @@
+"""Batched form of the engine: many geometries of a potential-curve grid
+(Autocip runs one cip per geometry, Autocip_13/calcul.f90:320) evaluated in
+one persistent launch per class, captured as a CUDA graph.
+
+`load_geometries` generates seeded geometries in worker processes (one temp
+directory each, in the reference's file formats), reads each into an engine
+context on the GPU and removes the directory, so only a few exist at a time.
+`autotune` picks the launch tuning (removed-electron blocks per work unit,
+CTAs per SM) by timing a sub-batch.
+"""
+from __future__ import annotations
+
+import multiprocessing as mp
+import os
+import shutil
+import tempfile
+import time
+from typing import List, Optional, Sequence, Tuple
+
+import numpy as np
+
+from . import engine, synth
+
+
+def _gen_one(args):
+    cfg, base = args
+    wd = os.path.join(base, cfg.name)
+    synth.generate(cfg, wd)
+    return wd
+
+
+def load_geometries(cfgs: Sequence[synth.SynthConfig], device: int = 0, workers: Optional[int] = None,
+                    base: Optional[str] = None):
+    """(inputs' opts, contexts) for every configuration, inputs on the GPU."""
+    base = base or tempfile.mkdtemp(prefix="cipsi_geos_")
+    workers = workers or max(1, min(16, (os.cpu_count() or 2) - 1))
+    ctxs, opts = [], []
+    ctx_mp = mp.get_context("spawn")
+    try:
+        with ctx_mp.Pool(workers) as pool:
+            for wd in pool.imap(_gen_one, [(c, base) for c in cfgs]):
+                inp = engine.Inputs(wd)
+                ctx = engine.Context(inp.dims, device=device)
+                ctx.upload(inp)
+                opts.append(engine.Opts.from_buffer_copy(inp.opts))
+                ctxs.append(ctx)
+                inp.close()
+                shutil.rmtree(wd, ignore_errors=True)
+    finally:
+        shutil.rmtree(base, ignore_errors=True)
+    return opts, ctxs
+
+
+def run_serial(ctxs, opts) -> Tuple[float, list]:
+    """The plain form, one geometry after another: wall seconds, results."""
+    res = []
+    t0 = time.perf_counter()
+    for c, o in zip(ctxs, opts):
+        c.run_async(o)
+        res.append(_fetch_allow_overflow(c))
+    return time.perf_counter() - t0, res
+
+
+def _fetch_allow_overflow(c):
+    import ctypes
+    r = engine.Result()
+    rc = c.lib.cipsi_fetch_result(c._c, ctypes.byref(r))
+    if rc not in (0, -4):
+        raise engine.CipsiError(c.lib.cipsi_last_error(c._c).decode())
+    d = engine.result_dict(r, c.dims.metat, getattr(c, "_last_nclass", engine.NCLASS))
+    d["overflow"] = rc == -4
+    return d
+
+
+CANDIDATES: List[Tuple[int, int]] = [(6, 0), (3, 0), (12, 0), (6, 2), (3, 2)]
+
+
+def autotune(ctxs, opts, sample: int = 16, candidates: Sequence[Tuple[int, int]] = CANDIDATES,
+             repeats: int = 1) -> Tuple[Tuple[int, int], dict]:
+    """Time each (r_chunk, ctas_per_sm) on a sub-batch of `sample` contexts
+    spread over the batch's size range; return the fastest and all times."""
+    order = np.argsort([c.dims.ncf * c.dims.norb for c in ctxs])
+    pick = sorted(set(int(order[int(i)]) for i in np.linspace(0, len(ctxs) - 1, min(sample, len(ctxs)))))
+    sub_c = [ctxs[i] for i in pick]
+    sub_o = [opts[i] for i in pick]
+    times = {}
+    for cand in candidates:
+        with engine.Batch(sub_c, sub_o, r_chunk=cand[0], ctas_per_sm=cand[1]) as b:
+            b.run()
+            b.wait()  # first replay: warm-up
+            ms = []
+            for _ in range(repeats):
+                b.run()
+                ms.append(b.wait())
+            b.fetch_all()
+        times[cand] = min(ms)
+    best = min(times, key=times.get)
+    return best, times

@@ -22,7 +22,8 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
 CXXFLAGS = ["-O2", "-std=c++17", "-fPIC", "-Wall"]
 
-SOURCES = ["cipsi_engine.cu", "cip_host.cpp", "cip_gpu_main.cpp"]
+CU_SOURCES = ["cipsi_engine.cu", "pt2_w1.cu", "pt2_w2.cu", "pt2_adj.cu"]
+SOURCES = CU_SOURCES + ["pt2_common.cuh", "pt2_kernel.cuh", "cip_host.cpp", "cip_gpu_main.cpp"]
 HEADERS = [os.path.join(ROOT, "include", "cipsi_gb300.h")]
 
 
@@ -55,24 +56,23 @@ def build(force: bool = False, verbose: bool = False) -> str:
     if not force and os.path.exists(LIB) and os.path.exists(EXE) and os.path.exists(stamp):
         if open(stamp).read().strip() == dig:
             return LIB
-    objs = {
-        "engine": os.path.join(OUT, "cipsi_engine.o"),
-        "host": os.path.join(OUT, "cip_host.o"),
-        "main": os.path.join(OUT, "cip_gpu_main.o"),
-    }
-    jobs = [
-        [nvcc] + ARCH + NVFLAGS + ["-Xptxas", "-v", "-c", os.path.join(CSRC, "cipsi_engine.cu"),
-                                   "-o", objs["engine"]],
+    objs = {c: os.path.join(OUT, c.replace(".cu", ".o")) for c in CU_SOURCES}
+    objs["host"] = os.path.join(OUT, "cip_host.o")
+    objs["main"] = os.path.join(OUT, "cip_gpu_main.o")
+    jobs = [[nvcc] + ARCH + NVFLAGS + ["-Xptxas", "-v", "-c", os.path.join(CSRC, c), "-o", objs[c]]
+            for c in CU_SOURCES]
+    jobs += [
         ["g++"] + CXXFLAGS + ["-c", os.path.join(CSRC, "cip_host.cpp"), "-o", objs["host"]],
         ["g++"] + CXXFLAGS + ["-c", os.path.join(CSRC, "cip_gpu_main.cpp"), "-o", objs["main"]],
     ]
-    with ThreadPoolExecutor(max_workers=3) as ex:
+    with ThreadPoolExecutor(max_workers=len(jobs)) as ex:
         outs = list(ex.map(_run, jobs))
+    ptxas = "".join(outs[:len(CU_SOURCES)])
     if verbose:
-        sys.stdout.write(outs[0])
+        sys.stdout.write(ptxas)
     with open(os.path.join(OUT, "ptxas_info.txt"), "w") as fh:
-        fh.write(outs[0])
-    _run([nvcc] + ARCH + ["-shared", "-o", LIB, objs["engine"], objs["host"], "-lcudart"])
+        fh.write(ptxas)
+    _run([nvcc] + ARCH + ["-shared", "-o", LIB] + [objs[c] for c in CU_SOURCES] + [objs["host"], "-lcudart"])
     _run(["g++", "-o", EXE, objs["main"], "-L" + OUT, "-lcipsi_gb300", "-Wl,-rpath,$ORIGIN",
           "-L" + os.path.join(os.path.dirname(os.path.dirname(nvcc)), "lib64"), "-lcudart"])
     with open(stamp, "w") as fh:

@@ -669,6 +669,50 @@ extern "C" int cipsi_inputs_dims(const cipsi_inputs* in, cipsi_dims* dims, cipsi
   return CIPSI_OK;
 }
 
+extern "C" int cipsi_inputs_array(const cipsi_inputs* in, const char* name, const void** data, int64_t* count,
+                                  int32_t* type) {
+  if (!in || !name || !data || !count || !type) return CIPSI_ERR_ARG;
+  const Run& R = in->R;
+  const std::string nm(name);
+  auto put = [&](const auto& v, int t) {
+    *data = v.data();
+    *count = (int64_t)v.size();
+    *type = t;
+    return CIPSI_OK;
+  };
+  // type codes: 1 int32, 2 int16, 3 float32, 4 float64, 5 uint8
+  if (nm == "itsym") return put(R.itsym, 1);
+  if (nm == "its") return put(R.its, 1);
+  if (nm == "ij0") return put(R.ij0, 2);
+  if (nm == "ntttt") return put(R.ntttt, 1);
+  if (nm == "F") return put(R.F, 4);
+  if (nm == "J") return put(R.J, 4);
+  if (nm == "K") return put(R.K, 4);
+  if (nm == "eri") return put(R.eri, 3);
+  if (nm == "c") return put(R.c, 4);
+  if (nm == "e") return put(R.e, 4);
+  if (nm == "eb") return put(R.eb, 4);
+  if (nm == "emp") return put(R.emp, 4);
+  if (nm == "teste") return put(R.teste, 4);
+  if (nm == "taum") return put(R.taum, 4);
+  if (nm == "fmpb") return put(R.fmpb, 4);
+  if (nm == "ne") return put(R.S.ne, 1);
+  if (nm == "nd") return put(R.S.nd, 1);
+  if (nm == "trou") return put(R.S.trou, 1);
+  if (nm == "part") return put(R.S.part, 1);
+  if (nm == "ygen") return put(R.S.ygen, 5);
+  if (nm == "ysaut") return put(R.S.ysaut, 5);
+  if (nm == "nesp") return put(R.S.nesp, 1);
+  if (nm == "yef1") return put(R.S.yef1, 5);
+  if (nm == "escf") {
+    *data = &R.escf;
+    *count = 1;
+    *type = 4;
+    return CIPSI_OK;
+  }
+  return CIPSI_ERR_ARG;
+}
+
 extern "C" int cipsi_inputs_upload(const cipsi_inputs* in, cipsi_ctx* ctx) {
   if (!in || !ctx) return CIPSI_ERR_ARG;
   const Run& R = in->R;

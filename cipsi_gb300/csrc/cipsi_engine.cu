@@ -1,34 +1,7 @@
-// cipsi_engine.cu -- GB300 (sm_103a) engine for the CIPSI second-order
-// perturbation / selection step (the work of cip/pertu.f + cip/diexcit.f).
-//
-// Algorithm (same perturber set, owners and weights as the reference, which
-// walks excitation lists one candidate at a time, cip/igene.f, pert1.f):
-//
-//   * S determinants are alpha/beta occupation bitstrings, W 64-bit words per
-//     spin (W = 1 for norb <= 64, 2 for norb <= 128).
-//   * One CTA owns one generator k at a time (persistent grid, atomic work
-//     queue).  It first gathers nb(k) = { j in S : degree(j,k) <= 4 } with the
-//     mask of k's electrons that j lacks.
-//   * Candidates I = k - R + A are processed in blocks of fixed removed
-//     electrons R (|R| = 1 or 2).  For a block, L_R = { j in nb(k) :
-//     |(k - R) \ j| <= 2 } is compacted into shared memory; it contains every
-//     S determinant that can be within two excitations of any I of the block.
-//     Each thread then takes added spin orbitals A and scans L_R only.
-//   * The reference's loop structure decides which excitations of k are
-//     examined (rank-change classes gated by the content of S,
-//     igene.f:34-35,89-90,199-200,296-298), the owner test (pert1.f:104-118,
-//     diexcit.f:246-259), the scan for interacting S determinants
-//     (pert1.f:129-144, diexcit.f:267-285), the spin-flip weights
-//     (pert1.f:150-164, diexcit.f:304-316), the MP / EN denominators and
-//     selection (pert1.f:171-295, diexcit.f:327-478).  All of that is
-//     restated here per candidate, as set rules on bitstrings.
-//   * Matrix elements use canonical (alpha string, beta string) phases; S
-//     coefficients are converted once on the host from the reference's
-//     excitation-list phase, so <I|H|Psi>^2 is identical.
-//   * (pq|rs) are read as real*4 (as cip stores them, cip/reijkl.f:27) and
-//     widened to double; everything else is double.  E2 sums are Kahan
-//     compensated per thread and reduced in a fixed order (deterministic).
-
+// cipsi_engine.cu -- host side of the GB300 engine for the CIPSI second-order
+// perturbation / selection step: contexts, run planning, launches, results,
+// the batched multi-geometry launch and the allocation-free entry point.
+// The kernel itself is in pt2_kernel.cuh (algorithm described there).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -39,1182 +12,84 @@
 #include <string>
 #include <vector>
 
-#include "../../include/cipsi_gb300.h"
+#include "pt2_common.cuh"
+
+using namespace cipsi_dev;
 
 namespace {
 
-constexpr int kNClass = CIPSI_NCLASS;
-constexpr int kMaxRoots = CIPSI_MAX_ROOTS;
-constexpr int kThreads = 256;
-constexpr int kMaxSym = 8;
-constexpr int kMaxElec = 64;
-constexpr int kMaxOrb = 128;
-constexpr int kRowCap = 128;  // per-warp list of |K' \ j| = 2 entries holding a1
-
-// counters[] slots
-enum {
-  C_IETAT = 0,
-  C_NPROC,
-  C_NSEL,
-  C_NCAND,
-  C_NCMP,
-  C_NP1,
-  C_NP2,
-  C_ALGB,
-  C_LRFALLBACK,
-  C_NCOUNTERS
-};
-
-struct Params {
-  int norb, noca, nel, ncf, metat, nsym, isym;
-  int ngen;
-  const int32_t* gens;       // generator indices (0-based); -1 = pertu block
-  const uint8_t* gen_dmask;  // allowed rank changes per generator, bit (D+2)
-  int nunits;                // work units: (generator slot, range of R blocks
-  const int32_t* unit_g;     //   or, for the pertu block, of candidates)
-  const int32_t* unit_r0;
-  const int32_t* unit_r1;
-  const uint64_t* S;         // ncf x 2W words (alpha words, beta words)
-  const uint8_t* ygen;
-  const int32_t* nesp;
-  const uint8_t* yef;
-  const double* c;           // ncf x metat, canonical phase
-  const float* eri;
-  const int32_t* pairtab;    // norb x norb: pair index | irrep << 24
-  const int32_t* ntttt;     // [irrep 1..nsym] first packed index (1-based)
-  const double* F;           // packed i*(i+1)/2 + j (i >= j, 0-based)
-  const double* J;
-  const double* K;
-  const double* fmpb;        // 2*norb by spin orbital
-  const int8_t* orbsym;      // 0-based irreps
-  int its[kMaxSym][kMaxSym]; // 0-based product table
-  double e[kMaxRoots], eb[kMaxRoots], emp[kMaxRoots], teste[kMaxRoots], taum[kMaxRoots];
-  int yen, ysele, ymoyen, ywdeg, symvar, nclass;
-  double tau, teseff;
-  double aval[kNClass];
-  long long aval_bits[kNClass];  // bit patterns of aval (non-negative, ascending)
-  int pertu_ref, pertu_mono;
-  // scratch
-  int32_t* nb_j;             // per block: ncf entries
-  uint64_t* nb_emask;
-  int32_t* lr_idx;           // per block: ncf entries (fallback path)
-  int lr_cap;                // shared-memory capacity of L_R
-  // outputs
-  double* gen_part;          // ngen x (5 * metat)
-  unsigned long long* counters;
-  unsigned long long* dpivot_bits;
-  unsigned long long* hist_nom;      // nclass
-  unsigned long long* hist_nam;      // nclass x metat
-  double* hist_tab;                  // 2 x nclass x metat (tabmp, tabvp)
-  uint64_t* sel_bits;                // cap x 2W
-  int32_t* sel_owner;
-  double* sel_xam;
-  double* sel_evp;                   // cap x metat
-  long long sel_cap;
-  int* work;                         // work counter
-};
-
-// ------------------------------------------------------------ bit helpers
-template <int W>
-__device__ __forceinline__ int popc_between(const uint64_t* s, int lo, int hi) {
-  // number of set bits strictly between orbital positions lo < hi
-  int cnt = 0;
-#pragma unroll
-  for (int w = 0; w < W; ++w) {
-    const int base = w * 64;
-    const int from = max(lo + 1 - base, 0);
-    const int to = min(hi - base, 64);
-    if (from < to) {
-      const uint64_t hiMask = (to >= 64) ? ~0ull : ((1ull << to) - 1ull);
-      const uint64_t loMask = (1ull << from) - 1ull;
-      cnt += __popcll(s[w] & hiMask & ~loMask);
-    }
-  }
-  return cnt;
-}
-
-template <int W>
-__device__ __forceinline__ int first_bit(const uint64_t* s) {
-#pragma unroll
-  for (int w = 0; w < W; ++w)
-    if (s[w]) return w * 64 + __ffsll((long long)s[w]) - 1;
-  return -1;
-}
-
-template <int W>
-__device__ __forceinline__ int last_bit(const uint64_t* s) {
-#pragma unroll
-  for (int w = W - 1; w >= 0; --w)
-    if (s[w]) return w * 64 + 63 - __clzll((long long)s[w]);
-  return -1;
-}
-
-__device__ __forceinline__ int tri(int i, int j) {
-  return i >= j ? i * (i + 1) / 2 + j : j * (j + 1) / 2 + i;
-}
-
-// (ij|kl) as cip/ai.f looks it up: packed pair indices, zero across irreps
-__device__ __forceinline__ double ai(const Params& p, int i, int j, int k, int l) {
-  const int pij = __ldg(&p.pairtab[i * p.norb + j]);
-  const int pkl = __ldg(&p.pairtab[k * p.norb + l]);
-  const int s1 = pij >> 24, s2 = pkl >> 24;
-  if (s1 != s2) return 0.0;
-  const long long a = pij & 0xFFFFFF, b = pkl & 0xFFFFFF;
-  const long long lo = a < b ? a : b, hi = a < b ? b : a;
-  const long long idx = lo + hi * (hi - 1) / 2 + __ldg(&p.ntttt[s1]) - 2;
-  return (double)__ldg(&p.eri[idx]);
-}
-
-// <I|H|J> for degree 1 or 2, canonical phases.  u = I bits, v = J bits
-// (alpha words then beta words).  rankI / rankJ: excitation degree relative
-// to the reference determinant; the one-difference element sums over the
-// holes and particles of the more excited determinant as cip/hntd.f does.
-template <int W>
-__device__ double hmat(const Params& p, const uint64_t* u, const uint64_t* v, int rankI, int rankJ,
-                       const uint64_t* hf, int& kind) {
-  uint64_t remv[2 * W], addv[2 * W];
-  int nrem[2] = {0, 0};
-#pragma unroll
-  for (int q = 0; q < 2 * W; ++q) {
-    const uint64_t x = u[q] ^ v[q];
-    remv[q] = x & v[q];  // occupied in J only
-    addv[q] = x & u[q];  // occupied in I only
-    nrem[q / W] += __popcll(remv[q]);
-  }
-  const int norb = p.norb;
-  if (nrem[0] + nrem[1] == 1) {
-    kind = 1;
-    const int s = nrem[0] ? 0 : 1;
-    const int pp = first_bit<W>(remv + s * W);
-    const int qq = first_bit<W>(addv + s * W);
-    const int lo = pp < qq ? pp : qq, hi = pp < qq ? qq : pp;
-    const int sign = (popc_between<W>(v + s * W, lo, hi) & 1) ? -1 : 1;
-    double val = __ldg(&p.F[tri(pp, qq)]);
-    const uint64_t* D = (rankI > rankJ) ? u : v;
-    // holes of D (occupied in the reference, empty in D)
-#pragma unroll
-    for (int sp = 0; sp < 2; ++sp) {
-#pragma unroll
-      for (int w = 0; w < W; ++w) {
-        uint64_t h = hf[sp * W + w] & ~D[sp * W + w];
-        while (h) {
-          const int r = w * 64 + __ffsll((long long)h) - 1;
-          h &= h - 1;
-          val -= ai(p, pp, qq, r, r);
-          if (sp == s) val += ai(p, pp, r, qq, r);
-        }
-        uint64_t t = D[sp * W + w] & ~hf[sp * W + w];
-        while (t) {
-          const int r = w * 64 + __ffsll((long long)t) - 1;
-          t &= t - 1;
-          val += ai(p, pp, qq, r, r);
-          if (sp == s) val -= ai(p, pp, r, qq, r);
-        }
-      }
-    }
-    (void)norb;
-    return sign * val;
-  }
-  kind = 2;
-  if (nrem[0] == 1 && nrem[1] == 1) {
-    const int pa = first_bit<W>(remv), qa = first_bit<W>(addv);
-    const int pb = first_bit<W>(remv + W), qb = first_bit<W>(addv + W);
-    const int sa = popc_between<W>(v, min(pa, qa), max(pa, qa));
-    const int sb = popc_between<W>(v + W, min(pb, qb), max(pb, qb));
-    const double val = ai(p, pa, qa, pb, qb);
-    return ((sa + sb) & 1) ? -val : val;
-  }
-  const int s = nrem[0] == 2 ? 0 : 1;
-  const uint64_t* rm = remv + s * W;
-  const uint64_t* ad = addv + s * W;
-  const int p1 = first_bit<W>(rm), p2 = last_bit<W>(rm);
-  const int q1 = first_bit<W>(ad), q2 = last_bit<W>(ad);
-  uint64_t mid[W];
-#pragma unroll
-  for (int w = 0; w < W; ++w) mid[w] = v[s * W + w];
-  const int s1 = popc_between<W>(mid, min(p1, q1), max(p1, q1));
-  mid[p1 >> 6] &= ~(1ull << (p1 & 63));
-  mid[q1 >> 6] |= (1ull << (q1 & 63));
-  const int s2 = popc_between<W>(mid, min(p2, q2), max(p2, q2));
-  const double val = ai(p, p1, q1, p2, q2) - ai(p, p1, q2, p2, q1);
-  return ((s1 + s2) & 1) ? -val : val;
-}
-
-// hmp (cip/hmp.f) and hdig (cip/hdig.f) of I, written over the sets of
-// holes H and particles P of I relative to the reference determinant.
-template <int W>
-__device__ void diag_terms(const Params& p, const uint64_t* u, const uint64_t* hf, double& hmpi,
-                           double& hdigi, bool want_hdig) {
-  int hs[24], ps[24];  // spin orbital codes: orb + spin * norb
-  int nh = 0, np = 0;
-#pragma unroll
-  for (int sp = 0; sp < 2; ++sp) {
-#pragma unroll
-    for (int w = 0; w < W; ++w) {
-      uint64_t h = hf[sp * W + w] & ~u[sp * W + w];
-      while (h && nh < 24) {
-        hs[nh++] = w * 64 + __ffsll((long long)h) - 1 + sp * p.norb;
-        h &= h - 1;
-      }
-      uint64_t t = u[sp * W + w] & ~hf[sp * W + w];
-      while (t && np < 24) {
-        ps[np++] = w * 64 + __ffsll((long long)t) - 1 + sp * p.norb;
-        t &= t - 1;
-      }
-    }
-  }
-  double mp = 0.0;
-  for (int i = 0; i < np; ++i) mp += __ldg(&p.fmpb[ps[i]]);
-  for (int i = 0; i < nh; ++i) mp -= __ldg(&p.fmpb[hs[i]]);
-  hmpi = mp;
-  if (!want_hdig) {
-    hdigi = 0.0;
-    return;
-  }
-  const int n = p.norb;
-  double e = 0.0;
-  for (int i = 0; i < np; ++i) {
-    const int o = ps[i] % n;
-    e += __ldg(&p.F[tri(o, o)]);
-  }
-  for (int i = 0; i < nh; ++i) {
-    const int o = hs[i] % n;
-    e -= __ldg(&p.F[tri(o, o)]);
-  }
-  auto jk = [&](int a, int b) -> double {
-    const int oa = a % n, ob = b % n;
-    const int t = tri(oa, ob);
-    double x = __ldg(&p.J[t]);
-    if ((a / n) == (b / n)) x -= __ldg(&p.K[t]);
-    return x;
-  };
-  // same-position terms of the reference's pair sum, 0.5*(J_tt-K_tt+J_pp-K_pp)
-  for (int i = 0; i < nh; ++i) e += 0.5 * jk(hs[i], hs[i]);
-  for (int i = 0; i < np; ++i) e += 0.5 * jk(ps[i], ps[i]);
-  for (int i = 0; i < nh; ++i)
-    for (int j = i + 1; j < nh; ++j) e += jk(hs[i], hs[j]);
-  for (int i = 0; i < np; ++i)
-    for (int j = i + 1; j < np; ++j) e += jk(ps[i], ps[j]);
-  for (int i = 0; i < nh; ++i)
-    for (int j = 0; j < np; ++j) e -= jk(hs[i], ps[j]);
-  hdigi = e;
-}
-
-// bit patterns of 0.05, 1e-6 and +inf
-constexpr long long kBits005 = 0x3fa999999999999all;
-constexpr long long kBits1em6 = 0x3eb0c6f7a0b5ed8dll;
-constexpr long long kBitsInf = 0x7ff0000000000000ll;
-// a < b for a >= 0 (a may be NaN: false), b >= 0
-__device__ __forceinline__ bool lt_nonneg(double a, double b) {
-  const long long x = __double_as_longlong(a), y = __double_as_longlong(b);
-  return x < y && x <= kBitsInf;
-}
-// max of a >= 0 (not NaN) and b >= 0 (may be NaN: fmax ignores it)
-__device__ __forceinline__ double max_nonneg(double a, double b) {
-  const long long x = __double_as_longlong(a), y = __double_as_longlong(b);
-  if (y > kBitsInf) return a;
-  return __longlong_as_double(x > y ? x : y);
-}
-
-__device__ __forceinline__ void kahan_add(double& s, double& c, double x) {
-  const double y = x - c;
-  const double t = s + y;
-  c = (t - s) - y;
-  s = t;
-}
-
-// Block-wide order-preserving compaction: calls emit(slot, i) for every i in
-// [0, n) with pred(i), slots dense and increasing with i (deterministic).
-// Must be called by every thread of the block.
-template <typename Pred, typename Emit>
-__device__ int ordered_compact(int n, Pred pred, Emit emit, int* warp_tmp /* >= 33 ints */) {
-  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5, nw = blockDim.x >> 5;
-  int total = 0;
-  for (int base = 0; base < n; base += blockDim.x) {
-    const int i = base + tid;
-    const bool keep = i < n && pred(i);
-    const unsigned m = __ballot_sync(0xffffffffu, keep);
-    if (lane == 0) warp_tmp[wid] = __popc(m);
-    __syncthreads();
-    if (wid == 0) {
-      const int v = lane < nw ? warp_tmp[lane] : 0;
-      int x = v;
-      for (int o = 1; o < 32; o <<= 1) {
-        const int y = __shfl_up_sync(0xffffffffu, x, o);
-        if (lane >= o) x += y;
-      }
-      if (lane < nw) warp_tmp[lane] = x - v;  // exclusive prefix
-      if (lane == 31) warp_tmp[32] = x;       // round total
-    }
-    __syncthreads();
-    if (keep) emit(total + warp_tmp[wid] + __popc(m & ((1u << lane) - 1u)), i);
-    total += warp_tmp[32];
-    __syncthreads();
-  }
-  return total;
-}
-
-template <int R>
-struct Acc {
-  double e2mp[R], cmp[R], e2vp[R], cvp[R], e2b[R], cb[R], psimp[R], psivp[R];
-  unsigned long long ietat, nproc, nsel, ncand, ncmp, np1, np2, algb;
-  double dpivot;
-  __device__ void zero() {
-#pragma unroll
-    for (int m = 0; m < R; ++m) {
-      e2mp[m] = cmp[m] = e2vp[m] = cvp[m] = e2b[m] = cb[m] = psimp[m] = psivp[m] = 0.0;
-    }
-    ietat = nproc = nsel = ncand = ncmp = np1 = np2 = algb = 0ull;
-    dpivot = 0.0;
-  }
-};
-
-// One thread's histogram (cip/isto.f): class sums and counts, indexed by
-// class at run time, so it lives in local memory (L1-resident); one FP64 add
-// per contribution, no atomics; merged into the block's at kernel end.
-template <int R>
-struct HistPriv {
-  double tab[kNClass][2][R];
-  unsigned long long nom[kNClass];
-  unsigned long long nam[kNClass][R];
-  __device__ void zero() {
-    for (int c = 0; c < kNClass; ++c) {
-      nom[c] = 0ull;
-      for (int m = 0; m < R; ++m) {
-        tab[c][0][m] = tab[c][1][m] = 0.0;
-        nam[c][m] = 0ull;
-      }
-    }
-  }
-};
-
-struct SmemHist {
-  unsigned long long nom[kNClass];
-  unsigned long long nam[kNClass * kMaxRoots];
-  double tab[2 * kNClass * kMaxRoots];
-};
-
-// histogram class of a non-negative value (cip/isto.f: first i with
-// val < aval(i)); compared as IEEE bit patterns, which order non-negative
-// doubles exactly as the values (integer pipe instead of FP64 compares)
-__device__ __forceinline__ int hist_class(const Params& p, double val) {
-  const long long v = __double_as_longlong(val);
-  const int nc = p.nclass - 1;
-  int c = 0;
-  for (int i = 0; i < nc; ++i) c += (v >= p.aval_bits[i]) ? 1 : 0;
-  return c;
-}
-
-// Everything the reference does with one candidate after its interaction
-// scan: denominators, E2, selection, histogram, unit-60 record.  Called by
-// all 32 lanes of a warp; `live` marks the lanes holding a perturber.
-template <int W, int R>
-__device__ void finish_candidate(const Params& p, bool live, const uint64_t* u, double hmpi,
-                                 double hvpi, const double* bc, int owner1 /*1-based, 0 = pertu*/,
-                                 double fmul, int nmul, bool ybis, bool is_pert1, Acc<R>& acc,
-                                 HistPriv<R>& hp) {
-  constexpr unsigned kFull = 0xffffffffu;
-  const int lane = threadIdx.x & 31;
-  double xam = 0.0;
-  bool ydeg = false;
-  double vil[R], semp[R], sevp[R];
-  // the reference adds each term and then term*fmul (spin-flip weight,
-  // pert1.f:280-287); one compensated add of term*(1+fmul) is used here
-  const double wgt = ybis ? 1.0 + fmul : 1.0;
-#pragma unroll
-  for (int m = 0; m < R; ++m) {
-    vil[m] = 0.0;
-    semp[m] = sevp[m] = 0.0;
-    if (!live || m >= p.metat) continue;
-    const double bcalc = bc[m];
-    const double dmp = p.emp[m] - hmpi;
-    double eivp = 0.0, cimp, xim, deno, eim;
-    if (p.yen) {
-      // the three denominators share one FP64 division (GB300's FP64 rate is
-      // 1/64 of FP32): r = 1/(dmp*dvp*db), 1/dmp = dvp*db*r, etc.
-      const double dvp = p.e[m] - hvpi;
-      const double db = p.eb[m] - hvpi;
-      const double pvb = dvp * db;
-      const double prod = dmp * pvb;
-      double civp, cib;
-      if (fabs(prod) > 1.0e-280 && fabs(prod) < 1.0e280) {
-        const double r = 1.0 / prod;
-        cimp = bcalc * (pvb * r);
-        civp = bcalc * ((dmp * db) * r);
-        cib = bcalc * ((dmp * dvp) * r);
-      } else {  // a denominator at (or near) zero or huge: divide one by one
-        cimp = bcalc / dmp;
-        civp = bcalc / dvp;
-        cib = bcalc / db;
-      }
-      eivp = bcalc * civp;
-      kahan_add(acc.e2vp[m], acc.cvp[m], eivp * wgt);
-      acc.psivp[m] = fma(civp * civp, wgt, acc.psivp[m]);
-      kahan_add(acc.e2b[m], acc.cb[m], (bcalc * cib) * wgt);
-      xim = p.ysele ? fabs(eivp) : fabs(civp);
-      deno = dvp;
-      eim = eivp;
-    } else {
-      cimp = bcalc / dmp;
-    }
-    const double eimp = bcalc * cimp;
-    kahan_add(acc.e2mp[m], acc.cmp[m], eimp * wgt);
-    acc.psimp[m] = fma(cimp * cimp, wgt, acc.psimp[m]);
-    if (!p.yen) {
-      xim = p.ysele ? fabs(eimp) : fabs(cimp);
-      deno = dmp;
-      eim = eimp;
-    }
-    // comparisons of magnitudes on their IEEE bit patterns (exact for
-    // non-negative doubles; NaN compares as in the reference: never below)
-    const long long bdeno = __double_as_longlong(deno) & 0x7fffffffffffffffll;
-    const long long beim = __double_as_longlong(eim) & 0x7fffffffffffffffll;
-    if (!(bdeno > kBits005 && bdeno <= kBitsInf) && !(beim < kBits1em6) && p.ywdeg) ydeg = true;
-    if (lt_nonneg(xim, p.teste[m])) acc.dpivot = max_nonneg(acc.dpivot, xim);
-    if (p.ymoyen) {
-      xim = xim * p.taum[m];
-      vil[m] = xim;
-      xam = max_nonneg(xam, xim);
-    }
-    semp[m] = eimp;
-    sevp[m] = eivp;
-  }
-  if (live) {
-    acc.ietat += (unsigned long long)(long long)(nmul + 1);
-    acc.nproc += 1;
-  }
-  // histogram (cip/isto.f; pert1 calls it always, diexcit only if ymoyen)
-  if (live && (is_pert1 || p.ymoyen) && xam >= p.teseff) {
-    const double fm = fmul + 1.0;
-    const int cls = hist_class(p, xam);
-    hp.nom[cls] += (unsigned long long)(1 + nmul);
-#pragma unroll
-    for (int m = 0; m < R; ++m) {
-      if (m >= p.metat || vil[m] < p.teseff) continue;
-      hp.tab[cls][0][m] += semp[m] * fm;
-      hp.tab[cls][1][m] += sevp[m] * fm;
-      hp.nam[hist_class(p, vil[m])][m] += (unsigned long long)(1 + nmul);
-    }
-  }
-  if (ydeg) xam = 1.0;
-  // unit-60 record (pie.f): one slot reservation per warp
-  const bool sel = live && xam > p.tau && p.ymoyen;
-  const unsigned sm = __ballot_sync(kFull, sel);
-  if (sm) {
-    unsigned long long base = 0;
-    if (lane == 0) base = atomicAdd(&p.counters[C_NSEL], (unsigned long long)__popc(sm));
-    base = __shfl_sync(kFull, base, 0);
-    if (sel) {
-      const unsigned long long slot = base + __popc(sm & ((1u << lane) - 1u));
-      if ((long long)slot < p.sel_cap) {
-#pragma unroll
-        for (int q = 0; q < 2 * W; ++q) p.sel_bits[slot * 2 * W + q] = u[q];
-        p.sel_owner[slot] = owner1;
-        p.sel_xam[slot] = xam;
-        // ENvp per root written by cipsym (cipsym/pert1.f:244): eivp*(fmul+1)
-#pragma unroll
-        for (int m = 0; m < R; ++m)
-          if (m < p.metat) p.sel_evp[slot * p.metat + m] = p.symvar ? sevp[m] * (fmul + 1.0) : 0.0;
-      }
-    }
-  }
-}
-
-template <int R>
-__device__ void block_flush(const Params& p, Acc<R>& acc, int gslot, double* red) {
-  // reduce 5*metat sums over the block in a fixed order; write gen_part[gslot]
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const int nw = blockDim.x >> 5;
-  const int nq = 5 * p.metat;
-  for (int q = 0; q < nq; ++q) {
-    const int m = q % p.metat, which = q / p.metat;
-    double v = 0.0;
-#pragma unroll
-    for (int mm = 0; mm < R; ++mm)
-      if (mm == m) {
-        v = which == 0   ? acc.e2mp[mm] - acc.cmp[mm]
-            : which == 1 ? acc.e2vp[mm] - acc.cvp[mm]
-            : which == 2 ? acc.e2b[mm] - acc.cb[mm]
-            : which == 3 ? acc.psimp[mm]
-                         : acc.psivp[mm];
-      }
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-    if (lane == 0) red[q * 32 + wid] = v;
-  }
-  __syncthreads();
-  if (threadIdx.x < nq) {
-    double s = 0.0, c = 0.0;
-    for (int w = 0; w < nw; ++w) kahan_add(s, c, red[threadIdx.x * 32 + w]);
-    p.gen_part[(long long)gslot * nq + threadIdx.x] = s - c;
-  }
-  __syncthreads();
-#pragma unroll
-  for (int m = 0; m < R; ++m) {
-    acc.e2mp[m] = acc.cmp[m] = acc.e2vp[m] = acc.cvp[m] = acc.e2b[m] = acc.cb[m] = 0.0;
-    acc.psimp[m] = acc.psivp[m] = 0.0;
-  }
-}
-
-// Per-warp queue of perturbers that survived the interaction scan.  The
-// FP64 epilogue (denominators, E2, selection) then runs on full warps: the
-// FP64 pipe of GB300 is narrow, and a warp instruction costs the same with
-// 32 lanes or with the few that would be live at the candidate level.
-constexpr int kQCap = 64;
-template <int W, int R>
-struct WarpQueue {
-  uint64_t u[2 * W][kQCap];
-  double bc[R][kQCap];
-  double hmp[kQCap], hvp[kQCap], fmul[kQCap];
-  int nmul[kQCap], owner[kQCap];
-  unsigned char flags[kQCap];  // bit 0 ybis, bit 1 is_pert1
-};
-
-// Enqueue the live lanes' perturbers (called by a whole warp); runs the
-// epilogue on every full batch of 32.
-template <int W, int R>
-__device__ void enqueue_candidate(const Params& p, WarpQueue<W, R>& q, int& qn, bool live,
-                                  const uint64_t* u, double hmpi, double hvpi, const double* bc,
-                                  int owner1, double fmul, int nmul, bool ybis, bool is_pert1,
-                                  Acc<R>& acc, HistPriv<R>& hp);
-
-template <int W, int R>
-__device__ __noinline__ void drain_queue(const Params& p, WarpQueue<W, R>& q, int& qn, bool all, Acc<R>& acc,
-                            HistPriv<R>& hp) {
-  const int lane = threadIdx.x & 31;
-  while (qn >= 32 || (all && qn > 0)) {
-    const int base = qn >= 32 ? qn - 32 : 0;
-    const int cnt = qn >= 32 ? 32 : qn;
-    const bool live = lane < cnt;
-    const int e = base + (live ? lane : 0);
-    uint64_t u[2 * W];
-#pragma unroll
-    for (int w = 0; w < 2 * W; ++w) u[w] = q.u[w][e];
-    double bc[R];
-#pragma unroll
-    for (int m = 0; m < R; ++m) bc[m] = q.bc[m][e];
-    const unsigned char f = q.flags[e];
-    finish_candidate<W, R>(p, live, u, q.hmp[e], q.hvp[e], bc, q.owner[e], q.fmul[e], q.nmul[e],
-                           (f & 1) != 0, (f & 2) != 0, acc, hp);
-    __syncwarp();
-    qn = base;
-  }
-}
-
-template <int W, int R>
-__device__ void enqueue_candidate(const Params& p, WarpQueue<W, R>& q, int& qn, bool live,
-                                  const uint64_t* u, double hmpi, double hvpi, const double* bc,
-                                  int owner1, double fmul, int nmul, bool ybis, bool is_pert1,
-                                  Acc<R>& acc, HistPriv<R>& hp) {
-  const int lane = threadIdx.x & 31;
-  const unsigned lm = __ballot_sync(0xffffffffu, live);
-  if (live) {
-    const int e = qn + __popc(lm & ((1u << lane) - 1u));
-#pragma unroll
-    for (int w = 0; w < 2 * W; ++w) q.u[w][e] = u[w];
-#pragma unroll
-    for (int m = 0; m < R; ++m) q.bc[m][e] = bc[m];
-    q.hmp[e] = hmpi;
-    q.hvp[e] = hvpi;
-    q.fmul[e] = fmul;
-    q.nmul[e] = nmul;
-    q.owner[e] = owner1;
-    q.flags[e] = (unsigned char)((ybis ? 1 : 0) | (is_pert1 ? 2 : 0));
-  }
-  qn += __popc(lm);
-  __syncwarp();
-  drain_queue<W, R>(p, q, qn, false, acc, hp);
-}
-
-// ------------------------------------------------------------------ kernel
-struct BlockShared {
-  double vdg[2 * kMaxOrb];  // hdig(K'+a) - hdig(K') without the pair term
-  double hK, mK;            // hdig(K'), hmp(K')
-  int dn_so[48];            // spin orbitals where K' differs from the reference
-  int dn_sg[48];            // +1 (occupied virtual) / -1 (empty reference orbital)
-  int ndn;
-  uint64_t kbits[2 * 2];
-  int occ[kMaxElec];      // spin orbital code (orb + spin*norb) of k's electrons
-  int vir[2][kMaxOrb];    // virtual orbitals of k per spin
-  int nvir[2];
-  int nel_s[2];
-  int nnb;
-  int nlr;
-  int gen;
-  int kidx;
-  int rank_k;
-};
-
-template <int W, int R>
-__global__ void __launch_bounds__(kThreads, 2) k_pt2(Params p) {
-  extern __shared__ __align__(16) unsigned char dyn[];
-  __shared__ BlockShared sh;
-  __shared__ SmemHist hist;
-  __shared__ double red[5 * kMaxRoots * 32];
-  __shared__ int ctmp[33];
-  __shared__ int16_t wrow[(kThreads / 32) * kRowCap];
-
-  const int tid = threadIdx.x;
-  // shared L_R arrays (fast path)
-  uint64_t* lr_bits = reinterpret_cast<uint64_t*>(dyn);          // cap x 2W
-  int32_t* lr_j = reinterpret_cast<int32_t*>(lr_bits + (size_t)p.lr_cap * 2 * W);
-  // per-warp epilogue queues, 16-byte aligned after the L_R arrays
-  const size_t qoff = (((size_t)p.lr_cap * (2 * W * 8 + 4)) + 15) & ~(size_t)15;
-  WarpQueue<W, R>& wq = reinterpret_cast<WarpQueue<W, R>*>(dyn + qoff)[threadIdx.x >> 5];
-  int qn = 0;
-  int32_t* my_nb_j = p.nb_j + (size_t)blockIdx.x * p.ncf;
-  uint64_t* my_nb_em = p.nb_emask + (size_t)blockIdx.x * p.ncf;
-  int32_t* my_lr_idx = p.lr_idx + (size_t)blockIdx.x * p.ncf;
-
-  for (int i = tid; i < kNClass; i += blockDim.x) hist.nom[i] = 0;
-  for (int i = tid; i < kNClass * kMaxRoots; i += blockDim.x) hist.nam[i] = 0;
-  for (int i = tid; i < 2 * kNClass * kMaxRoots; i += blockDim.x) hist.tab[i] = 0.0;
-
-  uint64_t hf[2 * W];
-#pragma unroll
-  for (int s = 0; s < 2; ++s)
-#pragma unroll
-    for (int w = 0; w < W; ++w) {
-      const int lo = w * 64;
-      const int n = min(max(p.noca - lo, 0), 64);
-      hf[s * W + w] = (n >= 64) ? ~0ull : ((1ull << n) - 1ull);
-    }
-
-  Acc<R> acc;
-  acc.zero();
-  HistPriv<R> hp;
-  hp.zero();
-  const int ncf = p.ncf;
-
-  for (;;) {
-    __syncthreads();
-    if (tid == 0) sh.gen = atomicAdd(p.work, 1);
-    __syncthreads();
-    const int unit = sh.gen;
-    if (unit >= p.nunits) break;
-    const int g = p.unit_g[unit];
-    const int ur0 = p.unit_r0[unit], ur1 = p.unit_r1[unit];
-    const int k = p.gens[g];
-
-    if (k < 0) {
-      // ---------------- pertu: reference and its singles, no owner test
-      // candidates: t = 0 -> reference (if pertu_ref), then singles
-      const int no = p.noca, nv = p.norb - p.noca;
-      for (int t0 = ur0; t0 < ur1; t0 += blockDim.x) {
-        const int t = t0 + tid;
-        bool live = t < ur1;
-        uint64_t u[2 * W];
-#pragma unroll
-        for (int q = 0; q < 2 * W; ++q) u[q] = hf[q];
-        const int tt = p.pertu_ref ? t - 1 : t;  // tt < 0: the reference itself
-        if (live && tt >= 0) {
-          const int s = tt / (no * nv);
-          const int rem = tt % (no * nv);
-          const int o = rem / nv, vv = no + rem % nv;
-          if (p.its[p.orbsym[o]][p.orbsym[vv]] != p.isym - 1) live = false;
-          u[s * W + (o >> 6)] &= ~(1ull << (o & 63));
-          u[s * W + (vv >> 6)] |= (1ull << (vv & 63));
-        }
-        double bc[R];
-#pragma unroll
-        for (int m = 0; m < R; ++m) bc[m] = 0.0;
-        double hmpi = 0.0, hvpi = 0.0;
-        if (live) {
-          acc.ncand++;
-          int rankI = 0;
-#pragma unroll
-          for (int q = 0; q < 2 * W; ++q) rankI += __popcll(hf[q] & ~u[q]);
-          int nint = 0;
-          bool drop = false;
-          for (int j = 0; j < ncf; ++j) {
-            const uint64_t* v = p.S + (size_t)j * 2 * W;
-            int x = 0;
-#pragma unroll
-            for (int q = 0; q < 2 * W; ++q) x += __popcll(u[q] ^ __ldg(&v[q]));
-            acc.ncmp++;
-            if (x > 4) continue;
-            if (x == 0) {
-              drop = true;
-              break;
-            }
-            uint64_t vv[2 * W];
-#pragma unroll
-            for (int q = 0; q < 2 * W; ++q) vv[q] = __ldg(&v[q]);
-            int rankJ = 0;
-#pragma unroll
-            for (int q = 0; q < 2 * W; ++q) rankJ += __popcll(hf[q] & ~vv[q]);
-            int kind;
-            const double h = hmat<W>(p, u, vv, rankI, rankJ, hf, kind);
-            if (kind == 1) acc.np1++; else acc.np2++;
-            ++nint;
-#pragma unroll
-            for (int m = 0; m < R; ++m)
-              if (m < p.metat) bc[m] += h * __ldg(&p.c[(size_t)j * p.metat + m]);
-          }
-          if (drop || nint == 0) live = false;
-          if (live) diag_terms<W>(p, u, hf, hmpi, hvpi, p.yen != 0);
-        }
-        enqueue_candidate<W, R>(p, wq, qn, live, u, hmpi, hvpi, bc, 0, 0.0, 0, false, true, acc, hp);
-      }
-      drain_queue<W, R>(p, wq, qn, true, acc, hp);
-      block_flush<R>(p, acc, unit, red);
-      continue;
-    }
-
-    // ---------------- generator k: neighbours within degree 4
-    if (tid == 0) {
-      sh.kidx = k;
-      sh.nnb = 0;
-    }
-    if (tid < 2 * W) sh.kbits[tid] = p.S[(size_t)k * 2 * W + tid];
-    __syncthreads();
-    uint64_t kb[2 * W];
-#pragma unroll
-    for (int q = 0; q < 2 * W; ++q) kb[q] = sh.kbits[q];
-    if (tid == 0) {
-      // electron list and virtual lists of k
-      int ne = 0;
-      for (int s = 0; s < 2; ++s) {
-        int nes = 0, nv = 0;
-        for (int o = 0; o < p.norb; ++o) {
-          if ((kb[s * W + (o >> 6)] >> (o & 63)) & 1ull) {
-            sh.occ[ne++] = o + s * p.norb;
-            ++nes;
-          } else {
-            sh.vir[s][nv++] = o;
-          }
-        }
-        sh.nel_s[s] = nes;
-        sh.nvir[s] = nv;
-      }
-      int rk = 0;
-      for (int q = 0; q < 2 * W; ++q) rk += __popcll(hf[q] & ~kb[q]);
-      sh.rank_k = rk;
-    }
-    __syncthreads();
-    const int nel = sh.nel_s[0] + sh.nel_s[1];
-    const int nnb = ordered_compact(
-        ncf,
-        [&](int j) {
-          int x = 0;
-#pragma unroll
-          for (int q = 0; q < 2 * W; ++q) x += __popcll(kb[q] ^ __ldg(&p.S[(size_t)j * 2 * W + q]));
-          return x <= 8;
-        },
-        [&](int slot, int j) {
-          // electrons of k missing in j, as a mask over k's electron indices
-          uint64_t em = 0;
-#pragma unroll
-          for (int q = 0; q < 2 * W; ++q) {
-            uint64_t miss = kb[q] & ~__ldg(&p.S[(size_t)j * 2 * W + q]);
-            while (miss) {
-              const int b = __ffsll((long long)miss) - 1;
-              miss &= miss - 1;
-              // electron index = occupied bits of k before this bit
-              int idx = 0;
-              const int s = q / W, w = q % W;
-              if (s == 1) idx += sh.nel_s[0];
-              for (int w2 = 0; w2 < w; ++w2) idx += __popcll(kb[s * W + w2]);
-              idx += __popcll(kb[q] & ((1ull << b) - 1ull));
-              em |= 1ull << idx;
-            }
-          }
-          my_nb_j[slot] = j;
-          my_nb_em[slot] = em;
-        },
-        ctmp);
-    const int rank_k = sh.rank_k;
-    const uint8_t dmask = p.gen_dmask[g];
-    const int k1 = k + 1;  // 1-based owner index
-    const int nespk = p.nesp[k];
-    const bool yefk = p.yef[k] != 0;
-
-    // ---------------- blocks of removed electrons R (this unit's range)
-    for (int r = ur0; r < ur1; ++r) {
-      int e1, e2 = -1;
-      if (r < nel) {
-        e1 = r;
-      } else {
-        // pair index -> (e1 < e2)
-        int t = r - nel;
-        e1 = 0;
-        while (t >= nel - 1 - e1) {
-          t -= nel - 1 - e1;
-          ++e1;
-        }
-        e2 = e1 + 1 + t;
-      }
-      const int so1 = sh.occ[e1];
-      const int so2 = e2 >= 0 ? sh.occ[e2] : -1;
-      const int sp1 = so1 / p.norb, o1 = so1 % p.norb;
-      const int sp2 = so2 >= 0 ? so2 / p.norb : -1, o2 = so2 >= 0 ? so2 % p.norb : -1;
-      const int nRr = e2 >= 0 ? 2 : 1;
-      const int hfR = (o1 < p.noca ? 1 : 0) + (e2 >= 0 && o2 < p.noca ? 1 : 0);
-      // achievable rank changes D = hfR + aV - |R| (aV = added HF-virtuals)
-      bool any = false;
-      for (int aV = 0; aV <= nRr; ++aV) {
-        const int D = hfR + aV - nRr;
-        if (dmask & (1u << (D + 2))) any = true;
-      }
-      if (!any) continue;
-      const uint64_t rmask = (1ull << e1) | (e2 >= 0 ? (1ull << e2) : 0ull);
-      // L_R, partitioned: entries with |K' \ j| <= 1 first, then those with
-      // |K' \ j| = 2; each part in ascending j, so every sum over interacting
-      // determinants runs in a fixed order (bitwise reproducible results)
-      auto lr_store = [&](int slot, int t) {
-        const int j = my_nb_j[t];
-        if (slot < p.lr_cap) {
-          lr_j[slot] = j;
-          const uint64_t* v = p.S + (size_t)j * 2 * W;
-#pragma unroll
-          for (int q = 0; q < 2 * W; ++q) lr_bits[(size_t)slot * 2 * W + q] = __ldg(&v[q]);
-        }
-        my_lr_idx[slot] = j;
-      };
-      auto lr_m = [&](int t) {
-        const uint64_t em = my_nb_em[t];
-        return __popcll(em) - __popcll(em & rmask);
-      };
-      const int n01 = ordered_compact(nnb, [&](int t) { return lr_m(t) <= 1; }, lr_store, ctmp);
-      const int n2 = ordered_compact(
-          nnb, [&](int t) { return lr_m(t) == 2; }, [&](int slot, int t) { lr_store(n01 + slot, t); },
-          ctmp);
-      const int nlr = n01 + n2;
-      const bool fast = nlr <= p.lr_cap;
-      if (!fast && tid == 0) atomicAdd(&p.counters[C_LRFALLBACK], 1ull);
-      // K' = k - R
-      uint64_t kp[2 * W];
-#pragma unroll
-      for (int q = 0; q < 2 * W; ++q) kp[q] = kb[q];
-      kp[sp1 * W + (o1 >> 6)] &= ~(1ull << (o1 & 63));
-      if (e2 >= 0) kp[sp2 * W + (o2 >> 6)] &= ~(1ull << (o2 & 63));
-      // diagonal energies of I = K' + A from those of K' (cip/hdig.f, hmp.f
-      // written over occupation changes dn relative to the reference):
-      //   hdig = sum_r dn_r F_rr + 1/2 sum_rs dn_r dn_s (J_rs - [same spin] K_rs)
-      //   hmp  = sum_r dn_r fmpb_r
-      if (tid == 0) {
-        int nd = 0;
-        for (int sp = 0; sp < 2; ++sp)
-          for (int w = 0; w < W; ++w) {
-            uint64_t h = hf[sp * W + w] & ~kp[sp * W + w];
-            while (h) {
-              const int b = __ffsll((long long)h) - 1;
-              h &= h - 1;
-              sh.dn_so[nd] = w * 64 + b + sp * p.norb;
-              sh.dn_sg[nd++] = -1;
-            }
-            uint64_t t2 = kp[sp * W + w] & ~hf[sp * W + w];
-            while (t2) {
-              const int b = __ffsll((long long)t2) - 1;
-              t2 &= t2 - 1;
-              sh.dn_so[nd] = w * 64 + b + sp * p.norb;
-              sh.dn_sg[nd++] = 1;
-            }
-          }
-        sh.ndn = nd;
-      }
-      __syncthreads();
-      {
-        const int ndn = sh.ndn, n = p.norb;
-        for (int a = tid; a < 2 * n; a += blockDim.x) {
-          const int oa = a % n, sa = a / n;
-          double g = 0.0;
-          for (int i = 0; i < ndn; ++i) {
-            const int r = sh.dn_so[i];
-            const int t = tri(oa, r % n);
-            double x = __ldg(&p.J[t]);
-            if (sa == r / n) x -= __ldg(&p.K[t]);
-            g += sh.dn_sg[i] * x;
-          }
-          const int ta = tri(oa, oa);
-          sh.vdg[a] = __ldg(&p.F[ta]) + g + 0.5 * (__ldg(&p.J[ta]) - __ldg(&p.K[ta]));
-        }
-        if (tid == 32) {
-          double e = 0.0, mp = 0.0;
-          for (int i = 0; i < ndn; ++i) {
-            const int r = sh.dn_so[i], orr = r % n;
-            e += sh.dn_sg[i] * __ldg(&p.F[tri(orr, orr)]);
-            mp += sh.dn_sg[i] * __ldg(&p.fmpb[r]);
-            for (int j = 0; j < ndn; ++j) {
-              const int q = sh.dn_so[j];
-              const int t = tri(orr, q % n);
-              double x = __ldg(&p.J[t]);
-              if (r / n == q / n) x -= __ldg(&p.K[t]);
-              e += 0.5 * sh.dn_sg[i] * sh.dn_sg[j] * x;
-            }
-          }
-          sh.hK = e;
-          sh.mK = mp;
-        }
-      }
-      __syncthreads();
-      const int symR = e2 >= 0 ? p.its[p.orbsym[o1]][p.orbsym[o2]] : p.orbsym[o1];
-      // added-orbital space
-      const int nv1 = sh.nvir[sp1];
-      int nA;
-      if (nRr == 1) {
-        nA = nv1;
-      } else if (sp1 == sp2) {
-        nA = nv1 * (nv1 - 1) / 2;
-      } else {
-        nA = sh.nvir[0] * sh.nvir[1];
-      }
-      // One candidate I = K' + {a1[, a2]}: rank-change class, symmetry and
-      // spin-pattern rules, then a scan of L_R entries [0, nscan) plus the
-      // listed entries rb[0..nrb) (owner test, already in S, <I|H|j>), then
-      // the E2 / selection epilogue.  Called by whole warps.
-      auto candidate = [&](bool live, int a1, int a2, int sa1, int sa2, int nscan, const int16_t* rb,
-                           int nrb) {
-        int D = 0;
-        bool ysyspi = true;
-        if (live) {
-          const int aV = (a1 >= p.noca ? 1 : 0) + (a2 >= 0 && a2 >= p.noca ? 1 : 0);
-          D = hfR + aV - nRr;
-          if (!(dmask & (1u << (D + 2)))) live = false;
-          const int symA = a2 >= 0 ? p.its[p.orbsym[a1]][p.orbsym[a2]] : p.orbsym[a1];
-          if (p.its[symR][symA] != 0) live = false;
-          // diexcit spin patterns for generators without a flip partner
-          if (live && D == 2) {
-            if (sp1 != sp2) {
-              // alpha hole orbital o1, beta hole o2, alpha particle a1, beta particle a2
-              ysyspi = !(o1 == o2 && a1 == a2);
-              const bool unflipped = (o1 < o2) || (o1 == o2 && a1 <= a2);
-              if (!yefk && !unflipped) live = false;
-            } else if (!yefk && sp1 == 1) {
-              live = false;
-            }
-          }
-        }
-        uint64_t u[2 * W];
-#pragma unroll
-        for (int q = 0; q < 2 * W; ++q) u[q] = kp[q];
-        double bc[R];
-#pragma unroll
-        for (int m = 0; m < R; ++m) bc[m] = 0.0;
-        int nint = 0, nnz = 0, lesp = 0;
-        if (live) {
-          acc.ncand++;
-          u[sa1 * W + (a1 >> 6)] |= (1ull << (a1 & 63));
-          if (a2 >= 0) u[sa2 * W + (a2 >> 6)] |= (1ull << (a2 & 63));
-          const int rankI = rank_k + D;
-          bool drop = false;
-          // one S determinant of L_R against I: owner test, already-in-S
-          // test, <I|H|j> accumulation; returns true when I is dropped
-          auto visit = [&](int i, int x) -> bool {
-            uint64_t vv[2 * W];
-            int j;
-            if (fast) {
-              j = lr_j[i];
-#pragma unroll
-              for (int q = 0; q < 2 * W; ++q) vv[q] = lr_bits[(size_t)i * 2 * W + q];
-            } else {
-              j = my_lr_idx[i];
-#pragma unroll
-              for (int q = 0; q < 2 * W; ++q) vv[q] = __ldg(&p.S[(size_t)j * 2 * W + q]);
-            }
-            if (j < k) return p.ygen[j] != 0;
-            if (x == 0) return true;
-            int rankJ = 0;
-#pragma unroll
-            for (int q = 0; q < 2 * W; ++q) rankJ += __popcll(hf[q] & ~vv[q]);
-            int kind;
-            const double h = hmat<W>(p, u, vv, rankI, rankJ, hf, kind);
-            if (kind == 1) acc.np1++; else acc.np2++;
-            ++nint;
-            if (h != 0.0) ++nnz;
-            if (j > k && j <= k + nespk) ++lesp;
-#pragma unroll
-            for (int m = 0; m < R; ++m)
-              if (m < p.metat) bc[m] += h * __ldg(&p.c[(size_t)j * p.metat + m]);
-            return false;
-          };
-          for (int i0 = 0; i0 < nscan && !drop; i0 += 4) {
-            // four independent compares per step (latency of the loads overlaps)
-            int xs[4];
-#pragma unroll
-            for (int g4 = 0; g4 < 4; ++g4) {
-              const int i = i0 + g4;
-              int x = 99;
-              if (i < nscan) {
-                x = 0;
-                if (fast) {
-#pragma unroll
-                  for (int q = 0; q < 2 * W; ++q) x += __popcll(u[q] ^ lr_bits[(size_t)i * 2 * W + q]);
-                } else {
-                  const int jj = my_lr_idx[i];
-#pragma unroll
-                  for (int q = 0; q < 2 * W; ++q) x += __popcll(u[q] ^ __ldg(&p.S[(size_t)jj * 2 * W + q]));
-                }
-              }
-              xs[g4] = x;
-            }
-            if (xs[0] > 4 && xs[1] > 4 && xs[2] > 4 && xs[3] > 4) continue;
-#pragma unroll 1
-            for (int g4 = 0; g4 < 4 && !drop; ++g4)
-              if (xs[g4] <= 4) drop = visit(i0 + g4, xs[g4]);
-          }
-          for (int q2 = 0; q2 < nrb && !drop; ++q2) {
-            const int i = rb[q2];
-            int x = 0;
-#pragma unroll
-            for (int q = 0; q < 2 * W; ++q) x += __popcll(u[q] ^ lr_bits[(size_t)i * 2 * W + q]);
-            if (x <= 4) drop = visit(i, x);
-          }
-          acc.ncmp += (unsigned long long)(nscan + nrb);
-          if (drop || nint == 0) live = false;
-          if (live && D == 2 && nnz == 0) live = false;  // diexcit drops zero couplings
-        }
-        const bool is_pert1 = (D != 2);
-        double fmul = 0.0, hmpi = 0.0, hvpi = 0.0;
-        int nmul = 0;
-        bool ybis = false;
-        if (live) {
-          if (is_pert1) {
-            if (nespk != 0) {
-              ybis = true;
-              fmul = (1.0 / (double)(lesp + 1)) * (double)(nespk + 1) - 1.0;
-              nmul = (int)fmul;
-            }
-          } else {
-            int nespf = nespk;
-            ybis = nespf > 0;
-            if (yefk || ysyspi) {
-              ybis = true;
-              if (!yefk) nespf = nespf + nespf + 1;
-            }
-            fmul = (1.0 / (double)(lesp + 1)) * (double)(nespf + 1) - 1.0;
-            nmul = (int)fmul;
-          }
-          hmpi = sh.mK + __ldg(&p.fmpb[a1 + sa1 * p.norb]);
-          hvpi = sh.hK + sh.vdg[a1 + sa1 * p.norb];
-          if (a2 >= 0) {
-            hmpi += __ldg(&p.fmpb[a2 + sa2 * p.norb]);
-            const int tq = tri(a1, a2);
-            double gq = __ldg(&p.J[tq]);
-            if (sa1 == sa2) gq -= __ldg(&p.K[tq]);
-            hvpi += sh.vdg[a2 + sa2 * p.norb] + gq;
-          }
-        }
-        enqueue_candidate<W, R>(p, wq, qn, live, u, hmpi, hvpi, bc, k1, fmul, nmul, ybis, is_pert1, acc, hp);
-      };
-      if (nRr == 1 || !fast) {
-        // flat: threads take candidates, every candidate scans all of L_R
-        for (int t0 = 0; t0 < nA; t0 += blockDim.x) {
-          const int t = t0 + tid;
-          const bool live = t < nA;
-          int a1 = 0, a2 = -1, sa1 = sp1, sa2 = sp2;
-          if (live) {
-            if (nRr == 1) {
-              a1 = sh.vir[sp1][t];
-            } else if (sp1 == sp2) {
-              // t -> (x < y) over nv1 virtuals
-              int x = 0, tt = t;
-              while (tt >= nv1 - 1 - x) {
-                tt -= nv1 - 1 - x;
-                ++x;
-              }
-              a1 = sh.vir[sp1][x];
-              a2 = sh.vir[sp1][x + 1 + tt];
-            } else {
-              a1 = sh.vir[0][t / sh.nvir[1]];
-              a2 = sh.vir[1][t % sh.nvir[1]];
-              sa1 = 0;
-              sa2 = 1;
-            }
-          }
-          candidate(live, a1, a2, sa1, sa2, nlr, nullptr, 0);
-        }
-      } else {
-        // rows: one warp per first added orbital a1; an entry with
-        // |K' \ j| = 2 interacts only if it occupies both added orbitals, so
-        // the warp lists the ones that occupy a1 and its lanes (columns a2)
-        // scan the |K' \ j| <= 1 part plus that short list
-        const int lane = tid & 31, wid = tid >> 5, nwarps = blockDim.x >> 5;
-        const bool same = sp1 == sp2;
-        const int sr = same ? sp1 : 0, sc = same ? sp1 : 1;
-        const int nrows = same ? nv1 - 1 : sh.nvir[0];
-        int16_t* rowbuf = wrow + wid * kRowCap;
-        for (int row = wid; row < nrows; row += nwarps) {
-          const int a1 = sh.vir[sr][row];
-          const int w1 = sr * W + (a1 >> 6);
-          const uint64_t b1 = 1ull << (a1 & 63);
-          int nrb = 0;
-          for (int i0 = n01; i0 < nlr; i0 += 32) {
-            const int i = i0 + lane;
-            const bool has = i < nlr && (lr_bits[(size_t)i * 2 * W + w1] & b1);
-            const unsigned bm = __ballot_sync(0xffffffffu, has);
-            if (has) {
-              const int pos = nrb + __popc(bm & ((1u << lane) - 1u));
-              if (pos < kRowCap) rowbuf[pos] = (int16_t)i;
-            }
-            nrb += __popc(bm);
-          }
-          __syncwarp();
-          const bool overflow = nrb > kRowCap;
-          const int ncols = same ? nv1 - 1 - row : sh.nvir[1];
-          for (int c0 = 0; c0 < ncols; c0 += 32) {
-            const int c = c0 + lane;
-            const bool live = c < ncols;
-            const int a2 = live ? (same ? sh.vir[sc][row + 1 + c] : sh.vir[sc][c]) : 0;
-            if (!overflow)
-              candidate(live, a1, a2, sr, sc, n01, rowbuf, nrb);
-            else
-              candidate(live, a1, a2, sr, sc, nlr, nullptr, 0);
-          }
-          __syncwarp();
-        }
-      }
-      __syncthreads();
-    }
-    drain_queue<W, R>(p, wq, qn, true, acc, hp);
-    block_flush<R>(p, acc, unit, red);
-  }
-
-  // block totals of the integer counters and the histogram
-  __syncthreads();
-  {
-    unsigned long long v[8] = {acc.ietat, acc.nproc, 0ull, acc.ncand, acc.ncmp, acc.np1, acc.np2, 0ull};
-    for (int q = 0; q < 8; ++q) {
-      unsigned long long x = v[q];
-      for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
-      if ((tid & 31) == 0 && x) atomicAdd(&p.counters[q], x);
-    }
-    unsigned long long db = __double_as_longlong(acc.dpivot);
-    for (int o = 16; o > 0; o >>= 1) {
-      const unsigned long long y = __shfl_down_sync(0xffffffffu, db, o);
-      db = y > db ? y : db;
-    }
-    if ((tid & 31) == 0) atomicMax(p.dpivot_bits, db);
-  }
-  // this thread's histogram into the block's
-  for (int c = 0; c < p.nclass; ++c) {
-    if (hp.nom[c]) atomicAdd(&hist.nom[c], hp.nom[c]);
-    for (int m = 0; m < R && m < p.metat; ++m) {
-      if (hp.tab[c][0][m] != 0.0) atomicAdd(&hist.tab[c * kMaxRoots + m], hp.tab[c][0][m]);
-      if (hp.tab[c][1][m] != 0.0)
-        atomicAdd(&hist.tab[kNClass * kMaxRoots + c * kMaxRoots + m], hp.tab[c][1][m]);
-      if (hp.nam[c][m]) atomicAdd(&hist.nam[c * kMaxRoots + m], hp.nam[c][m]);
-    }
-  }
-  __syncthreads();
-  for (int i = tid; i < p.nclass; i += blockDim.x)
-    if (hist.nom[i]) atomicAdd(&p.hist_nom[i], hist.nom[i]);
-  for (int i = tid; i < p.nclass * kMaxRoots; i += blockDim.x) {
-    const int c = i / kMaxRoots, m = i % kMaxRoots;
-    if (m >= p.metat) continue;
-    if (hist.nam[i]) atomicAdd(&p.hist_nam[c * p.metat + m], hist.nam[i]);
-    if (hist.tab[i] != 0.0) atomicAdd(&p.hist_tab[c * p.metat + m], hist.tab[i]);
-    const double tv = hist.tab[kNClass * kMaxRoots + i];
-    if (tv != 0.0) atomicAdd(&p.hist_tab[p.nclass * p.metat + c * p.metat + m], tv);
-  }
-}
-
-// fixed-order Kahan reduction of the per-generator partial sums
-__global__ void k_reduce(const double* part, int ngen, int nq, double* out) {
-  const int q = blockIdx.x * blockDim.x + threadIdx.x;
-  if (q >= nq) return;
+// fixed-order Kahan reduction of the per-unit partial sums: block q sums
+// column q; thread t takes a contiguous range of units, then thread 0 adds
+// the per-thread sums in thread order (bitwise reproducible)
+constexpr int kReduceThreads = 256;
+__global__ void __launch_bounds__(kReduceThreads) k_reduce(const double* part, int nunits, int nq,
+                                                           double* out) {
+  __shared__ double ps[kReduceThreads], pc[kReduceThreads];
+  const int q = blockIdx.x;
+  const int per = (nunits + kReduceThreads - 1) / kReduceThreads;
+  const int u0 = threadIdx.x * per, u1 = min(nunits, u0 + per);
   double s = 0.0, c = 0.0;
-  for (int g = 0; g < ngen; ++g) kahan_add(s, c, part[(long long)g * nq + q]);
-  out[q] = s - c;
+  for (int u = u0; u < u1; ++u) kahan_add(s, c, part[(long long)u * nq + q]);
+  ps[threadIdx.x] = s;
+  pc[threadIdx.x] = c;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double S = 0.0, C = 0.0;
+    for (int t = 0; t < kReduceThreads; ++t) {
+      kahan_add(S, C, ps[t]);
+      kahan_add(S, C, -pc[t]);
+    }
+    out[q] = S - C;
+  }
+}
+
+// k_reduce for every geometry of a batch: block (q, b) sums column q of
+// geometry b's per-unit partials into its reduced sums
+__global__ void __launch_bounds__(kReduceThreads) k_reduce_batch(const Params* geo) {
+  __shared__ double ps[kReduceThreads], pc[kReduceThreads];
+  const Params& p = geo[blockIdx.y];
+  const int nq = 5 * p.metat;
+  const int q = blockIdx.x;
+  if (q >= nq) return;
+  const int nunits = p.nunits;
+  const int per = (nunits + kReduceThreads - 1) / kReduceThreads;
+  const int u0 = threadIdx.x * per, u1 = min(nunits, u0 + per);
+  double s = 0.0, c = 0.0;
+  for (int u = u0; u < u1; ++u) kahan_add(s, c, p.gen_part[(long long)u * nq + q]);
+  ps[threadIdx.x] = s;
+  pc[threadIdx.x] = c;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double S = 0.0, C = 0.0;
+    for (int t = 0; t < kReduceThreads; ++t) {
+      kahan_add(S, C, ps[t]);
+      kahan_add(S, C, -pc[t]);
+    }
+    p.red[q] = S - C;
+  }
+}
+
+// adjoint: sum the per-block slices [F | J | K | fmpb] over blocks
+__global__ void k_slice_reduce(const double* sl, int nblocks, int stride, int nt, double* gF, double* gJ,
+                               double* gK, double* gf) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= stride) return;
+  double s = 0.0;
+  for (int b = 0; b < nblocks; ++b) s += sl[(size_t)b * stride + i];
+  if (i < nt) gF[i] += s;
+  else if (i < 2 * nt) gJ[i - nt] = s;
+  else if (i < 3 * nt) gK[i - 2 * nt] = s;
+  else gf[i - 3 * nt] = s;
+}
+
+// zero what every geometry of a batch accumulates into (block b: geometry b)
+__global__ void k_batch_clear(const Params* geo) {
+  const Params& p = geo[blockIdx.x];
+  const int ncount = C_NCOUNTERS + 1 + kNClass + kNClass * kMaxRoots;
+  for (int i = threadIdx.x; i < ncount; i += blockDim.x) p.counters[i] = 0ull;
+  for (int i = threadIdx.x; i < 2 * kNClass * kMaxRoots; i += blockDim.x) p.hist_tab[i] = 0.0;
+  const long long npart = (long long)max(p.nunits, 1) * 5 * p.metat;
+  for (long long i = threadIdx.x; i < npart; i += blockDim.x) p.gen_part[i] = 0.0;
 }
 
 }  // namespace
@@ -1244,6 +119,7 @@ struct cipsi_ctx {
   int32_t* dnesp = nullptr;
   double* dc = nullptr;
   float* deri = nullptr;
+  double* deri64 = nullptr;  // FP64 storage of (pq|rs) (cipsi_set_integrals_f64store)
   int32_t* dpairtab = nullptr;
   int32_t* dntttt = nullptr;
   double *dF = nullptr, *dJ = nullptr, *dK = nullptr, *dfmpb = nullptr;
@@ -1272,6 +148,18 @@ struct cipsi_ctx {
   double *dsel_xam = nullptr, *dsel_evp = nullptr;
   long long sel_cap = 0;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  // launch tuning (cipsi_set_tuning): R blocks per work unit for generators
+  // of excitation rank >= 2 (rank 0/1 generators get one block per unit),
+  // and CTAs per SM (0 = as many as the shared-memory L_R size allows)
+  int tune_r_chunk = 6;
+  int tune_ctas = 0;
+  // set by a batched run: the event that marks its end (fetch waits on it),
+  // and whether ev0/ev1 time this context's own launch
+  cudaEvent_t ext_done = nullptr;
+  bool ev_valid = false;
+  // bumped whenever a device buffer is (re)allocated: a batch built on this
+  // context refuses to run after that
+  unsigned long long buf_gen = 0;
   // pending run
   int ngen = 0;
   int nclass = kNClass;
@@ -1298,6 +186,7 @@ template <typename T>
 int upload(cipsi_ctx* ctx, T** dptr, const T* h, size_t n) {
   if (*dptr) cudaFree(*dptr);
   *dptr = nullptr;
+  ++ctx->buf_gen;
   CK(cudaMalloc((void**)dptr, std::max<size_t>(n, 1) * sizeof(T)));
   if (n) CK(cudaMemcpyAsync(*dptr, h, n * sizeof(T), cudaMemcpyHostToDevice, ctx->stream));
   return 0;
@@ -1361,6 +250,7 @@ void cipsi_ctx_destroy(cipsi_ctx* ctx) {
   dfree(ctx->dS); dfree(ctx->dygen); dfree(ctx->dyef); dfree(ctx->dnesp); dfree(ctx->dc);
   dfree(ctx->deri); dfree(ctx->dpairtab); dfree(ctx->dntttt); dfree(ctx->dF); dfree(ctx->dJ);
   dfree(ctx->dK); dfree(ctx->dfmpb); dfree(ctx->dorbsym); dfree(ctx->dgens); dfree(ctx->dgmask);
+  dfree(ctx->deri64);
   dfree(ctx->dunits);
   dfree(ctx->dnb_j); dfree(ctx->dnb_em); dfree(ctx->dlr_idx); dfree(ctx->dgen_part);
   dfree(ctx->dcounters); dfree(ctx->dhist_tab); dfree(ctx->dred); dfree(ctx->dwork);
@@ -1433,6 +323,10 @@ int cipsi_set_integrals(cipsi_ctx* ctx, const int32_t* itsym, const int32_t* its
   if (rc) return rc;
   if (!bijkl) return fail(ctx, CIPSI_ERR_ARG, "bijkl is null");
   if ((rc = upload(ctx, &ctx->deri, bijkl, (size_t)ninte))) return rc;
+  if (ctx->deri64) {
+    ++ctx->buf_gen;
+    dfree(ctx->deri64);
+  }
   CK(cudaStreamSynchronize(ctx->stream));
   ctx->have_int = true;
   return CIPSI_OK;
@@ -1447,6 +341,24 @@ int cipsi_set_integrals_fp64(cipsi_ctx* ctx, const int32_t* itsym, const int32_t
   std::vector<float> b((size_t)ninte);
   for (int64_t i = 0; i < ninte; ++i) b[i] = (float)pqrs[i];  // real*8 -> real*4 (RN)
   return cipsi_set_integrals(ctx, itsym, its, f, aj, ak, ij0, ntttt, b.data(), ninte);
+}
+
+int cipsi_set_integrals_f64store(cipsi_ctx* ctx, const int32_t* itsym, const int32_t* its,
+                                 const double* f, const double* aj, const double* ak,
+                                 const int16_t* ij0, const int32_t* ntttt, const double* pqrs,
+                                 int64_t ninte) {
+  if (!ctx) return CIPSI_ERR_ARG;
+  if (!pqrs) return fail(ctx, CIPSI_ERR_ARG, "pqrs is null");
+  int rc = set_integrals_common(ctx, itsym, its, f, aj, ak, ij0, ntttt, ninte);
+  if (rc) return rc;
+  if ((rc = upload(ctx, &ctx->deri64, pqrs, (size_t)ninte))) return rc;
+  if (!ctx->deri) {
+    const float zero = 0.f;
+    if ((rc = upload(ctx, &ctx->deri, &zero, 1))) return rc;
+  }
+  CK(cudaStreamSynchronize(ctx->stream));
+  ctx->have_int = true;
+  return CIPSI_OK;
 }
 
 int cipsi_set_space(cipsi_ctx* ctx, const int32_t* ne, const int32_t* nd, const int32_t* trou,
@@ -1570,24 +482,33 @@ static size_t queue_bytes(int W, int R) {
   }
 }
 
-template <int W, int R>
-static cudaError_t launch_pt2(const Params& p, int grid, size_t smem, cudaStream_t st) {
-  cudaError_t e = cudaFuncSetAttribute(k_pt2<W, R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)smem);
-  if (e != cudaSuccess) return e;
-  k_pt2<W, R><<<grid, kThreads, smem, st>>>(p);
-  return cudaGetLastError();
-}
 
-extern "C" {
 
-int cipsi_run_pt2_async(cipsi_ctx* ctx, const cipsi_opts* o) {
+namespace {
+
+int roots_pad(int mt) { return mt <= 1 ? 1 : mt <= 2 ? 2 : mt <= 4 ? 4 : 8; }
+
+int check_run_args(cipsi_ctx* ctx, const cipsi_opts* o) {
   if (!ctx || !o) return CIPSI_ERR_ARG;
   if (!ctx->have_int || !ctx->have_space || !ctx->have_roots)
     return fail(ctx, CIPSI_ERR_STATE, "run before set_integrals / set_space / set_roots");
   if (o->nclass < 2 || o->nclass > kNClass) return fail(ctx, CIPSI_ERR_ARG, "nclass must be in [2, 10]");
-  CK(cudaSetDevice(ctx->device));
-  const int ncf = ctx->d.ncf, W = ctx->W, mt = ctx->d.metat;
+  for (int i = 0; i + 1 < o->nclass; ++i)
+    if (!(o->aval[i] >= 0.0) || (i > 0 && !(o->aval[i] > o->aval[i - 1])))
+      return fail(ctx, CIPSI_ERR_ARG, "aval must be non-negative and increasing");
+  return CIPSI_OK;
+}
+
+// Generators, their allowed rank changes and the work units of one run.
+struct RunPlan {
+  std::vector<int32_t> gens;   // generator indices (0-based); -1 = pertu block
+  std::vector<uint8_t> gmask;  // allowed rank changes, bit (D + 2)
+  std::vector<int32_t> ug, ur0, ur1;
+  bool pertu_ref = false, pertu_mono = false;
+};
+
+void plan_run(const cipsi_ctx* ctx, const cipsi_opts* o, int r_chunk, RunPlan& pl) {
+  const int ncf = ctx->d.ncf, W = ctx->W;
   // flags on the content of S (pertu.f:52-61)
   bool yd = false, ym = false, yf = false;
   for (int k = 0; k < ncf; ++k) {
@@ -1596,10 +517,12 @@ int cipsi_run_pt2_async(cipsi_ctx* ctx, const cipsi_opts* o) {
     if (ctx->rank[k] == 2) yf = true;
   }
   if (ym) yf = true;
-  std::vector<int32_t> gens;
-  std::vector<uint8_t> gmask;
+  std::vector<int32_t>& gens = pl.gens;
+  std::vector<uint8_t>& gmask = pl.gmask;
   const bool pertu_ref = yf && !yd && ctx->d.isym == 1;  // isz == 0, !yion
   const bool pertu_mono = yf && ym;
+  pl.pertu_ref = pertu_ref;
+  pl.pertu_mono = pertu_mono;
   if (o->run_pertu && (pertu_ref || pertu_mono)) {
     gens.push_back(-1);
     gmask.push_back(0);
@@ -1609,6 +532,7 @@ int cipsi_run_pt2_async(cipsi_ctx* ctx, const cipsi_opts* o) {
     if (o->gen_mask && !o->gen_mask[k]) continue;
     const int nec = ctx->rank[k];
     // allowed rank changes, bit (D + 2); D = +2 (diexcit) always
+    // (igene.f:34-35, 89-90, 199-200, 296-298)
     uint8_t m = 1u << 4;
     if (!((nec == 0 && ym) || (nec == 1 && yd))) {
       m |= 1u << 3;  // +1
@@ -1625,124 +549,139 @@ int cipsi_run_pt2_async(cipsi_ctx* ctx, const cipsi_opts* o) {
     gmask.push_back(m);
   }
   const int ngen = (int)gens.size();
-  ctx->ngen = ngen;
-  // work units: a generator's R blocks are split into chunks of at most
-  // kRChunk blocks that have an allowed rank-change class, so one heavy
-  // generator does not serialise on one SM; low-rank generators (which meet
-  // most of S) are queued first.
-  constexpr int kRChunk = 6;
+  // work units: a generator's R blocks that have an allowed rank-change class
+  // are split into chunks (one block per unit for generators of rank 0 and 1,
+  // which meet most of S; r_chunk blocks for the others), so one heavy
+  // generator does not serialise on one SM; low-rank generators are queued
+  // first.
+  const int kRChunkHigh = std::max(1, r_chunk);
   constexpr int kPertuChunk = 128;
-  std::vector<int32_t> ug, ur0, ur1;
-  {
-    const int n = ctx->d.norb, noca = ctx->d.noca, nel = 2 * noca;
-    const int nR = nel + nel * (nel - 1) / 2;
-    std::vector<int> order(ngen);
-    for (int g = 0; g < ngen; ++g) order[g] = g;
-    std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
-      const int ra = gens[a] < 0 ? -1 : ctx->rank[gens[a]];
-      const int rb = gens[b] < 0 ? -1 : ctx->rank[gens[b]];
-      return ra < rb;
-    });
-    std::vector<int> hfe(nel);
-    for (int g : order) {
-      const int k = gens[g];
-      if (k < 0) {
-        const int ntot = (pertu_ref ? 1 : 0) + (pertu_mono ? 2 * noca * (n - noca) : 0);
-        for (int t = 0; t < ntot; t += kPertuChunk) {
-          ug.push_back(g);
-          ur0.push_back(t);
-          ur1.push_back(std::min(ntot, t + kPertuChunk));
-        }
-        continue;
+  std::vector<int32_t>& ug = pl.ug;
+  std::vector<int32_t>& ur0 = pl.ur0;
+  std::vector<int32_t>& ur1 = pl.ur1;
+  const int n = ctx->d.norb, noca = ctx->d.noca, nel = 2 * noca;
+  const int nR = nel + nel * (nel - 1) / 2;
+  std::vector<int> order(ngen);
+  for (int g = 0; g < ngen; ++g) order[g] = g;
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+    const int ra = gens[a] < 0 ? -1 : ctx->rank[gens[a]];
+    const int rb = gens[b] < 0 ? -1 : ctx->rank[gens[b]];
+    return ra < rb;
+  });
+  std::vector<int> hfe(nel);
+  for (int g : order) {
+    const int k = gens[g];
+    if (k < 0) {
+      const int ntot = (pertu_ref ? 1 : 0) + (pertu_mono ? 2 * noca * (n - noca) : 0);
+      for (int t = 0; t < ntot; t += kPertuChunk) {
+        ug.push_back(g);
+        ur0.push_back(t);
+        ur1.push_back(std::min(ntot, t + kPertuChunk));
       }
-      // electrons of k: alpha orbitals ascending, then beta; HF-occupied?
-      int ne = 0;
-      for (int sp = 0; sp < 2; ++sp)
-        for (int o = 0; o < n; ++o)
-          if ((ctx->Sbits[(size_t)k * 2 * W + sp * W + (o >> 6)] >> (o & 63)) & 1ull) hfe[ne++] = o < noca;
-      const uint8_t m = gmask[g];
-      auto allowed = [&](int r) {
-        int hfR, nRr;
-        if (r < nel) {
-          hfR = hfe[r];
-          nRr = 1;
-        } else {
-          int t = r - nel, e1 = 0;
-          while (t >= nel - 1 - e1) {
-            t -= nel - 1 - e1;
-            ++e1;
-          }
-          hfR = hfe[e1] + hfe[e1 + 1 + t];
-          nRr = 2;
+      continue;
+    }
+    // electrons of k: alpha orbitals ascending, then beta; HF-occupied?
+    int ne = 0;
+    for (int sp = 0; sp < 2; ++sp)
+      for (int orb = 0; orb < n; ++orb)
+        if ((ctx->Sbits[(size_t)k * 2 * W + sp * W + (orb >> 6)] >> (orb & 63)) & 1ull) hfe[ne++] = orb < noca;
+    const uint8_t m = gmask[g];
+    auto allowed = [&](int r) {
+      int hfR, nRr;
+      if (r < nel) {
+        hfR = hfe[r];
+        nRr = 1;
+      } else {
+        int t = r - nel, e1 = 0;
+        while (t >= nel - 1 - e1) {
+          t -= nel - 1 - e1;
+          ++e1;
         }
-        for (int aV = 0; aV <= nRr; ++aV)
-          if (m & (1u << (hfR + aV - nRr + 2))) return true;
-        return false;
-      };
-      int cnt = 0, start = -1;
-      for (int r = 0; r < nR; ++r) {
-        if (!allowed(r)) continue;
-        if (start < 0) start = r;
-        if (++cnt == kRChunk) {
-          ug.push_back(g);
-          ur0.push_back(start);
-          ur1.push_back(r + 1);
-          cnt = 0;
-          start = -1;
-        }
+        hfR = hfe[e1] + hfe[e1 + 1 + t];
+        nRr = 2;
       }
-      if (start >= 0) {
+      for (int aV = 0; aV <= nRr; ++aV)
+        if (m & (1u << (hfR + aV - nRr + 2))) return true;
+      return false;
+    };
+    const int kRChunk = ctx->rank[k] <= 1 ? 1 : kRChunkHigh;
+    int cnt = 0, start = -1;
+    for (int r = 0; r < nR; ++r) {
+      if (!allowed(r)) continue;
+      if (start < 0) start = r;
+      if (++cnt == kRChunk) {
         ug.push_back(g);
         ur0.push_back(start);
-        ur1.push_back(nR);
+        ur1.push_back(r + 1);
+        cnt = 0;
+        start = -1;
       }
     }
+    if (start >= 0) {
+      ug.push_back(g);
+      ur0.push_back(start);
+      ur1.push_back(nR);
+    }
   }
-  const int nunits = (int)ug.size();
-  ctx->nunits = nunits;
-  int dev_sms = 0;
-  CK(cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, ctx->device));
-  // shared L_R capacity: enough for every neighbour list when it fits
+}
+
+// Shared-memory L_R capacity, dynamic shared memory and CTAs per SM.
+// ctas: 0 = 200 KB per CTA (two CTAs per SM when the list fits in half),
+// 1 = one CTA per SM, 2 = sized so that two CTAs fit per SM.
+struct LaunchShape {
+  int lr_cap;
+  size_t smem;
+  int blocks_per_sm;
+};
+
+LaunchShape launch_shape(int W, int R, int ncf_max, int ctas) {
   const size_t per_entry = (size_t)2 * W * 8 + 4;
-  const size_t qbytes = (size_t)(kThreads / 32) * queue_bytes(W, mt <= 1 ? 1 : mt <= 2 ? 2 : mt <= 4 ? 4 : 8);
-  const size_t smem_budget = (size_t)200 * 1024 - qbytes;  // L_R share of the dynamic smem
-  int lr_cap = (int)std::min<size_t>((size_t)ncf, smem_budget / per_entry);
-  const size_t smem = (((size_t)lr_cap * per_entry + 15) & ~(size_t)15) + qbytes + 16;
-  const int blocks_per_sm = smem <= 95 * 1024 ? 2 : 1;
-  int grid = std::max(1, std::min(nunits, dev_sms * blocks_per_sm));
-  // buffers
-  if ((size_t)grid > ctx->scratch_blocks || !ctx->dnb_j) {
-    dfree(ctx->dnb_j); dfree(ctx->dnb_em); dfree(ctx->dlr_idx);
-    CK(cudaMalloc(&ctx->dnb_j, (size_t)grid * ncf * sizeof(int32_t)));
-    CK(cudaMalloc(&ctx->dnb_em, (size_t)grid * ncf * sizeof(uint64_t)));
-    CK(cudaMalloc(&ctx->dlr_idx, (size_t)grid * ncf * sizeof(int32_t)));
-    ctx->scratch_blocks = grid;
-  }
+  const size_t qbytes = (size_t)(kThreads / 32) * queue_bytes(W, R);
+  const size_t smem_total = ctas == 2 ? (size_t)90 * 1024 : (size_t)200 * 1024;
+  const size_t smem_budget = smem_total > qbytes + 16 ? smem_total - qbytes - 16 : 0;
+  LaunchShape ls;
+  ls.lr_cap = (int)std::min<size_t>((size_t)ncf_max, smem_budget / per_entry);
+  ls.smem = (((size_t)ls.lr_cap * per_entry + 15) & ~(size_t)15) + qbytes + 16;
+  ls.blocks_per_sm = ctas == 1 ? 1 : ls.smem <= 95 * 1024 ? 2 : 1;
+  return ls;
+}
+
+// Device buffers of one run on ctx (generator and unit lists, per-unit
+// partial sums, counters, histogram, records), sized for the plan; the lists
+// are uploaded on stream st.
+int prepare_run(cipsi_ctx* ctx, const RunPlan& pl, cudaStream_t st) {
+  const int W = ctx->W, mt = ctx->d.metat;
+  const int ngen = (int)pl.gens.size(), nunits = (int)pl.ug.size();
+  ctx->ngen = ngen;
+  ctx->nunits = nunits;
   if (ngen > ctx->gens_cap) {
+    ++ctx->buf_gen;
     dfree(ctx->dgens); dfree(ctx->dgmask);
     CK(cudaMalloc(&ctx->dgens, (size_t)std::max(ngen, 1) * sizeof(int32_t)));
     CK(cudaMalloc(&ctx->dgmask, (size_t)std::max(ngen, 1)));
     ctx->gens_cap = ngen;
   }
   if (nunits > ctx->units_cap) {
+    ++ctx->buf_gen;
     dfree(ctx->dunits);
     CK(cudaMalloc(&ctx->dunits, (size_t)std::max(nunits, 1) * 3 * sizeof(int32_t)));
     ctx->units_cap = nunits;
   }
   if (ngen) {
-    CK(cudaMemcpyAsync(ctx->dgens, gens.data(), ngen * sizeof(int32_t), cudaMemcpyHostToDevice, ctx->stream));
-    CK(cudaMemcpyAsync(ctx->dgmask, gmask.data(), ngen, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(ctx->dgens, pl.gens.data(), ngen * sizeof(int32_t), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(ctx->dgmask, pl.gmask.data(), ngen, cudaMemcpyHostToDevice, st));
   }
   if (nunits) {
     ctx->hunits.resize((size_t)3 * nunits);
-    std::copy(ug.begin(), ug.end(), ctx->hunits.begin());
-    std::copy(ur0.begin(), ur0.end(), ctx->hunits.begin() + nunits);
-    std::copy(ur1.begin(), ur1.end(), ctx->hunits.begin() + 2 * nunits);
+    std::copy(pl.ug.begin(), pl.ug.end(), ctx->hunits.begin());
+    std::copy(pl.ur0.begin(), pl.ur0.end(), ctx->hunits.begin() + nunits);
+    std::copy(pl.ur1.begin(), pl.ur1.end(), ctx->hunits.begin() + 2 * nunits);
     CK(cudaMemcpyAsync(ctx->dunits, ctx->hunits.data(), (size_t)3 * nunits * sizeof(int32_t),
-                       cudaMemcpyHostToDevice, ctx->stream));
+                       cudaMemcpyHostToDevice, st));
   }
   const size_t nq = (size_t)5 * mt;
   if ((size_t)std::max(nunits, 1) * nq > ctx->gen_part_cap) {
+    ++ctx->buf_gen;
     dfree(ctx->dgen_part);
     ctx->gen_part_cap = (size_t)std::max(nunits, 1) * nq;
     CK(cudaMalloc(&ctx->dgen_part, ctx->gen_part_cap * sizeof(double)));
@@ -1750,32 +689,35 @@ int cipsi_run_pt2_async(cipsi_ctx* ctx, const cipsi_opts* o) {
   // counters [C_NCOUNTERS] + dpivot + nom[10] + nam[10*8]
   const size_t ncount = C_NCOUNTERS + 1 + kNClass + kNClass * kMaxRoots;
   if (!ctx->dcounters) {
+    ++ctx->buf_gen;
     CK(cudaMalloc(&ctx->dcounters, ncount * sizeof(unsigned long long)));
     CK(cudaMalloc(&ctx->dhist_tab, 2 * kNClass * kMaxRoots * sizeof(double)));
     CK(cudaMalloc(&ctx->dred, 5 * kMaxRoots * sizeof(double)));
     CK(cudaMalloc(&ctx->dwork, sizeof(int)));
   }
   if (ctx->sel_cap == 0) {
+    ++ctx->buf_gen;
     ctx->sel_cap = 1 << 20;
     CK(cudaMalloc(&ctx->dsel_bits, (size_t)ctx->sel_cap * 2 * W * sizeof(uint64_t)));
     CK(cudaMalloc(&ctx->dsel_owner, (size_t)ctx->sel_cap * sizeof(int32_t)));
     CK(cudaMalloc(&ctx->dsel_xam, (size_t)ctx->sel_cap * sizeof(double)));
     CK(cudaMalloc(&ctx->dsel_evp, (size_t)ctx->sel_cap * mt * sizeof(double)));
   }
-  CK(cudaMemsetAsync(ctx->dcounters, 0, ncount * sizeof(unsigned long long), ctx->stream));
-  CK(cudaMemsetAsync(ctx->dhist_tab, 0, 2 * kNClass * kMaxRoots * sizeof(double), ctx->stream));
-  CK(cudaMemsetAsync(ctx->dwork, 0, sizeof(int), ctx->stream));
-  CK(cudaMemsetAsync(ctx->dgen_part, 0, (size_t)std::max(nunits, 1) * nq * sizeof(double), ctx->stream));
+  return CIPSI_OK;
+}
 
-  Params p{};
+// Kernel parameters of one run on ctx (everything but the neighbour scratch
+// and the L_R capacity).
+void fill_params(const cipsi_ctx* ctx, const cipsi_opts* o, const RunPlan& pl, Params& p) {
+  const int mt = ctx->d.metat, nunits = (int)pl.ug.size();
   p.norb = ctx->d.norb;
   p.noca = ctx->d.noca;
   p.nel = 2 * ctx->d.noca;
-  p.ncf = ncf;
+  p.ncf = ctx->d.ncf;
   p.metat = mt;
   p.nsym = ctx->d.nsym;
   p.isym = ctx->d.isym;
-  p.ngen = ngen;
+  p.ngen = (int)pl.gens.size();
   p.gens = ctx->dgens;
   p.gen_dmask = ctx->dgmask;
   p.nunits = nunits;
@@ -1788,6 +730,7 @@ int cipsi_run_pt2_async(cipsi_ctx* ctx, const cipsi_opts* o) {
   p.yef = ctx->dyef;
   p.c = ctx->dc;
   p.eri = ctx->deri;
+  p.eri64 = ctx->deri64;
   p.pairtab = ctx->dpairtab;
   p.ntttt = ctx->dntttt;
   p.F = ctx->dF;
@@ -1816,50 +759,96 @@ int cipsi_run_pt2_async(cipsi_ctx* ctx, const cipsi_opts* o) {
     p.aval[i] = o->aval[i];
     std::memcpy(&p.aval_bits[i], &o->aval[i], 8);
   }
-  for (int i = 0; i + 1 < o->nclass; ++i)
-    if (!(o->aval[i] >= 0.0) || (i > 0 && !(o->aval[i] > o->aval[i - 1])))
-      return fail(ctx, CIPSI_ERR_ARG, "aval must be non-negative and increasing");
-  p.pertu_ref = pertu_ref ? 1 : 0;
-  p.pertu_mono = pertu_mono ? 1 : 0;
-  p.nb_j = ctx->dnb_j;
-  p.nb_emask = ctx->dnb_em;
-  p.lr_idx = ctx->dlr_idx;
-  p.lr_cap = lr_cap;
+  p.pertu_ref = pl.pertu_ref ? 1 : 0;
+  p.pertu_mono = pl.pertu_mono ? 1 : 0;
   p.gen_part = ctx->dgen_part;
   p.counters = ctx->dcounters;
   p.dpivot_bits = ctx->dcounters + C_NCOUNTERS;
   p.hist_nom = ctx->dcounters + C_NCOUNTERS + 1;
   p.hist_nam = ctx->dcounters + C_NCOUNTERS + 1 + kNClass;
   p.hist_tab = ctx->dhist_tab;
+  p.red = ctx->dred;
   p.sel_bits = ctx->dsel_bits;
   p.sel_owner = ctx->dsel_owner;
   p.sel_xam = ctx->dsel_xam;
   p.sel_evp = ctx->dsel_evp;
   p.sel_cap = ctx->sel_cap;
   p.work = ctx->dwork;
+}
+
+}  // namespace
+
+extern "C" {
+
+int cipsi_set_tuning(cipsi_ctx* ctx, int32_t r_chunk, int32_t ctas_per_sm) {
+  if (!ctx) return CIPSI_ERR_ARG;
+  if (r_chunk < 1 || r_chunk > 4096) return fail(ctx, CIPSI_ERR_ARG, "r_chunk must be in [1, 4096]");
+  if (ctas_per_sm < 0 || ctas_per_sm > 2) return fail(ctx, CIPSI_ERR_ARG, "ctas_per_sm must be 0, 1 or 2");
+  ctx->tune_r_chunk = r_chunk;
+  ctx->tune_ctas = ctas_per_sm;
+  return CIPSI_OK;
+}
+
+int cipsi_run_pt2_async(cipsi_ctx* ctx, const cipsi_opts* o) {
+  int rc = check_run_args(ctx, o);
+  if (rc) return rc;
+  CK(cudaSetDevice(ctx->device));
+  const int ncf = ctx->d.ncf, W = ctx->W, mt = ctx->d.metat;
+  RunPlan pl;
+  plan_run(ctx, o, ctx->tune_r_chunk, pl);
+  const int nunits = (int)pl.ug.size();
+  int dev_sms = 0;
+  CK(cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, ctx->device));
+  const LaunchShape ls = launch_shape(W, roots_pad(mt), ncf, ctx->tune_ctas);
+  const int grid = std::max(1, std::min(nunits, dev_sms * ls.blocks_per_sm));
+  // per-block neighbour scratch
+  if ((size_t)grid > ctx->scratch_blocks || !ctx->dnb_j) {
+    dfree(ctx->dnb_j); dfree(ctx->dnb_em); dfree(ctx->dlr_idx);
+    CK(cudaMalloc(&ctx->dnb_j, (size_t)grid * ncf * sizeof(int32_t)));
+    CK(cudaMalloc(&ctx->dnb_em, (size_t)grid * ncf * sizeof(uint64_t)));
+    CK(cudaMalloc(&ctx->dlr_idx, (size_t)grid * ncf * sizeof(int32_t)));
+    ctx->scratch_blocks = grid;
+  }
+  rc = prepare_run(ctx, pl, ctx->stream);
+  if (rc) return rc;
+  const size_t nq = (size_t)5 * mt;
+  const size_t ncount = C_NCOUNTERS + 1 + kNClass + kNClass * kMaxRoots;
+  CK(cudaMemsetAsync(ctx->dcounters, 0, ncount * sizeof(unsigned long long), ctx->stream));
+  CK(cudaMemsetAsync(ctx->dhist_tab, 0, 2 * kNClass * kMaxRoots * sizeof(double), ctx->stream));
+  CK(cudaMemsetAsync(ctx->dwork, 0, sizeof(int), ctx->stream));
+  CK(cudaMemsetAsync(ctx->dgen_part, 0, (size_t)std::max(nunits, 1) * nq * sizeof(double), ctx->stream));
+
+  Params p{};
+  fill_params(ctx, o, pl, p);
+  p.nb_j = ctx->dnb_j;
+  p.nb_emask = ctx->dnb_em;
+  p.lr_idx = ctx->dlr_idx;
+  p.lr_cap = ls.lr_cap;
+  p.nb_stride = ncf;
 
   CK(cudaEventRecord(ctx->ev0, ctx->stream));
   if (nunits > 0) {
     cudaError_t e;
-    const int R = mt <= 1 ? 1 : mt <= 2 ? 2 : mt <= 4 ? 4 : 8;
+    const int R = roots_pad(mt);
     if (W == 1) {
-      e = R == 1 ? launch_pt2<1, 1>(p, grid, smem, ctx->stream)
-        : R == 2 ? launch_pt2<1, 2>(p, grid, smem, ctx->stream)
-        : R == 4 ? launch_pt2<1, 4>(p, grid, smem, ctx->stream)
-                 : launch_pt2<1, 8>(p, grid, smem, ctx->stream);
+      e = R == 1 ? launch_pt2<1, 1, false>(p, BatchArgs{}, grid, ls.smem, ctx->stream)
+        : R == 2 ? launch_pt2<1, 2, false>(p, BatchArgs{}, grid, ls.smem, ctx->stream)
+        : R == 4 ? launch_pt2<1, 4, false>(p, BatchArgs{}, grid, ls.smem, ctx->stream)
+                 : launch_pt2<1, 8, false>(p, BatchArgs{}, grid, ls.smem, ctx->stream);
     } else {
-      e = R == 1 ? launch_pt2<2, 1>(p, grid, smem, ctx->stream)
-        : R == 2 ? launch_pt2<2, 2>(p, grid, smem, ctx->stream)
-        : R == 4 ? launch_pt2<2, 4>(p, grid, smem, ctx->stream)
-                 : launch_pt2<2, 8>(p, grid, smem, ctx->stream);
+      e = R == 1 ? launch_pt2<2, 1, false>(p, BatchArgs{}, grid, ls.smem, ctx->stream)
+        : R == 2 ? launch_pt2<2, 2, false>(p, BatchArgs{}, grid, ls.smem, ctx->stream)
+        : R == 4 ? launch_pt2<2, 4, false>(p, BatchArgs{}, grid, ls.smem, ctx->stream)
+                 : launch_pt2<2, 8, false>(p, BatchArgs{}, grid, ls.smem, ctx->stream);
     }
     if (e != cudaSuccess) return fail(ctx, CIPSI_ERR_CUDA, std::string("k_pt2 launch: ") + cudaGetErrorString(e));
-    k_reduce<<<1, 64, 0, ctx->stream>>>(ctx->dgen_part, nunits, (int)nq, ctx->dred);
+    k_reduce<<<(unsigned)nq, kReduceThreads, 0, ctx->stream>>>(ctx->dgen_part, nunits, (int)nq, ctx->dred);
     CK(cudaGetLastError());
   } else {
     CK(cudaMemsetAsync(ctx->dred, 0, nq * sizeof(double), ctx->stream));
   }
   CK(cudaEventRecord(ctx->ev1, ctx->stream));
+  ctx->ev_valid = true;
   ctx->nclass = o->nclass;
   ctx->pending = true;
   ctx->last_opts = *o;
@@ -1870,6 +859,10 @@ int cipsi_fetch_result(cipsi_ctx* ctx, cipsi_result* r) {
   if (!ctx || !r) return CIPSI_ERR_ARG;
   if (!ctx->pending) return fail(ctx, CIPSI_ERR_STATE, "fetch_result without a run");
   CK(cudaSetDevice(ctx->device));
+  if (ctx->ext_done) {
+    CK(cudaEventSynchronize(ctx->ext_done));
+    ctx->ext_done = nullptr;
+  }
   CK(cudaStreamSynchronize(ctx->stream));
   ctx->pending = false;
   const int mt = ctx->d.metat;
@@ -1914,8 +907,8 @@ int cipsi_fetch_result(cipsi_ctx* ctx, cipsi_result* r) {
   r->alg_bytes = (int64_t)(cnt[C_NP2] * (8.0 * mt + 2 * 4.0 + 8.0) +
                            cnt[C_NP1] * (8.0 * mt + 8.0 + 2.0 * avg_rank * 2 * 4.0) +
                            cnt[C_NPROC] * (8.0 * avg_rank + 8.0 * (avg_rank + avg_rank * avg_rank) + 8.0 * mt));
-  float ms = 0.f;
-  CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+  float ms = -1.f;  // batched runs: the batch's time is reported by the batch
+  if (ctx->ev_valid) CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
   r->kernel_ms = ms;
   // selection: records stay on the device until cipsi_selection_get/raw
   const long long nsel = (long long)cnt[C_NSEL];
@@ -1938,6 +931,7 @@ int cipsi_run_pt2(cipsi_ctx* ctx, const cipsi_opts* opts, cipsi_result* res) {
     unsigned long long nsel = 0;
     CK(cudaMemcpy(&nsel, ctx->dcounters + C_NSEL, 8, cudaMemcpyDeviceToHost));
     dfree(ctx->dsel_bits); dfree(ctx->dsel_owner); dfree(ctx->dsel_xam); dfree(ctx->dsel_evp);
+    ++ctx->buf_gen;
     ctx->sel_cap = (long long)(nsel + nsel / 8 + 1024);
     const int W = ctx->W, mt = ctx->d.metat;
     CK(cudaMalloc(&ctx->dsel_bits, (size_t)ctx->sel_cap * 2 * W * sizeof(uint64_t)));
@@ -1946,6 +940,113 @@ int cipsi_run_pt2(cipsi_ctx* ctx, const cipsi_opts* opts, cipsi_result* res) {
     CK(cudaMalloc(&ctx->dsel_evp, (size_t)ctx->sel_cap * mt * sizeof(double)));
   }
   return fail(ctx, CIPSI_ERR_OVERFLOW, "selection buffer could not be grown");
+}
+
+int cipsi_run_pt2_adjoint(cipsi_ctx* ctx, const cipsi_opts* o, const double* seed, double* gF,
+                          double* gJ, double* gK, double* geri, double* gfmpb, double* groots) {
+  int rc = check_run_args(ctx, o);
+  if (rc) return rc;
+  if (!seed || !gF || !gJ || !gK || !geri || !gfmpb || !groots)
+    return fail(ctx, CIPSI_ERR_ARG, "run_pt2_adjoint: null seed or gradient array");
+  if (ctx->pending) return fail(ctx, CIPSI_ERR_STATE, "an asynchronous run is pending: fetch its result first");
+  CK(cudaSetDevice(ctx->device));
+  const int ncf = ctx->d.ncf, W = ctx->W, mt = ctx->d.metat, n = ctx->d.norb;
+  const int nt = n * (n + 1) / 2;
+  RunPlan pl;
+  plan_run(ctx, o, ctx->tune_r_chunk, pl);
+  const int nunits = (int)pl.ug.size();
+  int dev_sms = 0;
+  CK(cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, ctx->device));
+  const int R = roots_pad(mt);
+  const LaunchShape ls = launch_shape(W, R, ncf, ctx->tune_ctas);
+  const int grid = std::max(1, std::min(nunits, dev_sms * ls.blocks_per_sm));
+  if ((size_t)grid > ctx->scratch_blocks || !ctx->dnb_j) {
+    dfree(ctx->dnb_j); dfree(ctx->dnb_em); dfree(ctx->dlr_idx);
+    CK(cudaMalloc(&ctx->dnb_j, (size_t)grid * ncf * sizeof(int32_t)));
+    CK(cudaMalloc(&ctx->dnb_em, (size_t)grid * ncf * sizeof(uint64_t)));
+    CK(cudaMalloc(&ctx->dlr_idx, (size_t)grid * ncf * sizeof(int32_t)));
+    ctx->scratch_blocks = grid;
+  }
+  rc = prepare_run(ctx, pl, ctx->stream);
+  if (rc) return rc;
+  const size_t nq = (size_t)5 * mt;
+  const size_t ncount = C_NCOUNTERS + 1 + kNClass + kNClass * kMaxRoots;
+  CK(cudaMemsetAsync(ctx->dcounters, 0, ncount * sizeof(unsigned long long), ctx->stream));
+  CK(cudaMemsetAsync(ctx->dhist_tab, 0, 2 * kNClass * kMaxRoots * sizeof(double), ctx->stream));
+  CK(cudaMemsetAsync(ctx->dwork, 0, sizeof(int), ctx->stream));
+  CK(cudaMemsetAsync(ctx->dgen_part, 0, (size_t)std::max(nunits, 1) * nq * sizeof(double), ctx->stream));
+  // gradient buffers (this call only)
+  const int stride = 3 * nt + 2 * n;
+  double *d_eri = nullptr, *d_F = nullptr, *d_J = nullptr, *d_K = nullptr, *d_f = nullptr, *d_sl = nullptr,
+         *d_roots = nullptr;
+  auto release = [&]() {
+    dfree(d_eri); dfree(d_F); dfree(d_J); dfree(d_K); dfree(d_f); dfree(d_sl); dfree(d_roots);
+  };
+  auto ck = [&](cudaError_t e, const char* what) {
+    if (e == cudaSuccess) return 0;
+    release();
+    return fail(ctx, CIPSI_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+  };
+  if ((rc = ck(cudaMalloc(&d_eri, (size_t)ctx->ninte * sizeof(double)), "cudaMalloc"))) return rc;
+  if ((rc = ck(cudaMalloc(&d_F, (size_t)nt * sizeof(double)), "cudaMalloc"))) return rc;
+  if ((rc = ck(cudaMalloc(&d_J, (size_t)nt * sizeof(double)), "cudaMalloc"))) return rc;
+  if ((rc = ck(cudaMalloc(&d_K, (size_t)nt * sizeof(double)), "cudaMalloc"))) return rc;
+  if ((rc = ck(cudaMalloc(&d_f, (size_t)2 * n * sizeof(double)), "cudaMalloc"))) return rc;
+  if ((rc = ck(cudaMalloc(&d_sl, (size_t)grid * stride * sizeof(double)), "cudaMalloc"))) return rc;
+  if ((rc = ck(cudaMalloc(&d_roots, (size_t)3 * mt * sizeof(double)), "cudaMalloc"))) return rc;
+  if ((rc = ck(cudaMemsetAsync(d_eri, 0, (size_t)ctx->ninte * sizeof(double), ctx->stream), "memset"))) return rc;
+  if ((rc = ck(cudaMemsetAsync(d_F, 0, (size_t)nt * sizeof(double), ctx->stream), "memset"))) return rc;
+  if ((rc = ck(cudaMemsetAsync(d_sl, 0, (size_t)grid * stride * sizeof(double), ctx->stream), "memset"))) return rc;
+  if ((rc = ck(cudaMemsetAsync(d_roots, 0, (size_t)3 * mt * sizeof(double), ctx->stream), "memset"))) return rc;
+
+  Params p{};
+  fill_params(ctx, o, pl, p);
+  p.nb_j = ctx->dnb_j;
+  p.nb_emask = ctx->dnb_em;
+  p.lr_idx = ctx->dlr_idx;
+  p.lr_cap = ls.lr_cap;
+  p.nb_stride = ncf;
+  p.sel_cap = 0;  // no records from an adjoint launch
+  for (int m = 0; m < mt; ++m) {
+    p.seed_mp[m] = seed[m];
+    p.seed_vp[m] = seed[mt + m];
+    p.seed_b[m] = seed[2 * mt + m];
+  }
+  p.g_eri = d_eri;
+  p.g_F = d_F;
+  p.g_slice = d_sl;
+  p.slice_stride = stride;
+  p.g_roots = d_roots;
+  if (nunits > 0) {
+    cudaError_t e;
+    if (W == 1) {
+      e = R == 1 ? launch_pt2<1, 1, false, true>(p, BatchArgs{}, grid, ls.smem, ctx->stream)
+        : R == 2 ? launch_pt2<1, 2, false, true>(p, BatchArgs{}, grid, ls.smem, ctx->stream)
+        : R == 4 ? launch_pt2<1, 4, false, true>(p, BatchArgs{}, grid, ls.smem, ctx->stream)
+                 : launch_pt2<1, 8, false, true>(p, BatchArgs{}, grid, ls.smem, ctx->stream);
+    } else {
+      e = R == 1 ? launch_pt2<2, 1, false, true>(p, BatchArgs{}, grid, ls.smem, ctx->stream)
+        : R == 2 ? launch_pt2<2, 2, false, true>(p, BatchArgs{}, grid, ls.smem, ctx->stream)
+        : R == 4 ? launch_pt2<2, 4, false, true>(p, BatchArgs{}, grid, ls.smem, ctx->stream)
+                 : launch_pt2<2, 8, false, true>(p, BatchArgs{}, grid, ls.smem, ctx->stream);
+    }
+    if ((rc = ck(e, "adjoint k_pt2 launch"))) return rc;
+  }
+  k_slice_reduce<<<(stride + 255) / 256, 256, 0, ctx->stream>>>(d_sl, grid, stride, nt, d_F, d_J, d_K, d_f);
+  if ((rc = ck(cudaGetLastError(), "k_slice_reduce"))) return rc;
+  struct Out {
+    double* host;
+    const double* dev;
+    size_t n;
+  } outs[] = {{geri, d_eri, (size_t)ctx->ninte}, {gF, d_F, (size_t)nt}, {gJ, d_J, (size_t)nt},
+              {gK, d_K, (size_t)nt}, {gfmpb, d_f, (size_t)2 * n}, {groots, d_roots, (size_t)3 * mt}};
+  for (const Out& x : outs)
+    if ((rc = ck(cudaMemcpyAsync(x.host, x.dev, x.n * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream),
+                 "copy gradients")))
+      return rc;
+  if ((rc = ck(cudaStreamSynchronize(ctx->stream), "adjoint run"))) return rc;
+  release();
+  return CIPSI_OK;
 }
 
 int cipsi_selection_raw(cipsi_ctx* ctx, int64_t first, int64_t count, uint64_t* bits,
@@ -2010,6 +1111,262 @@ int cipsi_selection_get(cipsi_ctx* ctx, int64_t first, int64_t count, int32_t* n
   return CIPSI_OK;
 }
 
+
+// ------------------------------------------------------ batched geometries
+// One persistent launch per (words per spin string, roots) class runs the
+// work units of many contexts (Autocip grid geometries of different sizes);
+// the launches of all classes, the clearing and the reductions are captured
+// once in a CUDA graph and replayed by cipsi_batch_run.
+
+}  // extern "C"
+
+struct cipsi_batch {
+  int device = 0;
+  std::string err;
+  cudaStream_t stream = nullptr;
+  std::vector<cipsi_ctx*> ctxs;
+  std::vector<cipsi_opts> opts;
+  std::vector<unsigned long long> buf_gen;
+  Params* dgeo = nullptr;
+  struct Class {
+    int W = 1, R = 1;
+    std::vector<int> geos;
+    int nunits = 0, grid = 0, ncf_max = 0;
+    LaunchShape ls{};
+    int32_t* dunit_geo = nullptr;
+    int32_t* dunit_local = nullptr;
+    int* dwork = nullptr;
+    int32_t* dnb_j = nullptr;
+    uint64_t* dnb_em = nullptr;
+    int32_t* dlr_idx = nullptr;
+    cudaStream_t st = nullptr;
+    cudaEvent_t ev_join = nullptr;
+  };
+  std::vector<Class> classes;
+  int max_nq = 0;
+  cudaEvent_t ev_fork = nullptr, ev0 = nullptr, ev1 = nullptr, done = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  bool pending = false;
+};
+
+namespace {
+
+int bfail(cipsi_batch* b, int code, const std::string& msg) {
+  if (b) b->err = msg;
+  return code;
+}
+
+#define BCK(call)                                                                       \
+  do {                                                                                  \
+    cudaError_t e_ = (call);                                                            \
+    if (e_ != cudaSuccess)                                                              \
+      return bfail(b, CIPSI_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+template <int W>
+cudaError_t launch_batch_class(const Params& p0, const BatchArgs& ba, int R, int grid, size_t smem,
+                               cudaStream_t st) {
+  return R == 1 ? launch_pt2<W, 1, true>(p0, ba, grid, smem, st)
+       : R == 2 ? launch_pt2<W, 2, true>(p0, ba, grid, smem, st)
+       : R == 4 ? launch_pt2<W, 4, true>(p0, ba, grid, smem, st)
+                : launch_pt2<W, 8, true>(p0, ba, grid, smem, st);
+}
+
+void batch_free(cipsi_batch* b) {
+  cudaSetDevice(b->device);
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  if (b->graph) cudaGraphDestroy(b->graph);
+  for (auto& c : b->classes) {
+    dfree(c.dunit_geo); dfree(c.dunit_local); dfree(c.dwork);
+    dfree(c.dnb_j); dfree(c.dnb_em); dfree(c.dlr_idx);
+    if (c.st) cudaStreamDestroy(c.st);
+    if (c.ev_join) cudaEventDestroy(c.ev_join);
+  }
+  dfree(b->dgeo);
+  for (cudaEvent_t e : {b->ev_fork, b->ev0, b->ev1, b->done})
+    if (e) cudaEventDestroy(e);
+  if (b->stream) cudaStreamDestroy(b->stream);
+}
+
+}  // namespace
+
+extern "C" {
+
+int cipsi_batch_create(cipsi_batch** out, cipsi_ctx* const* ctxs, int32_t n, const cipsi_opts* opts,
+                       int32_t r_chunk, int32_t ctas_per_sm) {
+  if (!out) return CIPSI_ERR_ARG;
+  *out = nullptr;
+  cipsi_batch* b = new cipsi_batch();
+  *out = b;
+  if (!ctxs || !opts || n < 1) return bfail(b, CIPSI_ERR_ARG, "batch needs at least one context and its options");
+  if (r_chunk < 1 || r_chunk > 4096 || ctas_per_sm < 0 || ctas_per_sm > 2)
+    return bfail(b, CIPSI_ERR_ARG, "r_chunk must be in [1, 4096] and ctas_per_sm 0, 1 or 2");
+  b->device = ctxs[0] ? ctxs[0]->device : 0;
+  for (int i = 0; i < n; ++i) {
+    cipsi_ctx* ctx = ctxs[i];
+    if (!ctx) return bfail(b, CIPSI_ERR_ARG, "null context in batch");
+    if (ctx->device != b->device) return bfail(b, CIPSI_ERR_ARG, "all contexts of a batch must use one device");
+    if (ctx->pending) return bfail(b, CIPSI_ERR_STATE, "a context of the batch has a pending run");
+    for (int j = 0; j < i; ++j)
+      if (ctxs[j] == ctx) return bfail(b, CIPSI_ERR_ARG, "a context appears twice in the batch");
+    const int rc = check_run_args(ctx, &opts[i]);
+    if (rc) return bfail(b, rc, "context " + std::to_string(i) + ": " + ctx->err);
+  }
+  BCK(cudaSetDevice(b->device));
+  BCK(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
+  for (cudaEvent_t* e : {&b->ev_fork, &b->done})
+    BCK(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+  BCK(cudaEventCreate(&b->ev0));
+  BCK(cudaEventCreate(&b->ev1));
+  int dev_sms = 0;
+  BCK(cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, b->device));
+
+  // plan every geometry; per-context buffers as for a plain run
+  std::vector<Params> P(n);
+  std::vector<long long> work(n);
+  b->ctxs.assign(ctxs, ctxs + n);
+  b->opts.assign(opts, opts + n);
+  for (int i = 0; i < n; ++i) {
+    cipsi_ctx* ctx = ctxs[i];
+    b->opts[i].gen_mask = nullptr;  // used by the plan below only
+    RunPlan pl;
+    plan_run(ctx, &opts[i], r_chunk, pl);
+    if (prepare_run(ctx, pl, b->stream)) return bfail(b, CIPSI_ERR_CUDA, "context " + std::to_string(i) + ": " + ctx->err);
+    fill_params(ctx, &opts[i], pl, P[i]);
+    work[i] = (long long)pl.ug.size() * ctx->d.ncf;
+    const int W = ctx->W, R = roots_pad(ctx->d.metat);
+    int c = 0;
+    while (c < (int)b->classes.size() && !(b->classes[c].W == W && b->classes[c].R == R)) ++c;
+    if (c == (int)b->classes.size()) {
+      b->classes.emplace_back();
+      b->classes[c].W = W;
+      b->classes[c].R = R;
+    }
+    b->classes[c].geos.push_back(i);
+    b->max_nq = std::max(b->max_nq, 5 * ctx->d.metat);
+  }
+  BCK(cudaStreamSynchronize(b->stream));  // host plan vectors die here
+
+  // per class: unit order (heaviest geometry first), launch shape, scratch
+  for (auto& c : b->classes) {
+    std::stable_sort(c.geos.begin(), c.geos.end(), [&](int x, int y) { return work[x] > work[y]; });
+    std::vector<int32_t> ugeo, ulocal;
+    for (int i : c.geos) {
+      c.ncf_max = std::max(c.ncf_max, ctxs[i]->d.ncf);
+      for (int u = 0; u < P[i].nunits; ++u) {
+        ugeo.push_back(i);
+        ulocal.push_back(u);
+      }
+    }
+    c.nunits = (int)ugeo.size();
+    c.ls = launch_shape(c.W, c.R, c.ncf_max, ctas_per_sm);
+    c.grid = std::max(1, std::min(c.nunits, dev_sms * c.ls.blocks_per_sm));
+    BCK(cudaMalloc(&c.dunit_geo, (size_t)std::max(c.nunits, 1) * sizeof(int32_t)));
+    BCK(cudaMalloc(&c.dunit_local, (size_t)std::max(c.nunits, 1) * sizeof(int32_t)));
+    BCK(cudaMalloc(&c.dwork, sizeof(int)));
+    BCK(cudaMalloc(&c.dnb_j, (size_t)c.grid * c.ncf_max * sizeof(int32_t)));
+    BCK(cudaMalloc(&c.dnb_em, (size_t)c.grid * c.ncf_max * sizeof(uint64_t)));
+    BCK(cudaMalloc(&c.dlr_idx, (size_t)c.grid * c.ncf_max * sizeof(int32_t)));
+    if (c.nunits) {
+      BCK(cudaMemcpy(c.dunit_geo, ugeo.data(), (size_t)c.nunits * sizeof(int32_t), cudaMemcpyHostToDevice));
+      BCK(cudaMemcpy(c.dunit_local, ulocal.data(), (size_t)c.nunits * sizeof(int32_t), cudaMemcpyHostToDevice));
+    }
+    for (int i : c.geos) {
+      P[i].nb_j = c.dnb_j;
+      P[i].nb_emask = c.dnb_em;
+      P[i].lr_idx = c.dlr_idx;
+      P[i].nb_stride = c.ncf_max;
+      P[i].lr_cap = c.ls.lr_cap;
+    }
+    BCK(cudaStreamCreateWithFlags(&c.st, cudaStreamNonBlocking));
+    BCK(cudaEventCreateWithFlags(&c.ev_join, cudaEventDisableTiming));
+  }
+  BCK(cudaMalloc(&b->dgeo, (size_t)n * sizeof(Params)));
+  BCK(cudaMemcpy(b->dgeo, P.data(), (size_t)n * sizeof(Params), cudaMemcpyHostToDevice));
+  for (int i = 0; i < n; ++i) b->buf_gen.push_back(ctxs[i]->buf_gen);
+
+  // capture: clear, the class launches side by side, the reductions
+  BCK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeRelaxed));
+  k_batch_clear<<<n, 256, 0, b->stream>>>(b->dgeo);
+  BCK(cudaEventRecord(b->ev_fork, b->stream));
+  for (auto& c : b->classes) {
+    BCK(cudaStreamWaitEvent(c.st, b->ev_fork, 0));
+    BCK(cudaMemsetAsync(c.dwork, 0, sizeof(int), c.st));
+    if (c.nunits) {
+      BatchArgs ba{b->dgeo, c.dunit_geo, c.dunit_local, c.nunits, c.dwork};
+      const Params& p0 = P[c.geos[0]];
+      cudaError_t e = c.W == 1 ? launch_batch_class<1>(p0, ba, c.R, c.grid, c.ls.smem, c.st)
+                               : launch_batch_class<2>(p0, ba, c.R, c.grid, c.ls.smem, c.st);
+      if (e != cudaSuccess) {
+        cudaGraph_t g = nullptr;
+        cudaStreamEndCapture(b->stream, &g);
+        if (g) cudaGraphDestroy(g);
+        return bfail(b, CIPSI_ERR_CUDA, std::string("batched k_pt2 launch: ") + cudaGetErrorString(e));
+      }
+    }
+    BCK(cudaEventRecord(c.ev_join, c.st));
+    BCK(cudaStreamWaitEvent(b->stream, c.ev_join, 0));
+  }
+  k_reduce_batch<<<dim3((unsigned)b->max_nq, (unsigned)n), kReduceThreads, 0, b->stream>>>(b->dgeo);
+  BCK(cudaStreamEndCapture(b->stream, &b->graph));
+  BCK(cudaGraphInstantiate(&b->exec, b->graph, 0));
+  return CIPSI_OK;
+}
+
+int cipsi_batch_run(cipsi_batch* b) {
+  if (!b || !b->exec) return CIPSI_ERR_ARG;
+  for (size_t i = 0; i < b->ctxs.size(); ++i) {
+    const cipsi_ctx* ctx = b->ctxs[i];
+    if (ctx->buf_gen != b->buf_gen[i])
+      return bfail(b, CIPSI_ERR_STATE, "context " + std::to_string(i) +
+                                           " reallocated its buffers after the batch was built; rebuild the batch");
+    // a result left pending by this batch's previous run is simply replaced
+    if (ctx->pending && ctx->ext_done != b->done)
+      return bfail(b, CIPSI_ERR_STATE, "context " + std::to_string(i) + " has a pending run");
+  }
+  BCK(cudaSetDevice(b->device));
+  BCK(cudaEventRecord(b->ev0, b->stream));
+  BCK(cudaGraphLaunch(b->exec, b->stream));
+  BCK(cudaEventRecord(b->ev1, b->stream));
+  BCK(cudaEventRecord(b->done, b->stream));
+  for (size_t i = 0; i < b->ctxs.size(); ++i) {
+    cipsi_ctx* ctx = b->ctxs[i];
+    ctx->ext_done = b->done;
+    ctx->ev_valid = false;
+    ctx->nclass = b->opts[i].nclass;
+    ctx->last_opts = b->opts[i];
+    ctx->pending = true;
+  }
+  b->pending = true;
+  return CIPSI_OK;
+}
+
+int cipsi_batch_wait(cipsi_batch* b, double* ms) {
+  if (!b) return CIPSI_ERR_ARG;
+  if (!b->pending) return bfail(b, CIPSI_ERR_STATE, "batch_wait without batch_run");
+  BCK(cudaSetDevice(b->device));
+  BCK(cudaEventSynchronize(b->done));
+  b->pending = false;
+  float t = 0.f;
+  BCK(cudaEventElapsedTime(&t, b->ev0, b->ev1));
+  if (ms) *ms = t;
+  return CIPSI_OK;
+}
+
+const char* cipsi_batch_last_error(const cipsi_batch* b) { return b ? b->err.c_str() : "null batch"; }
+
+void cipsi_batch_destroy(cipsi_batch* b) {
+  if (!b) return;
+  batch_free(b);
+  for (cipsi_ctx* ctx : b->ctxs)
+    if (ctx && ctx->ext_done == b->done) {
+      ctx->ext_done = nullptr;
+      ctx->pending = false;
+    }
+  delete b;
+}
 
 // ------------------------------------------------- run without allocation
 // cipsi_run_pt2_static runs k_pt2 + k_reduce with every per-run buffer taken
@@ -2253,6 +1610,7 @@ int cipsi_run_pt2_static(cipsi_ctx* ctx, const cipsi_opts* o, cipsi_result* r) {
   p.yef = ctx->dyef;
   p.c = ctx->dc;
   p.eri = ctx->deri;
+  p.eri64 = ctx->deri64;
   p.pairtab = ctx->dpairtab;
   p.ntttt = ctx->dntttt;
   p.F = ctx->dF;
@@ -2289,6 +1647,7 @@ int cipsi_run_pt2_static(cipsi_ctx* ctx, const cipsi_opts* o, cipsi_result* r) {
   p.nb_emask = reinterpret_cast<uint64_t*>(nb0 + (size_t)grid * nb_stride);
   p.lr_idx = reinterpret_cast<int32_t*>(nb0 + (size_t)2 * grid * nb_stride);
   p.lr_cap = lr_cap;
+  p.nb_stride = ncf;
   p.gen_part = reinterpret_cast<double*>(base + off_part);
   unsigned long long* dcounters = reinterpret_cast<unsigned long long*>(base + off_counters);
   p.counters = dcounters;
@@ -2309,18 +1668,18 @@ int cipsi_run_pt2_static(cipsi_ctx* ctx, const cipsi_opts* o, cipsi_result* r) {
   if (nunits > 0) {
     cudaError_t e;
     if (W == 1) {
-      e = R == 1 ? launch_pt2<1, 1>(p, grid, smem, ctx->stream)
-        : R == 2 ? launch_pt2<1, 2>(p, grid, smem, ctx->stream)
-        : R == 4 ? launch_pt2<1, 4>(p, grid, smem, ctx->stream)
-                 : launch_pt2<1, 8>(p, grid, smem, ctx->stream);
+      e = R == 1 ? launch_pt2<1, 1, false>(p, BatchArgs{}, grid, smem, ctx->stream)
+        : R == 2 ? launch_pt2<1, 2, false>(p, BatchArgs{}, grid, smem, ctx->stream)
+        : R == 4 ? launch_pt2<1, 4, false>(p, BatchArgs{}, grid, smem, ctx->stream)
+                 : launch_pt2<1, 8, false>(p, BatchArgs{}, grid, smem, ctx->stream);
     } else {
-      e = R == 1 ? launch_pt2<2, 1>(p, grid, smem, ctx->stream)
-        : R == 2 ? launch_pt2<2, 2>(p, grid, smem, ctx->stream)
-        : R == 4 ? launch_pt2<2, 4>(p, grid, smem, ctx->stream)
-                 : launch_pt2<2, 8>(p, grid, smem, ctx->stream);
+      e = R == 1 ? launch_pt2<2, 1, false>(p, BatchArgs{}, grid, smem, ctx->stream)
+        : R == 2 ? launch_pt2<2, 2, false>(p, BatchArgs{}, grid, smem, ctx->stream)
+        : R == 4 ? launch_pt2<2, 4, false>(p, BatchArgs{}, grid, smem, ctx->stream)
+                 : launch_pt2<2, 8, false>(p, BatchArgs{}, grid, smem, ctx->stream);
     }
     if (e != cudaSuccess) return fail(ctx, CIPSI_ERR_CUDA, std::string("k_pt2 launch: ") + cudaGetErrorString(e));
-    k_reduce<<<1, 64, 0, ctx->stream>>>(p.gen_part, nunits, (int)nq, dred);
+    k_reduce<<<(unsigned)nq, kReduceThreads, 0, ctx->stream>>>(p.gen_part, nunits, (int)nq, dred);
     CK(cudaGetLastError());
   }
   CK(cudaEventRecord(ctx->ev1, ctx->stream));

@@ -1,0 +1,136 @@
+// pt2_common.cuh -- types shared by the perturbation kernels (pt2_kernel.cuh,
+// compiled in pt2_w1.cu / pt2_w2.cu) and the host side (cipsi_engine.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+
+#include "../../include/cipsi_gb300.h"
+
+namespace cipsi_dev {
+
+constexpr int kNClass = CIPSI_NCLASS;
+constexpr int kMaxRoots = CIPSI_MAX_ROOTS;
+constexpr int kThreads = 256;
+constexpr int kMaxSym = 8;
+constexpr int kMaxElec = 64;
+constexpr int kMaxOrb = 128;
+constexpr int kRowCap = 128;  // per-warp list of |K' \ j| = 2 entries holding a1
+
+// counters[] slots
+enum {
+  C_IETAT = 0,
+  C_NPROC,
+  C_NSEL,
+  C_NCAND,
+  C_NCMP,
+  C_NP1,
+  C_NP2,
+  C_ALGB,
+  C_LRFALLBACK,
+  C_NCOUNTERS
+};
+
+struct Params {
+  int norb, noca, nel, ncf, metat, nsym, isym;
+  int ngen;
+  const int32_t* gens;       // generator indices (0-based); -1 = pertu block
+  const uint8_t* gen_dmask;  // allowed rank changes per generator, bit (D+2)
+  int nunits;                // work units: (generator slot, range of R blocks
+  const int32_t* unit_g;     //   or, for the pertu block, of candidates)
+  const int32_t* unit_r0;
+  const int32_t* unit_r1;
+  const uint64_t* S;         // ncf x 2W words (alpha words, beta words)
+  const uint8_t* ygen;
+  const int32_t* nesp;
+  const uint8_t* yef;
+  const double* c;           // ncf x metat, canonical phase
+  const float* eri;
+  const int32_t* pairtab;    // norb x norb: pair index | irrep << 24
+  const int32_t* ntttt;     // [irrep 1..nsym] first packed index (1-based)
+  const double* F;           // packed i*(i+1)/2 + j (i >= j, 0-based)
+  const double* J;
+  const double* K;
+  const double* fmpb;        // 2*norb by spin orbital
+  const int8_t* orbsym;      // 0-based irreps
+  int its[kMaxSym][kMaxSym]; // 0-based product table
+  double e[kMaxRoots], eb[kMaxRoots], emp[kMaxRoots], teste[kMaxRoots], taum[kMaxRoots];
+  int yen, ysele, ymoyen, ywdeg, symvar, nclass;
+  double tau, teseff;
+  double aval[kNClass];
+  long long aval_bits[kNClass];  // bit patterns of aval (non-negative, ascending)
+  int pertu_ref, pertu_mono;
+  // scratch
+  int32_t* nb_j;             // per block: ncf entries
+  uint64_t* nb_emask;
+  int32_t* lr_idx;           // per block: ncf entries (fallback path)
+  int lr_cap;                // shared-memory capacity of L_R
+  int nb_stride;             // entries per block in nb_j / nb_emask / lr_idx
+  // outputs
+  double* gen_part;          // ngen x (5 * metat)
+  unsigned long long* counters;
+  unsigned long long* dpivot_bits;
+  unsigned long long* hist_nom;      // nclass
+  unsigned long long* hist_nam;      // nclass x metat
+  double* hist_tab;                  // 2 x nclass x metat (tabmp, tabvp)
+  double* red;                       // 5 x metat reduced sums (k_reduce output)
+  uint64_t* sel_bits;                // cap x 2W
+  int32_t* sel_owner;
+  double* sel_xam;
+  double* sel_evp;                   // cap x metat
+  long long sel_cap;
+  int* work;                         // work counter
+  // FP64 storage of (pq|rs) (derivative checks); null = the real*4 `eri`
+  const double* eri64;
+  // adjoint launch (k_pt2<..., ADJ = true>): seeds dE/d e2mp[m], e2vp[m],
+  // e2b[m] and the gradient outputs
+  double seed_mp[kMaxRoots], seed_vp[kMaxRoots], seed_b[kMaxRoots];
+  double* g_eri;    // ninte: dE/d(pq|rs) in the packed order
+  double* g_F;      // n(n+1)/2: dE/dF (off-diagonal terms of one-difference elements)
+  double* g_slice;  // per block: [F | J | K] packed triangles, then fmpb[2n]
+  int slice_stride; // doubles per block slice (3 n(n+1)/2 + 2n)
+  double* g_roots;  // 3 x metat: dE/d e, d eb, d emp
+};
+
+static_assert(sizeof(Params) % sizeof(int) == 0, "Params is copied as ints");
+
+// Batched launch: many geometries (each with its own Params) in one
+// persistent launch.  Global unit u belongs to geometry unit_geo[u] and is
+// unit unit_local[u] of that geometry's unit list.
+struct BatchArgs {
+  const Params* geo;
+  const int32_t* unit_geo;
+  const int32_t* unit_local;
+  int nunits;
+  int* work;
+};
+
+__device__ __forceinline__ void kahan_add(double& s, double& c, double x) {
+  const double y = x - c;
+  const double t = s + y;
+  c = (t - s) - y;
+  s = t;
+}
+
+// Per-warp queue of perturbers that survived the interaction scan.  The
+// FP64 epilogue (denominators, E2, selection) then runs on full warps: the
+// FP64 pipe of GB300 is narrow, and a warp instruction costs the same with
+// 32 lanes or with the few that would be live at the candidate level.
+constexpr int kQCap = 64;
+template <int W, int R>
+struct WarpQueue {
+  uint64_t u[2 * W][kQCap];
+  double bc[R][kQCap];
+  double hmp[kQCap], hvp[kQCap], fmul[kQCap];
+  int nmul[kQCap], owner[kQCap];
+  unsigned char flags[kQCap];  // bit 0 ybis, bit 1 is_pert1
+};
+
+// k_pt2<W, R, B, ADJ> launched with `smem` bytes of dynamic shared memory
+// (pt2_w1.cu / pt2_w2.cu: forward, plain and batched; pt2_adj.cu: adjoint).
+template <int W, int R, bool B, bool ADJ = false>
+cudaError_t launch_pt2(const Params& p, const BatchArgs& ba, int grid, size_t smem, cudaStream_t st);
+
+}  // namespace cipsi_dev

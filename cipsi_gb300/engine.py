@@ -65,6 +65,7 @@ def _lib():
         "cipsi_set_stream": ([P, P], ctypes.c_int),
         "cipsi_run_pt2": ([P, ctypes.POINTER(Opts), ctypes.POINTER(Result)], ctypes.c_int),
         "cipsi_run_pt2_async": ([P, ctypes.POINTER(Opts)], ctypes.c_int),
+        "cipsi_set_tuning": ([P, ctypes.c_int32, ctypes.c_int32], ctypes.c_int),
         "cipsi_fetch_result": ([P, ctypes.POINTER(Result)], ctypes.c_int),
         "cipsi_selection_get": ([P, ctypes.c_int64, ctypes.c_int64, P, P, P, P, P, P], ctypes.c_int),
         "cipsi_selection_raw": ([P, ctypes.c_int64, ctypes.c_int64, P, P, P, P], ctypes.c_int),
@@ -73,6 +74,17 @@ def _lib():
         "cipsi_inputs_dims": ([P, ctypes.POINTER(Dims), ctypes.POINTER(Opts)], ctypes.c_int),
         "cipsi_inputs_upload": ([P, P], ctypes.c_int),
         "cipsi_inputs_free": ([P], None),
+        "cipsi_batch_create": ([ctypes.POINTER(P), ctypes.POINTER(P), ctypes.c_int32, ctypes.POINTER(Opts),
+                                ctypes.c_int32, ctypes.c_int32], ctypes.c_int),
+        "cipsi_batch_run": ([P], ctypes.c_int),
+        "cipsi_batch_wait": ([P, ctypes.POINTER(ctypes.c_double)], ctypes.c_int),
+        "cipsi_batch_last_error": ([P], ctypes.c_char_p),
+        "cipsi_batch_destroy": ([P], None),
+        "cipsi_inputs_array": ([P, ctypes.c_char_p, ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(ctypes.c_int64),
+                                ctypes.POINTER(ctypes.c_int32)], ctypes.c_int),
+        "cipsi_set_integrals_f64store": ([P, P, P, P, P, P, P, P, P, ctypes.c_int64], ctypes.c_int),
+        "cipsi_set_roots": ([P, P, P, P, P, P, P, P], ctypes.c_int),
+        "cipsi_run_pt2_adjoint": ([P, ctypes.POINTER(Opts), P, P, P, P, P, P, P], ctypes.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)
@@ -110,6 +122,30 @@ class Inputs:
         self.opts = Opts()
         lib.cipsi_inputs_dims(self._h, ctypes.byref(self.dims), ctypes.byref(self.opts))
 
+    _TYPES = {1: np.int32, 2: np.int16, 3: np.float32, 4: np.float64, 5: np.uint8}
+
+    def count(self, name: str) -> int:
+        data, count, typ = ctypes.c_void_p(), ctypes.c_int64(), ctypes.c_int32()
+        if _lib().cipsi_inputs_array(self._h, name.encode(), ctypes.byref(data), ctypes.byref(count),
+                                     ctypes.byref(typ)) != 0:
+            raise CipsiError(f"no input array named {name!r}")
+        return count.value
+
+    def array(self, name: str) -> np.ndarray:
+        """A copy of one input array (cipsi_inputs_array)."""
+        data = ctypes.c_void_p()
+        count = ctypes.c_int64()
+        typ = ctypes.c_int32()
+        rc = _lib().cipsi_inputs_array(self._h, name.encode(), ctypes.byref(data), ctypes.byref(count),
+                                       ctypes.byref(typ))
+        if rc != 0:
+            raise CipsiError(f"no input array named {name!r}")
+        dt = np.dtype(self._TYPES[typ.value])
+        if count.value == 0:
+            return np.zeros(0, dt)
+        buf = (ctypes.c_char * (count.value * dt.itemsize)).from_address(data.value)
+        return np.frombuffer(buf, dtype=dt).copy()
+
     def close(self):
         if self._h:
             _lib().cipsi_inputs_free(self._h)
@@ -144,8 +180,42 @@ class Context:
     def set_stream(self, stream_handle: int):
         self._check(self.lib.cipsi_set_stream(self._c, ctypes.c_void_p(stream_handle)), "set_stream")
 
+    def set_tuning(self, r_chunk: int = 6, ctas_per_sm: int = 0):
+        self._check(self.lib.cipsi_set_tuning(self._c, r_chunk, ctas_per_sm), "set_tuning")
+
+    def set_integrals_f64store(self, itsym, its, F, J, K, ij0, ntttt, eri):
+        """Integrals with (pq|rs) kept in FP64 on the device."""
+        a = [np.ascontiguousarray(itsym, np.int32), np.ascontiguousarray(its, np.int32),
+             np.ascontiguousarray(F, np.float64), np.ascontiguousarray(J, np.float64),
+             np.ascontiguousarray(K, np.float64), np.ascontiguousarray(ij0, np.int16),
+             np.ascontiguousarray(ntttt, np.int32), np.ascontiguousarray(eri, np.float64)]
+        self._check(self.lib.cipsi_set_integrals_f64store(self._c, *[x.ctypes.data for x in a], len(a[7])),
+                    "set_integrals_f64store")
+        self._ninte = len(a[7])
+
+    def set_roots(self, c, e, eb, emp, teste, taum, fmpb):
+        a = [np.ascontiguousarray(x, np.float64) for x in (c, e, eb, emp, teste, taum, fmpb)]
+        self._check(self.lib.cipsi_set_roots(self._c, *[x.ctypes.data for x in a]), "set_roots")
+
+    def adjoint(self, opts: Opts, seed) -> dict:
+        """Gradients of sum(seed * [e2mp; e2vp; e2b]) (cipsi_run_pt2_adjoint)."""
+        n, mt = self.dims.norb, self.dims.metat
+        nt = n * (n + 1) // 2
+        seed = np.ascontiguousarray(np.asarray(seed, np.float64).reshape(3 * mt))
+        out = {"F": np.zeros(nt), "J": np.zeros(nt), "K": np.zeros(nt), "eri": np.zeros(self._ninte),
+               "fmpb": np.zeros(2 * n), "roots": np.zeros(3 * mt)}
+        o = Opts.from_buffer_copy(opts)
+        self._check(self.lib.cipsi_run_pt2_adjoint(
+            self._c, ctypes.byref(o), seed.ctypes.data, out["F"].ctypes.data, out["J"].ctypes.data,
+            out["K"].ctypes.data, out["eri"].ctypes.data, out["fmpb"].ctypes.data, out["roots"].ctypes.data),
+            "run_pt2_adjoint")
+        r = out.pop("roots")
+        out["e"], out["eb"], out["emp"] = r[:mt], r[mt:2 * mt], r[2 * mt:]
+        return out
+
     def upload(self, inp: Inputs):
         self._check(self.lib.cipsi_inputs_upload(inp._h, self._c), "inputs_upload")
+        self._ninte = inp.count("eri")
 
     def _opts(self, opts: Opts, gen_mask: Optional[np.ndarray], run_pertu: Optional[bool]) -> Opts:
         o = Opts.from_buffer_copy(opts)
@@ -206,6 +276,85 @@ class Context:
         if self._c:
             self.lib.cipsi_ctx_destroy(self._c)
             self._c = ctypes.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Batch:
+    """Runs of many contexts (geometries) in one persistent launch per class,
+    captured as a CUDA graph (cipsi_batch_* in the C ABI).
+
+        b = Batch(contexts, [inp.opts for inp in inputs])
+        b.run(); ms = b.wait()
+        results = [ctx.fetch() for ctx in contexts]
+    """
+
+    def __init__(self, contexts, opts_list, r_chunk: int = 6, ctas_per_sm: int = 0, gen_masks=None):
+        self.lib = _lib()
+        n = len(contexts)
+        if n == 0 or len(opts_list) != n:
+            raise CipsiError("Batch needs one Opts per context")
+        self.contexts = list(contexts)
+        arr = (ctypes.c_void_p * n)(*[c._c.value for c in contexts])
+        opts = (Opts * n)()
+        keep = []
+        for i, o in enumerate(opts_list):
+            opts[i] = Opts.from_buffer_copy(o)
+            if gen_masks is not None and gen_masks[i] is not None:
+                m = np.ascontiguousarray(gen_masks[i], dtype=np.uint8)
+                keep.append(m)
+                opts[i].gen_mask = m.ctypes.data
+        self._h = ctypes.c_void_p()
+        rc = self.lib.cipsi_batch_create(ctypes.byref(self._h), arr, n, opts, r_chunk, ctas_per_sm)
+        if rc != 0:
+            msg = self.lib.cipsi_batch_last_error(self._h).decode()
+            self.lib.cipsi_batch_destroy(self._h)
+            self._h = ctypes.c_void_p()
+            raise CipsiError(f"batch_create: {msg}")
+        self.nclass = [o.nclass for o in opts_list]
+
+    def _check(self, rc, what):
+        if rc != 0:
+            raise CipsiError(f"{what}: {self.lib.cipsi_batch_last_error(self._h).decode()}")
+
+    def run(self):
+        self._check(self.lib.cipsi_batch_run(self._h), "batch_run")
+        for c, nc in zip(self.contexts, self.nclass):
+            c._last_nclass = nc
+
+    def wait(self) -> float:
+        ms = ctypes.c_double()
+        self._check(self.lib.cipsi_batch_wait(self._h, ctypes.byref(ms)), "batch_wait")
+        return ms.value
+
+    def fetch_all(self, allow_overflow: bool = True) -> list:
+        """Every context's result; a selection-capacity overflow (records
+        counted but not all stored) is accepted when allow_overflow."""
+        out = []
+        for c, nc in zip(self.contexts, self.nclass):
+            r = Result()
+            rc = c.lib.cipsi_fetch_result(c._c, ctypes.byref(r))
+            if rc != 0 and not (allow_overflow and rc == -4):
+                raise CipsiError(f"fetch_result: {c.lib.cipsi_last_error(c._c).decode()}")
+            d = result_dict(r, c.dims.metat, nc)
+            d["overflow"] = rc == -4
+            out.append(d)
+        return out
+
+    def close(self):
+        if self._h:
+            self.lib.cipsi_batch_destroy(self._h)
+            self._h = ctypes.c_void_p()
 
     def __enter__(self):
         return self

@@ -88,6 +88,10 @@ class SynthConfig:
     variant: str = "cipsym"  # or "cip"
     extra_icinp: str = ""
     virt_shift: float = 0.0  # added to h_aa of virtual orbitals (0 = the plain recipe)
+    curve_R: Optional[float] = None  # potential-curve geometry R (bohr): integrals from
+                                     # L(R) = L0 + exp(-R/3) L1, eps(R) = eps0 + 0.1 exp(-R/2) eps1
+    energy: str = "rayleigh"  # root energies: "rayleigh" (<Psi|H|Psi>) or "diagonal"
+                              # (sum_k c_k^2 H_kk: no O(ncf^2) pass, for many large geometries)
 
 
 CONFIGS: Dict[str, SynthConfig] = {
@@ -115,6 +119,8 @@ def make_integrals(cfg: SynthConfig, rng: np.random.Generator):
         irrep = rng.integers(0, nsym, size=n)
         # keep the reference det totally symmetric-friendly: any assignment works
     eps = np.sort(rng.uniform(-2.0, 1.0, size=n))
+    if cfg.curve_R is not None:
+        eps = eps + 0.1 * np.exp(-cfg.curve_R / 2.0) * rng.normal(0.0, 1.0, size=n)
     h = np.diag(eps)
     off = rng.normal(0.0, 0.05, size=(n, n))
     off = np.triu(off, 1)
@@ -125,16 +131,22 @@ def make_integrals(cfg: SynthConfig, rng: np.random.Generator):
         # a gap between occupied and virtual orbital energies keeps every
         # perturbation denominator away from zero (well-conditioned E2)
         h[np.arange(cfg.nocc, n), np.arange(cfg.nocc, n)] += cfg.virt_shift
-    L = np.zeros((cfg.ncholesky, n, n))
-    for K in range(cfg.ncholesky):
-        a = rng.normal(0.0, 0.3 * 0.85 ** K, size=(n, n))
-        a = np.triu(a)
-        a = a + np.triu(a, 1).T
-        if nsym > 1:
-            gK = K % nsym
-            mask = (irrep[:, None] ^ irrep[None, :]) == gK
-            a = a * mask
-        L[K] = a
+    def cholesky_vectors():
+        out = np.zeros((cfg.ncholesky, n, n))
+        for K in range(cfg.ncholesky):
+            a = rng.normal(0.0, 0.3 * 0.85 ** K, size=(n, n))
+            a = np.triu(a)
+            a = a + np.triu(a, 1).T
+            if nsym > 1:
+                gK = K % nsym
+                mask = (irrep[:, None] ^ irrep[None, :]) == gK
+                a = a * mask
+            out[K] = a
+        return out
+
+    L = cholesky_vectors()
+    if cfg.curve_R is not None:
+        L = L + np.exp(-cfg.curve_R / 3.0) * cholesky_vectors()
     return h, L, irrep
 
 
@@ -479,6 +491,41 @@ class SlaterCondon:
         return 0.0
 
 
+def diagonal_energy(F, J, K, dets, norb: int, C: np.ndarray) -> np.ndarray:
+    """sum_k c_km^2 (H_kk - E_HF) for the columns of C, with H_kk - E_HF from
+    the closed-shell F, J, K over the occupation changes dn of each
+    determinant: sum_r dn_r F_rr + 1/2 sum_rs dn_r dn_s (J_rs - [same spin] K_rs)."""
+    n = norb
+    D = np.zeros((len(dets), 2 * n))
+    for k, (hl, pt) in enumerate(dets):
+        if hl:
+            D[k, np.asarray(hl) - 1] -= 1.0
+            D[k, np.asarray(pt) - 1] += 1.0
+    Fso = np.concatenate([np.diag(F), np.diag(F)])
+    orb = np.tile(np.arange(n), 2)
+    spin = np.repeat([0, 1], n)
+    X = J[np.ix_(orb, orb)] - (spin[:, None] == spin[None, :]) * K[np.ix_(orb, orb)]
+    dg = D @ Fso + 0.5 * np.einsum("kr,rs,ks->k", D, X, D)
+    return np.einsum("im,im,i->m", C, C, dg)
+
+
+def curve_geometries(n: int = 256, seed: int = 100) -> List[SynthConfig]:
+    """Potential-curve batch: n geometries with R uniform on [2, 12] bohr,
+    norb uniform in {40..100}, |S| uniform in [500, 5000] (before spin-flip
+    closure), 20 electrons, 1 root, S = reference + singles/doubles/triples
+    with coefficients N(0,1) 0.9^rank, tau = 0.01, 2 norb Cholesky vectors."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n):
+        R = float(rng.uniform(2.0, 12.0))
+        norb = int(rng.integers(40, 101))
+        ncf = int(rng.integers(500, 5001))
+        out.append(SynthConfig(f"geo{i:03d}", norb=norb, nocc=10, ncholesky=2 * norb, ncf=ncf, metat=1,
+                               tau=0.01, ranks=(1, 2, 3), coef_mode="decay09", seed=seed * 1000 + i,
+                               curve_R=R, energy="diagonal"))
+    return out
+
+
 def rayleigh(sc: SlaterCondon, bits: List[Tuple[int, int]], C: np.ndarray) -> np.ndarray:
     """<Psi_m|H - E_HF|Psi_m> for the columns of C (canonical phases)."""
     ncf = len(bits)
@@ -543,7 +590,10 @@ def generate(cfg: SynthConfig, workdir: str, verbose: bool = False) -> dict:
     C = Q * np.sign(np.diag(R))[None, :]
     bits = [det_from_lists(hl, pt, cfg.norb, cfg.nocc) for hl, pt in dets]
     sc = SlaterCondon(h, L, cfg.norb, cfg.nocc)
-    E = rayleigh(sc, bits, C) + escf
+    if cfg.energy == "rayleigh":
+        E = rayleigh(sc, bits, C) + escf
+    else:
+        E = diagonal_energy(F, J, K, dets, cfg.norb, C) + escf
     sigma = np.array([cip_phase(hl, pt, cfg.norb, cfg.nocc) for hl, pt in dets], dtype=np.float64)
     Ccip = C * sigma[:, None]
     # unit 60: S in cip/pie.f records (v = 1)

@@ -149,6 +149,17 @@ int cipsi_set_roots(cipsi_ctx* ctx, const double* c, const double* e, const doub
 /* pertu + diexcit on the GPU (cip.f:238-241).  Blocks until done. */
 int cipsi_run_pt2(cipsi_ctx* ctx, const cipsi_opts* opts, cipsi_result* res);
 
+/* Launch shape of later runs on this context (no counterpart in the
+   reference; results do not depend on it beyond summation order):
+     r_chunk      removed-electron blocks per work unit for generators of
+                  excitation rank >= 2 (rank 0 and 1 generators always get
+                  one block per unit); default 6
+     ctas_per_sm  0 = shared-memory list as large as one CTA allows (two
+                  CTAs per SM when it fits in half), 1 = one CTA per SM,
+                  2 = list sized so that two CTAs fit per SM
+   cipsi_gb300.tune (Python) picks both by timing a generator sample. */
+int cipsi_set_tuning(cipsi_ctx* ctx, int32_t r_chunk, int32_t ctas_per_sm);
+
 /* Enqueue the same work on the context stream without waiting; the result is
    collected by cipsi_fetch_result.  Used to time the kernels alone. */
 int cipsi_run_pt2_async(cipsi_ctx* ctx, const cipsi_opts* opts);
@@ -198,6 +209,71 @@ int cipsi_cip_main(const char* workdir, const char* stdin_path, int32_t sym_vari
    output pointer may be NULL. */
 int cipsi_selection_raw(cipsi_ctx* ctx, int64_t first, int64_t count, uint64_t* bits,
                         int32_t* owner, double* xam, double* evp);
+
+/* Read access to an array of the inputs, by the name of its COMMON
+   variable: itsym, its, ij0, ntttt, F (f), J (aj), K (ak), eri (bijkl),
+   c, e, eb, emp, teste, taum, fmpb, ne, nd, trou, part, ygen, ysaut, nesp,
+   yef1, escf.  *data points into `in` (valid until cipsi_inputs_free);
+   *type: 1 int32, 2 int16, 3 float32, 4 float64, 5 uint8.  CIPSI_ERR_ARG
+   for an unknown name.  Not in the reference (its arrays are COMMONs). */
+int cipsi_inputs_array(const cipsi_inputs* in, const char* name, const void** data, int64_t* count,
+                       int32_t* type);
+
+/* Same as cipsi_set_integrals_fp64 but (pq|rs) stay in FP64 on the device
+   instead of the reference's real*4 (cip/reijkl.f:27): for derivative
+   checks, where real*4 steps (~1e-8 relative) would swamp a finite
+   difference.  cipsi_set_integrals returns the context to real*4. */
+int cipsi_set_integrals_f64store(cipsi_ctx* ctx, const int32_t* itsym, const int32_t* its,
+                                 const double* f, const double* aj, const double* ak,
+                                 const int16_t* ij0, const int32_t* ntttt, const double* pqrs,
+                                 int64_t ninte);
+
+/* Adjoint of cipsi_run_pt2 (no counterpart in the reference): gradients of
+   L = sum_m seed[m] e2mp[m] + seed[metat+m] e2vp[m] + seed[2 metat+m] e2b[m]
+   with respect to the engine's inputs, the S coefficients held fixed:
+     gF, gJ, gK [norb(norb+1)/2]  packed like f, aj, ak
+     geri [ninte]                 packed like bijkl
+     gfmpb [2 norb]               by spin orbital
+     groots [3 metat]             dL/de, dL/deb, dL/demp
+   The perturber set, weights and denominators are those of the forward run
+   (pert1.f:151-191, diexcit.f:327-376); dL/d<I|H|j> = sum_m dL/db_m c_jm is
+   spread over the integrals of each interacting pair (hntd.f:138-163), and
+   dL/dhdig, dL/dhmp over F, J, K, fmpb (hdig.f, hmp.f).  Blocks until done;
+   allocates its gradient buffers for the call. */
+int cipsi_run_pt2_adjoint(cipsi_ctx* ctx, const cipsi_opts* opts, const double* seed, double* gF,
+                          double* gJ, double* gK, double* geri, double* gfmpb, double* groots);
+
+/* Batched form: the runs of many contexts (the geometries of an Autocip
+   grid, of different sizes) in one persistent launch per class of contexts
+   with the same string width (norb <= 64 or not) and padded root count,
+   all captured once as a CUDA graph.  No counterpart in the reference, which
+   runs one cip process per geometry (Autocip_13/calcul.f90:320).
+     cipsi_batch_create  plans every context's run with opts[i] (as
+                         cipsi_run_pt2_async would, gen_mask read here only),
+                         sizes its buffers and captures the graph; r_chunk
+                         and ctas_per_sm as in cipsi_set_tuning.  On failure
+                         *b still holds a batch: read cipsi_batch_last_error
+                         and destroy it.
+     cipsi_batch_run     replays the graph on the batch's own stream (no
+                         wait); afterwards cipsi_fetch_result(ctx_i) gives
+                         each geometry's result (it waits for the batch) and
+                         the selection calls its records; kernel_ms is -1
+                         there, cipsi_batch_wait gives the batch's time.
+     cipsi_batch_wait    waits for the last replay; *ms = its device time.
+   Records beyond a context's selection capacity are counted but not stored
+   (cipsi_fetch_result then returns CIPSI_ERR_OVERFLOW for that context; a
+   cipsi_run_pt2 on it grows the capacity).  A context whose buffers are
+   reallocated after the batch was built (set_* calls, a plain run that grows
+   a buffer) makes cipsi_batch_run fail with CIPSI_ERR_STATE: rebuild the
+   batch.  Member contexts must not run other work while a replay is in
+   flight. */
+typedef struct cipsi_batch cipsi_batch;
+int cipsi_batch_create(cipsi_batch** b, cipsi_ctx* const* ctxs, int32_t n, const cipsi_opts* opts,
+                       int32_t r_chunk, int32_t ctas_per_sm);
+int cipsi_batch_run(cipsi_batch* b);
+int cipsi_batch_wait(cipsi_batch* b, double* ms);
+const char* cipsi_batch_last_error(const cipsi_batch* b);
+void cipsi_batch_destroy(cipsi_batch* b);
 
 /* pertu + diexcit like cipsi_run_pt2, but the call allocates no device
    memory.  This entry point has no counterpart in the reference.

@@ -57,3 +57,25 @@ def test_integral_file_layout(tmp_path):
     for i in range(1, n + 1):
         t = i * (i + 1) // 2
         assert inp.J[t] == inp.K[t]
+
+
+def test_curve_geometries_follow_the_batch_recipe():
+    a = synth.curve_geometries(256, seed=100)
+    b = synth.curve_geometries(256, seed=100)
+    assert [(g.norb, g.ncf, g.curve_R, g.seed) for g in a] == [(g.norb, g.ncf, g.curve_R, g.seed) for g in b]
+    assert all(40 <= g.norb <= 100 and 500 <= g.ncf <= 5000 and 2.0 <= g.curve_R <= 12.0 for g in a)
+    assert len({g.seed for g in a}) == 256
+    assert min(g.norb for g in a) <= 45 and max(g.norb for g in a) >= 95
+
+
+def test_curve_integrals_move_with_R(tmp_path):
+    import dataclasses
+    import numpy as np
+    base = synth.SynthConfig("c", norb=10, nocc=3, ncholesky=20, ncf=30, metat=1, tau=0.02,
+                             ranks=(1, 2), coef_mode="decay09", seed=3, curve_R=2.0, energy="diagonal")
+    h1, L1, _ = synth.make_integrals(base, np.random.default_rng(base.seed))
+    h2, L2, _ = synth.make_integrals(dataclasses.replace(base, curve_R=12.0), np.random.default_rng(base.seed))
+    assert not np.allclose(L1, L2) and not np.allclose(np.diag(h1), np.diag(h2))
+    # the R-independent parts are shared: the difference is exp(-R/3) L1 scaled
+    info = synth.generate(base, str(tmp_path / "g"))
+    assert info["ncf"] >= 30
