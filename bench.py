@@ -247,6 +247,127 @@ def run_batched(args, rank: int, world: int, local_rank: int):
         print(json.dumps(line), flush=True)
 
 
+# ------------------------------------------------------------ large system
+def _oracle_on_mask(wd: str, mask, tmpbase: str):
+    """CPU oracle restricted to the generators of `mask` (no pertu block):
+    (oracle JSON, seconds)."""
+    from oracle import build as ob
+    run = tempfile.mkdtemp(dir=tmpbase)
+    shutil.rmtree(run)
+    shutil.copytree(wd, run)
+    mp_ = os.path.join(run, "mask.bin")
+    mask.tofile(mp_)
+    t0 = time.perf_counter()
+    j = json.load(open(ob.run(run, genmask=mp_, no_pertu_ref=True)))
+    dt = time.perf_counter() - t0
+    shutil.rmtree(run, ignore_errors=True)
+    return j, dt
+
+
+def run_large(args, rank: int, world: int, local_rank: int):
+    """The 120-orbital, 30-electron, S = 20,000, 2-root system: E2 time of
+    the whole step.  This recipe selects ~1.5e10 perturbers for unit 60,
+    more than device memory holds, so the records are counted and not
+    stored (a cipsi_fetch_result overflow, results valid).  The CPU oracle
+    is timed on two generators of S (one process each) and the GPU run on
+    the same two generators is compared with it (E2 parity at this size)."""
+    import numpy as np
+    import torch
+    from concurrent.futures import ProcessPoolExecutor
+    import multiprocessing as mpm
+    from cipsi_gb300 import batch, build, engine, synth
+    from oracle import build as ob
+    import dataclasses
+    torch.cuda.set_device(local_rank)
+    build.build()
+    ob.build()
+    base = tempfile.mkdtemp(prefix="cipsi_large_")
+    cfg = dataclasses.replace(synth.CONFIGS["large"])
+    cfg.seed += rank
+    wd = os.path.join(base, "large")
+    t0 = time.perf_counter()
+    synth.generate(cfg, wd)
+    t_gen = time.perf_counter() - t0
+    inp = engine.Inputs(wd)
+    ysaut = inp.array("ysaut")
+    ncf = inp.dims.ncf
+    picks = []
+    for start in (ncf // 3, (2 * ncf) // 3):
+        k = start
+        while ysaut[k]:
+            k += 1
+        picks.append(k)
+    # CPU oracle on the two generators, in parallel (started before any GPU work)
+    cpu = []
+    if rank == 0 and not args.no_cpu_baseline:
+        masks = []
+        for k in picks:
+            m = np.zeros(ncf, np.uint8)
+            m[k] = 1
+            masks.append(m)
+        with ProcessPoolExecutor(max_workers=len(masks), mp_context=mpm.get_context("spawn")) as ex:
+            futs = [ex.submit(_oracle_on_mask, wd, m, base) for m in masks]
+            cpu = [f.result() for f in futs]
+    ctx = engine.Context(inp.dims, device=local_rank)
+    ctx.upload(inp)
+    ctx.set_tuning(6, 0)
+    for _ in range(args.warmup):
+        ctx.run_async(inp.opts)
+        r = batch._fetch_allow_overflow(ctx)
+    clocks = Clocks(local_rank)
+    clocks.start()
+    ms = []
+    for _ in range(args.steps):
+        torch.cuda.synchronize()
+        ctx.run_async(inp.opts)
+        r = batch._fetch_allow_overflow(ctx)
+        ms.append(r["kernel_ms"])
+    # end to end: upload from host + run + results (records not stored)
+    t0 = time.perf_counter()
+    ctx.upload(inp)
+    ctx.run_async(inp.opts)
+    r2 = batch._fetch_allow_overflow(ctx)
+    e2e_ms = 1e3 * (time.perf_counter() - t0)
+    clk = clocks.stop()
+    contrib = r["n_processed"] * inp.dims.metat
+    line = {"metric": "perturber contributions/s", "value": contrib / (statistics.mean(ms) / 1e3),
+            "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": statistics.mean(ms), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded integrals and reference space)",
+            "config": {"workload": "large: 120 MOs, 30 e-, Ms=0, S=20000 dets (ref + doubles, spin-flip closed), "
+                                   "2 roots, MP+EN, tau=0.005", "records": "counted, not stored"},
+            "e2e": {"value": contrib / (e2e_ms / 1e3), "unit": UNIT, "ms_per_step": e2e_ms},
+            "work": {"perturbers": r["n_processed"], "selected": r["n_selected"], "ietat": r["ietat"],
+                     "compares": r["n_compares"], "e2vp": r["e2vp"]},
+            "clocks": clk, "generation_s": t_gen}
+    if cpu:
+        # the GPU on the same two generators
+        m = np.zeros(ncf, np.uint8)
+        m[picks] = 1
+        ctx.run_async(inp.opts, gen_mask=m, run_pertu=False)
+        rs = batch._fetch_allow_overflow(ctx)
+        cpu_contrib = sum(j["n_processed"] * j["metat"] for j, _ in cpu)
+        cpu_s = sum(dt for _, dt in cpu)
+        par = {}
+        for key in ("e2mp", "e2vp", "e2b"):
+            ref = np.sum([np.array(j[key]) for j, _ in cpu], axis=0)
+            cond = np.sum([np.array(j.get("cond_" + key, [0.0] * len(j[key]))) for j, _ in cpu], axis=0)
+            diff = np.abs(np.array(rs[key]) - ref)
+            par[key] = {"max_abs_diff": float(diff.max()), "tolerance": float((1e-10 + cond).max()),
+                        "ok": bool(np.all(diff <= 1e-10 + cond))}
+        par["n_processed_equal"] = rs["n_processed"] == sum(j["n_processed"] for j, _ in cpu)
+        line["cpu_baseline"] = {"value": cpu_contrib / cpu_s, "unit": UNIT, "cores": 1, "kind": "port",
+                                "sample": f"generators {picks} of S (one process each), {cpu_s:.0f} core-s; "
+                                          "rate per core, extrapolated to the whole step linearly in "
+                                          "contributions"}
+        line["parity_sample"] = par
+    ctx.close()
+    inp.close()
+    shutil.rmtree(base, ignore_errors=True)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 # ------------------------------------------------------------ adjoint form
 def run_adjoint_form(args, rank: int, world: int, local_rank: int):
     """The medium system plus a seeded symmetric dipole matrix mu ~ N(0, 0.5):
@@ -322,9 +443,10 @@ def run_adjoint_form(args, rank: int, world: int, local_rank: int):
 
     dip = dipole_check(S, h_tri, eri)
     S.close()
-    # the same system with a 3 Eh occupied/virtual gap (denominators away from
-    # zero): there the finite-field difference converges and checks the dipole
-    cfg_w = dataclasses.replace(cfg, name="medium_gap", virt_shift=3.0)
+    # the same sizes with HF-dominated roots (coefficients N(0, 0.05), HF = 1)
+    # and a 10 Eh occupied/virtual gap: the denominators stay away from zero,
+    # the finite-field difference converges and checks the dipole
+    cfg_w = dataclasses.replace(cfg, name="medium_hf_gap", virt_shift=10.0, coef_mode="gauss005")
     wd_w = os.path.join(base, "gap")
     synth.generate(cfg_w, wd_w)
     h_w, L_w, _ = synth.make_integrals(cfg_w, np.random.default_rng(cfg_w.seed))
@@ -341,9 +463,10 @@ def run_adjoint_form(args, rank: int, world: int, local_rank: int):
             "config": {"workload": "medium (60 MOs, S = 2000, 3 roots), integrals in FP64, seed on e2vp[0]"},
             "forward_ms": statistics.mean(fwd_ms), "adjoint_ms": statistics.mean(adj_ms),
             "fd_check": {"elements": len(picks), "step": step, "max_rel_err": worst},
-            "dipole_medium": dip, "dipole_medium_gap3": dip_w,
-            "note": "the medium recipe has EN denominators near zero, so its finite-field differences do not "
-                    "converge with the field; the gap-3 variant is the dipole check"}
+            "dipole_medium": dip, "dipole_medium_hf_gap10": dip_w,
+            "note": "the medium recipe (random decay-0.9 roots) has EN denominators near zero, so its "
+                    "finite-field differences do not converge with the field; the HF-dominated gap-10 "
+                    "variant of the same sizes is the dipole check"}
     if rank == 0:
         print(json.dumps(line), flush=True)
 
@@ -495,6 +618,8 @@ def main():
                     help="batched: the potential-curve batch (geometries/s, batched vs plain); "
                          "adjoint: dE2/d integrals on the medium system with checks")
     ap.add_argument("--fd-elements", type=int, default=200)
+    ap.add_argument("--workload", choices=["medium", "large"], default="medium",
+                    help="large: the 120-orbital S = 20,000 system (plain form, records counted only)")
     ap.add_argument("--geometries", type=int, default=256)
     ap.add_argument("--batch-steps", type=int, default=2)
     ap.add_argument("--batch-warmup", type=int, default=1)
@@ -514,6 +639,9 @@ def main():
         return
     if args.form == "adjoint":
         run_adjoint_form(args, rank, world, local_rank)
+        return
+    if args.workload == "large":
+        run_large(args, rank, world, local_rank)
         return
     run_gpu(args, rank, world, local_rank)
 
