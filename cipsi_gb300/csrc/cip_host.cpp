@@ -169,6 +169,7 @@ struct Options {
   double aval[10] = {0.128e-6, 0.64e-6, 0.32e-5, 0.16e-4, 0.8e-4, 0.4e-3, 0.2e-2, 0.1e-1, 0.5e-1, 1.0};
   std::string title = "                    ";
   std::vector<double> tocom;
+  std::vector<int> numero;  // state numbers (default 1..metat)
   // &cipfil
   std::string f60 = "det", f40 = "ijkl", f04 = "f04", f59 = "bdvec", f33 = "ener";
 };
@@ -207,6 +208,8 @@ Options read_options(const std::string& text, const std::string& dir) {
     for (size_t i = 0; i < v->size() && i < 10; ++i) o.aval[i] = to_real((*v)[i]);
   if (auto v = ic.get("tocom"))
     for (auto& x : *v) o.tocom.push_back(to_real(x));
+  if (auto v = ic.get("numero"))
+    for (auto& x : *v) o.numero.push_back(std::stoi(x));
   if (auto v = ic.get("title"); v && !v->empty()) {
     o.title = (*v)[0];
     o.title.resize(20, ' ');
@@ -240,6 +243,7 @@ struct Run {
   double escf = 0.0;
   Space S;
   std::vector<double> c, e, eb, emp, teste, taum, fmpb, fdiag;
+  std::vector<double> tocom, empdet;  // faifoc.f occupations (after cip.f:75-84), hmp of S
 };
 
 // transf.f: sort, validate, dedup and append one determinant
@@ -544,7 +548,10 @@ void read_inputs(Run& R, bool sym_variant) {
   R.eb.assign(R.metat, 0.0);
   R.teste.assign(R.metat, o.test);
   R.taum.assign(R.metat, 1.0);
-  std::vector<double> empdet(R.ncf), hdiag(R.ncf);
+  R.tocom = tocom;
+  std::vector<double>& empdet = R.empdet;
+  empdet.assign(R.ncf, 0.0);
+  std::vector<double> hdiag(R.ncf);
   for (int k = 0; k < R.ncf; ++k) {
     empdet[k] = hmp_list(R, k);
     hdiag[k] = hdig_list(R, k);
@@ -563,6 +570,145 @@ void read_inputs(Run& R, bool sym_variant) {
       R.taum[m] = 1.0 / t;
     }
   }
+}
+
+// ------------------------------------------------------------------ unit 4
+// dimension of nblock / nstart in the reference's parameter file (pshf.prm
+// ndetz): the zero-order record carries both arrays in full
+constexpr int kUnit4Ndetz = 500000;
+
+bool yocd_of(const Run& R, int so, int k) {
+  for (int l = 0; l < R.S.ne[k]; ++l)
+    if (R.S.trou[R.S.nd[k] + l] == so || R.S.part[R.S.nd[k] + l] == so) return true;
+  return false;
+}
+
+// cip.f:136-150: the zero-order record that cip writes on unit 4 (rewinding
+// it) before the perturbation
+void write_unit4_zero_order(const Run& R) {
+  std::FILE* f = std::fopen(R.o.f04.c_str(), "wb");
+  if (!f) throw Error("cannot rewrite " + R.o.f04);
+  const int ncf = R.ncf, mt = R.metat, n = R.norb, mn = 2 * R.norb;
+  const int jj = ncf * mt, ii = R.S.nd[ncf - 1] + R.S.ne[ncf - 1] + 1;
+  const double e0 = R.o.ityper == 0 ? R.escf : 0.0;
+  RecWriter w;
+  for (int32_t v : {(int32_t)n, (int32_t)R.noc, (int32_t)(R.noc + n), (int32_t)mt, (int32_t)ncf, (int32_t)0})
+    w.put<int32_t>(v);
+  w.put<uint8_t>(0);  // yion
+  w.put<int32_t>(ii);
+  w.put<int32_t>(jj);
+  for (int k = 0; k < ncf; ++k) {
+    w.put<int32_t>(R.S.ne[k]);
+    w.put<int32_t>(R.S.nd[k]);
+  }
+  for (int j = 0; j < ii; ++j) {
+    const bool in = j < (int)R.S.trou.size();
+    w.put<int32_t>(in ? R.S.trou[j] : 0);
+    w.put<int32_t>(in ? R.S.part[j] : 0);
+  }
+  for (int j = 0; j < jj; ++j) w.put<double>(R.c[j]);
+  for (int m = 0; m < mt; ++m) w.put<double>(R.e[m] + e0);
+  for (int m = 0; m < mt; ++m) w.put<double>(R.emp[m]);
+  for (int m = 0; m < mt; ++m) w.put<double>(R.eb[m]);
+  for (int m = 0; m < mt; ++m) w.put<int32_t>(m < (int)R.o.numero.size() ? R.o.numero[m] : m + 1);
+  for (int k = 0; k < ncf; ++k) w.put<double>(R.empdet[k]);
+  for (int i = 0; i < n; ++i) w.put<double>(R.fmpb[i]);
+  for (int i = 0; i < n; ++i) w.put<double>(R.tocom[i]);
+  for (int i = 0; i < 2 * kUnit4Ndetz; ++i) w.put<int32_t>(0);  // nblock, nstart (given.f): unused, lecdet = 5
+  for (int i = 1; i <= mn; ++i) w.put<int32_t>(i <= n ? i : i - n);  // iorb
+  for (int i = 1; i <= mn; ++i) w.put<int32_t>(i <= n ? 0 : 1);      // ispin
+  for (int k = 0; k < ncf; ++k)
+    for (int so = 1; so <= mn; ++so) w.put<uint8_t>(yocd_of(R, so, k) ? 1 : 0);
+  w.flush(f);
+  std::fclose(f);
+}
+
+// brdnee.f:38-135 for the spin flip alone (isz = 0, no spatial operation):
+// the signed index of the flipped image of every determinant of S and the
+// sign of each root under the flip
+std::vector<int> root_flip_signs(const Run& R) {
+  const int ncf = R.ncf, n = R.norb;
+  auto flip = [&](int so) { return so <= n ? so + n : so - n; };
+  std::vector<int> itk(ncf, 0);  // 1-based signed image, 0 = none
+  for (int k = 0; k < ncf; ++k) {
+    if (R.S.ysaut[k]) continue;
+    const int nespk = R.S.nesp[k] + 1, nec = R.S.ne[k];
+    if (nec == 0) {
+      itk[k] = k + 1;
+      continue;
+    }
+    for (int kg = 0; kg < nespk; ++kg) {
+      const int kk = k + kg, ndk = R.S.nd[kk];
+      int ntl[16], npl[16], ncr = 1, ii = kk + 1;
+      for (int i = 0; i < nec; ++i) {
+        ntl[i] = flip(R.S.trou[ndk + i]);
+        npl[i] = flip(R.S.part[ndk + i]);
+      }
+      bool sort = true;
+      if (R.S.yef1[k]) {
+        bool found = false;
+        for (int ig = 0; ig < nespk && !found; ++ig) {
+          ii = k + ig + 1;
+          bool all = true;
+          for (int i = 0; i < nec && all; ++i)
+            if (!yocd_of(R, ntl[i], ii - 1) || !yocd_of(R, npl[i], ii - 1)) all = false;
+          found = all;
+        }
+        if (!found && nec == 1) sort = false;
+      }
+      if (sort)
+        for (int i = 0; i < nec - 1; ++i)
+          for (int j = i + 1; j < nec; ++j) {
+            if (!(ntl[j] > ntl[i])) { std::swap(ntl[i], ntl[j]); ncr = -ncr; }
+            if (!(npl[j] > npl[i])) { std::swap(npl[i], npl[j]); ncr = -ncr; }
+          }
+      itk[kk] = ncr < 0 ? -ii : ii;
+    }
+  }
+  std::vector<int> itm(R.metat, 1);
+  for (int m = 0; m < R.metat; ++m) {
+    const double* cm = R.c.data() + (size_t)m * ncf;
+    double x = 0.0;
+    for (int k = 0; k < ncf; ++k) {
+      if (itk[k] == 0) continue;
+      const int ik = std::abs(itk[k]) - 1;
+      double ckk = cm[k] * cm[ik];
+      if (itk[k] < 0) ckk = -ckk;
+      x = x + ckk;
+    }
+    itm[m] = x < 0.0 ? -1 : 1;
+  }
+  return itm;
+}
+
+// cip.f:300-306 and 403-414: zero-order and perturbed effective Hamiltonians
+// (diagonal without QDPT) appended to unit 4 after the perturbation
+void write_unit4_results(const Run& R, const double* e2mp, const double* e2vp, const double* e2b,
+                         const std::vector<int>& itm) {
+  std::FILE* f = std::fopen(R.o.f04.c_str(), "ab");
+  if (!f) throw Error("cannot append to " + R.o.f04);
+  const int mt = R.metat, nbr = mt * (mt + 1) / 2;
+  std::vector<double> hz(nbr, 0.0), hm(nbr, 0.0), hv(nbr, 0.0), hb(nbr, 0.0);
+  for (int m = 1; m <= mt; ++m) {
+    const int mm = m * (m + 1) / 2 - 1;
+    const double eabs = R.e[m - 1] + R.escf;
+    hm[mm] = eabs + e2mp[m - 1];
+    hv[mm] = eabs + e2vp[m - 1];
+    hb[mm] = eabs + e2b[m - 1];
+    hz[mm] = eabs - R.escf;
+  }
+  RecWriter w;
+  for (double x : hz) w.put<double>(x);
+  w.put<double>(R.escf);
+  w.put<int32_t>(R.o.ityper);
+  w.put<int32_t>(1);  // ntrsy: the spin flip alone
+  for (int m = 0; m < mt; ++m) w.put<int32_t>(itm[m]);
+  w.flush(f);
+  for (double x : hm) w.put<double>(x);
+  for (double x : hv) w.put<double>(x);
+  for (double x : hb) w.put<double>(x);
+  w.flush(f);
+  std::fclose(f);
 }
 
 void write_pie_records(std::FILE* f, const std::vector<int32_t>& nec, const std::vector<int32_t>& h,
@@ -747,6 +893,8 @@ extern "C" int cipsi_cip_main(const char* workdir, const char* stdin_path, int32
     };
     chk(rc, "cipsi_ctx_create");
     chk(cipsi_inputs_upload(in, ctx), "cipsi_inputs_upload");
+    write_unit4_zero_order(R);
+    const std::vector<int> itm = root_flip_signs(R);
     cipsi_result res{};
     if (R.o.ityper != 0) chk(cipsi_run_pt2(ctx, &op, &res), "cipsi_run_pt2");
     const auto t1 = std::chrono::steady_clock::now();
@@ -780,6 +928,7 @@ extern "C" int cipsi_cip_main(const char* workdir, const char* stdin_path, int32
       ntot += ns;
     }
     std::fclose(f60);
+    write_unit4_results(R, res.e2mp, res.e2vp, res.e2b, itm);
     // listing lines the Autocip driver reads (cipsym/cip.f:253-254, cip.f:243-247)
     std::printf("0 ont ete generes:    %10lld  etats efficaces\n", (long long)res.ietat);
     std::printf(" la contribution du plus grand determinant non ecrit est %8.6f\n", res.dpivot);

@@ -166,6 +166,14 @@ struct cipsi_ctx {
   bool pending = false;
   cipsi_opts last_opts{};
   long long nsel = 0;  // records of the last fetched run
+  // caller-provided record arrays in pinned host memory (cipsi_set_selection_sink):
+  // the kernel writes the unit-60 records there directly
+  bool sink = false;
+  uint64_t* sink_bits = nullptr;
+  int32_t* sink_owner = nullptr;
+  double *sink_xam = nullptr, *sink_evp = nullptr;
+  long long sink_cap = 0;
+  void* sink_host[4] = {nullptr, nullptr, nullptr, nullptr};  // the caller's addresses
 };
 
 namespace {
@@ -773,6 +781,13 @@ void fill_params(const cipsi_ctx* ctx, const cipsi_opts* o, const RunPlan& pl, P
   p.sel_xam = ctx->dsel_xam;
   p.sel_evp = ctx->dsel_evp;
   p.sel_cap = ctx->sel_cap;
+  if (ctx->sink) {
+    p.sel_bits = ctx->sink_bits;
+    p.sel_owner = ctx->sink_owner;
+    p.sel_xam = ctx->sink_xam;
+    p.sel_evp = ctx->sink_evp;
+    p.sel_cap = ctx->sink_cap;
+  }
   p.work = ctx->dwork;
 }
 
@@ -786,6 +801,44 @@ int cipsi_set_tuning(cipsi_ctx* ctx, int32_t r_chunk, int32_t ctas_per_sm) {
   if (ctas_per_sm < 0 || ctas_per_sm > 2) return fail(ctx, CIPSI_ERR_ARG, "ctas_per_sm must be 0, 1 or 2");
   ctx->tune_r_chunk = r_chunk;
   ctx->tune_ctas = ctas_per_sm;
+  return CIPSI_OK;
+}
+
+int cipsi_set_selection_sink(cipsi_ctx* ctx, uint64_t* bits, int32_t* owner, double* xam, double* evp,
+                             int64_t capacity) {
+  if (!ctx) return CIPSI_ERR_ARG;
+  if (ctx->pending) return fail(ctx, CIPSI_ERR_STATE, "an asynchronous run is pending: fetch its result first");
+  ++ctx->buf_gen;
+  if (!bits) {
+    ctx->sink = false;
+    ctx->sink_bits = nullptr;
+    ctx->sink_owner = nullptr;
+    ctx->sink_xam = ctx->sink_evp = nullptr;
+    ctx->sink_cap = 0;
+    ctx->nsel = 0;
+    return CIPSI_OK;
+  }
+  if (!owner || !xam || !evp || capacity < 1)
+    return fail(ctx, CIPSI_ERR_ARG, "selection sink: null array or capacity < 1");
+  CK(cudaSetDevice(ctx->device));
+  void* host[4] = {bits, owner, xam, evp};
+  void* dev[4] = {nullptr, nullptr, nullptr, nullptr};
+  for (int i = 0; i < 4; ++i) {
+    cudaPointerAttributes a{};
+    CK(cudaPointerGetAttributes(&a, host[i]));
+    if (a.type != cudaMemoryTypeHost)
+      return fail(ctx, CIPSI_ERR_ARG, "selection sink: arrays must be pinned host memory (cudaHostAlloc or "
+                                      "cudaHostRegister)");
+    CK(cudaHostGetDevicePointer(&dev[i], host[i], 0));
+  }
+  ctx->sink = true;
+  ctx->sink_bits = static_cast<uint64_t*>(dev[0]);
+  ctx->sink_owner = static_cast<int32_t*>(dev[1]);
+  ctx->sink_xam = static_cast<double*>(dev[2]);
+  ctx->sink_evp = static_cast<double*>(dev[3]);
+  ctx->sink_cap = capacity;
+  for (int i = 0; i < 4; ++i) ctx->sink_host[i] = host[i];
+  ctx->nsel = 0;
   return CIPSI_OK;
 }
 
@@ -910,14 +963,18 @@ int cipsi_fetch_result(cipsi_ctx* ctx, cipsi_result* r) {
   float ms = -1.f;  // batched runs: the batch's time is reported by the batch
   if (ctx->ev_valid) CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
   r->kernel_ms = ms;
-  // selection: records stay on the device until cipsi_selection_get/raw
+  // selection: records stay on the device (or in the sink) until
+  // cipsi_selection_get/raw
   const long long nsel = (long long)cnt[C_NSEL];
-  if (nsel > ctx->sel_cap)
+  r->n_selected = nsel;
+  const long long cap = ctx->sink ? ctx->sink_cap : ctx->sel_cap;
+  ctx->nsel = std::min(nsel, cap);
+  if (nsel > cap)
     return fail(ctx, CIPSI_ERR_OVERFLOW,
                 "selection buffer overflow: " + std::to_string(nsel) + " records > capacity " +
-                    std::to_string(ctx->sel_cap) + " (cipsi_run_pt2 grows the buffer and reruns)");
-  ctx->nsel = nsel;
-  r->n_selected = nsel;
+                    std::to_string(cap) +
+                    (ctx->sink ? " (the sink holds the first records; the rest were counted only)"
+                               : " (cipsi_run_pt2 grows the buffer and reruns)"));
   return CIPSI_OK;
 }
 
@@ -926,7 +983,7 @@ int cipsi_run_pt2(cipsi_ctx* ctx, const cipsi_opts* opts, cipsi_result* res) {
     int rc = cipsi_run_pt2_async(ctx, opts);
     if (rc) return rc;
     rc = cipsi_fetch_result(ctx, res);
-    if (rc != CIPSI_ERR_OVERFLOW) return rc;
+    if (rc != CIPSI_ERR_OVERFLOW || ctx->sink) return rc;
     // grow the selection buffer to what the run needed and redo
     unsigned long long nsel = 0;
     CK(cudaMemcpy(&nsel, ctx->dcounters + C_NSEL, 8, cudaMemcpyDeviceToHost));
@@ -1057,6 +1114,17 @@ int cipsi_selection_raw(cipsi_ctx* ctx, int64_t first, int64_t count, uint64_t* 
   if (count == 0) return CIPSI_OK;
   CK(cudaSetDevice(ctx->device));
   const int W = ctx->W, mt = ctx->d.metat;
+  if (ctx->sink) {
+    // the records are already in host memory
+    auto cp = [](void* dst, const void* src, size_t n) {
+      if (dst && dst != src) std::memcpy(dst, src, n);
+    };
+    cp(bits, static_cast<const uint64_t*>(ctx->sink_host[0]) + (size_t)first * 2 * W, (size_t)count * 2 * W * 8);
+    cp(owner, static_cast<const int32_t*>(ctx->sink_host[1]) + first, (size_t)count * 4);
+    cp(xam, static_cast<const double*>(ctx->sink_host[2]) + first, (size_t)count * 8);
+    cp(evp, static_cast<const double*>(ctx->sink_host[3]) + (size_t)first * mt, (size_t)count * mt * 8);
+    return CIPSI_OK;
+  }
   if (bits)
     CK(cudaMemcpyAsync(bits, ctx->dsel_bits + (size_t)first * 2 * W, (size_t)count * 2 * W * 8,
                        cudaMemcpyDeviceToHost, ctx->stream));

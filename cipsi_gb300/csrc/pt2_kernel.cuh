@@ -458,8 +458,8 @@ struct Acc {
 template <int R>
 struct HistPriv {
   double tab[kNClass][2][R];
-  unsigned long long nom[kNClass];
-  unsigned long long nam[kNClass][R];
+  unsigned int nom[kNClass];  // per-thread counts stay far below 2^32
+  unsigned int nam[kNClass][R];
   __device__ void zero() {
     for (int c = 0; c < kNClass; ++c) {
       nom[c] = 0ull;
@@ -570,13 +570,13 @@ __device__ void finish_candidate(const Params& p, bool live, const uint64_t* u, 
   if (live && (is_pert1 || p.ymoyen) && xam >= p.teseff) {
     const double fm = fmul + 1.0;
     const int cls = hist_class(p, xam);
-    hp.nom[cls] += (unsigned long long)(1 + nmul);
+    hp.nom[cls] += (unsigned)(1 + nmul);
 #pragma unroll
     for (int m = 0; m < R; ++m) {
       if (m >= p.metat || vil[m] < p.teseff) continue;
       hp.tab[cls][0][m] += semp[m] * fm;
       hp.tab[cls][1][m] += sevp[m] * fm;
-      hp.nam[hist_class(p, vil[m])][m] += (unsigned long long)(1 + nmul);
+      hp.nam[hist_class(p, vil[m])][m] += (unsigned)(1 + nmul);
     }
   }
   if (ydeg) xam = 1.0;
@@ -718,12 +718,12 @@ __device__ void flush_totals(const Params& p, Acc<R>& acc, HistPriv<R>& hp, Smem
   }
   // this thread's histogram into the block's
   for (int c = 0; c < p.nclass; ++c) {
-    if (hp.nom[c]) atomicAdd(&hist.nom[c], hp.nom[c]);
+    if (hp.nom[c]) atomicAdd(&hist.nom[c], (unsigned long long)hp.nom[c]);
     for (int m = 0; m < R && m < p.metat; ++m) {
       if (hp.tab[c][0][m] != 0.0) atomicAdd(&hist.tab[c * kMaxRoots + m], hp.tab[c][0][m]);
       if (hp.tab[c][1][m] != 0.0)
         atomicAdd(&hist.tab[kNClass * kMaxRoots + c * kMaxRoots + m], hp.tab[c][1][m]);
-      if (hp.nam[c][m]) atomicAdd(&hist.nam[c * kMaxRoots + m], hp.nam[c][m]);
+      if (hp.nam[c][m]) atomicAdd(&hist.nam[c * kMaxRoots + m], (unsigned long long)hp.nam[c][m]);
     }
   }
   __syncthreads();
@@ -1395,7 +1395,11 @@ __global__ void __launch_bounds__(kThreads, 2) k_pt2(Params p0, BatchArgs ba) {
         const int sr = same ? sp1 : 0, sc = same ? sp1 : 1;
         const int nrows = same ? nv1 - 1 : sh.nvir[0];
         int16_t* rowbuf = wrow + wid * kRowCap;
-        for (int row = wid; row < nrows; row += nwarps) {
+        // rows in zig-zag order over the warps (row lengths fall with the
+        // row index for same-spin pairs): even stripes forward, odd backward
+        for (int t = 0; t * nwarps < nrows; ++t) {
+          const int row = (t & 1) ? t * nwarps + (nwarps - 1 - wid) : t * nwarps + wid;
+          if (row >= nrows) continue;
           const int a1 = sh.vir[sr][row];
           const int w1 = sr * W + (a1 >> 6);
           const uint64_t b1 = 1ull << (a1 & 63);

@@ -66,6 +66,7 @@ def _lib():
         "cipsi_run_pt2": ([P, ctypes.POINTER(Opts), ctypes.POINTER(Result)], ctypes.c_int),
         "cipsi_run_pt2_async": ([P, ctypes.POINTER(Opts)], ctypes.c_int),
         "cipsi_set_tuning": ([P, ctypes.c_int32, ctypes.c_int32], ctypes.c_int),
+        "cipsi_set_selection_sink": ([P, P, P, P, P, ctypes.c_int64], ctypes.c_int),
         "cipsi_fetch_result": ([P, ctypes.POINTER(Result)], ctypes.c_int),
         "cipsi_selection_get": ([P, ctypes.c_int64, ctypes.c_int64, P, P, P, P, P, P], ctypes.c_int),
         "cipsi_selection_raw": ([P, ctypes.c_int64, ctypes.c_int64, P, P, P, P], ctypes.c_int),
@@ -179,6 +180,21 @@ class Context:
 
     def set_stream(self, stream_handle: int):
         self._check(self.lib.cipsi_set_stream(self._c, ctypes.c_void_p(stream_handle)), "set_stream")
+
+    def set_selection_sink(self, out: Optional[dict]):
+        """Have the kernel write the unit-60 records into `out` (pinned host
+        arrays: bits [cap, 2W] uint64, owner [cap] int32, xam [cap] float64,
+        evp [cap, metat] float64, as selection_raw returns); None = device
+        buffers again."""
+        if out is None:
+            self._sink = None
+            self._check(self.lib.cipsi_set_selection_sink(self._c, None, None, None, None, 0), "set_selection_sink")
+            return
+        cap = len(out["owner"])
+        self._sink = out
+        self._check(self.lib.cipsi_set_selection_sink(
+            self._c, out["bits"].ctypes.data, out["owner"].ctypes.data, out["xam"].ctypes.data,
+            out["evp"].ctypes.data, cap), "set_selection_sink")
 
     def set_tuning(self, r_chunk: int = 6, ctas_per_sm: int = 0):
         self._check(self.lib.cipsi_set_tuning(self._c, r_chunk, ctas_per_sm), "set_tuning")

@@ -88,6 +88,7 @@ class SynthConfig:
     variant: str = "cipsym"  # or "cip"
     extra_icinp: str = ""
     virt_shift: float = 0.0  # added to h_aa of virtual orbitals (0 = the plain recipe)
+    coef_sigma: float = 0.05  # width of the non-HF coefficients in "gauss005" mode
     curve_R: Optional[float] = None  # potential-curve geometry R (bohr): integrals from
                                      # L(R) = L0 + exp(-R/3) L1, eps(R) = eps0 + 0.1 exp(-R/2) eps1
     energy: str = "rayleigh"  # root energies: "rayleigh" (<Psi|H|Psi>) or "diagonal"
@@ -578,7 +579,7 @@ def generate(cfg: SynthConfig, workdir: str, verbose: bool = False) -> dict:
         ranks[rep_of[i]] = len(hl)
     for m in range(cfg.metat):
         if cfg.coef_mode == "gauss005":
-            v = rng.normal(0.0, 0.05, size=nrep)
+            v = rng.normal(0.0, cfg.coef_sigma, size=nrep)
             if cfg.include_hf:
                 v[0] = 1.0 if m == 0 else v[0]
         else:

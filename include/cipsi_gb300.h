@@ -160,6 +160,20 @@ int cipsi_run_pt2(cipsi_ctx* ctx, const cipsi_opts* opts, cipsi_result* res);
    cipsi_gb300.tune (Python) picks both by timing a generator sample. */
 int cipsi_set_tuning(cipsi_ctx* ctx, int32_t r_chunk, int32_t ctas_per_sm);
 
+/* Unit-60 records straight into caller memory (no counterpart in the
+   reference): pinned host arrays (cudaHostAlloc / cudaHostRegister) of
+   `capacity` records, laid out as cipsi_selection_raw returns them (bits
+   [capacity*2W], owner, xam, evp [capacity*metat]).  Later runs on this
+   context write their records there from the kernel, over the host link,
+   while they compute; cipsi_selection_raw then copies from these arrays
+   (or does nothing when given the same arrays).  Records beyond `capacity`
+   are counted, not stored: cipsi_fetch_result reports CIPSI_ERR_OVERFLOW with
+   the results valid and the first `capacity` records kept, and
+   cipsi_run_pt2 does not rerun.  bits = NULL returns to device buffers.
+   The arrays must stay allocated while the sink is set. */
+int cipsi_set_selection_sink(cipsi_ctx* ctx, uint64_t* bits, int32_t* owner, double* xam, double* evp,
+                             int64_t capacity);
+
 /* Enqueue the same work on the context stream without waiting; the result is
    collected by cipsi_fetch_result.  Used to time the kernels alone. */
 int cipsi_run_pt2_async(cipsi_ctx* ctx, const cipsi_opts* opts);

@@ -248,6 +248,9 @@ static int nl_set_int_arr(nlgroup_t* g, const char* k, int* dst, int max) {
 
 /* ------------------------------------------------------------ the state */
 /* COMMON /cipsi/ */
+/* dimension of nblock / nstart in the reference's parameter file
+   (pshf.prm ndetz): unit 4 carries both arrays in full */
+#define UNIT4_NDETZ 500000
 static double escf, test, teseff, tdet, twdet, coeff, tau;
 static int ndiag, norb, mnorb, noca, nocb, noc1, noc2, igela, igelb, ncf, nsym, isym, isz,
     ntrsy, metat, lecdet, maxdet, ityper, iselec, nclass, ninact;
@@ -1651,6 +1654,144 @@ static void build_space(void) {
   if (ncf == 0) die("aucun determinant dans le sous espace variationnel");
 }
 
+/* ------------------------------------------------------------- unit 4 */
+/* brdnee.f:38-135 for ntrsy == 1, isz == 0: the signed index itk(k) of the
+   spin-flip image of every determinant of S (0 = none) and the sign itm(m)
+   of each root under the flip. */
+static int itm_[64];
+static void brdnee_itm(void) {
+  int* itk = (int*)xcalloc((size_t)ncf + 4, sizeof(int));
+  for (int k = 1; k <= ncf; k++) {
+    if (ysaut[k]) continue;
+    int nespk = nesp[k] + 1, nec = ne[k];
+    if (nec == 0) {
+      itk[k] = k;
+      continue;
+    }
+    for (int kg = 1; kg <= nespk; kg++) {
+      int kk = k + kg - 1, ndk = nd[kk];
+      int ntl[16], npl[16], isigne = 1, ncr = 1, ii = kk, ok = 1;
+      for (int i = 1; i <= nec; i++) {
+        int ntli = isytr1[trou[i + ndk]], npli = isytr1[part[i + ndk]];
+        if (ntli == 0 || npli == 0) { ok = 0; break; }
+        if (ntli <= 0) isigne = -isigne;
+        if (npli <= 0) isigne = -isigne;
+        ntl[i] = abs(ntli);
+        npl[i] = abs(npli);
+      }
+      if (!ok) { itk[kk] = 0; continue; }
+      int sort = 1;
+      if (yef1[k]) {
+        int found = 0;
+        for (int ig = 1; ig <= nespk; ig++) {
+          ii = k + ig - 1;
+          int all = 1;
+          for (int i = 1; i <= nec && all; i++)
+            if (!YOCD(ntl[i], ii) || !YOCD(npl[i], ii)) all = 0;
+          if (all) { found = 1; break; }
+        }
+        if (!found && nec == 1) sort = 0;
+      } else {
+        ii = kk;
+      }
+      if (sort) {
+        for (int i = 1; i <= nec - 1; i++)
+          for (int j = i + 1; j <= nec; j++) {
+            if (!(ntl[j] > ntl[i])) { int t = ntl[j]; ntl[j] = ntl[i]; ntl[i] = t; ncr = -ncr; }
+            if (!(npl[j] > npl[i])) { int t = npl[j]; npl[j] = npl[i]; npl[i] = t; ncr = -ncr; }
+          }
+      }
+      if (isigne < 0) ii = -ii;
+      if (ncr < 0) ii = -ii;
+      itk[kk] = ii;
+    }
+  }
+  for (int m = 1; m <= metat; m++) {
+    int mncf = (m - 1) * ncf;
+    double x = 0.0;
+    for (int k = 1; k <= ncf; k++) {
+      if (itk[k] == 0) continue;
+      int kk = itk[k], ikk = abs(kk);
+      double ckk = c[mncf + k] * c[mncf + ikk];
+      if (kk < 0) ckk = -ckk;
+      x = x + ckk;
+    }
+    itm_[m] = x < 0.0 ? -1 : 1;
+  }
+  free(itk);
+}
+
+/* cip.f:136-150: zero-order record on unit 4 (rewinds the unit) */
+static void write_unit4_zero_order(const char* path, const double* empdet) {
+  FILE* f4 = fopen(path, "wb");
+  if (!f4) die("cannot rewrite unit 4 file %s", path);
+  int jj = ncf * metat, ii = nd[ncf] + ne[ncf] + 1;
+  double e0 = ityper == 0 ? escf : 0.0;
+  wbuf_t w = {0};
+  wb_i4(&w, norb); wb_i4(&w, noca); wb_i4(&w, nocb); wb_i4(&w, metat); wb_i4(&w, ncf); wb_i4(&w, isz);
+  unsigned char yb = yion ? 1 : 0;
+  wb_put(&w, &yb, 1);
+  wb_i4(&w, ii); wb_i4(&w, jj);
+  for (int j = 1; j <= ncf; j++) { wb_i4(&w, ne[j]); wb_i4(&w, nd[j]); }
+  for (int j = 1; j <= ii; j++) { wb_i4(&w, trou[j]); wb_i4(&w, part[j]); }
+  for (int j = 1; j <= jj; j++) wb_r8(&w, c[j]);
+  for (int j = 1; j <= metat; j++) wb_r8(&w, e[j] + e0);
+  for (int j = 1; j <= metat; j++) wb_r8(&w, emp[j]);
+  for (int j = 1; j <= metat; j++) wb_r8(&w, eb[j]);
+  for (int j = 1; j <= metat; j++) wb_i4(&w, numero[j]);
+  for (int j = 1; j <= ncf; j++) wb_r8(&w, empdet[j]);
+  for (int j = 1; j <= norb; j++) wb_r8(&w, fmpb[j]);
+  for (int j = 1; j <= norb; j++) wb_r8(&w, tocom[j]);
+  /* nblock, nstart (given.f, the S diagonalisation): zero for lecdet = 5 */
+  for (int j = 0; j < 2 * UNIT4_NDETZ; j++) wb_i4(&w, 0);
+  for (int j = 1; j <= mnorb; j++) wb_i4(&w, iorb[j]);
+  for (int j = 1; j <= mnorb; j++) wb_i4(&w, ispin[j]);
+  for (int j = 1; j <= ncf; j++)
+    for (int i = 1; i <= mnorb; i++) {
+      unsigned char y = YOCD(i, j) ? 1 : 0;
+      wb_put(&w, &y, 1);
+    }
+  wb_flush(f4, &w);
+  free(w.b);
+  fclose(f4);
+}
+
+/* cip.f:300-306 and 403-414: zero-order and perturbed effective Hamiltonians
+   (diagonal: ybrd = .false.) appended to unit 4 */
+static void write_unit4_results(const char* path) {
+  FILE* f4 = fopen(path, "ab");
+  if (!f4) die("cannot append to unit 4 file %s", path);
+  int nbr = metat * (metat + 1) / 2;
+  double* hz = (double*)xcalloc((size_t)nbr + 2, sizeof(double));
+  double* hm = (double*)xcalloc((size_t)nbr + 2, sizeof(double));
+  double* hv = (double*)xcalloc((size_t)nbr + 2, sizeof(double));
+  double* hb = (double*)xcalloc((size_t)nbr + 2, sizeof(double));
+  for (int m = 1; m <= metat; m++) {
+    int mm = m * (m + 1) / 2;
+    double eabs = e[m] + escf;
+    hm[mm] = eabs + e2mp[m];
+    hv[mm] = eabs + e2vp[m];
+    hb[mm] = eabs + e2b[m];
+    hz[mm] = eabs - escf;
+  }
+  wbuf_t w = {0};
+  for (int i = 1; i <= nbr; i++) wb_r8(&w, hz[i]);
+  wb_r8(&w, escf);
+  wb_i4(&w, ityper);
+  wb_i4(&w, ntrsy);
+  for (int m = 1; m <= metat; m++) wb_i4(&w, itm_[m]);
+  wb_flush(f4, &w);
+  free(w.b);
+  wbuf_t w2 = {0};
+  for (int i = 1; i <= nbr; i++) wb_r8(&w2, hm[i]);
+  for (int i = 1; i <= nbr; i++) wb_r8(&w2, hv[i]);
+  for (int i = 1; i <= nbr; i++) wb_r8(&w2, hb[i]);
+  wb_flush(f4, &w2);
+  free(w2.b);
+  free(hz); free(hm); free(hv); free(hb);
+  fclose(f4);
+}
+
 /* ------------------------------------------------------------- main */
 static char* read_all(FILE* f) {
   size_t cap = 4096, n = 0;
@@ -2105,6 +2246,8 @@ int main(int argc, char** argv) {
     }
   }
   printf(" energie de reference: %15.6f\n", escf);
+  write_unit4_zero_order(n04, empdet);
+  brdnee_itm();
   for (int m = 1; m <= metat; m++) {
     e2mp[m] = 0; psimp[m] = 0; psivp[m] = 0; e2vp[m] = 0; e2b[m] = 0;
   }
@@ -2159,6 +2302,7 @@ int main(int argc, char** argv) {
   fclose(f60);
   if (cand_log) fclose(cand_log);
 
+  write_unit4_results(n04);
   printf("0 ont ete generes:    %10lld  etats efficaces\n", ietat);
   printf(" la contribution du plus grand determinant non ecrit est %8.6f\n", dpivot);
   if (g_sym_variant) {

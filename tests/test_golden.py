@@ -27,3 +27,30 @@ def test_oracle_reproduces_golden(tmp_path, oracle_exe):
     n, dig = selection_digest(os.path.join(run, "det"), exp["metat"], True)
     assert n == exp["unit60_records"]
     assert dig == exp["unit60_sets_sha256"]
+
+
+def test_oracle_writes_unit4(tmp_path, oracle_exe):
+    """The oracle writes the three unit-4 records of cip.f:144-150, 410-414."""
+    import struct
+    import numpy as np
+    from cipsi_gb300 import synth
+    from conftest import copy_dir
+    from oracle import build as ob
+    wd = copy_dir(os.path.join(os.path.dirname(__file__), "golden", "small"), str(tmp_path / "w"))
+    j = json.load(open(ob.run(wd)))
+    recs = synth.read_records(os.path.join(wd, "f04"))
+    assert len(recs) == 3
+    norb, noca, nocb, metat, ncf, isz = struct.unpack_from("<6i", recs[0], 0)
+    assert (norb, noca, nocb, metat, ncf, isz) == (j["norb"], j["noca"], j["noca"] + j["norb"], j["metat"],
+                                                    j["ncf"], 0)
+    ii, jj = struct.unpack_from("<2i", recs[0], 25)
+    assert jj == ncf * metat
+    size = 33 + 8 * ncf + 8 * ii + 8 * jj + 24 * metat + 4 * metat + 8 * ncf + 16 * norb + 8 * 500000 \
+        + 16 * norb + 2 * norb * ncf
+    assert len(recs[0]) == size
+    nbr = metat * (metat + 1) // 2
+    assert len(recs[1]) == 8 * nbr + 8 + 4 + 4 + 4 * metat
+    assert len(recs[2]) == 24 * nbr
+    h = np.frombuffer(recs[2], dtype="<f8")
+    escf = struct.unpack_from("<d", recs[1], 8 * nbr)[0]
+    assert np.allclose(h[nbr - 1] - (j["e"][0] + escf), j["e2mp"][0])

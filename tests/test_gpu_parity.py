@@ -74,6 +74,28 @@ def check(jo, jg, wo, wg, variant, strict=False):
     dg = {x[0]: x for x in sg}
     for key, v, ev in so:
         assert v == pytest.approx(dg[key][1], rel=1e-9, abs=1e-12)
+    check_unit4(wo, wg, jo)
+
+
+def check_unit4(wo, wg, jo):
+    """Unit 4 (cip.f:144-150, 410-414): the zero-order record and the root
+    signs byte for byte, the perturbed effective Hamiltonians to the E2
+    tolerance."""
+    ro = synth.read_records(os.path.join(wo, "f04"))
+    rg = synth.read_records(os.path.join(wg, "f04"))
+    assert len(ro) == len(rg) == 3
+    assert ro[0] == rg[0]
+    assert ro[1] == rg[1]
+    a = np.frombuffer(ro[2], dtype="<f8")
+    b = np.frombuffer(rg[2], dtype="<f8")
+    mt = jo["metat"]
+    nbr = mt * (mt + 1) // 2
+    cond = np.concatenate([np.array(jo["cond_" + k]) for k in ("e2mp", "e2vp", "e2b")])
+    tol = np.zeros(3 * nbr)
+    for q in range(3):
+        for m in range(mt):
+            tol[q * nbr + (m + 1) * (m + 2) // 2 - 1] = cond[q * mt + m]
+    assert np.all(np.abs(a - b) <= 1e-10 + tol + 1e-15 * np.abs(a))
 
 
 @pytest.mark.parametrize("name,cfg", small_cases(), ids=[c[0] for c in small_cases()])
