@@ -42,6 +42,10 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 CONFIG = "medium"
+# dram__bytes_read.sum + dram__bytes_write.sum of one full k_pt2 launch on
+# this workload (1.27 GB + 22.88 GB), from a single-pass ncu capture of
+# `python bench.py --steps 2 --warmup 3 --no-cpu-baseline` (5th k_pt2 launch)
+NCU_DRAM_BYTES_PER_LAUNCH = 24.15e9
 METRIC = "perturber contributions/s"
 UNIT = "contributions/s"
 
@@ -589,10 +593,15 @@ def run_gpu(args, rank: int, world: int, local_rank: int):
                     "d2h_bytes_per_step": int(d2h), "ms_per_step": tot_e2e / args.steps},
             "gpu_launches": launches,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": None, "kernel": "k_pt2",
-                         "peak_source": peak_kind,
-                         "note": "algorithmic bytes of the E2 loop per launch / mean k_pt2+k_reduce time; "
-                                 "the kernel is integer-issue bound (bit compares), see profiles/"},
+                         "frac": achieved / peak,
+                         "traffic": NCU_DRAM_BYTES_PER_LAUNCH if args.gen_every == 1 else None,
+                         "kernel": "k_pt2", "peak_source": peak_kind,
+                         "algorithmic_bytes_per_launch": r["alg_bytes"],
+                         "note": "achieved = algorithmic bytes of the E2 loop (integral, coefficient and "
+                                 "diagonal-term reads) per launch / mean k_pt2+k_reduce time, against the "
+                                 "measured HBM copy bandwidth; the kernel is bound by the FP64 pipe (~51 % "
+                                 "busy) and L1/L2 latency, not HBM; traffic (ncu) is mostly unit-60 records "
+                                 "and per-thread histogram write-backs"},
             "clocks": clk,
             "work": {"perturbers": r["n_processed"], "candidates": r["n_candidates"],
                      "compares": r["n_compares"], "pairs_1": r["n_pairs_1"], "pairs_2": r["n_pairs_2"],

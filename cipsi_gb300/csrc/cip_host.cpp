@@ -589,7 +589,21 @@ void write_unit4_zero_order(const Run& R) {
   std::FILE* f = std::fopen(R.o.f04.c_str(), "wb");
   if (!f) throw Error("cannot rewrite " + R.o.f04);
   const int ncf = R.ncf, mt = R.metat, n = R.norb, mn = 2 * R.norb;
-  const int jj = ncf * mt, ii = R.S.nd[ncf - 1] + R.S.ne[ncf - 1] + 1;
+  // the reference's list offsets (transf.f:26-29, 86-87): a determinant
+  // without excitations (the reference) still takes one zero slot
+  std::vector<int32_t> ndr(ncf), tr, pa;
+  for (int k = 0; k < ncf; ++k) {
+    ndr[k] = (int32_t)tr.size();
+    if (R.S.ne[k] == 0) {
+      tr.push_back(0);
+      pa.push_back(0);
+    }
+    for (int l = 0; l < R.S.ne[k]; ++l) {
+      tr.push_back(R.S.trou[R.S.nd[k] + l]);
+      pa.push_back(R.S.part[R.S.nd[k] + l]);
+    }
+  }
+  const int jj = ncf * mt, ii = ndr[ncf - 1] + R.S.ne[ncf - 1] + 1;
   const double e0 = R.o.ityper == 0 ? R.escf : 0.0;
   RecWriter w;
   for (int32_t v : {(int32_t)n, (int32_t)R.noc, (int32_t)(R.noc + n), (int32_t)mt, (int32_t)ncf, (int32_t)0})
@@ -599,12 +613,12 @@ void write_unit4_zero_order(const Run& R) {
   w.put<int32_t>(jj);
   for (int k = 0; k < ncf; ++k) {
     w.put<int32_t>(R.S.ne[k]);
-    w.put<int32_t>(R.S.nd[k]);
+    w.put<int32_t>(ndr[k]);
   }
   for (int j = 0; j < ii; ++j) {
-    const bool in = j < (int)R.S.trou.size();
-    w.put<int32_t>(in ? R.S.trou[j] : 0);
-    w.put<int32_t>(in ? R.S.part[j] : 0);
+    const bool in = j < (int)tr.size();
+    w.put<int32_t>(in ? tr[j] : 0);
+    w.put<int32_t>(in ? pa[j] : 0);
   }
   for (int j = 0; j < jj; ++j) w.put<double>(R.c[j]);
   for (int m = 0; m < mt; ++m) w.put<double>(R.e[m] + e0);
@@ -883,6 +897,7 @@ extern "C" int cipsi_cip_main(const char* workdir, const char* stdin_path, int32
     if (rc) return rc;
     const Run& R = in->R;
     const auto t0 = std::chrono::steady_clock::now();
+    write_unit4_zero_order(R);  // cip.f:144, during the set-up
     cipsi_dims d{};
     cipsi_opts op{};
     cipsi_inputs_dims(in, &d, &op);
@@ -893,7 +908,6 @@ extern "C" int cipsi_cip_main(const char* workdir, const char* stdin_path, int32
     };
     chk(rc, "cipsi_ctx_create");
     chk(cipsi_inputs_upload(in, ctx), "cipsi_inputs_upload");
-    write_unit4_zero_order(R);
     const std::vector<int> itm = root_flip_signs(R);
     cipsi_result res{};
     if (R.o.ityper != 0) chk(cipsi_run_pt2(ctx, &op, &res), "cipsi_run_pt2");

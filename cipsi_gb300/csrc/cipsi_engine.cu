@@ -1198,6 +1198,7 @@ struct cipsi_batch {
   Params* dgeo = nullptr;
   struct Class {
     int W = 1, R = 1;
+    int big = 0;  // the plain form would run these contexts at one CTA per SM
     std::vector<int> geos;
     int nunits = 0, grid = 0, ncf_max = 0;
     LaunchShape ls{};
@@ -1305,12 +1306,18 @@ int cipsi_batch_create(cipsi_batch** out, cipsi_ctx* const* ctxs, int32_t n, con
     fill_params(ctx, &opts[i], pl, P[i]);
     work[i] = (long long)pl.ug.size() * ctx->d.ncf;
     const int W = ctx->W, R = roots_pad(ctx->d.metat);
+    // contexts whose shared-memory list needs a whole SM go to their own
+    // launch, so the others keep two CTAs per SM as in the plain form
+    const int big = ctas_per_sm == 0 && launch_shape(W, R, ctx->d.ncf, 0).blocks_per_sm == 1 ? 1 : 0;
     int c = 0;
-    while (c < (int)b->classes.size() && !(b->classes[c].W == W && b->classes[c].R == R)) ++c;
+    while (c < (int)b->classes.size() &&
+           !(b->classes[c].W == W && b->classes[c].R == R && b->classes[c].big == big))
+      ++c;
     if (c == (int)b->classes.size()) {
       b->classes.emplace_back();
       b->classes[c].W = W;
       b->classes[c].R = R;
+      b->classes[c].big = big;
     }
     b->classes[c].geos.push_back(i);
     b->max_nq = std::max(b->max_nq, 5 * ctx->d.metat);
@@ -1611,12 +1618,10 @@ int cipsi_run_pt2_static(cipsi_ctx* ctx, const cipsi_opts* o, cipsi_result* r) {
   int dev_sms = 0;
   CK(cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, ctx->device));
   const int R = mt <= 1 ? 1 : mt <= 2 ? 2 : mt <= 4 ? 4 : 8;
-  const size_t per_entry = (size_t)2 * W * 8 + 4;
-  const size_t qbytes = (size_t)(kThreads / 32) * queue_bytes(W, R);
-  const size_t smem_budget = (size_t)200 * 1024 - qbytes;
-  const int lr_cap = (int)std::min<size_t>((size_t)ncf, smem_budget / per_entry);
-  const size_t smem = (((size_t)lr_cap * per_entry + 15) & ~(size_t)15) + qbytes + 16;
-  const int blocks_per_sm = smem <= 95 * 1024 ? 2 : 1;
+  const LaunchShape ls = launch_shape(W, R, ncf, 0);
+  const int lr_cap = ls.lr_cap;
+  const size_t smem = ls.smem;
+  const int blocks_per_sm = ls.blocks_per_sm;
   const size_t nq = (size_t)5 * mt;
   const size_t ncount = C_NCOUNTERS + 1 + kNClass + kNClass * kMaxRoots;
   const size_t off_counters = 0;

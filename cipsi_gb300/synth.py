@@ -96,13 +96,13 @@ class SynthConfig:
 
 
 CONFIGS: Dict[str, SynthConfig] = {
-    # configs[0]: 20 MOs, 10 e-, HF + 49 doubles, 1 root, tau 0.02
+    # small: 20 MOs, 10 e-, HF + 49 doubles, 1 root, tau 0.02
     "small": SynthConfig("small", norb=20, nocc=5, ncholesky=40, ncf=50, metat=1,
                          tau=0.02, ranks=(2,), coef_mode="gauss005", seed=0),
-    # configs[1]: 60 MOs, 20 e-, S=2000 singles/doubles/triples, 3 roots, tau 0.01
+    # medium: 60 MOs, 20 e-, S=2000 singles/doubles/triples, 3 roots, tau 0.01
     "medium": SynthConfig("medium", norb=60, nocc=10, ncholesky=120, ncf=2000, metat=3,
                           tau=0.01, ranks=(1, 2, 3), coef_mode="decay09", seed=1),
-    # configs[2]: 120 MOs, 30 e-, S=20000 doubles, 2 roots, tau 0.005
+    # large: 120 MOs, 30 e-, S=20000 doubles, 2 roots, tau 0.005
     "large": SynthConfig("large", norb=120, nocc=15, ncholesky=240, ncf=20000, metat=2,
                          tau=0.005, ranks=(2,), coef_mode="gauss005", seed=2),
 }

@@ -12,8 +12,8 @@
  * Those subroutines take no arguments; they read and write COMMON blocks.
  * Each setter below takes the arrays of one group of COMMON variables, with
  * the reference's own layout and meaning, so that a patched cip.f can pass
- * its COMMON storage directly (see the Fortran ISO_C_BINDING interface in
- * INTEGRATION.md).  All arrays are owned by the caller and copied by the
+ * its COMMON storage directly through an ISO_C_BINDING interface whose
+ * types mirror the structs below.  All arrays are owned by the caller and copied by the
  * call; nothing is retained.  Indices stored in arrays (spin orbitals,
  * offsets) keep the reference's 1-based values.
  *
