@@ -72,7 +72,7 @@ def _fetch_allow_overflow(c):
     return d
 
 
-CANDIDATES: List[Tuple[int, int]] = [(6, 0), (3, 0), (12, 0), (6, 2), (3, 2)]
+CANDIDATES: List[Tuple[int, int]] = [(6, 2), (3, 2), (12, 2), (6, 1), (12, 1)]
 
 
 def autotune(ctxs, opts, sample: int = 16, candidates: Sequence[Tuple[int, int]] = CANDIDATES,

@@ -135,7 +135,7 @@ struct cipsi_ctx {
   int gens_cap = 0;
   int32_t* dnb_j = nullptr;
   uint64_t* dnb_em = nullptr;
-  int32_t* dlr_idx = nullptr;
+  uint64_t* dlr_ent = nullptr;
   size_t scratch_blocks = 0;
   double* dgen_part = nullptr;
   size_t gen_part_cap = 0;
@@ -260,7 +260,7 @@ void cipsi_ctx_destroy(cipsi_ctx* ctx) {
   dfree(ctx->dK); dfree(ctx->dfmpb); dfree(ctx->dorbsym); dfree(ctx->dgens); dfree(ctx->dgmask);
   dfree(ctx->deri64);
   dfree(ctx->dunits);
-  dfree(ctx->dnb_j); dfree(ctx->dnb_em); dfree(ctx->dlr_idx); dfree(ctx->dgen_part);
+  dfree(ctx->dnb_j); dfree(ctx->dnb_em); dfree(ctx->dlr_ent); dfree(ctx->dgen_part);
   dfree(ctx->dcounters); dfree(ctx->dhist_tab); dfree(ctx->dred); dfree(ctx->dwork);
   dfree(ctx->dsel_bits); dfree(ctx->dsel_owner); dfree(ctx->dsel_xam); dfree(ctx->dsel_evp);
   if (ctx->ev0) cudaEventDestroy(ctx->ev0);
@@ -643,9 +643,12 @@ struct LaunchShape {
 };
 
 LaunchShape launch_shape(int W, int R, int ncf_max, int ctas) {
-  const size_t per_entry = (size_t)2 * W * 8 + 4;
+  const size_t per_entry = 8;  // compact L_R entry
   const size_t qbytes = (size_t)(kThreads / 32) * queue_bytes(W, R);
-  const size_t smem_total = ctas == 2 ? (size_t)90 * 1024 : (size_t)200 * 1024;
+  // two CTAs per SM unless one is asked for: the part of a long L_R list
+  // beyond shared memory is read from the block's global scratch, 8 bytes
+  // per entry, which costs less than halving the resident warps
+  const size_t smem_total = ctas == 1 ? (size_t)200 * 1024 : (size_t)90 * 1024;
   const size_t smem_budget = smem_total > qbytes + 16 ? smem_total - qbytes - 16 : 0;
   LaunchShape ls;
   ls.lr_cap = (int)std::min<size_t>((size_t)ncf_max, smem_budget / per_entry);
@@ -856,10 +859,10 @@ int cipsi_run_pt2_async(cipsi_ctx* ctx, const cipsi_opts* o) {
   const int grid = std::max(1, std::min(nunits, dev_sms * ls.blocks_per_sm));
   // per-block neighbour scratch
   if ((size_t)grid > ctx->scratch_blocks || !ctx->dnb_j) {
-    dfree(ctx->dnb_j); dfree(ctx->dnb_em); dfree(ctx->dlr_idx);
+    dfree(ctx->dnb_j); dfree(ctx->dnb_em); dfree(ctx->dlr_ent);
     CK(cudaMalloc(&ctx->dnb_j, (size_t)grid * ncf * sizeof(int32_t)));
     CK(cudaMalloc(&ctx->dnb_em, (size_t)grid * ncf * sizeof(uint64_t)));
-    CK(cudaMalloc(&ctx->dlr_idx, (size_t)grid * ncf * sizeof(int32_t)));
+    CK(cudaMalloc(&ctx->dlr_ent, (size_t)grid * ncf * sizeof(uint64_t)));
     ctx->scratch_blocks = grid;
   }
   rc = prepare_run(ctx, pl, ctx->stream);
@@ -875,7 +878,7 @@ int cipsi_run_pt2_async(cipsi_ctx* ctx, const cipsi_opts* o) {
   fill_params(ctx, o, pl, p);
   p.nb_j = ctx->dnb_j;
   p.nb_emask = ctx->dnb_em;
-  p.lr_idx = ctx->dlr_idx;
+  p.lr_ent = ctx->dlr_ent;
   p.lr_cap = ls.lr_cap;
   p.nb_stride = ncf;
 
@@ -1018,10 +1021,10 @@ int cipsi_run_pt2_adjoint(cipsi_ctx* ctx, const cipsi_opts* o, const double* see
   const LaunchShape ls = launch_shape(W, R, ncf, ctx->tune_ctas);
   const int grid = std::max(1, std::min(nunits, dev_sms * ls.blocks_per_sm));
   if ((size_t)grid > ctx->scratch_blocks || !ctx->dnb_j) {
-    dfree(ctx->dnb_j); dfree(ctx->dnb_em); dfree(ctx->dlr_idx);
+    dfree(ctx->dnb_j); dfree(ctx->dnb_em); dfree(ctx->dlr_ent);
     CK(cudaMalloc(&ctx->dnb_j, (size_t)grid * ncf * sizeof(int32_t)));
     CK(cudaMalloc(&ctx->dnb_em, (size_t)grid * ncf * sizeof(uint64_t)));
-    CK(cudaMalloc(&ctx->dlr_idx, (size_t)grid * ncf * sizeof(int32_t)));
+    CK(cudaMalloc(&ctx->dlr_ent, (size_t)grid * ncf * sizeof(uint64_t)));
     ctx->scratch_blocks = grid;
   }
   rc = prepare_run(ctx, pl, ctx->stream);
@@ -1060,7 +1063,7 @@ int cipsi_run_pt2_adjoint(cipsi_ctx* ctx, const cipsi_opts* o, const double* see
   fill_params(ctx, o, pl, p);
   p.nb_j = ctx->dnb_j;
   p.nb_emask = ctx->dnb_em;
-  p.lr_idx = ctx->dlr_idx;
+  p.lr_ent = ctx->dlr_ent;
   p.lr_cap = ls.lr_cap;
   p.nb_stride = ncf;
   p.sel_cap = 0;  // no records from an adjoint launch
@@ -1207,7 +1210,7 @@ struct cipsi_batch {
     int* dwork = nullptr;
     int32_t* dnb_j = nullptr;
     uint64_t* dnb_em = nullptr;
-    int32_t* dlr_idx = nullptr;
+    uint64_t* dlr_ent = nullptr;
     cudaStream_t st = nullptr;
     cudaEvent_t ev_join = nullptr;
   };
@@ -1249,7 +1252,7 @@ void batch_free(cipsi_batch* b) {
   if (b->graph) cudaGraphDestroy(b->graph);
   for (auto& c : b->classes) {
     dfree(c.dunit_geo); dfree(c.dunit_local); dfree(c.dwork);
-    dfree(c.dnb_j); dfree(c.dnb_em); dfree(c.dlr_idx);
+    dfree(c.dnb_j); dfree(c.dnb_em); dfree(c.dlr_ent);
     if (c.st) cudaStreamDestroy(c.st);
     if (c.ev_join) cudaEventDestroy(c.ev_join);
   }
@@ -1343,7 +1346,7 @@ int cipsi_batch_create(cipsi_batch** out, cipsi_ctx* const* ctxs, int32_t n, con
     BCK(cudaMalloc(&c.dwork, sizeof(int)));
     BCK(cudaMalloc(&c.dnb_j, (size_t)c.grid * c.ncf_max * sizeof(int32_t)));
     BCK(cudaMalloc(&c.dnb_em, (size_t)c.grid * c.ncf_max * sizeof(uint64_t)));
-    BCK(cudaMalloc(&c.dlr_idx, (size_t)c.grid * c.ncf_max * sizeof(int32_t)));
+    BCK(cudaMalloc(&c.dlr_ent, (size_t)c.grid * c.ncf_max * sizeof(uint64_t)));
     if (c.nunits) {
       BCK(cudaMemcpy(c.dunit_geo, ugeo.data(), (size_t)c.nunits * sizeof(int32_t), cudaMemcpyHostToDevice));
       BCK(cudaMemcpy(c.dunit_local, ulocal.data(), (size_t)c.nunits * sizeof(int32_t), cudaMemcpyHostToDevice));
@@ -1351,7 +1354,7 @@ int cipsi_batch_create(cipsi_batch** out, cipsi_ctx* const* ctxs, int32_t n, con
     for (int i : c.geos) {
       P[i].nb_j = c.dnb_j;
       P[i].nb_emask = c.dnb_em;
-      P[i].lr_idx = c.dlr_idx;
+      P[i].lr_ent = c.dlr_ent;
       P[i].nb_stride = c.ncf_max;
       P[i].lr_cap = c.ls.lr_cap;
     }
@@ -1449,7 +1452,7 @@ void cipsi_batch_destroy(cipsi_batch* b) {
 // Layout of the array (each region 256-byte aligned): counters + dpivot +
 // histogram counts | histogram sums | reduced sums | work counter |
 // generator list | generator masks | work units | per-unit partial sums |
-// per-block neighbour scratch (nb_j, nb_emask, lr_idx).  The generator and
+// per-block neighbour scratch (nb_j, nb_emask, lr_ent).  The generator and
 // unit lists are staged in file-scope host arrays of fixed size.
 
 }  // extern "C"
@@ -1714,11 +1717,11 @@ int cipsi_run_pt2_static(cipsi_ctx* ctx, const cipsi_opts* o, cipsi_result* r) {
   }
   p.pertu_ref = pertu_ref ? 1 : 0;
   p.pertu_mono = pertu_mono ? 1 : 0;
-  // nb_j, nb_emask, lr_idx: grid x ncf entries each (k_pt2 indexes block b at
+  // nb_j, nb_emask, lr_ent: grid x ncf entries each (k_pt2 indexes block b at
   // b * ncf), in three regions of grid * nb_stride >= grid * ncf * 8 bytes
   p.nb_j = reinterpret_cast<int32_t*>(nb0);
   p.nb_emask = reinterpret_cast<uint64_t*>(nb0 + (size_t)grid * nb_stride);
-  p.lr_idx = reinterpret_cast<int32_t*>(nb0 + (size_t)2 * grid * nb_stride);
+  p.lr_ent = reinterpret_cast<uint64_t*>(nb0 + (size_t)2 * grid * nb_stride);
   p.lr_cap = lr_cap;
   p.nb_stride = ncf;
   p.gen_part = reinterpret_cast<double*>(base + off_part);

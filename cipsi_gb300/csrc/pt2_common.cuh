@@ -65,9 +65,9 @@ struct Params {
   // scratch
   int32_t* nb_j;             // per block: ncf entries
   uint64_t* nb_emask;
-  int32_t* lr_idx;           // per block: ncf entries (fallback path)
+  uint64_t* lr_ent;          // per block: ncf compact L_R entries beyond lr_cap
   int lr_cap;                // shared-memory capacity of L_R
-  int nb_stride;             // entries per block in nb_j / nb_emask / lr_idx
+  int nb_stride;             // entries per block in nb_j / nb_emask / lr_ent
   // outputs
   double* gen_part;          // ngen x (5 * metat)
   unsigned long long* counters;

@@ -104,6 +104,26 @@ __device__ __forceinline__ void ai_adj(const Params& p, int i, int j, int k, int
   atomicAdd(&p.g_eri[idx], w);
 }
 
+// Compact L_R entry of a determinant j for a block of removed electrons R
+// (K' = k - R): bits 0-31 the spin orbitals of E = j \ K' (code orb +
+// spin * norb, one byte each; |E| = |R| + m <= 4, unused bytes repeat the
+// first code), bits 32-33 m = |K' \ j|, bits 34-63 the index j.
+__device__ __forceinline__ uint64_t lr_entry(uint32_t ebytes, int ne, int m, int j) {
+  const uint32_t first = ebytes & 0xFFu;
+  for (int q = ne; q < 4; ++q) ebytes |= first << (8 * q);
+  return (uint64_t)ebytes | ((uint64_t)m << 32) | ((uint64_t)j << 34);
+}
+__device__ __forceinline__ int lr_entry_j(uint64_t e) { return (int)(e >> 34); }
+// bit difference |I xor j| = 2 (m + |A \ E|) of I = K' + A, A = {c1[, c2]}
+// (c1x4, c2x4: the codes repeated in four bytes)
+__device__ __forceinline__ int lr_diff(uint64_t e, uint32_t c1x4, uint32_t c2x4, bool two) {
+  const uint32_t E = (uint32_t)e;
+  int d = (int)((e >> 32) & 3u);
+  d += __vcmpeq4(E, c1x4) ? 0 : 1;
+  if (two) d += __vcmpeq4(E, c2x4) ? 0 : 1;
+  return 2 * d;
+}
+
 // <I|H|J> for degree 1 or 2, canonical phases.  u = I bits, v = J bits
 // (alpha words then beta words).  rankI / rankJ: excitation degree relative
 // to the reference determinant; the one-difference element sums over the
@@ -783,10 +803,11 @@ __global__ void __launch_bounds__(kThreads, 2) k_pt2(Params p0, BatchArgs ba) {
   const int tid = threadIdx.x;
   // shared L_R arrays (fast path)
   // (lr_cap is the same for every geometry of a batched launch)
-  uint64_t* lr_bits = reinterpret_cast<uint64_t*>(dyn);          // cap x 2W
-  int32_t* lr_j = reinterpret_cast<int32_t*>(lr_bits + (size_t)p0.lr_cap * 2 * W);
-  // per-warp epilogue queues, 16-byte aligned after the L_R arrays
-  const size_t qoff = (((size_t)p0.lr_cap * (2 * W * 8 + 4)) + 15) & ~(size_t)15;
+  // L_R entries (compact form, lr_entry) up to lr_cap in shared memory; the
+  // rest of a longer list stays in the block's global scratch
+  uint64_t* lr_ent = reinterpret_cast<uint64_t*>(dyn);
+  // per-warp epilogue queues, 16-byte aligned after the L_R entries
+  const size_t qoff = (((size_t)p0.lr_cap * 8) + 15) & ~(size_t)15;
   WarpQueue<W, R>& wq = reinterpret_cast<WarpQueue<W, R>*>(dyn + qoff)[threadIdx.x >> 5];
   int qn = 0;
 
@@ -797,13 +818,13 @@ __global__ void __launch_bounds__(kThreads, 2) k_pt2(Params p0, BatchArgs ba) {
   // per-geometry state
   int32_t* my_nb_j = nullptr;
   uint64_t* my_nb_em = nullptr;
-  int32_t* my_lr_idx = nullptr;
+  uint64_t* my_lr_ent = nullptr;
   uint64_t hf[2 * W];
   int ncf = 0;
   auto geo_init = [&]() {
     my_nb_j = p.nb_j + (size_t)blockIdx.x * p.nb_stride;
     my_nb_em = p.nb_emask + (size_t)blockIdx.x * p.nb_stride;
-    my_lr_idx = p.lr_idx + (size_t)blockIdx.x * p.nb_stride;
+    my_lr_ent = p.lr_ent + (size_t)blockIdx.x * p.nb_stride;
 #pragma unroll
     for (int s = 0; s < 2; ++s)
 #pragma unroll
@@ -1055,22 +1076,42 @@ __global__ void __launch_bounds__(kThreads, 2) k_pt2(Params p0, BatchArgs ba) {
       }
       if (!any) continue;
       const uint64_t rmask = (1ull << e1) | (e2 >= 0 ? (1ull << e2) : 0ull);
-      // L_R, partitioned: entries with |K' \ j| <= 1 first, then those with
-      // |K' \ j| = 2; each part in ascending j, so every sum over interacting
-      // determinants runs in a fixed order (bitwise reproducible results)
-      auto lr_store = [&](int slot, int t) {
-        const int j = my_nb_j[t];
-        if (slot < p.lr_cap) {
-          lr_j[slot] = j;
-          const uint64_t* v = p.S + (size_t)j * 2 * W;
+      // K' = k - R
+      uint64_t kp[2 * W];
 #pragma unroll
-          for (int q = 0; q < 2 * W; ++q) lr_bits[(size_t)slot * 2 * W + q] = __ldg(&v[q]);
-        }
-        my_lr_idx[slot] = j;
-      };
+      for (int q = 0; q < 2 * W; ++q) kp[q] = kb[q];
+      kp[sp1 * W + (o1 >> 6)] &= ~(1ull << (o1 & 63));
+      if (e2 >= 0) kp[sp2 * W + (o2 >> 6)] &= ~(1ull << (o2 & 63));
       auto lr_m = [&](int t) {
         const uint64_t em = my_nb_em[t];
         return __popcll(em) - __popcll(em & rmask);
+      };
+      // L_R, partitioned: entries with |K' \ j| <= 1 first, then those with
+      // |K' \ j| = 2; each part in ascending j, so every sum over interacting
+      // determinants runs in a fixed order (bitwise reproducible results).
+      // Entry of j: m = |K' \ j| and E = j \ K' (at most 4 spin orbitals),
+      // since for I = K' + A, |I \ j| = m + |A \ E|.
+      auto lr_store = [&](int slot, int t) {
+        const int j = my_nb_j[t];
+        const uint64_t* v = p.S + (size_t)j * 2 * W;
+        uint32_t ebytes = 0;
+        int ne = 0;
+#pragma unroll
+        for (int q = 0; q < 2 * W; ++q) {
+          uint64_t d = __ldg(&v[q]) & ~kp[q];
+          while (d) {
+            const int b = __ffsll((long long)d) - 1;
+            d &= d - 1;
+            const uint32_t code = (uint32_t)((q % W) * 64 + b + (q / W) * p.norb);
+            if (ne < 4) ebytes |= code << (8 * ne);
+            ++ne;
+          }
+        }
+        const uint64_t ent = lr_entry(ebytes, ne, lr_m(t), j);
+        if (slot < p.lr_cap)
+          lr_ent[slot] = ent;
+        else
+          my_lr_ent[slot] = ent;
       };
       const int n01 = ordered_compact(nnb, [&](int t) { return lr_m(t) <= 1; }, lr_store, ctmp);
       const int n2 = ordered_compact(
@@ -1079,12 +1120,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_pt2(Params p0, BatchArgs ba) {
       const int nlr = n01 + n2;
       const bool fast = nlr <= p.lr_cap;
       if (!fast && tid == 0) atomicAdd(&p.counters[C_LRFALLBACK], 1ull);
-      // K' = k - R
-      uint64_t kp[2 * W];
-#pragma unroll
-      for (int q = 0; q < 2 * W; ++q) kp[q] = kb[q];
-      kp[sp1 * W + (o1 >> 6)] &= ~(1ull << (o1 & 63));
-      if (e2 >= 0) kp[sp2 * W + (o2 >> 6)] &= ~(1ull << (o2 & 63));
+      auto ent_at = [&](int i) -> uint64_t { return i < p.lr_cap ? lr_ent[i] : my_lr_ent[i]; };
       // diagonal energies of I = K' + A from those of K' (cip/hdig.f, hmp.f
       // written over occupation changes dn relative to the reference):
       //   hdig = sum_r dn_r F_rr + 1/2 sum_rs dn_r dn_s (J_rs - [same spin] K_rs)
@@ -1195,21 +1231,17 @@ __global__ void __launch_bounds__(kThreads, 2) k_pt2(Params p0, BatchArgs ba) {
           if (a2 >= 0) u[sa2 * W + (a2 >> 6)] |= (1ull << (a2 & 63));
           const int rankI = rank_k + D;
           bool drop = false;
+          const bool two = a2 >= 0;
+          const uint32_t c1x4 = (uint32_t)(a1 + sa1 * p.norb) * 0x01010101u;
+          const uint32_t c2x4 = two ? (uint32_t)(a2 + sa2 * p.norb) * 0x01010101u : 0u;
           // one S determinant of L_R against I: owner test, already-in-S
           // test, <I|H|j> accumulation; returns true when I is dropped
           auto visit = [&](int i, int x) -> bool {
-            uint64_t vv[2 * W];
-            int j;
-            if (fast) {
-              j = lr_j[i];
-#pragma unroll
-              for (int q = 0; q < 2 * W; ++q) vv[q] = lr_bits[(size_t)i * 2 * W + q];
-            } else {
-              j = my_lr_idx[i];
-#pragma unroll
-              for (int q = 0; q < 2 * W; ++q) vv[q] = __ldg(&p.S[(size_t)j * 2 * W + q]);
-            }
+            const int j = lr_entry_j(ent_at(i));
             if (j < k) return p.ygen[j] != 0;
+            uint64_t vv[2 * W];
+#pragma unroll
+            for (int q = 0; q < 2 * W; ++q) vv[q] = __ldg(&p.S[(size_t)j * 2 * W + q]);
             if (x == 0) return true;
             int rankJ = 0;
 #pragma unroll
@@ -1231,19 +1263,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_pt2(Params p0, BatchArgs ba) {
 #pragma unroll
             for (int g4 = 0; g4 < 4; ++g4) {
               const int i = i0 + g4;
-              int x = 99;
-              if (i < nscan) {
-                x = 0;
-                if (fast) {
-#pragma unroll
-                  for (int q = 0; q < 2 * W; ++q) x += __popcll(u[q] ^ lr_bits[(size_t)i * 2 * W + q]);
-                } else {
-                  const int jj = my_lr_idx[i];
-#pragma unroll
-                  for (int q = 0; q < 2 * W; ++q) x += __popcll(u[q] ^ __ldg(&p.S[(size_t)jj * 2 * W + q]));
-                }
-              }
-              xs[g4] = x;
+              xs[g4] = i < nscan ? lr_diff(ent_at(i), c1x4, c2x4, two) : 99;
             }
             if (xs[0] > 4 && xs[1] > 4 && xs[2] > 4 && xs[3] > 4) continue;
 #pragma unroll 1
@@ -1252,9 +1272,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_pt2(Params p0, BatchArgs ba) {
           }
           for (int q2 = 0; q2 < nrb && !drop; ++q2) {
             const int i = rb[q2];
-            int x = 0;
-#pragma unroll
-            for (int q = 0; q < 2 * W; ++q) x += __popcll(u[q] ^ lr_bits[(size_t)i * 2 * W + q]);
+            const int x = lr_diff(ent_at(i), c1x4, c2x4, two);
             if (x <= 4) drop = visit(i, x);
           }
           acc.ncmp += (unsigned long long)(nscan + nrb);
@@ -1299,19 +1317,15 @@ __global__ void __launch_bounds__(kThreads, 2) k_pt2(Params p0, BatchArgs ba) {
           if (!p.yen) gh = 0.0;
           // second pass over the same entries: dE/dH_Ij = sum_m gb[m] c_jm
           const int rankI = rank_k + D;
+          const bool two = a2 >= 0;
+          const uint32_t c1x4 = (uint32_t)(a1 + sa1 * p.norb) * 0x01010101u;
+          const uint32_t c2x4 = two ? (uint32_t)(a2 + sa2 * p.norb) * 0x01010101u : 0u;
           auto visit_adj = [&](int i, int x) {
-            uint64_t vv[2 * W];
-            int j;
-            if (fast) {
-              j = lr_j[i];
-#pragma unroll
-              for (int q = 0; q < 2 * W; ++q) vv[q] = lr_bits[(size_t)i * 2 * W + q];
-            } else {
-              j = my_lr_idx[i];
-#pragma unroll
-              for (int q = 0; q < 2 * W; ++q) vv[q] = __ldg(&p.S[(size_t)j * 2 * W + q]);
-            }
+            const int j = lr_entry_j(ent_at(i));
             if (j < k || x == 0) return;
+            uint64_t vv[2 * W];
+#pragma unroll
+            for (int q = 0; q < 2 * W; ++q) vv[q] = __ldg(&p.S[(size_t)j * 2 * W + q]);
             int rankJ = 0;
 #pragma unroll
             for (int q = 0; q < 2 * W; ++q) rankJ += __popcll(hf[q] & ~vv[q]);
@@ -1322,22 +1336,12 @@ __global__ void __launch_bounds__(kThreads, 2) k_pt2(Params p0, BatchArgs ba) {
             hmat_adj<W>(p, u, vv, rankI, rankJ, hf, w);
           };
           for (int i = 0; i < nscan; ++i) {
-            int x = 0;
-            if (fast) {
-#pragma unroll
-              for (int q = 0; q < 2 * W; ++q) x += __popcll(u[q] ^ lr_bits[(size_t)i * 2 * W + q]);
-            } else {
-              const int jj = my_lr_idx[i];
-#pragma unroll
-              for (int q = 0; q < 2 * W; ++q) x += __popcll(u[q] ^ __ldg(&p.S[(size_t)jj * 2 * W + q]));
-            }
+            const int x = lr_diff(ent_at(i), c1x4, c2x4, two);
             if (x <= 4) visit_adj(i, x);
           }
           for (int q2 = 0; q2 < nrb; ++q2) {
             const int i = rb[q2];
-            int x = 0;
-#pragma unroll
-            for (int q = 0; q < 2 * W; ++q) x += __popcll(u[q] ^ lr_bits[(size_t)i * 2 * W + q]);
+            const int x = lr_diff(ent_at(i), c1x4, c2x4, two);
             if (x <= 4) visit_adj(i, x);
           }
           // diagonal terms: hdig(I) = hdig(K') + vdg[a1] + vdg[a2] + G(a1,a2),
@@ -1401,12 +1405,11 @@ __global__ void __launch_bounds__(kThreads, 2) k_pt2(Params p0, BatchArgs ba) {
           const int row = (t & 1) ? t * nwarps + (nwarps - 1 - wid) : t * nwarps + wid;
           if (row >= nrows) continue;
           const int a1 = sh.vir[sr][row];
-          const int w1 = sr * W + (a1 >> 6);
-          const uint64_t b1 = 1ull << (a1 & 63);
+          const uint32_t r1x4 = (uint32_t)(a1 + sr * p.norb) * 0x01010101u;
           int nrb = 0;
           for (int i0 = n01; i0 < nlr; i0 += 32) {
             const int i = i0 + lane;
-            const bool has = i < nlr && (lr_bits[(size_t)i * 2 * W + w1] & b1);
+            const bool has = i < nlr && __vcmpeq4((uint32_t)ent_at(i), r1x4) != 0;
             const unsigned bm = __ballot_sync(0xffffffffu, has);
             if (has) {
               const int pos = nrb + __popc(bm & ((1u << lane) - 1u));

@@ -154,9 +154,9 @@ int cipsi_run_pt2(cipsi_ctx* ctx, const cipsi_opts* opts, cipsi_result* res);
      r_chunk      removed-electron blocks per work unit for generators of
                   excitation rank >= 2 (rank 0 and 1 generators always get
                   one block per unit); default 6
-     ctas_per_sm  0 = shared-memory list as large as one CTA allows (two
-                  CTAs per SM when it fits in half), 1 = one CTA per SM,
-                  2 = list sized so that two CTAs fit per SM
+     ctas_per_sm  0 or 2 = shared-memory list sized so that two CTAs fit
+                  per SM (the rest of a longer list is read from global
+                  memory), 1 = one CTA per SM with a 200 KB list
    cipsi_gb300.tune (Python) picks both by timing a generator sample. */
 int cipsi_set_tuning(cipsi_ctx* ctx, int32_t r_chunk, int32_t ctas_per_sm);
 

@@ -81,7 +81,7 @@ def test_batch_generator_masks_and_tuning(loaded):
         o2 = engine.Opts.from_buffer_copy(o)
         o2.run_pertu = 0
         opts_np.append(o2)
-    for r_chunk, ctas in ((1, 0), (12, 2)):
+    for r_chunk, ctas in ((1, 0), (12, 1)):
         with engine.Batch(ctxs, opts_np, r_chunk=r_chunk, ctas_per_sm=ctas, gen_masks=masks) as b:
             b.run()
             b.wait()
