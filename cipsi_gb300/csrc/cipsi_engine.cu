@@ -120,6 +120,7 @@ struct cipsi_ctx {
   double* dc = nullptr;
   float* deri = nullptr;
   double* deri64 = nullptr;  // FP64 storage of (pq|rs) (cipsi_set_integrals_f64store)
+  double* deri_w = nullptr;  // the real*4 (pq|rs) widened to double (small integral sets)
   int32_t* dpairtab = nullptr;
   int32_t* dntttt = nullptr;
   double *dF = nullptr, *dJ = nullptr, *dK = nullptr, *dfmpb = nullptr;
@@ -190,6 +191,17 @@ int fail(cipsi_ctx* c, int code, const std::string& msg) {
       return fail(ctx, CIPSI_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
   } while (0)
 
+// Integral sets up to this size are also kept widened to double on the
+// device (13 MB for 60 orbitals; the 120-orbital set stays real*4 only, so
+// that it still fits in L2).  The values are the real*4 ones, exactly; the
+// kernel then loads a double per integral instead of converting a float.
+constexpr size_t kWidenMaxBytes = (size_t)48 << 20;
+
+__global__ void k_widen(const float* __restrict__ in, double* __restrict__ out, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = (double)in[i];
+}
+
 template <typename T>
 int upload(cipsi_ctx* ctx, T** dptr, const T* h, size_t n) {
   if (*dptr) cudaFree(*dptr);
@@ -259,6 +271,7 @@ void cipsi_ctx_destroy(cipsi_ctx* ctx) {
   dfree(ctx->deri); dfree(ctx->dpairtab); dfree(ctx->dntttt); dfree(ctx->dF); dfree(ctx->dJ);
   dfree(ctx->dK); dfree(ctx->dfmpb); dfree(ctx->dorbsym); dfree(ctx->dgens); dfree(ctx->dgmask);
   dfree(ctx->deri64);
+  dfree(ctx->deri_w);
   dfree(ctx->dunits);
   dfree(ctx->dnb_j); dfree(ctx->dnb_em); dfree(ctx->dlr_ent); dfree(ctx->dgen_part);
   dfree(ctx->dcounters); dfree(ctx->dhist_tab); dfree(ctx->dred); dfree(ctx->dwork);
@@ -335,6 +348,13 @@ int cipsi_set_integrals(cipsi_ctx* ctx, const int32_t* itsym, const int32_t* its
     ++ctx->buf_gen;
     dfree(ctx->deri64);
   }
+  dfree(ctx->deri_w);
+  if ((size_t)ninte * sizeof(double) <= kWidenMaxBytes) {
+    CK(cudaMalloc((void**)&ctx->deri_w, (size_t)ninte * sizeof(double)));
+    const int grid = (int)std::min<int64_t>((ninte + 255) / 256, 4096);
+    k_widen<<<grid, 256, 0, ctx->stream>>>(ctx->deri, ctx->deri_w, ninte);
+    CK(cudaGetLastError());
+  }
   CK(cudaStreamSynchronize(ctx->stream));
   ctx->have_int = true;
   return CIPSI_OK;
@@ -360,6 +380,7 @@ int cipsi_set_integrals_f64store(cipsi_ctx* ctx, const int32_t* itsym, const int
   int rc = set_integrals_common(ctx, itsym, its, f, aj, ak, ij0, ntttt, ninte);
   if (rc) return rc;
   if ((rc = upload(ctx, &ctx->deri64, pqrs, (size_t)ninte))) return rc;
+  dfree(ctx->deri_w);
   if (!ctx->deri) {
     const float zero = 0.f;
     if ((rc = upload(ctx, &ctx->deri, &zero, 1))) return rc;
@@ -741,7 +762,7 @@ void fill_params(const cipsi_ctx* ctx, const cipsi_opts* o, const RunPlan& pl, P
   p.yef = ctx->dyef;
   p.c = ctx->dc;
   p.eri = ctx->deri;
-  p.eri64 = ctx->deri64;
+  p.eri64 = ctx->deri64 ? ctx->deri64 : ctx->deri_w;
   p.pairtab = ctx->dpairtab;
   p.ntttt = ctx->dntttt;
   p.F = ctx->dF;
@@ -1686,7 +1707,7 @@ int cipsi_run_pt2_static(cipsi_ctx* ctx, const cipsi_opts* o, cipsi_result* r) {
   p.yef = ctx->dyef;
   p.c = ctx->dc;
   p.eri = ctx->deri;
-  p.eri64 = ctx->deri64;
+  p.eri64 = ctx->deri64 ? ctx->deri64 : ctx->deri_w;
   p.pairtab = ctx->dpairtab;
   p.ntttt = ctx->dntttt;
   p.F = ctx->dF;

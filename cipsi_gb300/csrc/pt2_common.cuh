@@ -82,7 +82,8 @@ struct Params {
   double* sel_evp;                   // cap x metat
   long long sel_cap;
   int* work;                         // work counter
-  // FP64 storage of (pq|rs) (derivative checks); null = the real*4 `eri`
+  // (pq|rs) as doubles: the caller's FP64 integrals (derivative checks) or
+  // the real*4 ones widened on the device; null = read the real*4 `eri`
   const double* eri64;
   // adjoint launch (k_pt2<..., ADJ = true>): seeds dE/d e2mp[m], e2vp[m],
   // e2b[m] and the gradient outputs

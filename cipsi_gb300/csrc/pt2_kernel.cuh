@@ -78,6 +78,34 @@ __device__ __forceinline__ int tri(int i, int j) {
   return i >= j ? i * (i + 1) / 2 + j : j * (j + 1) / 2 + i;
 }
 
+// Word updates and half selections of the small bitstring arrays with
+// compile-time indices only: a run-time index into a local array makes the
+// compiler place it in local memory (stack), one of the kernel's largest
+// traffic sources.
+template <int N>
+__device__ __forceinline__ void or_word(uint64_t* x, int idx, uint64_t m) {
+#pragma unroll
+  for (int q = 0; q < N; ++q) x[q] |= (q == idx) ? m : 0ull;
+}
+template <int N>
+__device__ __forceinline__ void clear_word(uint64_t* x, int idx, uint64_t m) {
+#pragma unroll
+  for (int q = 0; q < N; ++q) x[q] &= (q == idx) ? ~m : ~0ull;
+}
+template <int N>
+__device__ __forceinline__ uint64_t get_word(const uint64_t* x, int idx) {
+  uint64_t r = 0ull;
+#pragma unroll
+  for (int q = 0; q < N; ++q) r = (q == idx) ? x[q] : r;
+  return r;
+}
+// out[w] = x[s * W + w] (s = 0: alpha words, 1: beta words)
+template <int W>
+__device__ __forceinline__ void pick_spin(const uint64_t* x, int s, uint64_t* out) {
+#pragma unroll
+  for (int w = 0; w < W; ++w) out[w] = s ? x[W + w] : x[w];
+}
+
 // (ij|kl) as cip/ai.f looks it up: packed pair indices, zero across irreps
 __device__ __forceinline__ double ai(const Params& p, int i, int j, int k, int l) {
   const int pij = __ldg(&p.pairtab[i * p.norb + j]);
@@ -129,7 +157,7 @@ __device__ __forceinline__ int lr_diff(uint64_t e, uint32_t c1x4, uint32_t c2x4,
 // to the reference determinant; the one-difference element sums over the
 // holes and particles of the more excited determinant as cip/hntd.f does.
 template <int W>
-__device__ double hmat(const Params& p, const uint64_t* u, const uint64_t* v, int rankI, int rankJ,
+__device__ __forceinline__ double hmat(const Params& p, const uint64_t* u, const uint64_t* v, int rankI, int rankJ,
                        const uint64_t* hf, int& kind) {
   uint64_t remv[2 * W], addv[2 * W];
   int nrem[2] = {0, 0};
@@ -144,12 +172,19 @@ __device__ double hmat(const Params& p, const uint64_t* u, const uint64_t* v, in
   if (nrem[0] + nrem[1] == 1) {
     kind = 1;
     const int s = nrem[0] ? 0 : 1;
-    const int pp = first_bit<W>(remv + s * W);
-    const int qq = first_bit<W>(addv + s * W);
+    uint64_t rs[W], as[W], vs[W];
+    pick_spin<W>(remv, s, rs);
+    pick_spin<W>(addv, s, as);
+    pick_spin<W>(v, s, vs);
+    const int pp = first_bit<W>(rs);
+    const int qq = first_bit<W>(as);
     const int lo = pp < qq ? pp : qq, hi = pp < qq ? qq : pp;
-    const int sign = (popc_between<W>(v + s * W, lo, hi) & 1) ? -1 : 1;
+    const int sign = (popc_between<W>(vs, lo, hi) & 1) ? -1 : 1;
     double val = __ldg(&p.F[tri(pp, qq)]);
-    const uint64_t* D = (rankI > rankJ) ? u : v;
+    const bool dI = rankI > rankJ;
+    uint64_t D[2 * W];
+#pragma unroll
+    for (int q = 0; q < 2 * W; ++q) D[q] = dI ? u[q] : v[q];
     // holes of D (occupied in the reference, empty in D)
 #pragma unroll
     for (int sp = 0; sp < 2; ++sp) {
@@ -184,16 +219,15 @@ __device__ double hmat(const Params& p, const uint64_t* u, const uint64_t* v, in
     return ((sa + sb) & 1) ? -val : val;
   }
   const int s = nrem[0] == 2 ? 0 : 1;
-  const uint64_t* rm = remv + s * W;
-  const uint64_t* ad = addv + s * W;
+  uint64_t rm[W], ad[W], mid[W];
+  pick_spin<W>(remv, s, rm);
+  pick_spin<W>(addv, s, ad);
+  pick_spin<W>(v, s, mid);
   const int p1 = first_bit<W>(rm), p2 = last_bit<W>(rm);
   const int q1 = first_bit<W>(ad), q2 = last_bit<W>(ad);
-  uint64_t mid[W];
-#pragma unroll
-  for (int w = 0; w < W; ++w) mid[w] = v[s * W + w];
   const int s1 = popc_between<W>(mid, min(p1, q1), max(p1, q1));
-  mid[p1 >> 6] &= ~(1ull << (p1 & 63));
-  mid[q1 >> 6] |= (1ull << (q1 & 63));
+  clear_word<W>(mid, p1 >> 6, 1ull << (p1 & 63));
+  or_word<W>(mid, q1 >> 6, 1ull << (q1 & 63));
   const int s2 = popc_between<W>(mid, min(p2, q2), max(p2, q2));
   const double val = ai(p, p1, q1, p2, q2) - ai(p, p1, q2, p2, q1);
   return ((s1 + s2) & 1) ? -val : val;
@@ -216,12 +250,19 @@ __device__ void hmat_adj(const Params& p, const uint64_t* u, const uint64_t* v, 
   }
   if (nrem[0] + nrem[1] == 1) {
     const int s = nrem[0] ? 0 : 1;
-    const int pp = first_bit<W>(remv + s * W);
-    const int qq = first_bit<W>(addv + s * W);
+    uint64_t rs[W], as[W], vs[W];
+    pick_spin<W>(remv, s, rs);
+    pick_spin<W>(addv, s, as);
+    pick_spin<W>(v, s, vs);
+    const int pp = first_bit<W>(rs);
+    const int qq = first_bit<W>(as);
     const int lo = pp < qq ? pp : qq, hi = pp < qq ? qq : pp;
-    const double sw = (popc_between<W>(v + s * W, lo, hi) & 1) ? -w : w;
+    const double sw = (popc_between<W>(vs, lo, hi) & 1) ? -w : w;
     atomicAdd(&p.g_F[tri(pp, qq)], sw);
-    const uint64_t* D = (rankI > rankJ) ? u : v;
+    const bool dI = rankI > rankJ;
+    uint64_t D[2 * W];
+#pragma unroll
+    for (int q = 0; q < 2 * W; ++q) D[q] = dI ? u[q] : v[q];
 #pragma unroll
     for (int sp = 0; sp < 2; ++sp) {
 #pragma unroll
@@ -253,16 +294,15 @@ __device__ void hmat_adj(const Params& p, const uint64_t* u, const uint64_t* v, 
     return;
   }
   const int s = nrem[0] == 2 ? 0 : 1;
-  const uint64_t* rm = remv + s * W;
-  const uint64_t* ad = addv + s * W;
+  uint64_t rm[W], ad[W], mid[W];
+  pick_spin<W>(remv, s, rm);
+  pick_spin<W>(addv, s, ad);
+  pick_spin<W>(v, s, mid);
   const int p1 = first_bit<W>(rm), p2 = last_bit<W>(rm);
   const int q1 = first_bit<W>(ad), q2 = last_bit<W>(ad);
-  uint64_t mid[W];
-#pragma unroll
-  for (int ww = 0; ww < W; ++ww) mid[ww] = v[s * W + ww];
   const int s1 = popc_between<W>(mid, min(p1, q1), max(p1, q1));
-  mid[p1 >> 6] &= ~(1ull << (p1 & 63));
-  mid[q1 >> 6] |= (1ull << (q1 & 63));
+  clear_word<W>(mid, p1 >> 6, 1ull << (p1 & 63));
+  or_word<W>(mid, q1 >> 6, 1ull << (q1 & 63));
   const int s2 = popc_between<W>(mid, min(p2, q2), max(p2, q2));
   const double sw = ((s1 + s2) & 1) ? -w : w;
   ai_adj(p, p1, q1, p2, q2, sw);
@@ -409,6 +449,17 @@ __device__ void diag_terms(const Params& p, const uint64_t* u, const uint64_t* h
   hdigi = e;
 }
 
+// Spin-flip weight fmul = (1/(lesp+1)) * (nespf+1) - 1 (pert1.f:150-164,
+// diexcit.f:304-316), rounded step by step as the reference does (no fused
+// multiply-add).  lesp is 0 or 1 for almost every perturber: those two
+// reciprocals are exact constants, so the FP64 division is only taken for
+// lesp >= 2.
+__device__ __forceinline__ double spin_weight(int nespf, int lesp) {
+  if (lesp == 0) return (double)nespf;  // 1 * (nespf + 1) - 1, exact
+  const double inv = lesp == 1 ? 0.5 : 1.0 / (double)(lesp + 1);
+  return __dsub_rn(__dmul_rn(inv, (double)(nespf + 1)), 1.0);
+}
+
 // bit patterns of 0.05, 1e-6 and +inf
 constexpr long long kBits005 = 0x3fa999999999999all;
 constexpr long long kBits1em6 = 0x3eb0c6f7a0b5ed8dll;
@@ -426,50 +477,78 @@ __device__ __forceinline__ double max_nonneg(double a, double b) {
 }
 
 
-// Block-wide order-preserving compaction: calls emit(slot, i) for every i in
-// [0, n) with pred(i), slots dense and increasing with i (deterministic).
-// Must be called by every thread of the block.
-template <typename Pred, typename Emit>
-__device__ int ordered_compact(int n, Pred pred, Emit emit, int* warp_tmp /* >= 33 ints */) {
-  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5, nw = blockDim.x >> 5;
-  int total = 0;
-  for (int base = 0; base < n; base += blockDim.x) {
-    const int i = base + tid;
-    const bool keep = i < n && pred(i);
-    const unsigned m = __ballot_sync(0xffffffffu, keep);
-    if (lane == 0) warp_tmp[wid] = __popc(m);
-    __syncthreads();
-    if (wid == 0) {
-      const int v = lane < nw ? warp_tmp[lane] : 0;
-      int x = v;
-      for (int o = 1; o < 32; o <<= 1) {
-        const int y = __shfl_up_sync(0xffffffffu, x, o);
-        if (lane >= o) x += y;
-      }
-      if (lane < nw) warp_tmp[lane] = x - v;  // exclusive prefix
-      if (lane == 31) warp_tmp[32] = x;       // round total
-    }
-    __syncthreads();
-    if (keep) emit(total + warp_tmp[wid] + __popc(m & ((1u << lane) - 1u)), i);
-    total += warp_tmp[32];
-    __syncthreads();
+// Block-wide order-preserving two-way partition of [0, n): i with
+// part(i) == 0 gets the slots 0..n0-1, i with part(i) == 1 the slots
+// n0..n0+n1-1, each part in increasing i (deterministic, whatever the
+// scheduling); part(i) < 0 drops i.  Each warp owns one
+// contiguous chunk: it counts both parts, the warps' offsets come from one
+// exchange in shared memory, and the warp emits its chunk again at those
+// offsets.  Two block barriers whatever n.  Must be called by every thread
+// of the block; part() is evaluated twice per index.
+template <typename Part, typename Emit>
+__device__ int2 ordered_partition2(int n, Part part, Emit emit, int* warp_tmp /* >= 2 * warps ints */) {
+  constexpr unsigned kFull = 0xffffffffu;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const int chunk = (((n + nw - 1) / nw) + 31) & ~31;
+  const int lo = min(n, wid * chunk), hi = min(n, lo + chunk);
+  int c0 = 0, c1 = 0;
+  for (int base = lo; base < hi; base += 32) {
+    const int i = base + lane;
+    const int pt = i < hi ? part(i) : -1;
+    c0 += __popc(__ballot_sync(kFull, pt == 0));
+    c1 += __popc(__ballot_sync(kFull, pt == 1));
   }
-  return total;
+  if (lane == 0) {
+    warp_tmp[wid] = c0;
+    warp_tmp[nw + wid] = c1;
+  }
+  __syncthreads();
+  int o0 = 0, o1 = 0, n0 = 0, n1 = 0;
+  for (int w = 0; w < nw; ++w) {
+    const int a = warp_tmp[w], b = warp_tmp[nw + w];
+    if (w < wid) {
+      o0 += a;
+      o1 += b;
+    }
+    n0 += a;
+    n1 += b;
+  }
+  const unsigned below = (1u << lane) - 1u;
+  for (int base = lo; base < hi; base += 32) {
+    const int i = base + lane;
+    const int pt = i < hi ? part(i) : -1;
+    const unsigned m0 = __ballot_sync(kFull, pt == 0);
+    const unsigned m1 = __ballot_sync(kFull, pt == 1);
+    if (pt == 0) emit(o0 + __popc(m0 & below), i);
+    if (pt == 1) emit(n0 + o1 + __popc(m1 & below), i);
+    o0 += __popc(m0);
+    o1 += __popc(m1);
+  }
+  __syncthreads();
+  return make_int2(n0, n1);
 }
 
 template <int R>
 struct Acc {
   double e2mp[R], cmp[R], e2vp[R], cvp[R], e2b[R], cb[R], psimp[R], psivp[R];
-  unsigned long long ietat, nproc, nsel, ncand, ncmp, np1, np2, algb;
+  unsigned long long ietat, nproc;
   double dpivot;
   __device__ void zero() {
 #pragma unroll
     for (int m = 0; m < R; ++m) {
       e2mp[m] = cmp[m] = e2vp[m] = cvp[m] = e2b[m] = cb[m] = psimp[m] = psivp[m] = 0.0;
     }
-    ietat = nproc = nsel = ncand = ncmp = np1 = np2 = algb = 0ull;
+    ietat = nproc = 0ull;
     dpivot = 0.0;
   }
+};
+
+// Counters of the candidate scan.  Kept apart from Acc: Acc is passed by
+// reference to the out-of-line queue drain, so it lives in local memory,
+// and these are incremented in the scan loop itself (registers).
+struct ScanCounts {
+  unsigned long long ncand, ncmp, np1, np2;
+  __device__ void zero() { ncand = ncmp = np1 = np2 = 0ull; }
 };
 
 // One thread's histogram (cip/isto.f): class sums and counts, indexed by
@@ -520,9 +599,13 @@ __device__ void finish_candidate(const Params& p, bool live, const uint64_t* u, 
   const int lane = threadIdx.x & 31;
   double xam = 0.0;
   bool ydeg = false;
+  // weighted E2 terms per root: term * (1 + fmul), which is also what the
+  // histogram (isto.f, fm = fmul + 1) and cipsym's unit-60 value
+  // (cipsym/pert1.f:244, eivp * (fmul + 1)) use
   double vil[R], semp[R], sevp[R];
   // the reference adds each term and then term*fmul (spin-flip weight,
-  // pert1.f:280-287); one compensated add of term*(1+fmul) is used here
+  // pert1.f:280-287); one compensated add of term*(1+fmul) is used here.
+  // fmul = 0 whenever ybis is false, so wgt = fmul + 1 for every perturber.
   const double wgt = ybis ? 1.0 + fmul : 1.0;
 #pragma unroll
   for (int m = 0; m < R; ++m) {
@@ -531,27 +614,31 @@ __device__ void finish_candidate(const Params& p, bool live, const uint64_t* u, 
     if (!live || m >= p.metat) continue;
     const double bcalc = bc[m];
     const double dmp = p.emp[m] - hmpi;
-    double eivp = 0.0, cimp, xim, deno, eim;
+    double eivp = 0.0, tvp = 0.0, cimp, xim, deno, eim;
     if (p.yen) {
       // the three denominators share one FP64 division (GB300's FP64 rate is
-      // 1/64 of FP32): r = 1/(dmp*dvp*db), 1/dmp = dvp*db*r, etc.
+      // 1/64 of FP32): br = b/(dmp*dvp*db), b/dmp = dvp*db*br, etc.
       const double dvp = p.e[m] - hvpi;
       const double db = p.eb[m] - hvpi;
       const double pvb = dvp * db;
       const double prod = dmp * pvb;
       double civp, cib;
-      if (fabs(prod) > 1.0e-280 && fabs(prod) < 1.0e280) {
-        const double r = 1.0 / prod;
-        cimp = bcalc * (pvb * r);
-        civp = bcalc * ((dmp * db) * r);
-        cib = bcalc * ((dmp * dvp) * r);
+      // 1e-280 < |prod| < 1e280 tested on the exponent field (integer pipe):
+      // binary exponent in [-930, 929]
+      const unsigned pex = (unsigned)(__double_as_longlong(prod) >> 52) & 0x7FFu;
+      if (pex - 93u < 1860u) {
+        const double br = bcalc / prod;
+        cimp = br * pvb;
+        civp = br * (dmp * db);
+        cib = br * (dmp * dvp);
       } else {  // a denominator at (or near) zero or huge: divide one by one
         cimp = bcalc / dmp;
         civp = bcalc / dvp;
         cib = bcalc / db;
       }
       eivp = bcalc * civp;
-      kahan_add(acc.e2vp[m], acc.cvp[m], eivp * wgt);
+      tvp = eivp * wgt;
+      kahan_add(acc.e2vp[m], acc.cvp[m], tvp);
       acc.psivp[m] = fma(civp * civp, wgt, acc.psivp[m]);
       kahan_add(acc.e2b[m], acc.cb[m], (bcalc * cib) * wgt);
       xim = p.ysele ? fabs(eivp) : fabs(civp);
@@ -561,7 +648,8 @@ __device__ void finish_candidate(const Params& p, bool live, const uint64_t* u, 
       cimp = bcalc / dmp;
     }
     const double eimp = bcalc * cimp;
-    kahan_add(acc.e2mp[m], acc.cmp[m], eimp * wgt);
+    const double tmp = eimp * wgt;
+    kahan_add(acc.e2mp[m], acc.cmp[m], tmp);
     acc.psimp[m] = fma(cimp * cimp, wgt, acc.psimp[m]);
     if (!p.yen) {
       xim = p.ysele ? fabs(eimp) : fabs(cimp);
@@ -579,8 +667,8 @@ __device__ void finish_candidate(const Params& p, bool live, const uint64_t* u, 
       vil[m] = xim;
       xam = max_nonneg(xam, xim);
     }
-    semp[m] = eimp;
-    sevp[m] = eivp;
+    semp[m] = tmp;
+    sevp[m] = tvp;
   }
   if (live) {
     acc.ietat += (unsigned long long)(long long)(nmul + 1);
@@ -588,14 +676,13 @@ __device__ void finish_candidate(const Params& p, bool live, const uint64_t* u, 
   }
   // histogram (cip/isto.f; pert1 calls it always, diexcit only if ymoyen)
   if (live && (is_pert1 || p.ymoyen) && xam >= p.teseff) {
-    const double fm = fmul + 1.0;
     const int cls = hist_class(p, xam);
     hp.nom[cls] += (unsigned)(1 + nmul);
 #pragma unroll
     for (int m = 0; m < R; ++m) {
       if (m >= p.metat || vil[m] < p.teseff) continue;
-      hp.tab[cls][0][m] += semp[m] * fm;
-      hp.tab[cls][1][m] += sevp[m] * fm;
+      hp.tab[cls][0][m] += semp[m];  // eimp * (fmul + 1)
+      hp.tab[cls][1][m] += sevp[m];  // eivp * (fmul + 1)
       hp.nam[hist_class(p, vil[m])][m] += (unsigned)(1 + nmul);
     }
   }
@@ -617,7 +704,7 @@ __device__ void finish_candidate(const Params& p, bool live, const uint64_t* u, 
         // ENvp per root written by cipsym (cipsym/pert1.f:244): eivp*(fmul+1)
 #pragma unroll
         for (int m = 0; m < R; ++m)
-          if (m < p.metat) p.sel_evp[slot * p.metat + m] = p.symvar ? sevp[m] * (fmul + 1.0) : 0.0;
+          if (m < p.metat) p.sel_evp[slot * p.metat + m] = p.symvar ? sevp[m] : 0.0;
       }
     }
   }
@@ -718,12 +805,14 @@ __device__ void enqueue_candidate(const Params& p, WarpQueue<W, R>& q, int& qn, 
 // Block totals of the integer counters and the histogram into the
 // geometry's global counters; then reset them for the next geometry.
 template <int R>
-__device__ void flush_totals(const Params& p, Acc<R>& acc, HistPriv<R>& hp, SmemHist& hist) {
+__device__ void flush_totals(const Params& p, Acc<R>& acc, HistPriv<R>& hp, SmemHist& hist,
+                             unsigned long long ncand, unsigned long long ncmp, unsigned long long np1,
+                             unsigned long long np2) {
   const int tid = threadIdx.x;
   // block totals of the integer counters and the histogram
   __syncthreads();
   {
-    unsigned long long v[8] = {acc.ietat, acc.nproc, 0ull, acc.ncand, acc.ncmp, acc.np1, acc.np2, 0ull};
+    unsigned long long v[8] = {acc.ietat, acc.nproc, 0ull, ncand, ncmp, np1, np2, 0ull};
     for (int q = 0; q < 8; ++q) {
       unsigned long long x = v[q];
       for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
@@ -758,7 +847,7 @@ __device__ void flush_totals(const Params& p, Acc<R>& acc, HistPriv<R>& hp, Smem
     if (tv != 0.0) atomicAdd(&p.hist_tab[p.nclass * p.metat + c * p.metat + m], tv);
   }
   __syncthreads();
-  acc.ietat = acc.nproc = acc.ncand = acc.ncmp = acc.np1 = acc.np2 = 0ull;
+  acc.ietat = acc.nproc = 0ull;
   acc.dpivot = 0.0;
   hp.zero();
   for (int i = tid; i < kNClass; i += blockDim.x) hist.nom[i] = 0;
@@ -844,6 +933,8 @@ __global__ void __launch_bounds__(kThreads, 2) k_pt2(Params p0, BatchArgs ba) {
 
   Acc<R> acc;
   acc.zero();
+  ScanCounts sc;
+  sc.zero();
   HistPriv<R> hp;
   hp.zero();
   // adjoint: per-thread root-energy gradients and per-block accumulators of
@@ -869,7 +960,10 @@ __global__ void __launch_bounds__(kThreads, 2) k_pt2(Params p0, BatchArgs ba) {
     if (B) {
       const int gi = ba.unit_geo[unit];
       if (gi != cur_geo) {
-        if (cur_geo >= 0) flush_totals<R>(p, acc, hp, hist);
+        if (cur_geo >= 0) {
+          flush_totals<R>(p, acc, hp, hist, sc.ncand, sc.ncmp, sc.np1, sc.np2);
+          sc.zero();
+        }
         __syncthreads();
         const int* src = reinterpret_cast<const int*>(ba.geo + gi);
         int* dst = reinterpret_cast<int*>(&sgeo);
@@ -900,15 +994,15 @@ __global__ void __launch_bounds__(kThreads, 2) k_pt2(Params p0, BatchArgs ba) {
           const int rem = tt % (no * nv);
           const int o = rem / nv, vv = no + rem % nv;
           if (p.its[p.orbsym[o]][p.orbsym[vv]] != p.isym - 1) live = false;
-          u[s * W + (o >> 6)] &= ~(1ull << (o & 63));
-          u[s * W + (vv >> 6)] |= (1ull << (vv & 63));
+          clear_word<2 * W>(u, s * W + (o >> 6), 1ull << (o & 63));
+          or_word<2 * W>(u, s * W + (vv >> 6), 1ull << (vv & 63));
         }
         double bc[R];
 #pragma unroll
         for (int m = 0; m < R; ++m) bc[m] = 0.0;
         double hmpi = 0.0, hvpi = 0.0;
         if (live) {
-          acc.ncand++;
+          sc.ncand++;
           int rankI = 0;
 #pragma unroll
           for (int q = 0; q < 2 * W; ++q) rankI += __popcll(hf[q] & ~u[q]);
@@ -919,7 +1013,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_pt2(Params p0, BatchArgs ba) {
             int x = 0;
 #pragma unroll
             for (int q = 0; q < 2 * W; ++q) x += __popcll(u[q] ^ __ldg(&v[q]));
-            acc.ncmp++;
+            sc.ncmp++;
             if (x > 4) continue;
             if (x == 0) {
               drop = true;
@@ -933,7 +1027,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_pt2(Params p0, BatchArgs ba) {
             for (int q = 0; q < 2 * W; ++q) rankJ += __popcll(hf[q] & ~vv[q]);
             int kind;
             const double h = hmat<W>(p, u, vv, rankI, rankJ, hf, kind);
-            if (kind == 1) acc.np1++; else acc.np2++;
+            if (kind == 1) sc.np1++; else sc.np2++;
             ++nint;
 #pragma unroll
             for (int m = 0; m < R; ++m)
@@ -995,7 +1089,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_pt2(Params p0, BatchArgs ba) {
       for (int s = 0; s < 2; ++s) {
         int nes = 0, nv = 0;
         for (int o = 0; o < p.norb; ++o) {
-          if ((kb[s * W + (o >> 6)] >> (o & 63)) & 1ull) {
+          if ((get_word<2 * W>(kb, s * W + (o >> 6)) >> (o & 63)) & 1ull) {
             sh.occ[ne++] = o + s * p.norb;
             ++nes;
           } else {
@@ -1011,13 +1105,13 @@ __global__ void __launch_bounds__(kThreads, 2) k_pt2(Params p0, BatchArgs ba) {
     }
     __syncthreads();
     const int nel = sh.nel_s[0] + sh.nel_s[1];
-    const int nnb = ordered_compact(
+    const int nnb = ordered_partition2(
         ncf,
         [&](int j) {
           int x = 0;
 #pragma unroll
           for (int q = 0; q < 2 * W; ++q) x += __popcll(kb[q] ^ __ldg(&p.S[(size_t)j * 2 * W + q]));
-          return x <= 8;
+          return x <= 8 ? 0 : -1;
         },
         [&](int slot, int j) {
           // electrons of k missing in j, as a mask over k's electron indices
@@ -1040,7 +1134,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_pt2(Params p0, BatchArgs ba) {
           my_nb_j[slot] = j;
           my_nb_em[slot] = em;
         },
-        ctmp);
+        ctmp).x;
     const int rank_k = sh.rank_k;
     const uint8_t dmask = p.gen_dmask[g];
     const int k1 = k + 1;  // 1-based owner index
@@ -1080,8 +1174,8 @@ __global__ void __launch_bounds__(kThreads, 2) k_pt2(Params p0, BatchArgs ba) {
       uint64_t kp[2 * W];
 #pragma unroll
       for (int q = 0; q < 2 * W; ++q) kp[q] = kb[q];
-      kp[sp1 * W + (o1 >> 6)] &= ~(1ull << (o1 & 63));
-      if (e2 >= 0) kp[sp2 * W + (o2 >> 6)] &= ~(1ull << (o2 & 63));
+      clear_word<2 * W>(kp, sp1 * W + (o1 >> 6), 1ull << (o1 & 63));
+      if (e2 >= 0) clear_word<2 * W>(kp, sp2 * W + (o2 >> 6), 1ull << (o2 & 63));
       auto lr_m = [&](int t) {
         const uint64_t em = my_nb_em[t];
         return __popcll(em) - __popcll(em & rmask);
@@ -1113,11 +1207,15 @@ __global__ void __launch_bounds__(kThreads, 2) k_pt2(Params p0, BatchArgs ba) {
         else
           my_lr_ent[slot] = ent;
       };
-      const int n01 = ordered_compact(nnb, [&](int t) { return lr_m(t) <= 1; }, lr_store, ctmp);
-      const int n2 = ordered_compact(
-          nnb, [&](int t) { return lr_m(t) == 2; }, [&](int slot, int t) { lr_store(n01 + slot, t); },
-          ctmp);
-      const int nlr = n01 + n2;
+      const int2 nparts = ordered_partition2(
+          nnb,
+          [&](int t) {
+            const int m = lr_m(t);
+            return m <= 1 ? 0 : (m == 2 ? 1 : -1);
+          },
+          lr_store, ctmp);
+      const int n01 = nparts.x;
+      const int nlr = nparts.x + nparts.y;
       const bool fast = nlr <= p.lr_cap;
       if (!fast && tid == 0) atomicAdd(&p.counters[C_LRFALLBACK], 1ull);
       auto ent_at = [&](int i) -> uint64_t { return i < p.lr_cap ? lr_ent[i] : my_lr_ent[i]; };
@@ -1226,9 +1324,9 @@ __global__ void __launch_bounds__(kThreads, 2) k_pt2(Params p0, BatchArgs ba) {
         for (int m = 0; m < R; ++m) bc[m] = 0.0;
         int nint = 0, nnz = 0, lesp = 0;
         if (live) {
-          acc.ncand++;
-          u[sa1 * W + (a1 >> 6)] |= (1ull << (a1 & 63));
-          if (a2 >= 0) u[sa2 * W + (a2 >> 6)] |= (1ull << (a2 & 63));
+          sc.ncand++;
+          or_word<2 * W>(u, sa1 * W + (a1 >> 6), 1ull << (a1 & 63));
+          if (a2 >= 0) or_word<2 * W>(u, sa2 * W + (a2 >> 6), 1ull << (a2 & 63));
           const int rankI = rank_k + D;
           bool drop = false;
           const bool two = a2 >= 0;
@@ -1248,7 +1346,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_pt2(Params p0, BatchArgs ba) {
             for (int q = 0; q < 2 * W; ++q) rankJ += __popcll(hf[q] & ~vv[q]);
             int kind;
             const double h = hmat<W>(p, u, vv, rankI, rankJ, hf, kind);
-            if (kind == 1) acc.np1++; else acc.np2++;
+            if (kind == 1) sc.np1++; else sc.np2++;
             ++nint;
             if (h != 0.0) ++nnz;
             if (j > k && j <= k + nespk) ++lesp;
@@ -1275,7 +1373,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_pt2(Params p0, BatchArgs ba) {
             const int x = lr_diff(ent_at(i), c1x4, c2x4, two);
             if (x <= 4) drop = visit(i, x);
           }
-          acc.ncmp += (unsigned long long)(nscan + nrb);
+          sc.ncmp += (unsigned long long)(nscan + nrb);
           if (drop || nint == 0) live = false;
           if (live && D == 2 && nnz == 0) live = false;  // diexcit drops zero couplings
         }
@@ -1287,7 +1385,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_pt2(Params p0, BatchArgs ba) {
           if (is_pert1) {
             if (nespk != 0) {
               ybis = true;
-              fmul = (1.0 / (double)(lesp + 1)) * (double)(nespk + 1) - 1.0;
+              fmul = spin_weight(nespk, lesp);
               nmul = (int)fmul;
             }
           } else {
@@ -1297,7 +1395,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_pt2(Params p0, BatchArgs ba) {
               ybis = true;
               if (!yefk) nespf = nespf + nespf + 1;
             }
-            fmul = (1.0 / (double)(lesp + 1)) * (double)(nespf + 1) - 1.0;
+            fmul = spin_weight(nespf, lesp);
             nmul = (int)fmul;
           }
           hmpi = sh.mK + __ldg(&p.fmpb[a1 + sa1 * p.norb]);
@@ -1496,7 +1594,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_pt2(Params p0, BatchArgs ba) {
     block_flush<R>(p, acc, unit, red);
   }
 
-  if (!B || cur_geo >= 0) flush_totals<R>(p, acc, hp, hist);
+  if (!B || cur_geo >= 0) flush_totals<R>(p, acc, hp, hist, sc.ncand, sc.ncmp, sc.np1, sc.np2);
   if (ADJ) {
 #pragma unroll
     for (int k3 = 0; k3 < 3; ++k3)
