@@ -1207,22 +1207,12 @@ __global__ void __launch_bounds__(kThreads, 2) k_pt2(Params p0, BatchArgs ba) {
         else
           my_lr_ent[slot] = ent;
       };
-      const int2 nparts = ordered_partition2(
-          nnb,
-          [&](int t) {
-            const int m = lr_m(t);
-            return m <= 1 ? 0 : (m == 2 ? 1 : -1);
-          },
-          lr_store, ctmp);
-      const int n01 = nparts.x;
-      const int nlr = nparts.x + nparts.y;
-      const bool fast = nlr <= p.lr_cap;
-      if (!fast && tid == 0) atomicAdd(&p.counters[C_LRFALLBACK], 1ull);
-      auto ent_at = [&](int i) -> uint64_t { return i < p.lr_cap ? lr_ent[i] : my_lr_ent[i]; };
       // diagonal energies of I = K' + A from those of K' (cip/hdig.f, hmp.f
       // written over occupation changes dn relative to the reference):
       //   hdig = sum_r dn_r F_rr + 1/2 sum_rs dn_r dn_s (J_rs - [same spin] K_rs)
       //   hmp  = sum_r dn_r fmpb_r
+      // (listed by thread 0 before the partition below, whose first barrier
+      // publishes it)
       if (tid == 0) {
         int nd = 0;
         for (int sp = 0; sp < 2; ++sp)
@@ -1244,7 +1234,18 @@ __global__ void __launch_bounds__(kThreads, 2) k_pt2(Params p0, BatchArgs ba) {
           }
         sh.ndn = nd;
       }
-      __syncthreads();
+      const int2 nparts = ordered_partition2(
+          nnb,
+          [&](int t) {
+            const int m = lr_m(t);
+            return m <= 1 ? 0 : (m == 2 ? 1 : -1);
+          },
+          lr_store, ctmp);
+      const int n01 = nparts.x;
+      const int nlr = nparts.x + nparts.y;
+      const bool fast = nlr <= p.lr_cap;
+      if (!fast && tid == 0) atomicAdd(&p.counters[C_LRFALLBACK], 1ull);
+      auto ent_at = [&](int i) -> uint64_t { return i < p.lr_cap ? lr_ent[i] : my_lr_ent[i]; };
       {
         const int ndn = sh.ndn, n = p.norb;
         for (int a = tid; a < 2 * n; a += blockDim.x) {
@@ -1260,22 +1261,33 @@ __global__ void __launch_bounds__(kThreads, 2) k_pt2(Params p0, BatchArgs ba) {
           const int ta = tri(oa, oa);
           sh.vdg[a] = __ldg(&p.F[ta]) + g + 0.5 * (__ldg(&p.J[ta]) - __ldg(&p.K[ta]));
         }
-        if (tid == 32) {
+        if ((tid >> 5) == (int)(blockDim.x >> 5) - 1) {
+          // the last warp: the ndn + ndn^2 terms of hdig(K') and hmp(K')
+          // spread over its lanes, then summed by shuffles in a fixed order
+          const int lane = tid & 31;
           double e = 0.0, mp = 0.0;
-          for (int i = 0; i < ndn; ++i) {
-            const int r = sh.dn_so[i], orr = r % n;
-            e += sh.dn_sg[i] * __ldg(&p.F[tri(orr, orr)]);
-            mp += sh.dn_sg[i] * __ldg(&p.fmpb[r]);
-            for (int j = 0; j < ndn; ++j) {
-              const int q = sh.dn_so[j];
-              const int t = tri(orr, q % n);
-              double x = __ldg(&p.J[t]);
-              if (r / n == q / n) x -= __ldg(&p.K[t]);
+          for (int t = lane; t < ndn * (ndn + 1); t += 32) {
+            if (t < ndn) {
+              const int r = sh.dn_so[t], orr = r % n;
+              e += sh.dn_sg[t] * __ldg(&p.F[tri(orr, orr)]);
+              mp += sh.dn_sg[t] * __ldg(&p.fmpb[r]);
+            } else {
+              const int i = (t - ndn) / ndn, j = (t - ndn) % ndn;
+              const int r = sh.dn_so[i], q = sh.dn_so[j];
+              const int tq = tri(r % n, q % n);
+              double x = __ldg(&p.J[tq]);
+              if (r / n == q / n) x -= __ldg(&p.K[tq]);
               e += 0.5 * sh.dn_sg[i] * sh.dn_sg[j] * x;
             }
           }
-          sh.hK = e;
-          sh.mK = mp;
+          for (int o = 16; o > 0; o >>= 1) {
+            e += __shfl_down_sync(0xffffffffu, e, o);
+            mp += __shfl_down_sync(0xffffffffu, mp, o);
+          }
+          if (lane == 0) {
+            sh.hK = e;
+            sh.mK = mp;
+          }
         }
       }
       __syncthreads();
