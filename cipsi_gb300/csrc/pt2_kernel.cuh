@@ -799,7 +799,9 @@ __device__ void enqueue_candidate(const Params& p, WarpQueue<W, R>& q, int& qn, 
   }
   qn += __popc(lm);
   __syncwarp();
-  drain_queue<W, R>(p, q, qn, false, acc, hp);
+  // the drain is out of line; calling it only with a full batch spares the
+  // register saves of a call on every other candidate round
+  if (qn >= 32) drain_queue<W, R>(p, q, qn, false, acc, hp);
 }
 
 // Block totals of the integer counters and the histogram into the
