@@ -42,14 +42,10 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 CONFIG = "medium"
-# dram__bytes_read.sum + dram__bytes_write.sum of one k_pt2 launch on this
-# workload: 0.190 GB + 2.164 GB measured by ncu on the every-7th-generator
-# sample (`--gen-every 7`, 36.49 M perturbers), scaled to the full launch
-# (255.88 M perturbers) by the perturber count.  The traffic is mostly the
-# unit-60 records and local-memory write-backs, which grow with the
-# perturbers: an earlier build measured 3.47 GB on the sample and 24.15 GB on
-# the full launch, a ratio of 6.96 against 7.01 for the perturber count.
-NCU_DRAM_BYTES_PER_LAUNCH = (0.190e9 + 2.164e9) * 255880490 / 36486644
+# dram__bytes_read.sum + dram__bytes_write.sum of one full k_pt2 launch on
+# this workload (0.984 GB + 14.616 GB), from a single-pass ncu capture of
+# `python bench.py --steps 2 --warmup 3 --no-cpu-baseline` (5th k_pt2 launch)
+NCU_DRAM_BYTES_PER_LAUNCH = 15.600e9
 METRIC = "perturber contributions/s"
 UNIT = "contributions/s"
 
@@ -604,9 +600,8 @@ def run_gpu(args, rank: int, world: int, local_rank: int):
                          "note": "achieved = algorithmic bytes of the E2 loop (integral, coefficient and "
                                  "diagonal-term reads) per launch / mean k_pt2+k_reduce time, against the "
                                  "measured HBM copy bandwidth; the kernel is bound by the FP64 pipe (~55 % "
-                                 "busy) and L1/L2/shared-memory latency, not HBM; traffic (ncu, sample "
-                                 "capture scaled by perturbers) is mostly unit-60 records and local-memory "
-                                 "write-backs"},
+                                 "busy) and L1/L2/shared-memory latency, not HBM; traffic (ncu) is mostly "
+                                 "unit-60 records and local-memory write-backs"},
             "clocks": clk,
             "work": {"perturbers": r["n_processed"], "candidates": r["n_candidates"],
                      "compares": r["n_compares"], "pairs_1": r["n_pairs_1"], "pairs_2": r["n_pairs_2"],

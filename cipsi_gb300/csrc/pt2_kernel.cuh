@@ -142,13 +142,19 @@ __device__ __forceinline__ uint64_t lr_entry(uint32_t ebytes, int ne, int m, int
   return (uint64_t)ebytes | ((uint64_t)m << 32) | ((uint64_t)j << 34);
 }
 __device__ __forceinline__ int lr_entry_j(uint64_t e) { return (int)(e >> 34); }
+// true when some byte of x equals the byte repeated in c4 (a zero byte of
+// x ^ c4; the borrow test flags a byte only if it or a lower byte is zero)
+__device__ __forceinline__ bool has_byte(uint32_t x, uint32_t c4) {
+  const uint32_t v = x ^ c4;
+  return ((v - 0x01010101u) & ~v & 0x80808080u) != 0u;
+}
 // bit difference |I xor j| = 2 (m + |A \ E|) of I = K' + A, A = {c1[, c2]}
 // (c1x4, c2x4: the codes repeated in four bytes)
 __device__ __forceinline__ int lr_diff(uint64_t e, uint32_t c1x4, uint32_t c2x4, bool two) {
   const uint32_t E = (uint32_t)e;
   int d = (int)((e >> 32) & 3u);
-  d += __vcmpeq4(E, c1x4) ? 0 : 1;
-  if (two) d += __vcmpeq4(E, c2x4) ? 0 : 1;
+  d += has_byte(E, c1x4) ? 0 : 1;
+  if (two) d += has_byte(E, c2x4) ? 0 : 1;
   return 2 * d;
 }
 
@@ -1521,7 +1527,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_pt2(Params p0, BatchArgs ba) {
           int nrb = 0;
           for (int i0 = n01; i0 < nlr; i0 += 32) {
             const int i = i0 + lane;
-            const bool has = i < nlr && __vcmpeq4((uint32_t)ent_at(i), r1x4) != 0;
+            const bool has = i < nlr && has_byte((uint32_t)ent_at(i), r1x4);
             const unsigned bm = __ballot_sync(0xffffffffu, has);
             if (has) {
               const int pos = nrb + __popc(bm & ((1u << lane) - 1u));
