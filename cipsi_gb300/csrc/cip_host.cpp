@@ -14,9 +14,13 @@
 // cip/hmp.f, cip/hdig.f, cip/pie.f, cip/stkener.f and the cipsym variants
 // (cipsym/cip.f:226-254, cipsym/pie.f, cipsym/ic001.f:179).
 //
-// Supported: lecdet 2, 3 (S from unit 60) and 5 (S from unit 60, vectors
-// from unit 59) with ityper >= 0; isz = 0.  Unsupported inputs are rejected
-// with a message (cip stops on them, or they need the S diagonalisation).
+// Supported: the perturbation run, lecdet 5 (S from unit 60, vectors from
+// unit 59) with ityper >= 0; and the run that only writes S (ityper < 0,
+// cip/cip.f:200-236), with S from unit 60 (lecdet 2, 3, 5) or generated as
+// a complete active space (lecdet 4, cip/cas.f) -- the two ways the Autocip
+// driver calls cipsym (Autocip_13/calcul.f90:318-353).  isz = 0.  Other
+// inputs are rejected with a message (cip stops on them, or they need the S
+// diagonalisation).
 
 #include <algorithm>
 #include <cctype>
@@ -170,6 +174,9 @@ struct Options {
   std::string title = "                    ";
   std::vector<double> tocom;
   std::vector<int> numero;  // state numbers (default 1..metat)
+  // complete active space of lecdet = 4 (COMMON /activ/, cip/cas.f)
+  int noac = 0, nelac = 0, nusym = 1, nemax = 8;
+  std::vector<int> numac;  // active orbitals (default 1..norb)
   // &cipfil
   std::string f60 = "det", f40 = "ijkl", f04 = "f04", f59 = "bdvec", f33 = "ener";
 };
@@ -203,6 +210,9 @@ Options read_options(const std::string& text, const std::string& dir) {
   r1("test", o.test); r1("teseff", o.teseff); r1("tau", o.tau); r1("tdet", o.tdet); r1("coeff", o.coeff);
   i1("isz", o.isz); i1("metat", o.metat); i1("ityper", o.ityper); i1("iselec", o.iselec);
   i1("lecdet", o.lecdet); i1("nclass", o.nclass); i1("maxdet", o.maxdet); i1("ninact", o.ninact);
+  i1("noac", o.noac); i1("nelac", o.nelac); i1("nusym", o.nusym); i1("nemax", o.nemax);
+  if (auto v = ic.get("numac"))
+    for (auto& x : *v) o.numac.push_back(std::stoi(x));
   l1("yion", o.yion); l1("ybrd", o.ybrd); l1("ymoyen", o.ymoyen); l1("ywdeg", o.ywdeg); l1("ytocom", o.ytocom);
   if (auto v = ic.get("aval"))
     for (size_t i = 0; i < v->size() && i < 10; ++i) o.aval[i] = to_real((*v)[i]);
@@ -215,6 +225,8 @@ Options read_options(const std::string& text, const std::string& dir) {
     o.title.resize(20, ' ');
   }
   if (ic.has("ygen")) throw Error("ygen given in &icinp is not supported");
+  if (ic.has("iord")) throw Error("iord given in &icinp is not supported");
+  if (o.lecdet == 5) o.tdet = 0.0;  // deter.f:224-226: the whole of unit 60
   return o;
 }
 
@@ -244,6 +256,7 @@ struct Run {
   Space S;
   std::vector<double> c, e, eb, emp, teste, taum, fmpb, fdiag;
   std::vector<double> tocom, empdet;  // faifoc.f occupations (after cip.f:75-84), hmp of S
+  std::vector<double> hdiag;          // hdig of S
 };
 
 // transf.f: sort, validate, dedup and append one determinant
@@ -285,10 +298,19 @@ void transf(Run& R, int nec, int* nt, int* np) {
   }
 }
 
-void build_space(Run& R, const std::string& f60) {
-  // lec60.f: determinants of unit 60 with v >= tdet, grouped by degree
-  std::vector<std::vector<std::vector<int>>> byrank(9);
+// The determinants of S before the spin-flip closure: whether the reference
+// determinant is there, and the others by excitation degree (holes then
+// particles, in the order in which deter.f:478-567 appends them).
+struct DetLists {
   bool hf = false;
+  std::vector<std::vector<std::vector<int>>> byrank = std::vector<std::vector<std::vector<int>>>(9);
+};
+
+// lec60.f: the determinants of unit 60 with v >= tdet
+DetLists read_unit60(const Run& R, const std::string& f60) {
+  DetLists L;
+  auto& byrank = L.byrank;
+  bool& hf = L.hf;
   int ndet = 0;
   for (auto& rec : read_records(f60)) {
     const int mw = rec.get<int32_t>(), nw = rec.get<int32_t>();
@@ -321,8 +343,90 @@ void build_space(Run& R, const std::string& f60) {
     }
   }
 done:
-  // deter.f:478-567: each determinant followed by its spin-flip partner
-  if (hf) transf(R, 0, nullptr, nullptr);
+  return L;
+}
+
+// cas.f: the complete active space of lecdet = 4.  Each spin has
+// n = (nelac+1)/2 electrons in the active orbitals numac[0..noac), of which
+// the first n are the ones the reference determinant occupies.  A spin string
+// is an increasing n-tuple of active positions, enumerated in lexicographic
+// order, and becomes the holes it leaves among the first n positions and the
+// particles it puts among the others (as orbital numbers, in position order).
+// Determinants run over alpha strings (outer loop) and beta strings (inner);
+// those with more than nemax excitations or a symmetry other than nusym (the
+// first determinant's when nusym = 0) are skipped.  Limits and messages are
+// the reference's: 20 active electrons, 25000 strings of one spin, 500000
+// determinants, 10 holes + particles per string.
+DetLists cas_space(Run& R) {
+  Options& o = R.o;
+  DetLists L;
+  if (o.nelac > 20) throw Error(" trop d electrons actifs  maximum 20");
+  const int n = (o.nelac + 1) / 2, noac = o.noac;
+  if (n > noac) throw Error("more active electrons of one spin than active orbitals (nelac, noac)");
+  if (n == 0) return L;  // no beta string: no determinant (cas.f:188-200)
+  std::vector<int> act(noac);
+  for (int k = 0; k < noac; ++k) {
+    act[k] = k < (int)o.numac.size() ? o.numac[k] : k + 1;  // deter.f:139 default numac(i) = i
+    if (act[k] < 1 || act[k] > R.norb) throw Error("numac names an orbital outside 1..norb");
+  }
+  struct Str {
+    std::vector<int> t, p;
+  };
+  std::vector<Str> strs;
+  std::vector<int> pos(n);
+  for (int i = 0; i < n; ++i) pos[i] = i;
+  for (;;) {
+    if ((int)strs.size() >= 25000) throw Error("  trop de combinaisons: max=25000");
+    std::vector<bool> in(noac, false);
+    for (int q : pos) in[q] = true;
+    Str st;
+    for (int k = 0; k < n; ++k)
+      if (!in[k]) st.t.push_back(act[k]);
+    for (int k = n; k < noac; ++k)
+      if (in[k]) st.p.push_back(act[k]);
+    if (st.t.size() + st.p.size() > 10) throw Error("more than 10 holes and particles in one CAS string");
+    strs.push_back(std::move(st));
+    int i = n - 1;  // lexicographic successor of pos
+    while (i >= 0 && pos[i] == noac - n + i) --i;
+    if (i < 0) break;
+    ++pos[i];
+    for (int k = i + 1; k < n; ++k) pos[k] = pos[k - 1] + 1;
+  }
+  const int norb = R.norb, nsym = R.nsym;
+  auto prod = [&](int a, int b) { return R.its[(size_t)(b - 1) * nsym + (a - 1)]; };
+  int ndet = 0;
+  for (const Str& a : strs)
+    for (const Str& b : strs) {
+      std::vector<int> t(a.t), p(a.p);
+      for (int x : b.t) t.push_back(x + norb);
+      for (int x : b.p) p.push_back(x + norb);
+      const int nec = (int)t.size();
+      if (nec > o.nemax) continue;
+      int is = 1;
+      for (int i = 0; i < nec; ++i) {
+        is = prod(is, R.itsym[(t[i] - 1) % norb]);
+        is = prod(is, R.itsym[(p[i] - 1) % norb]);
+      }
+      if (o.nusym == 0) o.nusym = is;
+      if (is != o.nusym) continue;
+      if (++ndet > 500000) throw Error(" espace actif trop grand  maximum=500000");
+      if (nec == 0) {
+        L.hf = true;
+        continue;
+      }
+      if (nec > 8) throw Error("CAS determinant with more than 8 excitations (nemax > 8)");
+      std::vector<int> d(t);
+      d.insert(d.end(), p.begin(), p.end());
+      L.byrank[nec].push_back(std::move(d));
+    }
+  return L;
+}
+
+// deter.f:478-567: S from the lists, each determinant followed by its
+// spin-flip partner
+void build_space(Run& R, const DetLists& L) {
+  const auto& byrank = L.byrank;
+  if (L.hf) transf(R, 0, nullptr, nullptr);
   R.S.ygen.assign(R.S.ne.size(), 0);
   R.S.ysaut.assign(R.S.ne.size(), 0);
   R.S.yef1.assign(R.S.ne.size(), 0);
@@ -400,6 +504,9 @@ double hdig_list(const Run& R, int k) {
   return ab;
 }
 
+void read_vectors(Run& R, bool sym_variant);
+void zero_order(Run& R);
+
 void read_inputs(Run& R, bool sym_variant) {
   const Options& o = R.o;
   if (o.yion) throw Error("yion (excitation to infinity) is not supported");
@@ -407,8 +514,10 @@ void read_inputs(Run& R, bool sym_variant) {
   if (o.ybrd && o.metat > 1) throw Error("ybrd (QDPT effective Hamiltonian) is not supported");
   if (o.ninact > 0) throw Error("ninact > 0 (restricted perturbation space) is not supported");
   if (o.ytocom) throw Error("ytocom (occupations from unit 21) is not supported");
-  if (o.ityper < 0) throw Error("ityper < 0 (writing S only) is not supported");
-  if (o.lecdet != 5) throw Error("lecdet must be 5 (vectors of S read from unit 59)");
+  if (o.lecdet < 2 || o.lecdet > 5) throw Error("lecdet 1 (determinants on cards) is not supported");
+  if (o.ityper >= 0 && o.lecdet != 5)
+    throw Error("a perturbation run needs lecdet = 5 (vectors of S read from unit 59)");
+  if (o.metat < 1 || o.metat > 60) throw Error("trop d etats demandes en perturbation");
   auto recs = read_records(o.f40);
   if (recs.size() < 9) throw Error("unit 40 too short");
   {
@@ -449,7 +558,7 @@ void read_inputs(Run& R, bool sym_variant) {
   R.fdiag.assign(2 * R.norb, 0.0);
   for (int i = 1; i <= R.norb; ++i) R.fdiag[i - 1] = R.fdiag[i - 1 + R.norb] = R.F[(size_t)i * (i + 1) / 2 - 1];
 
-  build_space(R, o.f60);
+  build_space(R, o.lecdet == 4 ? cas_space(R) : read_unit60(R, o.f60));
   // escf (rdener.f)
   bool found = false;
   for (auto& r : read_records(o.f33)) {
@@ -462,7 +571,21 @@ void read_inputs(Run& R, bool sym_variant) {
     }
   }
   if (!found) throw Error("energie du determinant de reference n'existe pas sur 33");
-  // ic001.f:44-76
+  if (o.ityper < 0) {
+    // ic001 is not called (cip.f:71): c and e stay zero
+    R.metat = o.metat;
+    R.c.assign((size_t)R.ncf * R.metat, 0.0);
+    R.e.assign(R.metat, 0.0);
+  } else {
+    read_vectors(R, sym_variant);
+  }
+  zero_order(R);
+}
+
+// ic001.f:44-76 (lecdet = 5): the vectors and energies of S from unit 59,
+// in the order of unit 4's iord60 for cip; generators from them
+void read_vectors(Run& R, bool sym_variant) {
+  const Options& o = R.o;
   auto r4 = read_records(o.f04);
   if (r4.empty()) throw Error("unit 4 is empty");
   for (int i = 0; i < 4; ++i) (void)r4[0].get<int32_t>();
@@ -502,6 +625,11 @@ void read_inputs(Run& R, bool sym_variant) {
         if (std::fabs(R.c[(size_t)m * R.ncf + k]) >= o.coeff) R.S.ygen[k] = 1;
     }
   }
+}
+
+// faifoc.f and the zero-order quantities of cip.f:75-135
+void zero_order(Run& R) {
+  const Options& o = R.o;
   // faifoc.f with the occupations of cip.f:75-84
   std::vector<double> tocom(2 * R.norb, 0.0);
   for (int i = 0; i < R.noc; ++i) tocom[i] = 2.0;
@@ -551,7 +679,8 @@ void read_inputs(Run& R, bool sym_variant) {
   R.tocom = tocom;
   std::vector<double>& empdet = R.empdet;
   empdet.assign(R.ncf, 0.0);
-  std::vector<double> hdiag(R.ncf);
+  std::vector<double>& hdiag = R.hdiag;
+  hdiag.assign(R.ncf, 0.0);
   for (int k = 0; k < R.ncf; ++k) {
     empdet[k] = hmp_list(R, k);
     hdiag[k] = hdig_list(R, k);
@@ -567,7 +696,7 @@ void read_inputs(Run& R, bool sym_variant) {
     }
     if (yselm) {
       R.teste[m] = t * o.test;
-      R.taum[m] = 1.0 / t;
+      if (o.ityper >= 0) R.taum[m] = 1.0 / t;
     }
   }
 }
@@ -695,22 +824,15 @@ std::vector<int> root_flip_signs(const Run& R) {
   return itm;
 }
 
-// cip.f:300-306 and 403-414: zero-order and perturbed effective Hamiltonians
-// (diagonal without QDPT) appended to unit 4 after the perturbation
-void write_unit4_results(const Run& R, const double* e2mp, const double* e2vp, const double* e2b,
-                         const std::vector<int>& itm) {
+// The two effective-Hamiltonian records appended to unit 4: the zero-order
+// one (packed triangle hz, escf, ityper, the root signs) and the perturbed
+// ones (hm, hv, hb: MP, EN eigenvalue, EN barycentric)
+void write_unit4_heff(const Run& R, const std::vector<double>& hz, const std::vector<double>& hm,
+                      const std::vector<double>& hv, const std::vector<double>& hb,
+                      const std::vector<int>& itm) {
   std::FILE* f = std::fopen(R.o.f04.c_str(), "ab");
   if (!f) throw Error("cannot append to " + R.o.f04);
-  const int mt = R.metat, nbr = mt * (mt + 1) / 2;
-  std::vector<double> hz(nbr, 0.0), hm(nbr, 0.0), hv(nbr, 0.0), hb(nbr, 0.0);
-  for (int m = 1; m <= mt; ++m) {
-    const int mm = m * (m + 1) / 2 - 1;
-    const double eabs = R.e[m - 1] + R.escf;
-    hm[mm] = eabs + e2mp[m - 1];
-    hv[mm] = eabs + e2vp[m - 1];
-    hb[mm] = eabs + e2b[m - 1];
-    hz[mm] = eabs - R.escf;
-  }
+  const int mt = R.metat;
   RecWriter w;
   for (double x : hz) w.put<double>(x);
   w.put<double>(R.escf);
@@ -723,6 +845,72 @@ void write_unit4_results(const Run& R, const double* e2mp, const double* e2vp, c
   for (double x : hb) w.put<double>(x);
   w.flush(f);
   std::fclose(f);
+}
+
+// cip.f:300-306 and 403-414: zero-order and perturbed effective Hamiltonians
+// (diagonal without QDPT) appended to unit 4 after the perturbation
+void write_unit4_results(const Run& R, const double* e2mp, const double* e2vp, const double* e2b,
+                         const std::vector<int>& itm) {
+  const int mt = R.metat, nbr = mt * (mt + 1) / 2;
+  std::vector<double> hz(nbr, 0.0), hm(nbr, 0.0), hv(nbr, 0.0), hb(nbr, 0.0);
+  for (int m = 1; m <= mt; ++m) {
+    const int mm = m * (m + 1) / 2 - 1;
+    const double eabs = R.e[m - 1] + R.escf;
+    hm[mm] = eabs + e2mp[m - 1];
+    hv[mm] = eabs + e2vp[m - 1];
+    hb[mm] = eabs + e2b[m - 1];
+    hz[mm] = eabs - R.escf;
+  }
+  write_unit4_heff(R, hz, hm, hv, hb, itm);
+}
+
+// shell.f: the order of S by increasing diagonal energy that cip.f:200-206
+// takes before writing S alone: Shell's diminishing-increment sort of -hdig
+// into decreasing order, increments n/2, n/4, .. (log2 n passes, the count
+// from single-precision logarithms as shell.f computes it).  Ties keep the
+// positions this sequence of exchanges gives them, so the order is the
+// reference's even among equal energies.  Returns 0-based indices of S.
+std::vector<int> energy_order(const Run& R) {
+  const int n = R.ncf;
+  std::vector<double> a(R.hdiag.size());
+  std::vector<int> ind(n);
+  for (int k = 0; k < n; ++k) {
+    a[k] = -R.hdiag[k];
+    ind[k] = k;
+  }
+  const double aln2i = (double)(1.0f / 0.69314748f), tiny = (double)1.0e-5f;
+  const int passes = (int)((double)std::log((float)n) * aln2i + tiny);
+  int m = n;
+  for (int pass = 0; pass < passes; ++pass) {
+    m /= 2;
+    for (int j = 0; j < n - m; ++j)
+      for (int i = j; i >= 0 && a[i + m] > a[i]; i -= m) {
+        std::swap(a[i], a[i + m]);
+        std::swap(ind[i], ind[i + m]);
+      }
+  }
+  return ind;
+}
+
+void write_pie_records(std::FILE* f, const std::vector<int32_t>& nec, const std::vector<int32_t>& h,
+                       const std::vector<int32_t>& p, const std::vector<double>& v,
+                       const std::vector<double>& evp, int metat, bool sym_variant, size_t hstride);
+
+// unit 60 as pie.f writes it: the determinants of S in the given order, v = 1
+long long write_space_unit60(std::FILE* f60, const Run& R, const std::vector<int>& order, bool sym_variant) {
+  const size_t n = order.size();
+  std::vector<int32_t> nec(n), h(n * 8, 0), p(n * 8, 0);
+  std::vector<double> v(n, 1.0), ev(n * R.metat, 0.0);
+  for (size_t q = 0; q < n; ++q) {
+    const int k = order[q];
+    nec[q] = R.S.ne[k];
+    for (int l = 0; l < nec[q]; ++l) {
+      h[q * 8 + l] = R.S.trou[R.S.nd[k] + l];
+      p[q * 8 + l] = R.S.part[R.S.nd[k] + l];
+    }
+  }
+  write_pie_records(f60, nec, h, p, v, ev, R.metat, sym_variant, 8);
+  return (long long)n;
 }
 
 void write_pie_records(std::FILE* f, const std::vector<int32_t>& nec, const std::vector<int32_t>& h,
@@ -898,6 +1086,28 @@ extern "C" int cipsi_cip_main(const char* workdir, const char* stdin_path, int32
     const Run& R = in->R;
     const auto t0 = std::chrono::steady_clock::now();
     write_unit4_zero_order(R);  // cip.f:144, during the set-up
+    if (R.o.ityper < 0) {
+      // cip.f:200-236: S by increasing diagonal energy, the (empty) effective
+      // Hamiltonians on unit 4, S on unit 60 when ymoyen, and stop: no
+      // perturbation, no device work
+      const int mt = R.metat, nbr = mt * (mt + 1) / 2;
+      const std::vector<double> zero(nbr, 0.0);
+      write_unit4_heff(R, zero, zero, zero, zero, root_flip_signs(R));
+      long long ntot = 0;
+      if (R.o.ymoyen) {
+        std::FILE* f60 = std::fopen(R.o.f60.c_str(), "wb");
+        if (!f60) throw Error("cannot rewrite " + R.o.f60);
+        ntot = write_space_unit60(f60, R, energy_order(R), sym_variant != 0);
+        std::fclose(f60);
+      }
+      if (json_path) {
+        std::ofstream j(json_path);
+        j << "{\n  \"ncf\": " << R.ncf << ", \"metat\": " << mt << ", \"norb\": " << R.norb
+          << ", \"noca\": " << R.noc << ", \"ntot60\": " << ntot << "\n}\n";
+      }
+      cipsi_inputs_free(in);
+      return 0;
+    }
     cipsi_dims d{};
     cipsi_opts op{};
     cipsi_inputs_dims(in, &d, &op);
@@ -912,22 +1122,15 @@ extern "C" int cipsi_cip_main(const char* workdir, const char* stdin_path, int32
     cipsi_result res{};
     if (R.o.ityper != 0) chk(cipsi_run_pt2(ctx, &op, &res), "cipsi_run_pt2");
     const auto t1 = std::chrono::steady_clock::now();
-    // unit 60: S (v = 1) then the selected perturbers
-    std::FILE* f60 = std::fopen(R.o.f60.c_str(), "wb");
-    if (!f60) throw Error("cannot rewrite " + R.o.f60);
+    // unit 60 when ymoyen: S (v = 1) then the selected perturbers; without
+    // ymoyen the reference writes nothing to it (cip.f:222, pert1.f:264)
     long long ntot = 0;
     if (R.o.ymoyen) {
-      std::vector<int32_t> nec(R.ncf), h((size_t)R.ncf * 8, 0), p((size_t)R.ncf * 8, 0);
-      std::vector<double> v(R.ncf, 1.0), ev((size_t)R.ncf * R.metat, 0.0);
-      for (int k = 0; k < R.ncf; ++k) {
-        nec[k] = R.S.ne[k];
-        for (int l = 0; l < nec[k]; ++l) {
-          h[(size_t)k * 8 + l] = R.S.trou[R.S.nd[k] + l];
-          p[(size_t)k * 8 + l] = R.S.part[R.S.nd[k] + l];
-        }
-      }
-      write_pie_records(f60, nec, h, p, v, ev, R.metat, sym_variant != 0, 8);
-      ntot += R.ncf;
+      std::FILE* f60 = std::fopen(R.o.f60.c_str(), "wb");
+      if (!f60) throw Error("cannot rewrite " + R.o.f60);
+      std::vector<int> identity(R.ncf);
+      for (int k = 0; k < R.ncf; ++k) identity[k] = k;
+      ntot += write_space_unit60(f60, R, identity, sym_variant != 0);
       const int64_t ns = res.n_selected;
       const int64_t chunk = 1 << 20;  // records converted per call (a multiple of lungo)
       for (int64_t first = 0; first < ns; first += chunk) {
@@ -940,8 +1143,8 @@ extern "C" int cipsi_cip_main(const char* workdir, const char* stdin_path, int32
         write_pie_records(f60, snec, sh, sp, sx, sev, R.metat, sym_variant != 0, 8);
       }
       ntot += ns;
+      std::fclose(f60);
     }
-    std::fclose(f60);
     write_unit4_results(R, res.e2mp, res.e2vp, res.e2b, itm);
     // listing lines the Autocip driver reads (cipsym/cip.f:253-254, cip.f:243-247)
     std::printf("0 ont ete generes:    %10lld  etats efficaces\n", (long long)res.ietat);

@@ -21,6 +21,9 @@
  *                                partners 478-567
  *   CIPSI_sources/cip/transf.f   sort / validate / dedup of one determinant
  *   CIPSI_sources/cip/lec60.f    reading S from unit 60
+ *   CIPSI_sources/cipsym/cas.f   complete active space (lecdet=4)
+ *   CIPSI_sources/cipsym/shell.f, cip.f:200-236   the run that only writes
+ *                                S (ityper<0): energy order, units 4 and 60
  *   CIPSI_sources/cip/ijkf.f, reijkl.f, rdener.f, ic001.f:44-76 (lecdet=5),
  *   CIPSI_sources/cip/brdnee.f:299-365 (degen)
  *   CIPSI_sources/cip/faifoc.f, hmp.f, hdig.f, hntd.f, ai.f
@@ -32,9 +35,10 @@
  * Arrays are 1-based (index 0 unused) to keep the restatement checkable
  * against the Fortran line by line.
  *
- * Not restated (rejected with an error): lecdet=1 (card input), lecdet=4
- * (CAS generation), S diagonalisation (ityper>=0 with lecdet!=5),
- * ybrd (QDPT effective Hamiltonian), yion (excitation to infinity).
+ * Not restated (rejected with an error): lecdet=1 (card input),
+ * S diagonalisation (ityper>=0 with lecdet!=5), ybrd (QDPT effective
+ * Hamiltonian), yion (excitation to infinity), iord or ygen given in the
+ * namelist.
  */
 #define _GNU_SOURCE
 #include <ctype.h>
@@ -317,6 +321,9 @@ static int cur_src = 0;                /* 0 pertu, 1 igene, 2 diexcit */
 static int noc_[3], igels_[3], norbs_[3]; /* equivalence (noca,noc(1)) etc. */
 
 static int hf_noc; /* noc from unit 40 */
+/* /activ/: the CAS of lecdet = 4 (numac(1..noac) active orbitals, nelac
+   active electrons, nusym its symmetry, nemax its largest excitation) */
+static int numac[520], noac, nusym, nelac, nemax;
 static char title[64] = "                    ";
 
 /* ------------------------------------------------------- ai (cip/ai.f) */
@@ -1528,6 +1535,156 @@ done:
   rewind(f);
 }
 
+/* cas.f:64-110: the increasing n-tuples of 1..noac in lexicographic order
+   (istr starts at (1, .., n-1, n-1) so that the first step gives 1..n).
+   Returns their number; the tuples go to out[ii*10 + k], k = 0..n-1. */
+#define NIIZ 25000
+static int cas_strings(int n, int noac, int* out) {
+  int istr[16] = {0};
+  for (int k = 1; k <= n; k++) istr[k] = k;
+  if (n != 0) istr[n] = n - 1;
+  int ii = 0, i = n + 1;
+L10:
+  i = i - 1;
+  if (i == 0) return ii;
+L14:;
+  int newoc = istr[i] + 1;
+  if (newoc > (noac - n + i)) goto L10;
+  istr[i] = newoc;
+  for (int k = i + 1; k <= n; k++) istr[k] = istr[k - 1] + 1;
+  i = n;
+  ii = ii + 1;
+  if (ii > NIIZ) die("  trop de combinaisons: max=%d", NIIZ);
+  for (int k = 1; k <= n; k++) out[(size_t)(ii - 1) * 10 + (k - 1)] = istr[k];
+  goto L14;
+}
+
+/* cas.f:111-166: one string's holes (orbitals numac(1..noc) it leaves
+   empty) then particles (numac(noc+1..noac) it fills), as orbital numbers.
+   Returns the hole count; *np gets the particle count. */
+static int cas_excitation(const int* occ, int n, int noc, int* mtp, int* np) {
+  unsigned char yocc[520] = {0};
+  for (int k = 1; k <= n; k++) yocc[occ[k - 1]] = 1;
+  int itp = 0;
+  for (int k = 1; k <= noc; k++)
+    if (!yocc[k]) {
+      if (itp >= 10) die("more than 10 holes and particles in one string of the CAS");
+      mtp[++itp] = numac[k];
+    }
+  int nt = itp;
+  for (int k = noc + 1; k <= noac; k++)
+    if (yocc[k]) {
+      if (itp >= 10) die("more than 10 holes and particles in one string of the CAS");
+      mtp[++itp] = numac[k];
+    }
+  *np = itp - nt;
+  return nt;
+}
+
+/* cas.f: the CAS determinants of symmetry nusym with at most nemax
+   excitations, alpha strings outer and beta strings inner, into the
+   per-degree lists that deter.f:478-567 turns into S (yion is rejected
+   before, so nalfa = nbeta = noc = (nelac+1)/2) */
+static void cas(void) {
+  int nalfa = (nelac + 1) / 2, nbeta = nalfa;
+  if (nelac > 20) die(" trop d electrons actifs  maximum 20");
+  int noc = nalfa;
+  if (nalfa > noac) die("more active electrons of one spin (%d) than active orbitals (%d)", nalfa, noac);
+  for (int k = 1; k <= noac; k++)
+    if (numac[k] < 1 || numac[k] > norb) die("numac(%d)=%d is not an orbital", k, numac[k]);
+  int* noma = (int*)xcalloc((size_t)NIIZ * 10 + 10, sizeof(int));
+  int* nomb = (int*)xcalloc((size_t)NIIZ * 10 + 10, sizeof(int));
+  int nca = cas_strings(nalfa, noac, noma);
+  int ncb = cas_strings(nbeta, noac, nomb);
+  int *nta = (int*)xcalloc((size_t)NIIZ + 2, sizeof(int)), *npa = (int*)xcalloc((size_t)NIIZ + 2, sizeof(int));
+  int *ntb = (int*)xcalloc((size_t)NIIZ + 2, sizeof(int)), *npb = (int*)xcalloc((size_t)NIIZ + 2, sizeof(int));
+  int mtp[12];
+  for (int ia = 1; ia <= (nca > 1 ? nca : 1); ia++) {
+    int* row = noma + (size_t)(ia - 1) * 10;
+    nta[ia] = cas_excitation(row, nca ? nalfa : 0, noc, mtp, &npa[ia]);
+    for (int k = 1; k <= nta[ia] + npa[ia]; k++) row[k - 1] = mtp[k];
+  }
+  for (int ib = 1; ib <= ncb; ib++) {
+    int* row = nomb + (size_t)(ib - 1) * 10;
+    ntb[ib] = cas_excitation(row, nbeta, noc, mtp, &npb[ib]);
+    for (int k = 1; k <= ntb[ib] + npb[ib]; k++) row[k - 1] = mtp[k];
+  }
+  int ndet = 0;
+  for (int ia = 1; ia <= (nca > 1 ? nca : 1); ia++) {
+    int kta = nta[ia], kpa = npa[ia];
+    int nts[24], nps[24];
+    const int* ra = noma + (size_t)(ia - 1) * 10;
+    for (int k = 1; k <= kta; k++) nts[k] = ra[k - 1];
+    for (int k = 1; k <= kpa; k++) nps[k] = ra[k - 1 + kta];
+    for (int ib = 1; ib <= ncb; ib++) {
+      int ktb = ntb[ib], kpb = npb[ib];
+      const int* rb = nomb + (size_t)(ib - 1) * 10;
+      for (int k = 1; k <= ktb; k++) nts[k + kta] = rb[k - 1] + norb;
+      for (int k = 1; k <= kpb; k++) nps[k + kpa] = rb[k - 1 + ktb] + norb;
+      int nect = kta + ktb, necp = kpa + kpb;
+      if (nect != necp) die("  attention necp et nect sont differents %d %d", nect, necp);
+      int nec = necp;
+      if (nec > nemax) continue;
+      int is = 1;
+      for (int i = 1; i <= nec; i++) {
+        int jps = itsym[nps[i]];
+        is = its[is][itsym[nts[i]]];
+        is = its[is][jps];
+      }
+      if (nusym == 0) nusym = is;
+      if (is != nusym) continue;
+      ndet = ndet + 1;
+      if (ndet > UNIT4_NDETZ) die(" espace actif trop grand  maximum=%d", UNIT4_NDETZ);
+      if (nec == 0) {
+        if (isz != 0) continue;
+        kf_ref++;
+        if (kf_ref != 1) {
+          kf_ref--;
+          printf(" fondamental deja present\n");
+        }
+        continue;
+      }
+      if (nec > 8) die("CAS determinant of excitation degree %d above 8", nec);
+      int itab[20];
+      for (int s = 1; s <= nec; s++) {
+        itab[s - 1] = nts[s];
+        itab[s - 1 + nec] = nps[s];
+      }
+      kex_push(nec, itab);
+    }
+  }
+  printf("   determinants engendres %d\n", ndet);
+  free(noma); free(nomb); free(nta); free(npa); free(ntb); free(npb);
+}
+
+/* shell.f: Shell's diminishing-increment sort of a[1..n] into decreasing
+   order, carrying ind along; log2(n) passes with increments n/2, n/4, ..
+   (the pass count from single-precision logarithms, as shell.f computes it) */
+static void shell(double* a, int* ind, int n) {
+  const double aln2i = (double)(1.0f / 0.69314748f), tiny = (double)1.0e-5f;
+  int lognb2 = (int)((double)logf((float)n) * aln2i + tiny);
+  int m = n;
+  for (int nn = 1; nn <= lognb2; nn++) {
+    m = m / 2;
+    int k = n - m;
+    for (int j = 1; j <= k; j++) {
+      int i = j;
+      for (;;) {
+        int l = i + m;
+        if (!(a[l] > a[i])) break;
+        double t = a[i];
+        a[i] = a[l];
+        a[l] = t;
+        int indi = ind[i];
+        ind[i] = ind[l];
+        ind[l] = indi;
+        i = i - m;
+        if (i < 1) break;
+      }
+    }
+  }
+}
+
 /* transf.f: validate, sort and append one determinant (nt/np 1-based) */
 static int tr_nt[12], tr_np[12];
 static int g_ntp_used = 0;
@@ -1756,24 +1913,14 @@ static void write_unit4_zero_order(const char* path, const double* empdet) {
   fclose(f4);
 }
 
-/* cip.f:300-306 and 403-414: zero-order and perturbed effective Hamiltonians
-   (diagonal: ybrd = .false.) appended to unit 4 */
-static void write_unit4_results(const char* path) {
+/* the two effective-Hamiltonian records cip appends to unit 4 (hzero with
+   escf, ityper and the root signs; then hefmp, hefvp, hefb), from the
+   packed triangles hz, hm, hv, hb [1..nbr] */
+static void write_unit4_heff(const char* path, const double* hz, const double* hm, const double* hv,
+                             const double* hb) {
   FILE* f4 = fopen(path, "ab");
   if (!f4) die("cannot append to unit 4 file %s", path);
   int nbr = metat * (metat + 1) / 2;
-  double* hz = (double*)xcalloc((size_t)nbr + 2, sizeof(double));
-  double* hm = (double*)xcalloc((size_t)nbr + 2, sizeof(double));
-  double* hv = (double*)xcalloc((size_t)nbr + 2, sizeof(double));
-  double* hb = (double*)xcalloc((size_t)nbr + 2, sizeof(double));
-  for (int m = 1; m <= metat; m++) {
-    int mm = m * (m + 1) / 2;
-    double eabs = e[m] + escf;
-    hm[mm] = eabs + e2mp[m];
-    hv[mm] = eabs + e2vp[m];
-    hb[mm] = eabs + e2b[m];
-    hz[mm] = eabs - escf;
-  }
   wbuf_t w = {0};
   for (int i = 1; i <= nbr; i++) wb_r8(&w, hz[i]);
   wb_r8(&w, escf);
@@ -1788,8 +1935,27 @@ static void write_unit4_results(const char* path) {
   for (int i = 1; i <= nbr; i++) wb_r8(&w2, hb[i]);
   wb_flush(f4, &w2);
   free(w2.b);
-  free(hz); free(hm); free(hv); free(hb);
   fclose(f4);
+}
+
+/* cip.f:300-306 and 403-414: zero-order and perturbed effective Hamiltonians
+   (diagonal: ybrd = .false.) appended to unit 4 */
+static void write_unit4_results(const char* path) {
+  int nbr = metat * (metat + 1) / 2;
+  double* hz = (double*)xcalloc((size_t)nbr + 2, sizeof(double));
+  double* hm = (double*)xcalloc((size_t)nbr + 2, sizeof(double));
+  double* hv = (double*)xcalloc((size_t)nbr + 2, sizeof(double));
+  double* hb = (double*)xcalloc((size_t)nbr + 2, sizeof(double));
+  for (int m = 1; m <= metat; m++) {
+    int mm = m * (m + 1) / 2;
+    double eabs = e[m] + escf;
+    hm[mm] = eabs + e2mp[m];
+    hv[mm] = eabs + e2vp[m];
+    hb[mm] = eabs + e2b[m];
+    hz[mm] = eabs - escf;
+  }
+  write_unit4_heff(path, hz, hm, hv, hb);
+  free(hz); free(hm); free(hv); free(hb);
 }
 
 /* ------------------------------------------------------------- main */
@@ -1877,8 +2043,6 @@ int main(int argc, char** argv) {
 
   FILE* f40 = fopen(n40, "rb");
   if (!f40) die("cannot open unit 40 file %s", n40);
-  f60 = fopen(n60, "r+b");
-  if (!f60) die("cannot open unit 60 file %s", n60);
 
   /* deter.f: header of unit 40 */
   rec_t r = {0};
@@ -1924,6 +2088,8 @@ int main(int argc, char** argv) {
   iselec = 1; lecdet = 1; nclass = 10; metat = 1; ywdeg = 1; coeff = 0.0; ninact = 0;
   maxdet = 500000; twdet = 0.0;
   for (int i = 1; i <= 60; i++) numero[i] = i;
+  for (int i = 1; i <= norb; i++) numac[i] = i; /* deter.f:139 */
+  noac = 0; nusym = 1; nelac = 0; nemax = 8;
   nlgroup_t gi;
   if (!nl_parse("icinp", &gi)) die("erreur dans la namelist icinp");
   nl_set_real(&gi, "test", &test);
@@ -1973,6 +2139,16 @@ int main(int argc, char** argv) {
   int nonact[512] = {0};
   nl_set_int_arr(&gi, "nonact", nonact, 512);
   if (nl_get(&gi, "ygen")) die("ygen given in the namelist is not restated");
+  if (nl_get(&gi, "iord")) die("iord given in the namelist is not restated");
+  nl_set_int(&gi, "noac", &noac);
+  nl_set_int(&gi, "nelac", &nelac);
+  nl_set_int(&gi, "nusym", &nusym);
+  nl_set_int(&gi, "nemax", &nemax);
+  {
+    int nu[520];
+    int n = nl_set_int_arr(&gi, "numac", nu, 512);
+    for (int i = 0; i < n; i++) numac[i + 1] = nu[i];
+  }
 
   if (teseff < 0.0) teseff = 0.05 * tau;
   if (lecdet == 5) tdet = 0.0;
@@ -1985,9 +2161,9 @@ int main(int argc, char** argv) {
   if (iselec == 3) ysele = 1;
   if (yion) die("yion is not restated");
   if (ybrd && metat > 1) die("ybrd (QDPT heff) is not restated");
-  if (lecdet != 5 && lecdet != 2 && lecdet != 3) die("lecdet=%d is not restated", lecdet);
-  if (ityper < 0) die("ityper<0 (S writing run) is not restated");
-  if (lecdet != 5) die("ityper>=0 requires lecdet=5 here (no S diagonalisation)");
+  if (lecdet < 2 || lecdet > 5) die("lecdet=%d is not restated", lecdet);
+  if (ityper >= 0 && lecdet != 5) die("ityper>=0 requires lecdet=5 here (no S diagonalisation)");
+  if (metat > 60) die("trop d etats demandes en perturbation");
 
   noca = 0; nocb = 0; igela = 0; igelb = 0;
   /* deter.f:241-251 */
@@ -2023,8 +2199,16 @@ int main(int argc, char** argv) {
     for (int i = 0; i < ninact; i++) yorper[nonact[i]] = 0;
   }
 
-  /* S: lec60 then the spin-flip closure */
-  lec60(f60);
+  /* S: lec60 (lecdet 2, 3, 5) or cas (lecdet 4), then the spin-flip closure */
+  if (lecdet == 4) {
+    cas();
+  } else {
+    f60 = fopen(n60, "rb");
+    if (!f60) die("cannot open unit 60 file %s", n60);
+    lec60(f60);
+    fclose(f60);
+    f60 = NULL;
+  }
   {
     long long tot = 1, ntp = 2;
     for (int nec = 1; nec <= 8; nec++) {
@@ -2115,8 +2299,11 @@ int main(int argc, char** argv) {
     if (!found) die("energie du determinant de reference n'existe pas sur 33");
   }
 
-  /* ic001.f:44-76 (ynoic, lecdet=5) */
-  {
+  /* ic001.f:44-76 (ynoic, lecdet=5); not called when ityper < 0
+     (cip.f:71), which leaves c and e at zero */
+  if (ityper < 0) {
+    c = (double*)xcalloc((size_t)metat * (size_t)ncf + 4, sizeof(double));
+  } else {
     FILE* f4 = fopen(n04, "rb");
     if (!f4) die("cannot open unit 4 file %s", n04);
     if (!rec_read(f4, &r)) die("unit 4: empty");
@@ -2273,15 +2460,31 @@ int main(int argc, char** argv) {
     if (!cand_log) die("cannot open %s", cand_path);
   }
 
-  /* rewrite unit 60: S (v=1) then the selected perturbers (cip.f:222-234) */
-  fclose(f60);
-  f60 = fopen(n60, "wb");
-  if (!f60) die("cannot rewrite %s", n60);
+  /* cip.f:200-221: with ityper < 0 the determinants are ordered by
+     increasing diagonal energy, the (empty) effective Hamiltonians written
+     to unit 4, S written to unit 60, and the run stops (cip.f:236) */
+  int* iord = (int*)xcalloc((size_t)ncf + 4, sizeof(int));
+  for (int k = 1; k <= ncf; k++) iord[k] = k; /* deter.f:184 */
+  if (ityper < 0) {
+    double* ee = (double*)xcalloc((size_t)ncf + 4, sizeof(double));
+    for (int ii = 1; ii <= ncf; ii++) ee[ii] = -hdig(ii);
+    shell(ee, iord, ncf);
+    free(ee);
+    int nbr = metat * (metat + 1) / 2;
+    double* zero = (double*)xcalloc((size_t)nbr + 2, sizeof(double));
+    write_unit4_heff(n04, zero, zero, zero, zero);
+    free(zero);
+  }
+  /* rewrite unit 60 when ymoyen: S (v=1) then the selected perturbers
+     (cip.f:222-234); without ymoyen nothing is written to it */
   det_m = det_n = 0;
   det_ntot = 0;
   if (ymoyen) {
+    f60 = fopen(n60, "wb");
+    if (!f60) die("cannot rewrite %s", n60);
     double zero[64] = {0};
-    for (int ks = 1; ks <= ncf; ks++) {
+    for (int kss = 1; kss <= ncf; kss++) {
+      int ks = iord[kss];
       int necst = ne[ks];
       int nts[16], nps[16];
       int necsv = necst == 0 ? 1 : necst;
@@ -2293,13 +2496,27 @@ int main(int argc, char** argv) {
     }
     fine();
   }
+  free(iord);
+  if (ityper < 0) {
+    if (f60) fclose(f60);
+    FILE* fj = fopen(json_path, "w");
+    if (fj) {
+      fprintf(fj, "{\n  \"ncf\": %d, \"metat\": %d, \"norb\": %d, \"noca\": %d, \"ntot60\": %lld\n}\n", ncf,
+              metat, norb, noca, det_ntot);
+      fclose(fj);
+    }
+    free(r.b);
+    return 0;
+  }
   double t0 = now_s();
   if (ypertu) pertu();
   double t1 = now_s();
   if (ypertu) diexcit();
   double t2 = now_s();
-  if (ymoyen) fine();
-  fclose(f60);
+  if (ymoyen) {
+    fine();
+    fclose(f60);
+  }
   if (cand_log) fclose(cand_log);
 
   write_unit4_results(n04);
