@@ -95,13 +95,35 @@ struct RecWriter {
 };
 
 // ---------------------------------------------------------------- namelists
+// A namelist group read as the Fortran runtime reads it: from "&group" to
+// "&end" or "/"; "name = values" with names in any case; values separated by
+// commas and/or blanks; "r*c" for r copies of c; "r*", or nothing between
+// two commas, for null values (the element keeps its value); "name(i) =
+// values" assigning from element i on; "!" starting a comment to the end of
+// the line.  Each name maps to the elements assigned (1-based index -> text).
 struct Namelist {
-  std::map<std::string, std::vector<std::string>> kv;
+  std::map<std::string, std::map<int, std::string>> kv;
+  std::map<std::string, int> last;  // the highest element a value (or a null) went to
   bool found = false;
+  std::string group;
   bool has(const std::string& k) const { return kv.count(k) != 0; }
-  const std::vector<std::string>* get(const std::string& k) const {
+  // the value of a scalar variable, or nullptr when not assigned
+  const std::string* scalar(const std::string& k) const {
     auto it = kv.find(k);
-    return it == kv.end() ? nullptr : &it->second;
+    if (it == kv.end()) return nullptr;
+    if (last.at(k) > 1) throw Error("erreur dans la namelist " + group + ": too many values for " + k);
+    auto e = it->second.find(1);
+    return e == it->second.end() ? nullptr : &e->second;
+  }
+  // the elements assigned to an array variable of `bound` elements
+  const std::map<int, std::string>& array(const std::string& k, int bound) const {
+    static const std::map<int, std::string> none;
+    auto it = kv.find(k);
+    if (it == kv.end()) return none;
+    if (last.at(k) > bound)
+      throw Error("erreur dans la namelist " + group + ": " + k + " has more than " + std::to_string(bound) +
+                  " elements");
+    return it->second;
   }
 };
 
@@ -110,8 +132,10 @@ std::string lower(std::string s) {
   return s;
 }
 
-Namelist parse_namelist(const std::string& text, const std::string& group) {
+Namelist parse_namelist(const std::string& text, const std::string& group,
+                        const std::set<std::string>& names) {
   Namelist nl;
+  nl.group = group;
   const std::string lt = lower(text), key = "&" + lower(group);
   size_t pos = std::string::npos;
   for (size_t p = lt.find(key); p != std::string::npos; p = lt.find(key, p + 1)) {
@@ -123,32 +147,91 @@ Namelist parse_namelist(const std::string& text, const std::string& group) {
   }
   if (pos == std::string::npos) return nl;
   nl.found = true;
+  auto bad = [&](const std::string& m) { throw Error("erreur dans la namelist " + group + ": " + m); };
   std::string cur;
+  int idx = 1;
+  bool need_sep = false;  // a value was just read: the next comma only separates
   size_t i = pos;
   const size_t n = text.size();
+  auto put = [&](const std::string& v) {
+    if (cur.empty()) bad("value without a name");
+    if (!v.empty()) nl.kv[cur][idx] = v;  // a null leaves the element as it is
+    nl.last[cur] = std::max(nl.last[cur], idx);
+    ++idx;
+  };
   while (i < n) {
-    while (i < n && (std::isspace((unsigned char)text[i]) || text[i] == ',')) ++i;
-    if (i >= n || text[i] == '/' || text[i] == '&') break;
+    const char ch = text[i];
+    if (std::isspace((unsigned char)ch)) {
+      ++i;
+      continue;
+    }
+    if (ch == '!') {
+      while (i < n && text[i] != '\n') ++i;
+      continue;
+    }
+    if (ch == '/' || ch == '&') break;
+    if (ch == ',') {
+      if (!need_sep && !cur.empty()) {  // null value
+        nl.last[cur] = std::max(nl.last[cur], idx);
+        ++idx;
+      }
+      need_sep = false;
+      ++i;
+      continue;
+    }
     std::string tok;
-    if (text[i] == '\'' || text[i] == '"') {
+    bool quoted = false;
+    if (ch == '\'' || ch == '"') {
+      quoted = true;
       const char q = text[i++];
-      while (i < n && text[i] != q) tok += text[i++];
-      if (i < n) ++i;
+      for (; i < n; ++i) {
+        if (text[i] == q) {
+          if (i + 1 < n && text[i + 1] == q) {  // doubled quote
+            tok += q;
+            ++i;
+            continue;
+          }
+          ++i;
+          break;
+        }
+        tok += text[i];
+      }
     } else {
       while (i < n && !std::isspace((unsigned char)text[i]) && text[i] != ',' && text[i] != '=' &&
-             text[i] != '/')
+             text[i] != '/' && text[i] != '!')
         tok += text[i++];
     }
     size_t r = i;
     while (r < n && std::isspace((unsigned char)text[r])) ++r;
-    if (r < n && text[r] == '=') {
-      cur = lower(tok);
-      nl.kv[cur].clear();  // a repeated key: the last assignment wins
+    if (!quoted && r < n && text[r] == '=') {
+      std::string name = lower(tok);
+      idx = 1;
+      if (const size_t lp = name.find('('); lp != std::string::npos) {
+        if (name.back() != ')') bad("bad subscript in " + tok);
+        idx = std::atoi(name.c_str() + lp + 1);
+        name = name.substr(0, lp);
+        if (idx < 1) bad("bad subscript in " + tok);
+      }
+      if (!names.count(name)) bad("unknown name " + name);
+      cur = name;
+      nl.kv[cur];
+      nl.last[cur];
+      need_sep = false;
       i = r + 1;
       continue;
     }
-    if (cur.empty()) throw Error("namelist &" + group + ": value without a key");
-    nl.kv[cur].push_back(tok);
+    const size_t star = quoted ? std::string::npos : tok.find('*');
+    if (star != std::string::npos && star > 0 &&
+        tok.find_first_not_of("0123456789") == star) {  // r*c or r*
+      const int rep = std::atoi(tok.substr(0, star).c_str());
+      std::string c = tok.substr(star + 1);
+      if (c.size() >= 2 && (c[0] == '\'' || c[0] == '"') && c.back() == c[0]) c = c.substr(1, c.size() - 2);
+      for (int q = 0; q < rep; ++q) put(c);
+    } else {
+      if (quoted && tok.empty()) tok = " ";  // an empty string is a value, not a null
+      put(tok);
+    }
+    need_sep = true;
   }
   return nl;
 }
@@ -156,12 +239,23 @@ Namelist parse_namelist(const std::string& text, const std::string& group) {
 double to_real(std::string s) {
   for (auto& c : s)
     if (c == 'd' || c == 'D') c = 'e';
-  return std::stod(s);
+  size_t used = 0;
+  const double v = std::stod(s, &used);
+  if (used != s.size()) throw Error("erreur dans la namelist icinp: bad real value " + s);
+  return v;
+}
+int to_int(const std::string& s) {
+  size_t used = 0;
+  const int v = std::stoi(s, &used);
+  if (used != s.size()) throw Error("erreur dans la namelist icinp: bad integer value " + s);
+  return v;
 }
 bool to_logical(const std::string& s) {
   size_t i = 0;
   while (i < s.size() && s[i] == '.') ++i;
-  return i < s.size() && (s[i] == 't' || s[i] == 'T');
+  if (i >= s.size() || !std::strchr("tTfF", s[i]))
+    throw Error("erreur dans la namelist icinp: bad logical value " + s);
+  return s[i] == 't' || s[i] == 'T';
 }
 
 struct Options {
@@ -170,64 +264,96 @@ struct Options {
   int isz = 0, metat = 1, ityper = 1, iselec = 1, lecdet = 1, nclass = 10, maxdet = 500000;
   int ninact = 0;
   bool yion = false, ybrd = false, ymoyen = false, ywdeg = true, ytocom = false;
+  int ydp = -1;  // -1: as the unit-40 header says; 0/1: set in &icinp
   double aval[10] = {0.128e-6, 0.64e-6, 0.32e-5, 0.16e-4, 0.8e-4, 0.4e-3, 0.2e-2, 0.1e-1, 0.5e-1, 1.0};
   std::string title = "                    ";
-  std::vector<double> tocom;
-  std::vector<int> numero;  // state numbers (default 1..metat)
-  // complete active space of lecdet = 4 (COMMON /activ/, cip/cas.f)
+  std::map<int, double> tocom;  // elements assigned in &icinp (1-based)
+  std::map<int, int> numero;    // state numbers (default 1..metat)
+  // complete active space of lecdet = 4 (COMMON /activ/, cip/cas.f); cip's
+  // cas.f has no nemax (cipsym/cas.f:227)
   int noac = 0, nelac = 0, nusym = 1, nemax = 8;
-  std::vector<int> numac;  // active orbitals (default 1..norb)
+  bool use_nemax = true;
+  std::map<int, int> numac;  // active orbitals (default 1..norb)
   // &cipfil
   std::string f60 = "det", f40 = "ijkl", f04 = "f04", f59 = "bdvec", f33 = "ener";
 };
 
-Options read_options(const std::string& text, const std::string& dir) {
+// the names of the namelists (cip/openf.f:5-6, cip/deter.f:52-57; cipsym's
+// &icinp adds nemax, cipsym/deter.f:58)
+const std::set<std::string> kCipfilNames = {"prefix", "det",   "ijkl",  "f04",   "det1",  "ijkl1", "f041",
+                                            "ocno1",  "bdvec", "bdvec1", "ocno", "ener", "ener1"};
+const std::set<std::string> kIcinpNames = {
+    "test",  "ndiag", "isz",    "metat",  "tocom", "yprt",   "yion",   "ybrd",   "ityper", "numero",
+    "coeff", "ygen",  "title",  "tau",    "ymoyen", "aval",  "nclass", "ytoul",  "lecdet", "tdet",
+    "maxdet", "teseff", "nvr",  "numac",  "nelac", "nusym",  "noac",   "ywvi",   "ywvf",   "ystkic",
+    "ywdeg", "ytocom", "iselec", "iord",  "twdet", "mspin",  "ydp",    "ninact", "nonact"};
+
+// nomf.f: a unit's file name is the prefix up to its first blank followed
+// by the root name (10 characters) up to its first blank -- nothing of the
+// root when its 10 characters hold no blank; a non-blank name1 (90
+// characters) replaces both (nomfil.f)
+std::string unit_file(const Namelist& cf, const char* root_key, const char* name1_key, const char* root_default,
+                      const std::string& dir) {
+  std::string f;
+  if (const std::string* v = cf.scalar(name1_key); v && v->find_first_not_of(' ') != std::string::npos) {
+    f = v->substr(0, 90);
+    while (!f.empty() && f.back() == ' ') f.pop_back();
+  } else {
+    std::string prefix, root = root_default;
+    if (const std::string* p = cf.scalar("prefix")) prefix = p->substr(0, 80);
+    prefix = prefix.substr(0, prefix.find(' '));
+    if (const std::string* r = cf.scalar(root_key)) root = *r;
+    root.resize(10, ' ');
+    const size_t b = root.find(' ');
+    f = prefix + (b == std::string::npos ? std::string() : root.substr(0, b));
+  }
+  if (!f.empty() && f[0] != '/') f = dir + "/" + f;
+  return f;
+}
+
+Options read_options(const std::string& text, const std::string& dir, bool sym_variant) {
   Options o;
-  Namelist cf = parse_namelist(text, "cipfil");
-  std::string prefix;
-  if (auto v = cf.get("prefix"); v && !v->empty()) prefix = (*v)[0];
-  auto unit = [&](const char* k, const char* k1, std::string& dst) {
-    if (auto v = cf.get(k1); v && !v->empty() && !(*v)[0].empty()) {
-      dst = (*v)[0];
-    } else {
-      std::string base = dst;
-      if (auto w = cf.get(k); w && !w->empty()) base = (*w)[0];
-      while (!base.empty() && base.back() == ' ') base.pop_back();
-      dst = prefix + base;
-    }
-    if (!dst.empty() && dst[0] != '/') dst = dir + "/" + dst;
-  };
-  unit("det", "det1", o.f60);
-  unit("ijkl", "ijkl1", o.f40);
-  unit("f04", "f041", o.f04);
-  unit("bdvec", "bdvec1", o.f59);
-  unit("ener", "ener1", o.f33);
-  Namelist ic = parse_namelist(text, "icinp");
+  Namelist cf = parse_namelist(text, "cipfil", kCipfilNames);
+  o.f60 = unit_file(cf, "det", "det1", "det", dir);
+  o.f40 = unit_file(cf, "ijkl", "ijkl1", "ijkl", dir);
+  o.f04 = unit_file(cf, "f04", "f041", "f04", dir);
+  o.f59 = unit_file(cf, "bdvec", "bdvec1", "bdvec", dir);
+  o.f33 = unit_file(cf, "ener", "ener1", "ener", dir);
+  std::set<std::string> names = kIcinpNames;
+  if (sym_variant) names.insert("nemax");
+  o.use_nemax = sym_variant;
+  Namelist ic = parse_namelist(text, "icinp", names);
   if (!ic.found) throw Error("erreur dans la namelist icinp");
-  auto r1 = [&](const char* k, double& d) { if (auto v = ic.get(k); v && !v->empty()) d = to_real((*v)[0]); };
-  auto i1 = [&](const char* k, int& d) { if (auto v = ic.get(k); v && !v->empty()) d = std::stoi((*v)[0]); };
-  auto l1 = [&](const char* k, bool& d) { if (auto v = ic.get(k); v && !v->empty()) d = to_logical((*v)[0]); };
+  auto r1 = [&](const char* k, double& d) { if (auto v = ic.scalar(k)) d = to_real(*v); };
+  auto i1 = [&](const char* k, int& d) { if (auto v = ic.scalar(k)) d = to_int(*v); };
+  auto l1 = [&](const char* k, bool& d) { if (auto v = ic.scalar(k)) d = to_logical(*v); };
   r1("test", o.test); r1("teseff", o.teseff); r1("tau", o.tau); r1("tdet", o.tdet); r1("coeff", o.coeff);
   i1("isz", o.isz); i1("metat", o.metat); i1("ityper", o.ityper); i1("iselec", o.iselec);
   i1("lecdet", o.lecdet); i1("nclass", o.nclass); i1("maxdet", o.maxdet); i1("ninact", o.ninact);
-  i1("noac", o.noac); i1("nelac", o.nelac); i1("nusym", o.nusym); i1("nemax", o.nemax);
-  if (auto v = ic.get("numac"))
-    for (auto& x : *v) o.numac.push_back(std::stoi(x));
+  i1("noac", o.noac); i1("nelac", o.nelac); i1("nusym", o.nusym);
+  if (sym_variant) i1("nemax", o.nemax);
   l1("yion", o.yion); l1("ybrd", o.ybrd); l1("ymoyen", o.ymoyen); l1("ywdeg", o.ywdeg); l1("ytocom", o.ytocom);
-  if (auto v = ic.get("aval"))
-    for (size_t i = 0; i < v->size() && i < 10; ++i) o.aval[i] = to_real((*v)[i]);
-  if (auto v = ic.get("tocom"))
-    for (auto& x : *v) o.tocom.push_back(to_real(x));
-  if (auto v = ic.get("numero"))
-    for (auto& x : *v) o.numero.push_back(std::stoi(x));
-  if (auto v = ic.get("title"); v && !v->empty()) {
-    o.title = (*v)[0];
+  if (const std::string* v = ic.scalar("ydp")) o.ydp = to_logical(*v);
+  for (auto& e : ic.array("numac", 512)) o.numac[e.first] = to_int(e.second);
+  for (auto& e : ic.array("aval", 10)) o.aval[e.first - 1] = to_real(e.second);
+  for (auto& e : ic.array("tocom", 512)) o.tocom[e.first] = to_real(e.second);
+  for (auto& e : ic.array("numero", 60)) o.numero[e.first] = to_int(e.second);
+  (void)ic.array("nonact", 512);
+  (void)ic.array("mspin", 60);
+  if (const std::string* v = ic.scalar("title")) {
+    o.title = *v;
     o.title.resize(20, ' ');
   }
   if (ic.has("ygen")) throw Error("ygen given in &icinp is not supported");
   if (ic.has("iord")) throw Error("iord given in &icinp is not supported");
   if (o.lecdet == 5) o.tdet = 0.0;  // deter.f:224-226: the whole of unit 60
   return o;
+}
+
+// numero(m+1): the number printed and stored for root m (default m+1)
+int state_number(const Options& o, int m) {
+  const auto it = o.numero.find(m + 1);
+  return it != o.numero.end() ? it->second : m + 1;
 }
 
 // ------------------------------------------------------------ the run state
@@ -366,7 +492,8 @@ DetLists cas_space(Run& R) {
   if (n == 0) return L;  // no beta string: no determinant (cas.f:188-200)
   std::vector<int> act(noac);
   for (int k = 0; k < noac; ++k) {
-    act[k] = k < (int)o.numac.size() ? o.numac[k] : k + 1;  // deter.f:139 default numac(i) = i
+    const auto it = o.numac.find(k + 1);
+    act[k] = it != o.numac.end() ? it->second : k + 1;  // deter.f:139 default numac(i) = i
     if (act[k] < 1 || act[k] > R.norb) throw Error("numac names an orbital outside 1..norb");
   }
   struct Str {
@@ -401,7 +528,7 @@ DetLists cas_space(Run& R) {
       for (int x : b.t) t.push_back(x + norb);
       for (int x : b.p) p.push_back(x + norb);
       const int nec = (int)t.size();
-      if (nec > o.nemax) continue;
+      if (o.use_nemax && nec > o.nemax) continue;
       int is = 1;
       for (int i = 0; i < nec; ++i) {
         is = prod(is, R.itsym[(t[i] - 1) % norb]);
@@ -530,6 +657,7 @@ void read_inputs(Run& R, bool sym_variant) {
     for (auto& x : R.itsym) x = h.get<int32_t>();
     (void)h.get<int32_t>();
     R.ydp = h.get<uint8_t>() != 0;
+    if (o.ydp >= 0) R.ydp = o.ydp != 0;  // ydp of &icinp is read after the header (deter.f:119,222)
     if (ntrans != 0) throw Error("degeneracy operations (ntrans > 0) are not supported");
   }
   R.its.resize((size_t)R.nsym * R.nsym);
@@ -633,7 +761,8 @@ void zero_order(Run& R) {
   // faifoc.f with the occupations of cip.f:75-84
   std::vector<double> tocom(2 * R.norb, 0.0);
   for (int i = 0; i < R.noc; ++i) tocom[i] = 2.0;
-  for (size_t i = 0; i < o.tocom.size() && i < (size_t)R.norb; ++i) tocom[i] = o.tocom[i];
+  for (auto& e : o.tocom)
+    if (e.first <= R.norb) tocom[e.first - 1] = e.second;
   for (int i = 0; i < R.norb; ++i) {
     if (tocom[i] > 1.0) {
       tocom[i + R.norb] = tocom[i] - 1.0;
@@ -753,7 +882,7 @@ void write_unit4_zero_order(const Run& R) {
   for (int m = 0; m < mt; ++m) w.put<double>(R.e[m] + e0);
   for (int m = 0; m < mt; ++m) w.put<double>(R.emp[m]);
   for (int m = 0; m < mt; ++m) w.put<double>(R.eb[m]);
-  for (int m = 0; m < mt; ++m) w.put<int32_t>(m < (int)R.o.numero.size() ? R.o.numero[m] : m + 1);
+  for (int m = 0; m < mt; ++m) w.put<int32_t>(state_number(R.o, m));
   for (int k = 0; k < ncf; ++k) w.put<double>(R.empdet[k]);
   for (int i = 0; i < n; ++i) w.put<double>(R.fmpb[i]);
   for (int i = 0; i < n; ++i) w.put<double>(R.tocom[i]);
@@ -992,7 +1121,7 @@ extern "C" int cipsi_inputs_read(cipsi_inputs** out, const char* workdir, const 
     auto* h = new cipsi_inputs();
     h->sym_variant = sym_variant != 0;
     try {
-      h->R.o = read_options(ss.str(), dir);
+      h->R.o = read_options(ss.str(), dir, sym_variant != 0);
       if (h->R.o.teseff < 0.0) h->R.o.teseff = 0.05 * h->R.o.tau;
       read_inputs(h->R, sym_variant != 0);
     } catch (...) {
@@ -1155,7 +1284,8 @@ extern "C" int cipsi_cip_main(const char* workdir, const char* stdin_path, int32
     }
     std::printf(" energies CIPSI envp\n");
     for (int m = 0; m < R.metat; ++m)
-      std::printf("  %2d  %14.8f  %14.8f  %14.8f  %14.8f\n", m + 1, R.e[m], res.e2mp[m], res.e2vp[m], res.e2b[m]);
+      std::printf("  %2d  %14.8f  %14.8f  %14.8f  %14.8f\n", state_number(R.o, m), R.e[m], res.e2mp[m],
+                  res.e2vp[m], res.e2b[m]);
     std::fflush(stdout);
     // unit 33 (stkener.f: char*40 then the values, no count)
     if (std::FILE* f33 = std::fopen(R.o.f33.c_str(), "ab")) {

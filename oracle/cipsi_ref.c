@@ -141,7 +141,13 @@ static void wb_flush(FILE* f, wbuf_t* w) {
 }
 
 /* ------------------------------------------------------ namelist parsing */
-/* Minimal Fortran namelist reader: "&group key=v1,v2 ... &end" or "/". */
+/* Fortran namelist reader: "&group" up to "&end" or "/"; "name = values"
+   (names in any case) with values separated by commas and/or blanks, "r*c"
+   for r copies of c, "r*" or nothing between two commas for a null value
+   (the element keeps its value), "name(i) = values" from element i on, "!"
+   comments to the end of the line.  An item holds its elements 1..nval
+   (val[i-1], NULL where not assigned); a name outside `names` is an error,
+   as it is for the Fortran runtime (deter.f:222 -> 9500). */
 typedef struct {
   char key[64];
   int nval;
@@ -158,7 +164,25 @@ static void lower(char* s) {
   for (; *s; s++) *s = (char)tolower((unsigned char)*s);
 }
 
-static int nl_parse(const char* group, nlgroup_t* g) {
+static nlitem_t* nl_get(nlgroup_t* g, const char* key) {
+  for (int i = 0; i < g->n; i++)
+    if (strcasecmp(g->it[i].key, key) == 0) return &g->it[i];
+  return NULL;
+}
+
+static void nl_put(nlitem_t* it, int idx, const char* v) {
+  if (idx > it->nval) {
+    it->val = (char**)realloc(it->val, sizeof(char*) * (size_t)idx);
+    for (int i = it->nval; i < idx; i++) it->val[i] = NULL;
+    it->nval = idx;
+  }
+  if (v) {
+    free(it->val[idx - 1]);
+    it->val[idx - 1] = strdup(v);
+  }
+}
+
+static int nl_parse(const char* group, nlgroup_t* g, const char* const* names) {
   memset(g, 0, sizeof(*g));
   const char* t = g_stdin_text;
   size_t gl = strlen(group);
@@ -171,83 +195,140 @@ static int nl_parse(const char* group, nlgroup_t* g) {
     }
   }
   if (!p) return 0;
-  /* tokenise until &end or a bare '/' */
   char tok[4096];
-  int cur = -1;
+  nlitem_t* cur = NULL;
+  int idx = 1, need_sep = 0;
   while (*p) {
-    while (*p && (isspace((unsigned char)*p) || *p == ',')) p++;
-    if (!*p) break;
-    if (*p == '/') break;
-    if (*p == '&') break; /* &end or next group */
-    int n = 0;
+    if (isspace((unsigned char)*p)) { p++; continue; }
+    if (*p == '!') {
+      while (*p && *p != '\n') p++;
+      continue;
+    }
+    if (*p == '/' || *p == '&') break; /* &end or next group */
+    if (*p == ',') {
+      if (!need_sep && cur) nl_put(cur, idx++, NULL); /* null value */
+      need_sep = 0;
+      p++;
+      continue;
+    }
+    int n = 0, quoted = 0;
     if (*p == '\'' || *p == '"') {
       char qc = *p++;
-      while (*p && *p != qc && n < 4095) tok[n++] = *p++;
-      if (*p == qc) p++;
+      quoted = 1;
+      while (*p && n < 4095) {
+        if (*p == qc) {
+          if (p[1] == qc) { tok[n++] = qc; p += 2; continue; }
+          p++;
+          break;
+        }
+        tok[n++] = *p++;
+      }
       tok[n] = 0;
     } else {
-      while (*p && !isspace((unsigned char)*p) && *p != ',' && *p != '=' && *p != '/' &&
+      while (*p && !isspace((unsigned char)*p) && *p != ',' && *p != '=' && *p != '/' && *p != '!' &&
              n < 4095)
         tok[n++] = *p++;
       tok[n] = 0;
     }
-    /* key? */
     const char* r = p;
     while (*r && isspace((unsigned char)*r)) r++;
-    if (*r == '=') {
+    if (!quoted && *r == '=') {
       p = r + 1;
-      if (g->n >= 128) die("namelist too long");
-      cur = g->n++;
-      snprintf(g->it[cur].key, sizeof g->it[cur].key, "%.60s", tok);
-      lower(g->it[cur].key);
+      lower(tok);
+      idx = 1;
+      char* lp = strchr(tok, '(');
+      if (lp) {
+        idx = atoi(lp + 1);
+        *lp = 0;
+        if (idx < 1) die("erreur dans la namelist %s: bad subscript", group);
+      }
+      int known = 0;
+      for (const char* const* nm = names; *nm; nm++)
+        if (!strcmp(*nm, tok)) known = 1;
+      if (!known) die("erreur dans la namelist %s: unknown name %s", group, tok);
+      cur = nl_get(g, tok);
+      if (!cur) {
+        if (g->n >= 128) die("namelist too long");
+        cur = &g->it[g->n++];
+        snprintf(cur->key, sizeof cur->key, "%.60s", tok);
+      }
+      need_sep = 0;
       continue;
     }
-    if (cur < 0) die("namelist &%s: value without key: %s", group, tok);
-    nlitem_t* it = &g->it[cur];
-    it->val = (char**)realloc(it->val, sizeof(char*) * (size_t)(it->nval + 1));
-    it->val[it->nval++] = strdup(tok);
+    if (!cur) die("namelist &%s: value without key: %s", group, tok);
+    char* star = quoted ? NULL : strchr(tok, '*');
+    int digits = star && star > tok;
+    for (char* c = tok; digits && c < star; c++)
+      if (!isdigit((unsigned char)*c)) digits = 0;
+    if (digits) { /* r*c or r* */
+      int rep = atoi(tok);
+      char* c = star + 1;
+      size_t cl = strlen(c);
+      if (cl >= 2 && (c[0] == '\'' || c[0] == '"') && c[cl - 1] == c[0]) {
+        c[cl - 1] = 0;
+        c++;
+      }
+      for (int q = 0; q < rep; q++) nl_put(cur, idx++, *c ? c : NULL);
+    } else {
+      nl_put(cur, idx++, (quoted && !n) ? " " : tok);
+    }
+    need_sep = 1;
   }
   return 1;
 }
-static nlitem_t* nl_get(nlgroup_t* g, const char* key) {
-  for (int i = g->n - 1; i >= 0; i--) /* a repeated key: the last one wins */
-    if (strcasecmp(g->it[i].key, key) == 0) return &g->it[i];
-  return NULL;
-}
 static double nl_real(const char* s) {
-  char b[128];
+  char b[128], *end;
   snprintf(b, sizeof b, "%s", s);
   for (char* c = b; *c; c++)
     if (*c == 'd' || *c == 'D') *c = 'e';
-  return strtod(b, NULL);
+  double v = strtod(b, &end);
+  if (end == b || *end) die("erreur dans la namelist icinp: bad real value %s", s);
+  return v;
+}
+static int nl_integer(const char* s) {
+  char* end;
+  long v = strtol(s, &end, 10);
+  if (end == s || *end) die("erreur dans la namelist icinp: bad integer value %s", s);
+  return (int)v;
 }
 static int nl_logical(const char* s) {
   while (*s == '.') s++;
+  if (!*s || !strchr("tTfF", *s)) die("erreur dans la namelist icinp: bad logical value %s", s);
   return *s == 't' || *s == 'T';
 }
-static void nl_set_int(nlgroup_t* g, const char* k, int* dst) {
+/* the value of a scalar, or NULL */
+static const char* nl_scalar(nlgroup_t* g, const char* k) {
   nlitem_t* it = nl_get(g, k);
-  if (it && it->nval) *dst = (int)strtol(it->val[0], NULL, 10);
+  if (!it || !it->nval) return NULL;
+  if (it->nval > 1) die("erreur dans la namelist: too many values for %s", k);
+  return it->val[0];
+}
+static void nl_set_int(nlgroup_t* g, const char* k, int* dst) {
+  const char* v = nl_scalar(g, k);
+  if (v) *dst = nl_integer(v);
 }
 static void nl_set_real(nlgroup_t* g, const char* k, double* dst) {
-  nlitem_t* it = nl_get(g, k);
-  if (it && it->nval) *dst = nl_real(it->val[0]);
+  const char* v = nl_scalar(g, k);
+  if (v) *dst = nl_real(v);
 }
 static void nl_set_log(nlgroup_t* g, const char* k, int* dst) {
-  nlitem_t* it = nl_get(g, k);
-  if (it && it->nval) *dst = nl_logical(it->val[0]);
+  const char* v = nl_scalar(g, k);
+  if (v) *dst = nl_logical(v);
 }
-static int nl_set_real_arr(nlgroup_t* g, const char* k, double* dst, int max) {
+/* array elements 1..bound: dst[i-1] for the assigned i <= napply */
+static void nl_set_real_arr(nlgroup_t* g, const char* k, double* dst, int napply, int bound) {
   nlitem_t* it = nl_get(g, k);
-  if (!it) return 0;
-  for (int i = 0; i < it->nval && i < max; i++) dst[i] = nl_real(it->val[i]);
-  return it->nval;
+  if (!it) return;
+  if (it->nval > bound) die("erreur dans la namelist: %s has more than %d elements", k, bound);
+  for (int i = 0; i < it->nval && i < napply; i++)
+    if (it->val[i]) dst[i] = nl_real(it->val[i]);
 }
-static int nl_set_int_arr(nlgroup_t* g, const char* k, int* dst, int max) {
+static void nl_set_int_arr(nlgroup_t* g, const char* k, int* dst, int napply, int bound) {
   nlitem_t* it = nl_get(g, k);
-  if (!it) return 0;
-  for (int i = 0; i < it->nval && i < max; i++) dst[i] = (int)strtol(it->val[i], NULL, 10);
-  return it->nval;
+  if (!it) return;
+  if (it->nval > bound) die("erreur dans la namelist: %s has more than %d elements", k, bound);
+  for (int i = 0; i < it->nval && i < napply; i++)
+    if (it->val[i]) dst[i] = nl_integer(it->val[i]);
 }
 
 /* ------------------------------------------------------------ the state */
@@ -1624,7 +1705,7 @@ static void cas(void) {
       int nect = kta + ktb, necp = kpa + kpb;
       if (nect != necp) die("  attention necp et nect sont differents %d %d", nect, necp);
       int nec = necp;
-      if (nec > nemax) continue;
+      if (g_sym_variant && nec > nemax) continue; /* cip/cas.f has no nemax */
       int is = 1;
       for (int i = 1; i <= nec; i++) {
         int jps = itsym[nps[i]];
@@ -1974,19 +2055,30 @@ static char* read_all(FILE* f) {
   return b;
 }
 
+/* nomfil.f / nomf.f: a non-blank name1 (90 characters) is the file name;
+   otherwise the prefix (80 characters) up to its first blank followed by
+   the root name (10 characters) up to its first blank -- nothing of the
+   root when its 10 characters hold no blank */
 static void unit_name(nlgroup_t* g, const char* key, const char* key1, const char* def,
                       const char* prefix, char* out, size_t outsz) {
-  nlitem_t* it1 = nl_get(g, key1);
-  if (it1 && it1->nval && it1->val[0][0]) {
-    snprintf(out, outsz, "%s", it1->val[0]);
+  const char* v1 = nl_scalar(g, key1);
+  if (v1 && strspn(v1, " ") < strlen(v1)) {
+    snprintf(out, outsz, "%.90s", v1);
+    size_t l = strlen(out);
+    while (l && out[l - 1] == ' ') out[--l] = 0;
     return;
   }
-  nlitem_t* it = nl_get(g, key);
-  const char* r = (it && it->nval) ? it->val[0] : def;
-  snprintf(out, outsz, "%s%s", prefix, r);
-  /* trim trailing blanks */
-  size_t l = strlen(out);
-  while (l && out[l - 1] == ' ') out[--l] = 0;
+  const char* r = nl_scalar(g, key);
+  char root[11];
+  snprintf(root, sizeof root, "%-10.10s", r ? r : def);
+  char* b = strchr(root, ' ');
+  if (b) *b = 0;
+  else root[0] = 0;
+  char pre[81];
+  snprintf(pre, sizeof pre, "%.80s", prefix);
+  char* pb = strchr(pre, ' ');
+  if (pb) *pb = 0;
+  snprintf(out, outsz, "%s%s", pre, root);
 }
 
 static double now_s(void) {
@@ -2024,13 +2116,13 @@ int main(int argc, char** argv) {
 
   /* openf.f */
   nlgroup_t gf;
-  nl_parse("cipfil", &gf);
+  static const char* const cipfil_names[] = {"prefix", "det", "ijkl", "f04", "det1", "ijkl1", "f041",
+                                             "ocno1", "bdvec", "bdvec1", "ocno", "ener", "ener1", NULL};
+  nl_parse("cipfil", &gf, cipfil_names);
   char prefix[256] = "";
   {
-    nlitem_t* it = nl_get(&gf, "prefix");
-    if (it && it->nval) snprintf(prefix, sizeof prefix, "%s", it->val[0]);
-    size_t l = strlen(prefix);
-    while (l && prefix[l - 1] == ' ') prefix[--l] = 0;
+    const char* v = nl_scalar(&gf, "prefix");
+    if (v) snprintf(prefix, sizeof prefix, "%s", v);
   }
   char n60[512], n40[512], n04[512], n21[512], n59[512], n33[512];
   unit_name(&gf, "det", "det1", "det", prefix, n60, sizeof n60);
@@ -2091,33 +2183,33 @@ int main(int argc, char** argv) {
   for (int i = 1; i <= norb; i++) numac[i] = i; /* deter.f:139 */
   noac = 0; nusym = 1; nelac = 0; nemax = 8;
   nlgroup_t gi;
-  if (!nl_parse("icinp", &gi)) die("erreur dans la namelist icinp");
+  /* deter.f:52-58 (cipsym adds nemax) */
+  static const char* const icinp_names[] = {
+      "test", "ndiag", "isz", "metat", "tocom", "yprt", "yion", "ybrd", "ityper", "numero", "coeff",
+      "ygen", "title", "tau", "ymoyen", "aval", "nclass", "ytoul", "lecdet", "tdet", "maxdet", "teseff",
+      "nvr", "numac", "nelac", "nusym", "noac", "ywvi", "ywvf", "ystkic", "ywdeg", "ytocom", "iselec",
+      "iord", "twdet", "mspin", "ydp", "ninact", "nonact", "nemax", NULL};
+  static const char* const icinp_names_cip[] = {
+      "test", "ndiag", "isz", "metat", "tocom", "yprt", "yion", "ybrd", "ityper", "numero", "coeff",
+      "ygen", "title", "tau", "ymoyen", "aval", "nclass", "ytoul", "lecdet", "tdet", "maxdet", "teseff",
+      "nvr", "numac", "nelac", "nusym", "noac", "ywvi", "ywvf", "ystkic", "ywdeg", "ytocom", "iselec",
+      "iord", "twdet", "mspin", "ydp", "ninact", "nonact", NULL};
+  if (!nl_parse("icinp", &gi, g_sym_variant ? icinp_names : icinp_names_cip))
+    die("erreur dans la namelist icinp");
   nl_set_real(&gi, "test", &test);
   nl_set_int(&gi, "ndiag", &ndiag);
   nl_set_int(&gi, "isz", &isz);
   nl_set_int(&gi, "metat", &metat);
-  {
-    double tc[512];
-    int n = nl_set_real_arr(&gi, "tocom", tc, 512);
-    for (int i = 0; i < n && i < norb; i++) tocom[i + 1] = tc[i];
-  }
+  nl_set_real_arr(&gi, "tocom", tocom + 1, norb, 512);
   nl_set_log(&gi, "yprt", &yprt);
   nl_set_log(&gi, "yion", &yion);
   nl_set_log(&gi, "ybrd", &ybrd);
   nl_set_int(&gi, "ityper", &ityper);
-  {
-    int nu[64];
-    int n = nl_set_int_arr(&gi, "numero", nu, 60);
-    for (int i = 0; i < n; i++) numero[i + 1] = nu[i];
-  }
+  nl_set_int_arr(&gi, "numero", numero + 1, 60, 60);
   nl_set_real(&gi, "coeff", &coeff);
   nl_set_real(&gi, "tau", &tau);
   nl_set_log(&gi, "ymoyen", &ymoyen);
-  {
-    double av[16];
-    int n = nl_set_real_arr(&gi, "aval", av, 10);
-    for (int i = 0; i < n; i++) aval[i + 1] = av[i];
-  }
+  nl_set_real_arr(&gi, "aval", aval + 1, 10, 10);
   nl_set_int(&gi, "nclass", &nclass);
   nl_set_log(&gi, "ytoul", &ytoul);
   nl_set_int(&gi, "lecdet", &lecdet);
@@ -2133,22 +2225,23 @@ int main(int argc, char** argv) {
   nl_set_real(&gi, "twdet", &twdet);
   nl_set_int(&gi, "ninact", &ninact);
   {
-    nlitem_t* t = nl_get(&gi, "title");
-    if (t && t->nval) snprintf(title, sizeof title, "%-20.20s", t->val[0]);
+    const char* t = nl_scalar(&gi, "title");
+    if (t) snprintf(title, sizeof title, "%-20.20s", t);
   }
+  nl_set_log(&gi, "ydp", &ydp); /* after the unit-40 header (deter.f:119,222) */
   int nonact[512] = {0};
-  nl_set_int_arr(&gi, "nonact", nonact, 512);
+  nl_set_int_arr(&gi, "nonact", nonact, 512, 512);
+  {
+    int ms[64];
+    nl_set_int_arr(&gi, "mspin", ms, 0, 60);
+  }
   if (nl_get(&gi, "ygen")) die("ygen given in the namelist is not restated");
   if (nl_get(&gi, "iord")) die("iord given in the namelist is not restated");
   nl_set_int(&gi, "noac", &noac);
   nl_set_int(&gi, "nelac", &nelac);
   nl_set_int(&gi, "nusym", &nusym);
-  nl_set_int(&gi, "nemax", &nemax);
-  {
-    int nu[520];
-    int n = nl_set_int_arr(&gi, "numac", nu, 512);
-    for (int i = 0; i < n; i++) numac[i + 1] = nu[i];
-  }
+  if (g_sym_variant) nl_set_int(&gi, "nemax", &nemax);
+  nl_set_int_arr(&gi, "numac", numac + 1, 512, 512);
 
   if (teseff < 0.0) teseff = 0.05 * tau;
   if (lecdet == 5) tdet = 0.0;
