@@ -710,6 +710,47 @@ void read_inputs(Run& R, bool sym_variant) {
   zero_order(R);
 }
 
+// degen (brdnee.f:299-365), called by ic001 once the vectors are read: a
+// root m whose energy is within 1e-6 of the next root's, and not of the one
+// after (a run of exactly two; the scan never pairs the last two roots, and
+// longer runs are left alone), is rotated with root m+1 by the angle that
+// gives the first spin-flip pair of unequal weights on root m equal weights
+// (to 1e-4), if such a pair exists.
+void rotate_degenerate_roots(Run& R) {
+  const int ncf = R.ncf, metat = R.metat;
+  const auto& e = R.e;
+  int last = -1;  // 0-based index of the last root of the latest degenerate run
+  for (int m = 0; m + 1 < metat; ++m) {
+    if (m <= last) continue;
+    int n = m + 1;
+    while (n < metat && std::fabs(e[n] - e[m]) <= 1.0e-6) ++n;
+    last = n == metat ? n - 2 : n - 1;  // a run reaching the last root ends one early
+    if (last != m + 1) continue;        // no pair, or more than two degenerate roots
+    double* c1v = R.c.data() + (size_t)m * ncf;
+    double* c2v = c1v + ncf;
+    bool rotated = false;
+    for (int k = 0; k < ncf && !rotated; ++k) {
+      if (R.S.ysaut[k] || R.S.nesp[k] == 0) continue;
+      for (int ll = 1; ll <= R.S.nesp[k]; ++ll) {
+        const double c11 = c1v[k], c12 = c1v[k + ll];
+        if (std::fabs(std::fabs(c11) - std::fabs(c12)) < 1.0e-5) continue;
+        const double c21 = c2v[k], c22 = c2v[k + ll], cc = c21 + c22;
+        if (std::fabs(cc) < 1.0e-8) continue;
+        const double phi = std::atan(-(c11 + c12) / cc), cs = std::cos(phi), si = std::sin(phi);
+        const double a1 = std::fabs(c11 * cs + c21 * si), a2 = std::fabs(c12 * cs + c22 * si);
+        if (std::fabs(a1 - a2) >= 1.0e-4) continue;
+        for (int i = 0; i < ncf; ++i) {
+          const double a = c1v[i] * cs + c2v[i] * si;
+          c2v[i] = -c1v[i] * si + c2v[i] * cs;
+          c1v[i] = a;
+        }
+        rotated = true;
+        break;
+      }
+    }
+  }
+}
+
 // ic001.f:44-76 (lecdet = 5): the vectors and energies of S from unit 59,
 // in the order of unit 4's iord60 for cip; generators from them
 void read_vectors(Run& R, bool sym_variant) {
@@ -742,9 +783,7 @@ void read_vectors(Run& R, bool sym_variant) {
       for (int k = 0; k < R.ncf; ++k) R.c[(size_t)m * R.ncf + k] = tmp[k];
     }
   }
-  for (int m = 0; m + 1 < R.metat; ++m)
-    if (std::fabs(R.e[m + 1] - R.e[m]) <= 1.0e-6)
-      throw Error("degenerate roots: the rotation of brdnee.f:299 is not supported");
+  rotate_degenerate_roots(R);
   for (int k = 0; k < R.ncf; ++k) {
     if (sym_variant) {
       R.S.ygen[k] = 1;

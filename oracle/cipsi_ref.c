@@ -25,7 +25,7 @@
  *   CIPSI_sources/cipsym/shell.f, cip.f:200-236   the run that only writes
  *                                S (ityper<0): energy order, units 4 and 60
  *   CIPSI_sources/cip/ijkf.f, reijkl.f, rdener.f, ic001.f:44-76 (lecdet=5),
- *   CIPSI_sources/cip/brdnee.f:299-365 (degen)
+ *   CIPSI_sources/cip/brdnee.f:299-365 (degen, the rotation of degenerate roots)
  *   CIPSI_sources/cip/faifoc.f, hmp.f, hdig.f, hntd.f, ai.f
  *   CIPSI_sources/cip/pertu.f, igene.f, cotra.f, pert1.f, diexcit.f,
  *   CIPSI_sources/cip/isto.f, pie.f, stkener.f
@@ -2449,7 +2449,42 @@ int main(int argc, char** argv) {
           printf(" attention degenerescence multiple\n");
           continue;
         }
-        die("degenerate roots (|e(m)-e(m+1)|<=1e-6): rotation not restated");
+        /* brdnee.f:420-480: the first spin-flip pair whose weights differ on
+           root m and whose rotation by atan(-(c11+c12)/(c21+c22)) makes
+           them equal (to 1e-4) rotates roots m and m+1 */
+        int mncf1 = m * ncf - ncf, mncf2 = mncf1 + ncf;
+        for (int k = 1; k <= ncf; k++) {
+          if (ysaut[k]) continue;
+          int nespk = nesp[k];
+          if (nespk == 0) continue;
+          int done = 0;
+          for (int ll = 1; ll <= nespk; ll++) {
+            double c11 = c[mncf1 + k], c12 = c[mncf1 + k + ll];
+            double c1 = fabs(c11), c2 = fabs(c12);
+            if (fabs(c1 - c2) < 1.0e-5) continue;
+            double c21 = c[mncf2 + k], c22 = c[mncf2 + k + ll];
+            double cc = c21 + c22;
+            if (fabs(cc) < 1.0e-8) continue;
+            double tgphi = -(c11 + c12) / cc;
+            double phi = atan(tgphi);
+            double cs = cos(phi), si = sin(phi);
+            c1 = c11 * cs + c21 * si;
+            c2 = c12 * cs + c22 * si;
+            c1 = fabs(c1);
+            c2 = fabs(c2);
+            double c3 = fabs(c1 - c2);
+            if (c3 >= 1.0e-4) continue;
+            printf(" les etats %2d et %2d sont degeneres: symmetrisation par rotation\n", m, mn1);
+            for (int i = 1; i <= ncf; i++) {
+              double a = c[mncf1 + i] * cs + c[mncf2 + i] * si;
+              c[mncf2 + i] = -c[mncf1 + i] * si + c[mncf2 + i] * cs;
+              c[mncf1 + i] = a;
+            }
+            done = 1;
+            break;
+          }
+          if (done) break;
+        }
       }
     }
     /* ygen: cipsym makes every determinant a generator (cipsym/ic001.f:179);
