@@ -275,7 +275,7 @@ struct Options {
   bool use_nemax = true;
   std::map<int, int> numac;  // active orbitals (default 1..norb)
   // &cipfil
-  std::string f60 = "det", f40 = "ijkl", f04 = "f04", f59 = "bdvec", f33 = "ener";
+  std::string f60 = "det", f40 = "ijkl", f04 = "f04", f59 = "bdvec", f33 = "ener", f21 = "ocno";
 };
 
 // the names of the namelists (cip/openf.f:5-6, cip/deter.f:52-57; cipsym's
@@ -319,6 +319,7 @@ Options read_options(const std::string& text, const std::string& dir, bool sym_v
   o.f04 = unit_file(cf, "f04", "f041", "f04", dir);
   o.f59 = unit_file(cf, "bdvec", "bdvec1", "bdvec", dir);
   o.f33 = unit_file(cf, "ener", "ener1", "ener", dir);
+  o.f21 = unit_file(cf, "ocno", "ocno1", "ocno", dir);
   std::set<std::string> names = kIcinpNames;
   if (sym_variant) names.insert("nemax");
   o.use_nemax = sym_variant;
@@ -383,6 +384,7 @@ struct Run {
   std::vector<double> c, e, eb, emp, teste, taum, fmpb, fdiag;
   std::vector<double> tocom, empdet;  // faifoc.f occupations (after cip.f:75-84), hmp of S
   std::vector<double> hdiag;          // hdig of S
+  std::vector<double> tocom21;        // occupations read from unit 21 (ytocom)
 };
 
 // transf.f: sort, validate, dedup and append one determinant
@@ -640,7 +642,6 @@ void read_inputs(Run& R, bool sym_variant) {
   if (o.isz != 0) throw Error("only isz = 0 is supported");
   if (o.ybrd && o.metat > 1) throw Error("ybrd (QDPT effective Hamiltonian) is not supported");
   if (o.ninact > 0) throw Error("ninact > 0 (restricted perturbation space) is not supported");
-  if (o.ytocom) throw Error("ytocom (occupations from unit 21) is not supported");
   if (o.lecdet < 2 || o.lecdet > 5) throw Error("lecdet 1 (determinants on cards) is not supported");
   if (o.ityper >= 0 && o.lecdet != 5)
     throw Error("a perturbation run needs lecdet = 5 (vectors of S read from unit 59)");
@@ -683,6 +684,12 @@ void read_inputs(Run& R, bool sym_variant) {
   for (size_t b = 0; b < nbuf; ++b)
     for (int i = 0; i < 8192 && pos < (size_t)ninte; ++i, ++pos)
       R.eri[pos] = R.ydp ? (float)recs[8 + b].get<double>() : recs[8 + b].get<float>();
+  if (o.ytocom) {  // deter.f:228-229: Fock-operator occupations from unit 21
+    auto r21 = read_records(o.f21);
+    if (r21.empty()) throw Error("unit 21: no occupation record");
+    R.tocom21.resize(R.norb);
+    for (auto& x : R.tocom21) x = r21[0].get<double>();
+  }
   R.fdiag.assign(2 * R.norb, 0.0);
   for (int i = 1; i <= R.norb; ++i) R.fdiag[i - 1] = R.fdiag[i - 1 + R.norb] = R.F[(size_t)i * (i + 1) / 2 - 1];
 
@@ -802,6 +809,7 @@ void zero_order(Run& R) {
   for (int i = 0; i < R.noc; ++i) tocom[i] = 2.0;
   for (auto& e : o.tocom)
     if (e.first <= R.norb) tocom[e.first - 1] = e.second;
+  for (size_t i = 0; i < R.tocom21.size(); ++i) tocom[i] = R.tocom21[i];
   for (int i = 0; i < R.norb; ++i) {
     if (tocom[i] > 1.0) {
       tocom[i + R.norb] = tocom[i] - 1.0;

@@ -2131,7 +2131,6 @@ int main(int argc, char** argv) {
   unit_name(&gf, "ocno", "ocno1", "ocno", prefix, n21, sizeof n21);
   unit_name(&gf, "bdvec", "bdvec1", "bdvec", prefix, n59, sizeof n59);
   unit_name(&gf, "ener", "ener1", "ener", prefix, n33, sizeof n33);
-  (void)n21;
 
   FILE* f40 = fopen(n40, "rb");
   if (!f40) die("cannot open unit 40 file %s", n40);
@@ -2245,7 +2244,15 @@ int main(int argc, char** argv) {
 
   if (teseff < 0.0) teseff = 0.05 * tau;
   if (lecdet == 5) tdet = 0.0;
-  if (ytocom) die("ytocom (unit 21 occupations) is not restated");
+  if (ytocom) { /* deter.f:228-229: occupations of the Fock operator from unit 21 */
+    FILE* f21 = fopen(n21, "rb");
+    if (!f21) die("cannot open unit 21 file %s", n21);
+    rec_t r21 = {0};
+    if (!rec_read(f21, &r21)) die("unit 21: no occupation record");
+    for (int i = 1; i <= norb; i++) tocom[i] = rec_r8(&r21);
+    free(r21.b);
+    fclose(f21);
+  }
   if (ityper == 0) ypertu = 0;
   if (ityper == 1) yen = 0;
   if (ityper == 2) yen = 1;

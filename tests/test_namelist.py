@@ -143,3 +143,43 @@ def test_cip_variant_cas_has_no_nemax_filter(tmp_path, engine_lib, oracle_exe):
     dc = _unit60_dets(os.path.join(f"{wd}_sym2_engine", "det"), 1, True)
     assert da == db and len(dc) < len(db) and all(len(h) <= 2 for h, _ in dc)
     assert a["f04"] == b["f04"]
+
+
+def _fmpb_model(wd, tocom_in, noca):
+    """faifoc.f from the closed-shell F, J, K of unit 40 and the occupations
+    transformed as cip.f:75-85 does (numpy restatement)."""
+    from test_autocip_s_runs import _fjk
+    F, J, K, _, _ = _fjk(wd)
+    n = F.shape[0]
+    ta, tb = np.zeros(n), np.zeros(n)
+    for i in range(n):
+        if tocom_in[i] > 1.0:
+            ta[i], tb[i] = 1.0, tocom_in[i] - 1.0
+        else:
+            ta[i], tb[i] = tocom_in[i], 0.0
+    ta[:noca] -= 1.0
+    tb[:noca] -= 1.0
+    t = np.diag(F) + J @ (ta + tb)
+    return 0.5 * ((t - K @ ta) + (t - K @ tb))
+
+
+def test_ytocom_reads_the_occupations_of_unit21(tmp_path, engine_lib, oracle_exe):
+    from cipsi_gb300 import engine
+    wd, cfg = _case(tmp_path)
+    occ = np.full(cfg.norb, 0.0)
+    occ[:cfg.nocc] = 2.0
+    occ[cfg.nocc - 1], occ[cfg.nocc] = 1.5, 0.5  # fractional frontier occupations
+    with open(os.path.join(wd, "ocno"), "wb") as fh:
+        synth.write_record(fh, occ.astype("<f8").tobytes())
+    body = f"  metat={cfg.metat}, ityper=-1, lecdet=5, ymoyen=t, ytocom=t, tocom=3*1.0"
+    a = _files_after(wd, body, "ocno")  # byte-equal with the oracle
+    b = _files_after(wd, f"  metat={cfg.metat}, ityper=-1, lecdet=5, ymoyen=t", "plain")
+    assert a["f04"] != b["f04"] and a["det"] == b["det"]
+    # the file wins over the namelist's tocom (read after it, deter.f:229)
+    _write(wd, body.replace("ityper=-1", "ityper=2"))
+    inp = engine.Inputs(wd)
+    fmpb = inp.array("fmpb")
+    inp.close()
+    want = _fmpb_model(wd, occ, cfg.nocc)
+    np.testing.assert_allclose(fmpb[:cfg.norb], want, rtol=0, atol=1e-12)
+    np.testing.assert_array_equal(fmpb[:cfg.norb], fmpb[cfg.norb:])
