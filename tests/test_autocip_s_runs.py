@@ -265,3 +265,34 @@ def test_s_run_rejects_what_it_does_not_support(tmp_path, engine_lib, oracle_exe
     with open(os.path.join(wd, "cip.in")) as fin:
         r = subprocess.run([ob.build(), "--sym"], cwd=wd, stdin=fin, capture_output=True, text=True)
     assert r.returncode != 0
+
+
+def test_executable_takes_the_autocip_s_only_call(tmp_path, engine_lib, oracle_exe):
+    """The process-level drop-in, as the driver calls it
+    (`cip_gpu --sym < f_bd > listing`, Autocip_13/calcul.f90:320), on the
+    first call of the loop: the CAS with ITYPER=-1, the namelist laid out as
+    makedata_cip.f90:201-221 writes it."""
+    import subprocess
+    from cipsi_gb300 import EXE_PATH
+    from oracle import build as ob
+    cfg = synth.SynthConfig("exe", norb=12, nocc=4, ncholesky=12, ncf=10, metat=3, tau=0.02,
+                            ranks=(1, 2), coef_mode="decay09", seed=51, nsym=2)
+    wd = str(tmp_path / "exe")
+    synth.generate(cfg, wd)
+    for u in ("det", "bdvec", "f04"):
+        os.remove(os.path.join(wd, u))
+    text = ("&cipfil\nprefix='',\nf04='f04',\n bdvec='bdvec',\n&END\n\n"
+            "&icinp\nNUMAC=3,4,5,6,7,8,9,\ntwdet=0.5\n ISZ=0,\n NUSYM=1,\n NOAC=7,\n METAT=3,\n"
+            " LECDET=4,\n ITYPER=-1,\n YMOYEN=T,\n NELAC=4,\n YBRD=F,\n NEMAX=4,\n YION=F,\n"
+            " ISELEC=  1,\n TEST=0d0,\n TAU=0d0,\n&END\n\n&MOYFIL\n&end\n")
+    with open(os.path.join(wd, "cip.in"), "w") as fh:
+        fh.write(text)
+    wo = wd + "_oracle"
+    shutil.copytree(wd, wo)
+    with open(os.path.join(wd, "cip.in")) as fin:
+        r = subprocess.run([EXE_PATH, "--sym"], cwd=wd, stdin=fin, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    ob.run(wo, variant="cipsym")
+    for unit in ("det", "f04"):
+        assert _same_file(os.path.join(wo, unit), os.path.join(wd, unit)), unit
+    assert len(_unit60_dets(os.path.join(wd, "det"), 3, True)) > 100
