@@ -8,13 +8,19 @@ F, J, K), and the textbook partitions of pert1.f:148-191 --
     E2_ENb(m)  = sum_I (1 + fmul_I) b_m^2 / (eb_m - hdig(I))
 
 with emp_m = sum_k c_km^2 hmp(k), eb_m = sum_k c_km^2 hdig(k) over S
-(cip.f:99-120).  Together with the set and coupling checks of
+(cip.f:99-120); and the selection of pert1.f:192-264: the unit-60 value
+xam = max_m |b_m / (e_m - hdig(I))| taum_m of every perturber, the
+near-degeneracy flag (|denominator| <= 0.05 with |term| >= 1e-6 selects it),
+dpivot, and the set written to unit 60 (values within 1e-9 of tau exempt).
+Together with the set and coupling checks of
 test_oracle_semantics this pins the oracle's arithmetic, not only its
 enumeration.  Tolerance: 1e-10 Eh plus the oracle's first-order rounding
 bound of each sum (cond_e2*), which is tiny on the well-conditioned systems
 (virtual orbitals shifted up) and covers the near-zero denominators of the
 plain recipe."""
+import collections
 import json
+import os
 
 import numpy as np
 import pytest
@@ -24,6 +30,7 @@ from cases import small_cases
 from cipsi_gb300 import synth
 from conftest import copy_dir
 from oracle import build as ob
+from test_autocip_chain import _all_records
 
 
 def _gap(seed, ranks, nsym):
@@ -40,7 +47,7 @@ def test_oracle_e2_matches_bruteforce_sums(tmp_path, oracle_exe, name, cfg):
     wd = str(tmp_path / "in")
     synth.generate(cfg, wd)
     run = copy_dir(wd, str(tmp_path / "run"))
-    jo = json.load(open(ob.run(run, variant="cipsym")))
+    jo = json.load(open(ob.run(run, variant="cipsym", candlog="cand.bin")))
     inp = bf.read_inputs(wd)
     model = bf.Model(inp)
     metat = inp.C.shape[1]
@@ -52,17 +59,53 @@ def test_oracle_e2_matches_bruteforce_sums(tmp_path, oracle_exe, name, cfg):
     np.testing.assert_allclose(jo["emp"], emp, rtol=1e-12, atol=1e-12)
     np.testing.assert_allclose(jo["eb"], eb, rtol=1e-12, atol=1e-12)
     e = np.asarray(inp.E)
+    # selection thresholds of cip.f:104-135 (iselec = 1): teste = t * test,
+    # taum = 1 / t with t the largest |c| of the root
+    t = np.abs(inp.C).max(axis=0)
+    teste, taum = t * inp.test, 1.0 / t
+    assert inp.ityper == 2 and inp.iselec == 1
     e2 = {k: np.zeros(metat) for k in ("e2mp", "e2vp", "e2b")}
     n = 0
+    dpivot = 0.0
+    xam_of, selected, near = {}, [], set()
     for src, k, x, nmul, fmul, b in bf.enumerate_semantic(inp, model):
         hmp, hdig = model.hmp_hdig(x)
         w = 1.0 + fmul
-        b2 = np.asarray(b) ** 2
+        b = np.asarray(b)
+        b2 = b ** 2
         e2["e2mp"] += w * b2 / (emp - hmp)
         e2["e2vp"] += w * b2 / (e - hdig)
         e2["e2b"] += w * b2 / (eb - hdig)
         n += 1
+        # pert1.f:192-244 with yen (EN eigenvalue partition sets the value)
+        dvp = e - hdig
+        cvp = b / dvp
+        xim = np.abs(cvp)
+        ydeg = bool(np.any((np.abs(dvp) <= 0.05) & (np.abs(b * cvp) >= 1e-6)))
+        below = xim < teste
+        if np.any(below):
+            dpivot = max(dpivot, float(xim[below].max()))
+        xam = float((xim * taum).max())
+        xam_of[(src, k, x)] = xam
+        v = 1.0 if ydeg else xam
+        if abs(v - inp.tau) <= 1e-9 * inp.tau:
+            near.add(x)
+        elif v > inp.tau:
+            selected.append(x)
     assert n == jo["n_processed"]
     for key, val in e2.items():
         tol = 1e-10 + np.asarray(jo["cond_" + key]) + 1e-12 * np.abs(val)
         assert np.all(np.abs(np.asarray(jo[key]) - val) <= tol), (key, jo[key], val, tol)
+    # the unit-60 value of every perturber, dpivot, and the selected set
+    ora = bf.read_candlog(os.path.join(run, "cand.bin"), metat)
+    for r in ora:
+        got = r[6]
+        want = xam_of[(r[0], r[1], model.to_bits(r[2], r[3]))]
+        assert abs(got - want) <= 1e-9 * abs(want) + 1e-300, (r[:4], got, want)
+    assert jo["dpivot"] == pytest.approx(dpivot, rel=1e-9, abs=1e-15)
+    recs = [d for d, _ in _all_records(synth.read_records(os.path.join(run, "det")), metat)]
+    got_sel = collections.Counter(model.to_bits(h, p) for h, p in recs[jo["ncf"]:])
+    want_sel = collections.Counter(selected)
+    for x in near:
+        got_sel.pop(x, None)
+    assert got_sel == want_sel
