@@ -11,7 +11,8 @@ with emp_m = sum_k c_km^2 hmp(k), eb_m = sum_k c_km^2 hdig(k) over S
 (cip.f:99-120); and the selection of pert1.f:192-264: the unit-60 value
 xam = max_m |b_m / (e_m - hdig(I))| taum_m of every perturber, the
 near-degeneracy flag (|denominator| <= 0.05 with |term| >= 1e-6 selects it),
-dpivot, and the set written to unit 60 (values within 1e-9 of tau exempt).
+dpivot, and the set written to unit 60 (values within 1e-9 of tau exempt);
+the norms psimp / psivp, ietat, and the histogram of isto.f.
 Together with the set and coupling checks of
 test_oracle_semantics this pins the oracle's arithmetic, not only its
 enumeration.  Tolerance: 1e-10 Eh plus the oracle's first-order rounding
@@ -68,6 +69,19 @@ def test_oracle_e2_matches_bruteforce_sums(tmp_path, oracle_exe, name, cfg):
     n = 0
     dpivot = 0.0
     xam_of, selected, near = {}, [], set()
+    psi = {"psimp": np.zeros(metat), "psivp": np.zeros(metat)}
+    ietat = 0
+    # isto.f: classes bounded by aval (deter.f:199-211 defaults), teseff = 0.05 tau
+    aval = np.array([0.128e-6, 0.64e-6, 0.32e-5, 0.16e-4, 0.8e-4, 0.4e-3, 0.2e-2, 0.1e-1, 0.5e-1, 1.0])
+    nclass, teseff = 10, 0.05 * inp.tau
+    nom = np.zeros(nclass, dtype=np.int64)
+    nam = np.zeros((metat, nclass), dtype=np.int64)
+    tab = {"tabmp": np.zeros((metat, nclass)), "tabvp": np.zeros((metat, nclass))}
+
+    def klass(v):
+        below = np.nonzero(v < aval[:nclass - 1])[0]
+        return int(below[0]) if len(below) else nclass - 1
+
     for src, k, x, nmul, fmul, b in bf.enumerate_semantic(inp, model):
         hmp, hdig = model.hmp_hdig(x)
         w = 1.0 + fmul
@@ -87,6 +101,18 @@ def test_oracle_e2_matches_bruteforce_sums(tmp_path, oracle_exe, name, cfg):
             dpivot = max(dpivot, float(xim[below].max()))
         xam = float((xim * taum).max())
         xam_of[(src, k, x)] = xam
+        psi["psimp"] += w * (b / (emp - hmp)) ** 2
+        psi["psivp"] += w * cvp ** 2
+        ietat += nmul + 1
+        if xam >= teseff:
+            vil = xim * taum
+            c = klass(xam)
+            nom[c] += 1 + nmul
+            for m in range(metat):
+                if vil[m] >= teseff:
+                    tab["tabmp"][m, c] += b2[m] / (emp[m] - hmp) * w
+                    tab["tabvp"][m, c] += b2[m] / dvp[m] * w
+                    nam[m, klass(vil[m])] += 1 + nmul
         v = 1.0 if ydeg else xam
         if abs(v - inp.tau) <= 1e-9 * inp.tau:
             near.add(x)
@@ -96,6 +122,15 @@ def test_oracle_e2_matches_bruteforce_sums(tmp_path, oracle_exe, name, cfg):
     for key, val in e2.items():
         tol = 1e-10 + np.asarray(jo["cond_" + key]) + 1e-12 * np.abs(val)
         assert np.all(np.abs(np.asarray(jo[key]) - val) <= tol), (key, jo[key], val, tol)
+    for key, val in psi.items():
+        np.testing.assert_allclose(jo[key], val, rtol=1e-9, atol=1e-14, err_msg=key)
+    assert jo["ietat"] == ietat
+    # histogram (isto.f): counts exact, sums to the E2 tolerance
+    assert list(jo["nom"]) == nom.tolist()
+    assert [list(r) for r in jo["nam"]] == nam.tolist()
+    for key, part in (("tabmp", "e2mp"), ("tabvp", "e2vp")):
+        tol = 1e-10 + np.asarray(jo["cond_" + part])[:, None] + 1e-12 * np.abs(tab[key])
+        assert np.all(np.abs(np.asarray(jo[key]) - tab[key]) <= tol), key
     # the unit-60 value of every perturber, dpivot, and the selected set
     ora = bf.read_candlog(os.path.join(run, "cand.bin"), metat)
     for r in ora:
