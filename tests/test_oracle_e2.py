@@ -45,6 +45,21 @@ CASES += small_cases()
 
 @pytest.mark.parametrize("name,cfg", CASES, ids=[c[0] for c in CASES])
 def test_oracle_e2_matches_bruteforce_sums(tmp_path, oracle_exe, name, cfg):
+    _check(tmp_path, cfg)
+
+
+@pytest.mark.parametrize("ityper,iselec", [(1, 1), (2, 2), (2, 3), (1, 3)])
+def test_oracle_options_match_bruteforce(tmp_path, oracle_exe, ityper, iselec):
+    """MP only (ityper = 1: the MP coefficient sets the selection value, no EN
+    sums), iselec = 2 (teste = test, taum = 1) and iselec = 3 (selection on
+    the energy term |b^2/d| instead of |b/d|)."""
+    import dataclasses
+    for seed, ranks, nsym in ((32, (1, 2, 3), 1), (33, (1, 2), 2)):
+        cfg = dataclasses.replace(_gap(seed, ranks, nsym), ityper=ityper, iselec=iselec)
+        _check(tmp_path / f"s{seed}", cfg)
+
+
+def _check(tmp_path, cfg):
     wd = str(tmp_path / "in")
     synth.generate(cfg, wd)
     run = copy_dir(wd, str(tmp_path / "run"))
@@ -60,11 +75,14 @@ def test_oracle_e2_matches_bruteforce_sums(tmp_path, oracle_exe, name, cfg):
     np.testing.assert_allclose(jo["emp"], emp, rtol=1e-12, atol=1e-12)
     np.testing.assert_allclose(jo["eb"], eb, rtol=1e-12, atol=1e-12)
     e = np.asarray(inp.E)
-    # selection thresholds of cip.f:104-135 (iselec = 1): teste = t * test,
-    # taum = 1 / t with t the largest |c| of the root
+    # selection thresholds of cip.f:104-135: with iselec = 1, teste = t * test
+    # and taum = 1 / t, t the largest |c| of the root; else test and 1
+    yen, ysele = inp.ityper == 2, inp.iselec == 3
     t = np.abs(inp.C).max(axis=0)
-    teste, taum = t * inp.test, 1.0 / t
-    assert inp.ityper == 2 and inp.iselec == 1
+    if inp.iselec == 1:
+        teste, taum = t * inp.test, 1.0 / t
+    else:
+        teste, taum = np.full(metat, inp.test), np.ones(metat)
     e2 = {k: np.zeros(metat) for k in ("e2mp", "e2vp", "e2b")}
     n = 0
     dpivot = 0.0
@@ -87,22 +105,27 @@ def test_oracle_e2_matches_bruteforce_sums(tmp_path, oracle_exe, name, cfg):
         w = 1.0 + fmul
         b = np.asarray(b)
         b2 = b ** 2
-        e2["e2mp"] += w * b2 / (emp - hmp)
-        e2["e2vp"] += w * b2 / (e - hdig)
-        e2["e2b"] += w * b2 / (eb - hdig)
+        dmp, dvp = emp - hmp, e - hdig
+        cmp_, cvp = b / dmp, b / dvp
+        e2["e2mp"] += w * b2 / dmp
+        if yen:
+            e2["e2vp"] += w * b2 / dvp
+            e2["e2b"] += w * b2 / (eb - hdig)
         n += 1
-        # pert1.f:192-244 with yen (EN eigenvalue partition sets the value)
-        dvp = e - hdig
-        cvp = b / dvp
-        xim = np.abs(cvp)
-        ydeg = bool(np.any((np.abs(dvp) <= 0.05) & (np.abs(b * cvp) >= 1e-6)))
+        # pert1.f:148-244: the last partition computed (EN eigenvalue with
+        # yen, else MP) gives the selection value, its denominator and term
+        deno, cim = (dvp, cvp) if yen else (dmp, cmp_)
+        eim = b * cim
+        xim = np.abs(eim) if ysele else np.abs(cim)
+        ydeg = bool(np.any((np.abs(deno) <= 0.05) & (np.abs(eim) >= 1e-6)))
         below = xim < teste
         if np.any(below):
             dpivot = max(dpivot, float(xim[below].max()))
         xam = float((xim * taum).max())
         xam_of[(src, k, x)] = xam
-        psi["psimp"] += w * (b / (emp - hmp)) ** 2
-        psi["psivp"] += w * cvp ** 2
+        psi["psimp"] += w * cmp_ ** 2
+        if yen:
+            psi["psivp"] += w * cvp ** 2
         ietat += nmul + 1
         if xam >= teseff:
             vil = xim * taum
@@ -110,8 +133,9 @@ def test_oracle_e2_matches_bruteforce_sums(tmp_path, oracle_exe, name, cfg):
             nom[c] += 1 + nmul
             for m in range(metat):
                 if vil[m] >= teseff:
-                    tab["tabmp"][m, c] += b2[m] / (emp[m] - hmp) * w
-                    tab["tabvp"][m, c] += b2[m] / dvp[m] * w
+                    tab["tabmp"][m, c] += b2[m] / dmp[m] * w
+                    if yen:
+                        tab["tabvp"][m, c] += b2[m] / dvp[m] * w
                     nam[m, klass(vil[m])] += 1 + nmul
         v = 1.0 if ydeg else xam
         if abs(v - inp.tau) <= 1e-9 * inp.tau:
