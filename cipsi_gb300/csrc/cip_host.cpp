@@ -1288,15 +1288,16 @@ extern "C" int cipsi_cip_main(const char* workdir, const char* stdin_path, int32
     cipsi_opts op{};
     cipsi_inputs_dims(in, &d, &op);
     op.gen_mask = gen_mask;
-    rc = cipsi_ctx_create(&ctx, &d, device);
     auto chk = [&](int code, const char* what) {
       if (code) throw Error(std::string(what) + ": " + cipsi_last_error(ctx));
     };
-    chk(rc, "cipsi_ctx_create");
-    chk(cipsi_inputs_upload(in, ctx), "cipsi_inputs_upload");
     const std::vector<int> itm = root_flip_signs(R);
     cipsi_result res{};
-    if (R.o.ityper != 0) chk(cipsi_run_pt2(ctx, &op, &res), "cipsi_run_pt2");
+    if (R.o.ityper != 0) {  // ityper = 0: no perturbation (deter.f:231), no device work
+      chk(cipsi_ctx_create(&ctx, &d, device), "cipsi_ctx_create");
+      chk(cipsi_inputs_upload(in, ctx), "cipsi_inputs_upload");
+      chk(cipsi_run_pt2(ctx, &op, &res), "cipsi_run_pt2");
+    }
     const auto t1 = std::chrono::steady_clock::now();
     // unit 60 when ymoyen: S (v = 1) then the selected perturbers; without
     // ymoyen the reference writes nothing to it (cip.f:222, pert1.f:264)
@@ -1329,27 +1330,31 @@ extern "C" int cipsi_cip_main(const char* workdir, const char* stdin_path, int32
       std::printf("nombre de determinants sur la file 60\n");
       std::printf("%12lld%12d\n", ntot, R.metat);
     }
-    std::printf(" energies CIPSI envp\n");
-    for (int m = 0; m < R.metat; ++m)
-      std::printf("  %2d  %14.8f  %14.8f  %14.8f  %14.8f\n", state_number(R.o, m), R.e[m], res.e2mp[m],
-                  res.e2vp[m], res.e2b[m]);
-    std::fflush(stdout);
-    // unit 33 (stkener.f: char*40 then the values, no count)
-    if (std::FILE* f33 = std::fopen(R.o.f33.c_str(), "ab")) {
-      const char* names[4] = {"energies CIPSI var ", "energies CIPSI mpb ", "energies CIPSI envp", "energies CIPSI enb "};
-      std::vector<double> etot(R.metat);
-      for (int m = 0; m < R.metat; ++m) etot[m] = R.e[m] + R.escf;
-      const double* vals[4] = {etot.data(), res.e2mp, res.e2vp, res.e2b};
-      for (int q = 0; q < 4; ++q) {
-        std::string typ = std::string(names[q]) + R.o.title;
-        typ.resize(40, ' ');
-        RecWriter w;
-        w.put_bytes(typ.data(), 40);
-        for (int m = 0; m < R.metat; ++m) w.put<double>(vals[q][m]);
-        w.flush(f33);
-      }
-      std::fclose(f33);
+    // unit 33 (stkener.f: char*40 then the values, no count), and the
+    // listing stkener prints for each record: the name, then a line with the
+    // values alone -- the Autocip driver finds ' energies CIPSI envp' and
+    // reads metat values list-directed from the next line
+    // (Autocip_13/calcul.f90:373-378)
+    std::FILE* f33 = std::fopen(R.o.f33.c_str(), "ab");
+    if (!f33) throw Error("cannot append to " + R.o.f33);
+    const char* names[4] = {"energies CIPSI var ", "energies CIPSI mpb ", "energies CIPSI envp", "energies CIPSI enb "};
+    std::vector<double> etot(R.metat);
+    for (int m = 0; m < R.metat; ++m) etot[m] = R.e[m] + R.escf;
+    const double* vals[4] = {etot.data(), res.e2mp, res.e2vp, res.e2b};
+    for (int q = 0; q < 4; ++q) {
+      std::string typ = std::string(names[q]) + R.o.title;
+      typ.resize(40, ' ');
+      RecWriter w;
+      w.put_bytes(typ.data(), 40);
+      for (int m = 0; m < R.metat; ++m) w.put<double>(vals[q][m]);
+      w.flush(f33);
+      std::printf(" *************************************\n");
+      std::printf(" %s stockee sur la file 33\n", typ.c_str());
+      for (int m = 0; m < R.metat; ++m) std::printf(" %24.16E", vals[q][m]);
+      std::printf("\n *************************************\n");
     }
+    std::fclose(f33);
+    std::fflush(stdout);
     if (json_path) {
       std::ofstream j(json_path);
       j.precision(17);

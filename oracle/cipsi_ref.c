@@ -2684,6 +2684,11 @@ int main(int argc, char** argv) {
         for (int m = 1; m <= metat; m++) wb_r8(&w, vals[q][m]);
         wb_flush(f33, &w);
         free(w.b);
+        /* stkener.f:9-12: the record's name, then its values on a line */
+        printf(" *************************************\n");
+        printf(" %s stockee sur la file 33\n", typ);
+        for (int m = 1; m <= metat; m++) printf(" %24.16E", vals[q][m]);
+        printf("\n *************************************\n");
       }
       fclose(f33);
     }
