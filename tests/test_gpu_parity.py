@@ -74,6 +74,9 @@ def check(jo, jg, wo, wg, variant, strict=False):
     dg = {x[0]: x for x in sg}
     for key, v, ev in so:
         assert v == pytest.approx(dg[key][1], rel=1e-9, abs=1e-12)
+        # cipsym's per-root ENvp of each record (cipsym/pert1.f:244), which the
+        # Autocip driver sums to choose its final threshold (calcul.f90:383-419)
+        assert np.allclose(ev, dg[key][2], rtol=1e-8, atol=1e-12), (key, ev, dg[key][2])
     check_unit4(wo, wg, jo)
 
 
