@@ -296,3 +296,38 @@ def test_executable_takes_the_autocip_s_only_call(tmp_path, engine_lib, oracle_e
     for unit in ("det", "f04"):
         assert _same_file(os.path.join(wo, unit), os.path.join(wd, unit)), unit
     assert len(_unit60_dets(os.path.join(wd, "det"), 3, True)) > 100
+
+
+@pytest.mark.parametrize("body,keep", [
+    ("lecdet=2, tdet=0.5", lambda v, i: v >= 0.5),          # lec60.f: v >= tdet
+    ("lecdet=3, maxdet=37", lambda v, i: i < 37),            # the first maxdet read
+    ("lecdet=2, tdet=0.0", lambda v, i: True),
+])
+def test_space_from_unit60_with_threshold_or_count(tmp_path, engine_lib, oracle_exe, body, keep):
+    """lecdet 2 (records with v >= tdet) and 3 (the first maxdet records) on
+    a unit 60 that holds S (v = 1) and earlier selected determinants with
+    values below and above the threshold."""
+    _lib_or_skip()
+    name, cfg = cases.small_cases()[1]
+    wd = _s_run_case(tmp_path, name, cfg)
+    S = _unit60_dets(os.path.join(wd, "det"), cfg.metat, True)
+    # rewrite unit 60: the first half of S with v = 1, the rest with values in (0, 1)
+    rng = np.random.default_rng(3)
+    vals = np.where(np.arange(len(S)) < len(S) // 2, 1.0, rng.uniform(0.01, 0.99, len(S)))
+    with open(os.path.join(wd, "det"), "wb") as fh:
+        for s0 in range(0, len(S), 25):
+            chunk = list(range(s0, min(len(S), s0 + 25)))
+            idet = [x for i in chunk for hp in zip(*S[i]) for x in hp]
+            payload = struct.pack("<ii", len(idet), len(chunk)) + np.array(idet, "<i4").tobytes()
+            payload += np.array([len(S[i][0]) for i in chunk], "<i4").tobytes()
+            payload += vals[chunk].astype("<f8").tobytes() + np.zeros(len(chunk) * cfg.metat, "<f8").tobytes()
+            synth.write_record(fh, payload)
+    _write_icinp(wd, f"metat={cfg.metat}, ityper=-1, {body}, ymoyen=t, iselec=1")
+    wo, wg = _run_both(wd, "cipsym")
+    for unit in ("det", "f04"):
+        assert _same_file(os.path.join(wo, unit), os.path.join(wg, unit)), unit
+    kept = [S[i] for i in range(len(S)) if keep(vals[i], i)]
+    out = set(_unit60_dets(os.path.join(wg, "det"), cfg.metat, True))
+    # the kept determinants and their spin-flip partners
+    want = set(kept) | {tuple(tuple(x) for x in synth.flip_lists(h, p, cfg.norb)) for h, p in kept}
+    assert out == want
