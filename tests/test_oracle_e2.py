@@ -59,13 +59,33 @@ def test_oracle_options_match_bruteforce(tmp_path, oracle_exe, ityper, iselec):
         _check(tmp_path / f"s{seed}", cfg)
 
 
-def _check(tmp_path, cfg):
+@pytest.mark.parametrize("coeff", [0.02, 0.1])
+def test_oracle_cip_generators_by_coeff(tmp_path, oracle_exe, coeff):
+    """cip (not cipsym) runs only the determinants with |c| >= coeff on some
+    root as generators (cip/ic001.f); the owner rule then sees only those."""
+    import dataclasses
+    cfg = dataclasses.replace(_gap(32, (1, 2, 3), 1), variant="cip", extra_icinp=f"coeff={coeff}")
+    _check(tmp_path, cfg, variant="cip", coeff=coeff)
+
+
+def test_oracle_without_ywdeg(tmp_path, oracle_exe):
+    """ywdeg = .false.: near-degenerate perturbers are not forced into the
+    selection (pert1.f:195-198), on the plain recipe where many are."""
+    import dataclasses
+    cfg = dataclasses.replace(small_cases()[0][1], extra_icinp="ywdeg=f")
+    _check(tmp_path, cfg, ywdeg=False)
+
+
+def _check(tmp_path, cfg, variant="cipsym", coeff=None, ywdeg=True):
     wd = str(tmp_path / "in")
     synth.generate(cfg, wd)
     run = copy_dir(wd, str(tmp_path / "run"))
-    jo = json.load(open(ob.run(run, variant="cipsym", candlog="cand.bin")))
+    jo = json.load(open(ob.run(run, variant=variant, candlog="cand.bin")))
     inp = bf.read_inputs(wd)
     model = bf.Model(inp)
+    if coeff is not None:
+        model.ygen = [bool(np.any(np.abs(inp.C[k]) >= coeff)) for k in range(len(inp.S))]
+        assert 0 < sum(model.ygen) < len(inp.S)
     metat = inp.C.shape[1]
     diag = [model.hmp_hdig(x) for x in model.bits]
     hmp_s = np.array([d[0] for d in diag])
@@ -117,7 +137,7 @@ def _check(tmp_path, cfg):
         deno, cim = (dvp, cvp) if yen else (dmp, cmp_)
         eim = b * cim
         xim = np.abs(eim) if ysele else np.abs(cim)
-        ydeg = bool(np.any((np.abs(deno) <= 0.05) & (np.abs(eim) >= 1e-6)))
+        ydeg = ywdeg and bool(np.any((np.abs(deno) <= 0.05) & (np.abs(eim) >= 1e-6)))
         below = xim < teste
         if np.any(below):
             dpivot = max(dpivot, float(xim[below].max()))
