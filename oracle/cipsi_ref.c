@@ -11,8 +11,11 @@
  * tests, fixtures or golden vectors, and its executables (ifort + MKL builds)
  * cannot run without the Intel runtime, and no Fortran compiler is available,
  * so this restatement cannot be cross-checked against cip.exe output.  It is
- * instead cross-checked against an independent brute-force enumerator
- * (tests/brute_force.py) on small systems.
+ * instead cross-checked against an independent brute-force model
+ * (tests/brute_force.py) on small systems: the perturber set, spin-flip
+ * weights and couplings (tests/test_oracle_semantics.py), and the E2 sums,
+ * norms, ietat, histogram, unit-60 values, dpivot and selected set, under
+ * several option sets (tests/test_oracle_e2.py).
  *
  * Followed sources (paths inside the reference project):
  *   CIPSI_sources/cip/cip.f      main flow 50-242, outputs 243-425
