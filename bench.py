@@ -22,7 +22,7 @@ per core, disjoint generator samples); the reference's Fortran cannot be
 built here (no Fortran compiler).
 
 For --gpus N (torchrun), every rank runs its own instance of the workload
-(seed + rank: independent geometries, as the batch driver runs them), so
+(seed + rank: independent geometries, as the Autocip driver runs its grid), so
 per-GPU work is fixed (weak scaling); value = all contributions / max time.
 """
 from __future__ import annotations

@@ -268,7 +268,7 @@ def test_s_run_rejects_what_it_does_not_support(tmp_path, engine_lib, oracle_exe
 
 
 def test_executable_takes_the_autocip_s_only_call(tmp_path, engine_lib, oracle_exe):
-    """The process-level drop-in, as the driver calls it
+    """The process-level drop-in, as the Autocip driver calls it
     (`cip_gpu --sym < f_bd > listing`, Autocip_13/calcul.f90:320), on the
     first call of the loop: the CAS with ITYPER=-1, the namelist laid out as
     makedata_cip.f90:201-221 writes it."""
