@@ -6,6 +6,13 @@ Writes tests/golden/small/ (the seeded 20-orbital configuration in the
 reference's file formats: ijkl, ener, det, bdvec, f04, cip.in) and
 tests/golden/small_expected.json: the CPU oracle's E2 totals, counters,
 histogram and a digest of the unit-60 selection for those exact files.
+
+    python tests/golden/make_golden.py --cas
+
+writes only tests/golden/cas_expected.json from the committed small/ files:
+the S-only run of Autocip's first cipsym call (CAS_ICINP: a complete active
+space of 4 electrons in orbitals 4..11, ordered and written with ityper = -1)
+as the oracle makes it, by SHA-256 of the unit-60 file and of unit 4.
 """
 import hashlib
 import json
@@ -42,6 +49,30 @@ def selection_digest(det_path, metat, sym):
     return len(items), hashlib.sha256(repr([(h, p) for h, p, _ in items]).encode()).hexdigest()
 
 
+CAS_ICINP = (" &cipfil\n &end\n &icinp\n  numac=4,5,6,7,8,9,10,11, noac=8, nelac=4, nusym=1,"
+             " metat=2, lecdet=4, ityper=-1, ymoyen=t, ybrd=f, yion=f, iselec=1, test=0d0,"
+             " tau=0d0\n &end\n")
+
+
+def cas_digests(run_dir):
+    """SHA-256 of the unit-60 file and of unit 4 after the CAS S-only run."""
+    return {u: hashlib.sha256(open(os.path.join(run_dir, u), "rb").read()).hexdigest() for u in ("det", "f04")}
+
+
+def cas_main():
+    with tempfile.TemporaryDirectory() as td:
+        run = os.path.join(td, "run")
+        shutil.copytree(os.path.join(HERE, "small"), run)
+        os.remove(os.path.join(run, "det"))
+        with open(os.path.join(run, "cip.in"), "w") as fh:
+            fh.write(CAS_ICINP)
+        j = json.load(open(ob.run(run, variant="cipsym")))
+        out = dict(ncf=j["ncf"], ntot60=j["ntot60"], sha256=cas_digests(run))
+    with open(os.path.join(HERE, "cas_expected.json"), "w") as fh:
+        json.dump(out, fh, indent=1, sort_keys=True)
+    print(json.dumps(out))
+
+
 def main():
     out = os.path.join(HERE, "small")
     shutil.rmtree(out, ignore_errors=True)
@@ -61,4 +92,4 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    cas_main() if "--cas" in sys.argv else main()

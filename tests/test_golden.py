@@ -54,3 +54,27 @@ def test_oracle_writes_unit4(tmp_path, oracle_exe):
     h = np.frombuffer(recs[2], dtype="<f8")
     escf = struct.unpack_from("<d", recs[1], 8 * nbr)[0]
     assert np.allclose(h[nbr - 1] - (j["e"][0] + escf), j["e2mp"][0])
+
+
+def test_cas_space_run_known_answer(tmp_path, oracle_exe, engine_lib):
+    """Autocip's first cipsym call (a CAS of 4 electrons in orbitals 4..11,
+    ityper = -1) on the committed 20-orbital files: the oracle and the drop-in
+    both write the committed unit 60 and unit 4, byte for byte (784
+    determinants in the order of shell.f).  Regenerate with
+    tests/golden/make_golden.py --cas."""
+    import sys
+    import cipsi_gb300
+    sys.path.insert(0, GOLD)
+    from make_golden import CAS_ICINP, cas_digests
+    exp = json.load(open(os.path.join(GOLD, "cas_expected.json")))
+    for who in ("oracle", "engine"):
+        run = copy_dir(os.path.join(GOLD, "small"), str(tmp_path / who))
+        os.remove(os.path.join(run, "det"))
+        with open(os.path.join(run, "cip.in"), "w") as fh:
+            fh.write(CAS_ICINP)
+        if who == "oracle":
+            got = json.load(open(ob.run(run, variant="cipsym")))
+        else:
+            got = cipsi_gb300.run_cip(run, variant="cipsym")
+        assert (got["ncf"], got["ntot60"]) == (exp["ncf"], exp["ntot60"]), who
+        assert cas_digests(run) == exp["sha256"], who
