@@ -331,3 +331,43 @@ def test_space_from_unit60_with_threshold_or_count(tmp_path, engine_lib, oracle_
     # the kept determinants and their spin-flip partners
     want = set(kept) | {tuple(tuple(x) for x in synth.flip_lists(h, p, cfg.norb)) for h, p in kept}
     assert out == want
+
+
+def test_zero_order_record_against_the_model(tmp_path, engine_lib, oracle_exe):
+    """Unit 4's zero-order record (cip.f:144-150) as the drop-in writes it:
+    the determinant lists are S in the order the brute-force model builds it,
+    empdet is the model's MP diagonal hmp of each determinant, and fmpb the
+    closed-shell orbital energies F_pp (faifoc.f with closed-shell tocom)."""
+    _lib_or_skip()
+    import cipsi_gb300
+    import brute_force as bf
+    name, cfg = cases.small_cases()[2]
+    wd = _s_run_case(tmp_path, name, cfg)
+    inp = bf.read_inputs(wd)
+    model = bf.Model(inp)
+    wg = wd + "_engine"
+    shutil.copytree(wd, wg)
+    _write_icinp(wg, f"metat={cfg.metat}, ityper=-1, lecdet=5, ymoyen=f, iselec=1")
+    cipsi_gb300.run_cip(wg, variant="cipsym")
+    rec = synth.read_records(os.path.join(wg, "f04"))[0]
+    norb, noca, nocb, metat, ncf, isz = struct.unpack_from("<6i", rec, 0)
+    assert (norb, noca, nocb, metat, ncf, isz) == (cfg.norb, cfg.nocc, cfg.nocc + cfg.norb, cfg.metat,
+                                                    len(inp.S), 0)
+    off = 25
+    ii, jj = struct.unpack_from("<ii", rec, off)
+    off += 8
+    nend = np.frombuffer(rec, dtype="<i4", count=2 * ncf, offset=off).reshape(ncf, 2)
+    off += 8 * ncf
+    tp = np.frombuffer(rec, dtype="<i4", count=2 * ii, offset=off).reshape(ii, 2)
+    off += 8 * ii
+    dets = [(tuple(int(x) for x in tp[nd:nd + ne, 0]), tuple(int(x) for x in tp[nd:nd + ne, 1])) for ne, nd in nend]
+    assert dets == [(tuple(h), tuple(p)) for h, p in inp.S]
+    c = np.frombuffer(rec, dtype="<f8", count=jj, offset=off)
+    assert jj == ncf * metat and np.all(c == 0.0)  # ityper < 0: ic001 not called
+    off += 8 * jj + 3 * 8 * metat + 4 * metat  # e, emp, eb, numero
+    empdet = np.frombuffer(rec, dtype="<f8", count=ncf, offset=off)
+    off += 8 * ncf
+    fmpb = np.frombuffer(rec, dtype="<f8", count=norb, offset=off)
+    want = np.array([model.hmp_hdig(x)[0] for x in model.bits])
+    np.testing.assert_allclose(empdet, want, rtol=0, atol=1e-12)
+    np.testing.assert_allclose(fmpb, model.fdiag[1:norb + 1], rtol=0, atol=1e-13)
