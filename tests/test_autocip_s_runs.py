@@ -183,6 +183,7 @@ CAS_CASES = [
     (12, 4, 4, [4, 5, 6, 7, 9], 2, 0, 8, 13),
     (14, 4, 2, [3, 4, 5, 6, 7, 8, 9], 4, 2, 3, 14),
     (12, 3, 4, [1, 2, 3, 4, 5, 6, 7, 8], 6, 1, 4, 15),
+    (14, 4, 8, [3, 4, 5, 6, 7, 8, 9, 10, 11], 4, 0, 8, 16),
 ]
 
 

@@ -39,7 +39,8 @@ def _gap(seed, ranks, nsym):
                              coef_mode="gauss005", seed=seed, nsym=nsym, virt_shift=3.0)
 
 
-CASES = [("gap31", _gap(31, (2,), 1)), ("gap32", _gap(32, (1, 2, 3), 1)), ("gap33", _gap(33, (1, 2), 2))]
+CASES = [("gap31", _gap(31, (2,), 1)), ("gap32", _gap(32, (1, 2, 3), 1)), ("gap33", _gap(33, (1, 2), 2)),
+         ("gap34_d2h", _gap(34, (1, 2, 3), 8))]
 CASES += small_cases()
 
 
