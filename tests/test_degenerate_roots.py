@@ -1,10 +1,13 @@
-"""Roots degenerate within 1e-6 Eh (degen, brdnee.f:299-365, called by
+"""The vectors of S as ic001 leaves them after reading unit 59 (lecdet = 5).
+
+Roots degenerate within 1e-6 Eh (degen, brdnee.f:299-365, called by
 ic001 after unit 59 is read): a run of exactly two degenerate roots is
 rotated so that the first spin-flip pair of unequal weights on the first
 root gets equal weights; the last two roots are never paired by the scan,
 and a run of three ending at the last root is treated as a pair.  The host
 inputs of the drop-in (the vectors it uploads) are compared bit for bit with
-the vectors the oracle writes to unit 4 before its perturbation loop."""
+the vectors the oracle writes to unit 4 before its perturbation loop.  cip's
+reordering by unit 4's iord60 (cip/ic001.f:46-73) is checked the same way."""
 import os
 import struct
 
@@ -104,3 +107,34 @@ def test_degenerate_roots_rotate_like_the_oracle(tmp_path, engine_lib, oracle_ex
         if not ysaut[k] and nesp[k] == 1 and abs(abs(c[0, k]) - abs(c[0, k + 1])) >= 1e-5:
             assert abs(abs(host_c[0, k]) - abs(host_c[0, k + 1])) < 1e-4
             break
+
+
+def test_cip_reorders_vectors_by_iord60(tmp_path, engine_lib, oracle_exe):
+    """cip (not cipsym) reads a permutation iord60 as unit 4's second record
+    and moves coefficient k of unit 59 to position iord60(k)
+    (cip/ic001.f:46-73); the host's vectors equal the oracle's and the
+    permutation applied to unit 59."""
+    from cipsi_gb300 import engine
+    cfg = synth.SynthConfig("perm", norb=10, nocc=3, ncholesky=12, ncf=40, metat=2, tau=0.02,
+                            ranks=(1, 2), coef_mode="decay09", seed=61, variant="cip")
+    wd = str(tmp_path / "perm")
+    synth.generate(cfg, wd)
+    c59, _ = _read59(wd)
+    ncf = c59.shape[1]
+    perm = np.random.default_rng(7).permutation(ncf) + 1
+    recs = synth.read_records(os.path.join(wd, "f04"))
+    with open(os.path.join(wd, "f04"), "wb") as fh:
+        synth.write_record(fh, recs[0])
+        synth.write_record(fh, perm.astype("<i4").tobytes())
+    inp = engine.Inputs(wd, variant="cip")
+    host_c = inp.array("c").reshape(2, -1)
+    inp.close()
+    want = np.empty_like(c59)
+    want[:, perm - 1] = c59
+    np.testing.assert_array_equal(host_c, want)
+    from oracle import build as ob
+    ob.run(wd, variant="cip")
+    rec = synth.read_records(os.path.join(wd, "f04"))[0]
+    ii, jj = struct.unpack_from("<ii", rec, 25)
+    np.testing.assert_array_equal(np.frombuffer(rec, dtype="<f8", count=jj, offset=33 + 8 * ncf + 8 * ii),
+                                  want.reshape(-1))
