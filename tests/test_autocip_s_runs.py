@@ -372,3 +372,34 @@ def test_zero_order_record_against_the_model(tmp_path, engine_lib, oracle_exe):
     want = np.array([model.hmp_hdig(x)[0] for x in model.bits])
     np.testing.assert_allclose(empdet, want, rtol=0, atol=1e-12)
     np.testing.assert_allclose(fmpb, model.fdiag[1:norb + 1], rtol=0, atol=1e-13)
+
+
+@pytest.mark.parametrize("fault", ["degree9", "marker"])
+def test_corrupt_unit60_fails_cleanly(tmp_path, engine_lib, oracle_exe, fault):
+    """A unit-60 record with an excitation degree above 8 (lec60.f:52-56
+    stops) or a record whose trailing length marker disagrees: both the
+    drop-in (an error code and message, no exit) and the oracle refuse it."""
+    _lib_or_skip()
+    import subprocess
+    import cipsi_gb300
+    from oracle import build as ob
+    name, cfg = cases.small_cases()[1]
+    wd = _s_run_case(tmp_path, name, cfg)
+    path = os.path.join(wd, "det")
+    if fault == "degree9":
+        idet = list(range(1, 10)) + list(range(cfg.norb + 1, cfg.norb + 10))
+        payload = struct.pack("<ii", 18, 1) + np.array(idet, "<i4").tobytes() + struct.pack("<i", 9)
+        payload += struct.pack("<d", 1.0) + np.zeros(cfg.metat, "<f8").tobytes()
+        with open(path, "ab") as fh:
+            synth.write_record(fh, payload)
+        msg = "degre"
+    else:
+        with open(path, "ab") as fh:
+            fh.write(struct.pack("<i", 8) + b"\0" * 8 + struct.pack("<i", 9))
+        msg = "marker"
+    _write_icinp(wd, f"metat={cfg.metat}, ityper=-1, lecdet=5, ymoyen=t, iselec=1")
+    with pytest.raises(cipsi_gb300.CipsiError, match=msg):
+        cipsi_gb300.run_cip(wd, variant="cipsym")
+    with open(os.path.join(wd, "cip.in")) as fin:
+        r = subprocess.run([ob.build(), "--sym"], cwd=wd, stdin=fin, capture_output=True, text=True)
+    assert r.returncode != 0
