@@ -40,7 +40,9 @@ def _gap(seed, ranks, nsym):
 
 
 CASES = [("gap31", _gap(31, (2,), 1)), ("gap32", _gap(32, (1, 2, 3), 1)), ("gap33", _gap(33, (1, 2), 2)),
-         ("gap34_d2h", _gap(34, (1, 2, 3), 8))]
+         ("gap34_d2h", _gap(34, (1, 2, 3), 8)),
+         ("gap35_6roots", synth.SynthConfig("gap", norb=14, nocc=4, ncholesky=14, ncf=60, metat=6, tau=0.01,
+                                            ranks=(1, 2), coef_mode="decay09", seed=35, virt_shift=3.0))]
 CASES += small_cases()
 
 
