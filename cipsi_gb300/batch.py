@@ -6,10 +6,12 @@ one persistent launch per class, captured as a CUDA graph.
 directory each, in the reference's file formats), reads each into an engine
 context on the GPU and removes the directory, so only a few exist at a time.
 `autotune` picks the launch tuning (removed-electron blocks per work unit,
-CTAs per SM) by timing a sub-batch.
+CTAs per SM) by timing a sub-batch.  `run_grid` runs a whole grid in
+batches with a checkpoint per geometry, and resumes a stopped run.
 """
 from __future__ import annotations
 
+import json
 import multiprocessing as mp
 import os
 import shutil
@@ -96,3 +98,57 @@ def autotune(ctxs, opts, sample: int = 16, candidates: Sequence[Tuple[int, int]]
         times[cand] = min(ms)
     best = min(times, key=times.get)
     return best, times
+
+
+def run_batch(cfgs: Sequence[synth.SynthConfig], device: int = 0, r_chunk: int = 6, ctas_per_sm: int = 0,
+              workers: Optional[int] = None) -> list:
+    """The geometries of `cfgs` in one batched launch: each one's result."""
+    opts, ctxs = load_geometries(cfgs, device=device, workers=workers)
+    try:
+        with engine.Batch(ctxs, opts, r_chunk=r_chunk, ctas_per_sm=ctas_per_sm) as b:
+            b.run()
+            b.wait()
+            return b.fetch_all()
+    finally:
+        for c in ctxs:
+            c.close()
+
+
+def _result_path(results_dir: str, cfg: synth.SynthConfig) -> str:
+    return os.path.join(results_dir, cfg.name + ".json")
+
+
+def run_grid(cfgs: Sequence[synth.SynthConfig], results_dir: str, batch_size: int = 32, runner=run_batch,
+             **runner_kw) -> dict:
+    """A grid of geometries with checkpoints: the geometries run in batches of
+    `batch_size`, and each one's result goes to results_dir/<name>.json
+    (written to a temporary name, then renamed, so a file is complete or
+    absent) as soon as its batch finishes.  Geometries that already have a
+    result file are not run again, so a run that stopped -- killed, out of
+    time, a failed batch -- continues where it stopped when called again,
+    as the Autocip driver re-reads finished geometries instead of
+    recomputing them (Autocip_13/autocip13.f90:162, l_calc).  Returns every
+    geometry's result by name."""
+    os.makedirs(results_dir, exist_ok=True)
+    names = [c.name for c in cfgs]
+    if len(set(names)) != len(names):
+        raise ValueError("geometry names must be unique: they name the result files")
+    todo = [c for c in cfgs if not os.path.exists(_result_path(results_dir, c))]
+    for s in range(0, len(todo), batch_size):
+        chunk = todo[s:s + batch_size]
+        results = runner(chunk, **runner_kw)
+        if len(results) != len(chunk):
+            raise RuntimeError("the batch returned %d results for %d geometries" % (len(results), len(chunk)))
+        for cfg, res in zip(chunk, results):
+            rec = {"name": cfg.name, "norb": cfg.norb, "ncf": cfg.ncf, "metat": cfg.metat, "seed": cfg.seed,
+                   "curve_R": cfg.curve_R, "result": res}
+            path = _result_path(results_dir, cfg)
+            tmp = path + ".tmp"
+            with open(tmp, "w") as fh:
+                json.dump(rec, fh)
+            os.replace(tmp, path)
+    out = {}
+    for c in cfgs:
+        with open(_result_path(results_dir, c)) as fh:
+            out[c.name] = json.load(fh)["result"]
+    return out
