@@ -118,37 +118,67 @@ def _result_path(results_dir: str, cfg: synth.SynthConfig) -> str:
     return os.path.join(results_dir, cfg.name + ".json")
 
 
+# configuration fields saved with each result and compared on resume
+_KEY_FIELDS = ("norb", "ncf", "metat", "seed", "curve_R")
+
+
+def _saved_result(results_dir: str, cfg: synth.SynthConfig):
+    """The saved result of `cfg`, or None when there is none to reuse: no
+    file, a file that does not parse (cut short by a crash), or a file
+    written for a different configuration under the same name (another
+    seed, grid or system size in the same results directory)."""
+    path = _result_path(results_dir, cfg)
+    try:
+        with open(path) as fh:
+            rec = json.load(fh)
+    except (OSError, ValueError):
+        return None
+    if not isinstance(rec, dict) or "result" not in rec:
+        return None
+    if any(rec.get(f) != getattr(cfg, f) for f in _KEY_FIELDS):
+        return None
+    return rec["result"]
+
+
 def run_grid(cfgs: Sequence[synth.SynthConfig], results_dir: str, batch_size: int = 32, runner=run_batch,
              **runner_kw) -> dict:
     """A grid of geometries with checkpoints: the geometries run in batches of
     `batch_size`, and each one's result goes to results_dir/<name>.json
-    (written to a temporary name, then renamed, so a file is complete or
-    absent) as soon as its batch finishes.  Geometries that already have a
-    result file are not run again, so a run that stopped -- killed, out of
-    time, a failed batch -- continues where it stopped when called again,
-    as the Autocip driver re-reads finished geometries instead of
-    recomputing them (Autocip_13/autocip13.f90:162, l_calc).  Returns every
-    geometry's result by name."""
+    (written to a temporary name, flushed to disk, then renamed, so a file is
+    complete or absent) as soon as its batch finishes.  Geometries that
+    already have a result for the same configuration (norb, ncf, metat, seed,
+    curve_R) are not run again, so a run that stopped -- killed, out of time,
+    a failed batch -- continues where it stopped when called again, as the
+    Autocip driver re-reads finished geometries instead of recomputing them
+    (Autocip_13/autocip13.f90:162, l_calc).  A result file that does not
+    parse, or that was written for another configuration of the same name,
+    is run again and replaced.  Returns every geometry's result by name."""
     os.makedirs(results_dir, exist_ok=True)
     names = [c.name for c in cfgs]
     if len(set(names)) != len(names):
         raise ValueError("geometry names must be unique: they name the result files")
-    todo = [c for c in cfgs if not os.path.exists(_result_path(results_dir, c))]
+    out = {}
+    todo = []
+    for c in cfgs:
+        r = _saved_result(results_dir, c)
+        if r is None:
+            todo.append(c)
+        else:
+            out[c.name] = r
     for s in range(0, len(todo), batch_size):
         chunk = todo[s:s + batch_size]
         results = runner(chunk, **runner_kw)
         if len(results) != len(chunk):
             raise RuntimeError("the batch returned %d results for %d geometries" % (len(results), len(chunk)))
         for cfg, res in zip(chunk, results):
-            rec = {"name": cfg.name, "norb": cfg.norb, "ncf": cfg.ncf, "metat": cfg.metat, "seed": cfg.seed,
-                   "curve_R": cfg.curve_R, "result": res}
+            rec = {f: getattr(cfg, f) for f in _KEY_FIELDS}
+            rec.update(name=cfg.name, result=res)
             path = _result_path(results_dir, cfg)
             tmp = path + ".tmp"
             with open(tmp, "w") as fh:
                 json.dump(rec, fh)
+                fh.flush()
+                os.fsync(fh.fileno())
             os.replace(tmp, path)
-    out = {}
-    for c in cfgs:
-        with open(_result_path(results_dir, c)) as fh:
-            out[c.name] = json.load(fh)["result"]
-    return out
+            out[cfg.name] = json.loads(json.dumps(res))
+    return {c.name: out[c.name] for c in cfgs}

@@ -1780,15 +1780,18 @@ int cipsi_run_pt2_static(cipsi_ctx* ctx, const cipsi_opts* o, cipsi_result* r) {
     CK(cudaGetLastError());
   }
   CK(cudaEventRecord(ctx->ev1, ctx->stream));
-  CK(cudaStreamSynchronize(ctx->stream));
 
-  // results (same fields as cipsi_fetch_result; no records are kept)
+  // results (same fields as cipsi_fetch_result; no records are kept), read
+  // on the context's stream: a legacy-stream cudaMemcpy would also wait for
+  // every other blocking stream of the device
   double red[5 * kMaxRoots];
   unsigned long long cnt[C_NCOUNTERS + 1 + kNClass + kNClass * kMaxRoots];
   double tab[2 * kNClass * kMaxRoots];
-  CK(cudaMemcpy(red, dred, nq * sizeof(double), cudaMemcpyDeviceToHost));
-  CK(cudaMemcpy(cnt, dcounters, ncount * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
-  CK(cudaMemcpy(tab, p.hist_tab, 2 * kNClass * kMaxRoots * sizeof(double), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpyAsync(red, dred, nq * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemcpyAsync(cnt, dcounters, ncount * sizeof(unsigned long long), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemcpyAsync(tab, p.hist_tab, 2 * kNClass * kMaxRoots * sizeof(double), cudaMemcpyDeviceToHost,
+                     ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
   memset(r, 0, sizeof(*r));
   for (int m = 0; m < mt; ++m) {
     r->e2mp[m] = red[0 * mt + m];

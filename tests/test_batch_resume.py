@@ -57,3 +57,34 @@ def test_grid_refuses_duplicate_names_and_short_batches(tmp_path):
         batch.run_grid(cfgs + cfgs[:1], str(tmp_path / "a"), runner=Runner())
     with pytest.raises(RuntimeError, match="results"):
         batch.run_grid(cfgs, str(tmp_path / "b"), runner=lambda cs, **kw: [{}])
+
+
+def test_grid_reruns_results_of_another_configuration(tmp_path):
+    # the same geometry names (geo000, geo001, ...) with another seed in the
+    # same directory: the saved results belong to other systems
+    out = str(tmp_path / "res")
+    old = synth.curve_geometries(4, seed=5)
+    batch.run_grid(old, out, batch_size=4, runner=Runner())
+    new = synth.curve_geometries(4, seed=7)
+    assert [c.name for c in new] == [c.name for c in old]
+    assert any((a.seed, a.norb, a.curve_R) != (b.seed, b.norb, b.curve_R) for a, b in zip(old, new))
+    second = Runner()
+    res = batch.run_grid(new, out, batch_size=4, runner=second)
+    changed = [b.name for a, b in zip(old, new) if any(getattr(a, f) != getattr(b, f) for f in batch._KEY_FIELDS)]
+    assert second.calls == [changed]
+    for c in new:
+        assert res[c.name] == {"e2vp": [float(c.seed) + 0.5], "ncf": c.ncf}
+        assert json.load(open(os.path.join(out, c.name + ".json")))["seed"] == c.seed
+
+
+def test_grid_reruns_a_result_file_that_does_not_parse(tmp_path):
+    out = str(tmp_path / "res")
+    cfgs = synth.curve_geometries(3, seed=5)
+    batch.run_grid(cfgs, out, batch_size=3, runner=Runner())
+    # a renamed file whose data never reached the disk (power loss)
+    with open(os.path.join(out, cfgs[1].name + ".json"), "w") as fh:
+        fh.write('{"name": "geo0')
+    second = Runner()
+    res = batch.run_grid(cfgs, out, batch_size=3, runner=second)
+    assert second.calls == [[cfgs[1].name]]
+    assert res[cfgs[1].name] == {"e2vp": [float(cfgs[1].seed) + 0.5], "ncf": cfgs[1].ncf}

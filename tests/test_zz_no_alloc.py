@@ -3,7 +3,8 @@ against cipsi_run_pt2 on the same context, through the C ABI.
 
 Two static calls in a row must both give cipsi_run_pt2's energies (within
 1e-10 relative, plus 1e-12 absolute), and identical counters, histogram
-counts and selection count.  This file is collected last so that it also runs
+counts and selection count, and must leave the device's free memory as it
+was.  This file is collected last so that it also runs
 after every other GPU test in the same process."""
 import ctypes
 import dataclasses
@@ -35,6 +36,13 @@ def _run_static(ctx, opts):
     return engine.result_dict(r, ctx.dims.metat, opts.nclass)
 
 
+def _free_bytes():
+    """Free device memory (cudaMemGetInfo through torch's runtime)."""
+    import torch
+    torch.cuda.synchronize()
+    return torch.cuda.mem_get_info(0)[0]
+
+
 def _compare(ref, got):
     for k in ("ietat", "n_processed", "n_selected", "n_candidates", "n_pairs_1", "n_pairs_2", "nom", "nam"):
         assert got[k] == ref[k], k
@@ -61,8 +69,12 @@ def test_static_matches_run_pt2(tmp_path, engine_lib, name, cfg):
     with engine.Context(inp.dims) as ctx:
         ctx.upload(inp)
         ref = ctx.run(inp.opts)
+        # the context and the library's device code are set up by now, so
+        # the two static calls must leave the device's free memory unchanged
+        free0 = _free_bytes()
         first = _run_static(ctx, inp.opts)
         second = _run_static(ctx, inp.opts)
+        assert _free_bytes() == free0, "a static call allocated device memory"
         # the records of the cipsi_run_pt2 run stay readable
         sel = ctx.selection_raw(min(ref["n_selected"], 16))
     assert ref["n_processed"] > 0
