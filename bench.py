@@ -1,25 +1,34 @@
 #!/usr/bin/env python3
 """Benchmark of the CIPSI perturbation / selection step on GB300.
 
-Workload ("medium"): 60 orbitals, 20 electrons (Ms = 0), S = 2000
-determinants (reference + singles/doubles/triples, spin-flip closed), 3 roots,
-MP + EN partitions, selection threshold 0.01; seeded synthetic integrals.
+Workload (default "large", the configuration the engine's target is quoted
+on): 120 orbitals, 30 electrons (Ms = 0), S = 20,000 determinants (the
+reference plus doubles, spin-flip closed), 2 roots, MP + EN partitions,
+selection threshold 0.005; seeded synthetic integrals (240 Cholesky
+vectors).  "--workload medium": 60 orbitals, 20 electrons, S = 2000
+(singles/doubles/triples), 3 roots, threshold 0.01.
 
 A step is one full pass of the hot path (the work of pertu + diexcit) over
-the workload.  Metric: perturber contributions per second, one contribution
-being one (perturber that reaches the E2 loop, root) term.
+the workload, with every selected perturber's unit-60 record produced.
+Metric: perturber contributions per second, one contribution being one
+(perturber that reaches the E2 loop, root) term.
 
-  value   device time of the engine's kernels, inputs resident in HBM, L2
-          flushed (256 MiB write) before every step;
+  value   device time of a streamed run (cipsi_run_pt2_stream without a
+          consumer: the records are made and gathered in device memory,
+          chunk after chunk), inputs resident in HBM, L2 flushed (256 MiB
+          write) before every step;
   e2e     the same through the C ABI from host buffers: every step uploads
-          the inputs (cipsi_inputs_upload), runs, fetches the result and the
-          selected determinants;
+          the inputs (cipsi_inputs_upload) and streams the run to a consumer
+          that folds every record, in order, into a digest on the host cores
+          (cipsi_record_digest): the unit-60 records are delivered to host
+          memory inside the timed region;
   cpu_baseline  the CPU oracle (a restatement of the reference's loop nest)
-          on one core, on a sample of the generators.
+          on one core, on a systematic sample of one generator's candidates.
 
---impl reference times that CPU restatement on all host cores (one process
-per core, disjoint generator samples); the reference's Fortran cannot be
-built here (no Fortran compiler).
+--impl reference times that CPU restatement on all host cores: one
+long-lived process per core reads the inputs once and runs one sampled
+generator per step (its own clock around the perturbation loop); the
+reference's Fortran cannot be built here (no Fortran compiler).
 
 For --gpus N (torchrun), every rank runs its own instance of the workload
 (seed + rank: independent geometries, as the Autocip driver runs its grid), so
@@ -28,6 +37,8 @@ per-GPU work is fixed (weak scaling); value = all contributions / max time.
 from __future__ import annotations
 
 import argparse
+import hashlib
+import importlib.util
 import json
 import os
 import shutil
@@ -41,31 +52,49 @@ import time
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-CONFIG = "medium"
-# dram__bytes_read.sum + dram__bytes_write.sum of one full k_pt2 launch on
-# this workload (0.984 GB + 14.616 GB), from a single-pass ncu capture of
-# `python bench.py --steps 2 --warmup 3 --no-cpu-baseline` (5th k_pt2 launch)
-NCU_DRAM_BYTES_PER_LAUNCH = 15.600e9
 METRIC = "perturber contributions/s"
 UNIT = "contributions/s"
+WORKLOADS = {
+    "large": {"workload": "large: 120 MOs, 30 e-, Ms=0, S=20000 dets (ref + doubles, spin-flip closed), "
+                          "2 roots, MP+EN, tau=0.005",
+              "norb": 120, "electrons": 30, "ncf": 20000, "roots": 2, "tau": 0.005},
+    "medium": {"workload": "medium: 60 MOs, 20 e-, Ms=0, S=2000 dets (ref+S/D/T, spin-flip closed), "
+                           "3 roots, MP+EN, tau=0.01",
+               "norb": 60, "electrons": 20, "ncf": 2000, "roots": 3, "tau": 0.01},
+}
+# systematic CPU sample: one candidate (and one diexcit quadruple) in
+# CPU_SAMPLE of the sampled generators, per process and step
+CPU_SAMPLE = {"large": 200, "medium": 10}
 
 
-def workload_desc():
-    return {"workload": "medium: 60 MOs, 20 e-, Ms=0, S=2000 dets (ref+S/D/T, spin-flip closed), "
-                        "3 roots, MP+EN, tau=0.01",
-            "norb": 60, "electrons": 20, "ncf": 2000, "roots": 3, "tau": 0.01,
-            "l2": "flushed before each step (256 MiB write)"}
+def workload_desc(name: str) -> dict:
+    d = dict(WORKLOADS[name])
+    d["l2"] = "flushed before each step (256 MiB write)"
+    d["records"] = "every selected perturber's unit-60 record made each step (value: in device memory; " \
+                   "e2e: delivered to host memory and folded into a digest)"
+    return d
 
 
-def make_workload(seed_offset: int, base: str):
-    from cipsi_gb300 import synth
+def _synth():
+    """The synthetic-input generator, loaded from its file (numpy only), so
+    the reference arm runs without importing the engine's package."""
+    mod = sys.modules.get("cipsi_synth")
+    if mod is None:
+        spec = importlib.util.spec_from_file_location("cipsi_synth", os.path.join(ROOT, "cipsi_gb300", "synth.py"))
+        mod = importlib.util.module_from_spec(spec)
+        sys.modules["cipsi_synth"] = mod
+        spec.loader.exec_module(mod)
+    return mod
+
+
+def make_workload(name: str, seed_offset: int, base: str):
     import dataclasses
-    cfg = dataclasses.replace(synth.CONFIGS[CONFIG])
+    synth = _synth()
+    cfg = dataclasses.replace(synth.CONFIGS[name])
     cfg.seed = cfg.seed + seed_offset
-    wd = os.path.join(base, f"{CONFIG}_s{cfg.seed}")
-    if not os.path.exists(os.path.join(wd, "cip.in")):
-        synth.generate(cfg, wd)
-    return wd
+    wd = os.path.join(base, f"{name}_s{cfg.seed}")
+    info = synth.generate(cfg, wd)
+    return wd, info
 
 
 # ------------------------------------------------------------ clocks sampler
@@ -122,69 +151,104 @@ def measured_peaks():
 
 
 # ------------------------------------------------------------ CPU baseline
-def oracle_sample(wd: str, every: int, offset: int, run_pertu: bool, tmpbase: str):
-    """Run the CPU oracle on generators k with (k % every == offset)."""
+def sample_plan(ncf: int, ysaut, nsteps: int, nproc: int, sample: int, seed: int = 7):
+    """Per process, one line per step: (residue, generator).  Generators are
+    drawn without repetition from the determinants of S that are not
+    spin-flip partners (the generators); residue m keeps one candidate in
+    `sample`, in enumeration order."""
     import numpy as np
+    rng = np.random.default_rng(seed)
+    gens = [k for k in range(ncf) if not ysaut[k]]
+    pick = rng.choice(len(gens), size=min(len(gens), nsteps * nproc), replace=False)
+    lines = [[] for _ in range(nproc)]
+    for i, g in enumerate(pick):
+        c, st = i % nproc, i // nproc
+        if st < nsteps:
+            lines[c].append((int(rng.integers(0, sample)), gens[int(g)] + 1))
+    return lines
+
+
+def oracle_plan(wd: str, lines, sample: int, tmpbase: str):
+    """One oracle process on its plan (inputs read once): [(perturbers,
+    loop seconds)] per line, by the oracle's own clock, and metat."""
     from oracle import build as ob
     run = tempfile.mkdtemp(dir=tmpbase)
-    shutil.rmtree(run)
-    shutil.copytree(wd, run)
-    info = json.load(open(os.path.join(wd, "..", "info_" + os.path.basename(wd) + ".json")))
-    m = np.zeros(info["ncf"], dtype=np.uint8)
-    m[offset::every] = 1
-    mp = os.path.join(run, "mask.bin")
-    m.tofile(mp)
-    t0 = time.perf_counter()
-    j = json.load(open(ob.run(run, genmask=mp, no_pertu_ref=not run_pertu)))
-    dt = time.perf_counter() - t0
+    for f in os.listdir(wd):  # the integrals are only read: linked, not copied
+        src = os.path.join(wd, f)
+        if f == "ijkl":
+            os.symlink(src, os.path.join(run, f))
+        elif os.path.isfile(src):
+            shutil.copy(src, os.path.join(run, f))
+    plan = os.path.join(run, "plan.txt")
+    with open(plan, "w") as fh:
+        for m, k in lines:
+            fh.write(f"{m} {k}\n")
+    j = json.load(open(ob.run(run, sample=sample, plan=plan)))
     shutil.rmtree(run, ignore_errors=True)
-    return j["n_processed"] * j["metat"], dt
+    return [(int(n), float(t)) for n, t in j["plan"]], int(j["metat"])
 
 
-def write_info(wd: str):
-    from cipsi_gb300 import engine
-    inp = engine.Inputs(wd)
-    info = {"ncf": inp.dims.ncf, "metat": inp.dims.metat}
-    with open(os.path.join(wd, "..", "info_" + os.path.basename(wd) + ".json"), "w") as fh:
-        json.dump(info, fh)
-    return info
+def _ysaut(wd: str, info: dict):
+    """Spin-flip partner flags of S from the generator's output (partners
+    follow their representative in the file)."""
+    synth = _synth()
+    flags = []
+    for r in synth.read_records(os.path.join(wd, "det")):
+        import struct
+        m, n = struct.unpack_from("<ii", r, 0)
+        idet = struct.unpack_from(f"<{m}i", r, 8)
+        nex = struct.unpack_from(f"<{n}i", r, 8 + 4 * m)
+        pos = 0
+        for ne in nex:
+            flags.append((tuple(idet[pos:pos + 2 * ne:2]), tuple(idet[pos + 1:pos + 2 * ne:2])))
+            pos += 2 * ne
+    norb = info["norb"]
+    seen, out = set(), []
+    for h, p in flags:
+        fl = (tuple(sorted((x - norb if x > norb else x + norb) for x in h)),
+              tuple(sorted((x - norb if x > norb else x + norb) for x in p)))
+        out.append(1 if fl in seen and fl != (h, p) else 0)
+        seen.add((h, p))
+    return out
 
 
 def run_reference(args, rank: int, world: int):
-    """CPU restatement on all host cores; rank 0 only."""
+    """CPU restatement on all host cores; rank 0 only.  One long-lived
+    oracle process per core reads the inputs once, then runs one sampled
+    generator per step (W + K lines); a step's time is the slowest
+    process's loop time for that line, by the oracle's own clock."""
     if rank != 0:
         return
-    from oracle import build as ob
     from concurrent.futures import ProcessPoolExecutor
     import multiprocessing as mpm
+    from oracle import build as ob
     ob.build()
     base = tempfile.mkdtemp(prefix="cipsi_ref_bench_")
-    wd = make_workload(0, base)
-    write_info(wd)
+    wd, info = make_workload(args.workload, 0, base)
     ncores = os.cpu_count() or 1
-    every = 240  # about 4 generators per process per step
-    steps_t, contribs = [], []
+    sample = CPU_SAMPLE[args.workload]
+    nsteps = args.warmup + args.steps
+    plans = sample_plan(info["ncf"], _ysaut(wd, info), nsteps, ncores, sample)
     ctx = mpm.get_context("spawn")
     with ProcessPoolExecutor(max_workers=ncores, mp_context=ctx) as ex:
-        for it in range(args.warmup + args.steps):
-            t0 = time.perf_counter()
-            futs = [ex.submit(oracle_sample, wd, every * ncores, (it * ncores + c) % (every * ncores),
-                              c == 0 and it == 0, base) for c in range(ncores)]
-            res = [f.result() for f in futs]
-            dt = time.perf_counter() - t0
-            if it >= args.warmup:
-                steps_t.append(dt)
-                contribs.append(sum(r[0] for r in res))
+        futs = [ex.submit(oracle_plan, wd, plans[c], sample, base) for c in range(ncores)]
+        res = [f.result() for f in futs]
     shutil.rmtree(base, ignore_errors=True)
-    tot_t = sum(steps_t)
-    val = sum(contribs) / tot_t
+    metat = res[0][1]
+    contrib = tot_t = 0.0
+    for st in range(args.warmup, nsteps):
+        step = [r[0][st] for r in res if st < len(r[0])]
+        contrib += sum(n for n, _ in step) * metat
+        tot_t += max(t for _, t in step)
+    val = contrib / tot_t
     line = {"impl": "reference", "metric": METRIC, "value": val, "unit": UNIT, "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot_t / len(steps_t),
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot_t / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic (seeded integrals and reference space)", "config": workload_desc(),
+            "data": "synthetic (seeded integrals and reference space)", "config": workload_desc(args.workload),
             "cpu_baseline": {"value": val, "unit": UNIT, "cores": ncores, "kind": "port",
-                             "sample": f"each step: {ncores} processes, each on a disjoint 1/{every * ncores} "
-                                       "sample of the generators of S (all of diexcit's per-double set-up)"},
+                             "sample": f"each step: {ncores} processes (inputs read once per process), each on "
+                                       f"one generator of S with 1 candidate in {sample} kept (systematic "
+                                       "sample); rate = contributions / slowest loop time; extrapolated"},
             "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -251,127 +315,6 @@ def run_batched(args, rank: int, world: int, local_rank: int):
         print(json.dumps(line), flush=True)
 
 
-# ------------------------------------------------------------ large system
-def _oracle_on_mask(wd: str, mask, tmpbase: str):
-    """CPU oracle restricted to the generators of `mask` (no pertu block):
-    (oracle JSON, seconds)."""
-    from oracle import build as ob
-    run = tempfile.mkdtemp(dir=tmpbase)
-    shutil.rmtree(run)
-    shutil.copytree(wd, run)
-    mp_ = os.path.join(run, "mask.bin")
-    mask.tofile(mp_)
-    t0 = time.perf_counter()
-    j = json.load(open(ob.run(run, genmask=mp_, no_pertu_ref=True)))
-    dt = time.perf_counter() - t0
-    shutil.rmtree(run, ignore_errors=True)
-    return j, dt
-
-
-def run_large(args, rank: int, world: int, local_rank: int):
-    """The 120-orbital, 30-electron, S = 20,000, 2-root system: E2 time of
-    the whole step.  This recipe selects ~1.5e10 perturbers for unit 60,
-    more than device memory holds, so the records are counted and not
-    stored (a cipsi_fetch_result overflow, results valid).  The CPU oracle
-    is timed on two generators of S (one process each) and the GPU run on
-    the same two generators is compared with it (E2 parity at this size)."""
-    import numpy as np
-    import torch
-    from concurrent.futures import ProcessPoolExecutor
-    import multiprocessing as mpm
-    from cipsi_gb300 import batch, build, engine, synth
-    from oracle import build as ob
-    import dataclasses
-    torch.cuda.set_device(local_rank)
-    build.build()
-    ob.build()
-    base = tempfile.mkdtemp(prefix="cipsi_large_")
-    cfg = dataclasses.replace(synth.CONFIGS["large"])
-    cfg.seed += rank
-    wd = os.path.join(base, "large")
-    t0 = time.perf_counter()
-    synth.generate(cfg, wd)
-    t_gen = time.perf_counter() - t0
-    inp = engine.Inputs(wd)
-    ysaut = inp.array("ysaut")
-    ncf = inp.dims.ncf
-    picks = []
-    for start in (ncf // 3, (2 * ncf) // 3):
-        k = start
-        while ysaut[k]:
-            k += 1
-        picks.append(k)
-    # CPU oracle on the two generators, in parallel (started before any GPU work)
-    cpu = []
-    if rank == 0 and not args.no_cpu_baseline:
-        masks = []
-        for k in picks:
-            m = np.zeros(ncf, np.uint8)
-            m[k] = 1
-            masks.append(m)
-        with ProcessPoolExecutor(max_workers=len(masks), mp_context=mpm.get_context("spawn")) as ex:
-            futs = [ex.submit(_oracle_on_mask, wd, m, base) for m in masks]
-            cpu = [f.result() for f in futs]
-    ctx = engine.Context(inp.dims, device=local_rank)
-    ctx.upload(inp)
-    ctx.set_tuning(6, 0)
-    for _ in range(args.warmup):
-        ctx.run_async(inp.opts)
-        r = batch._fetch_allow_overflow(ctx)
-    clocks = Clocks(local_rank)
-    clocks.start()
-    ms = []
-    for _ in range(args.steps):
-        torch.cuda.synchronize()
-        ctx.run_async(inp.opts)
-        r = batch._fetch_allow_overflow(ctx)
-        ms.append(r["kernel_ms"])
-    # end to end: upload from host + run + results (records not stored)
-    t0 = time.perf_counter()
-    ctx.upload(inp)
-    ctx.run_async(inp.opts)
-    r2 = batch._fetch_allow_overflow(ctx)
-    e2e_ms = 1e3 * (time.perf_counter() - t0)
-    clk = clocks.stop()
-    contrib = r["n_processed"] * inp.dims.metat
-    line = {"metric": "perturber contributions/s", "value": contrib / (statistics.mean(ms) / 1e3),
-            "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": statistics.mean(ms), "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded integrals and reference space)",
-            "config": {"workload": "large: 120 MOs, 30 e-, Ms=0, S=20000 dets (ref + doubles, spin-flip closed), "
-                                   "2 roots, MP+EN, tau=0.005", "records": "counted, not stored"},
-            "e2e": {"value": contrib / (e2e_ms / 1e3), "unit": UNIT, "ms_per_step": e2e_ms},
-            "work": {"perturbers": r["n_processed"], "selected": r["n_selected"], "ietat": r["ietat"],
-                     "compares": r["n_compares"], "e2vp": r["e2vp"]},
-            "clocks": clk, "generation_s": t_gen}
-    if cpu:
-        # the GPU on the same two generators
-        m = np.zeros(ncf, np.uint8)
-        m[picks] = 1
-        ctx.run_async(inp.opts, gen_mask=m, run_pertu=False)
-        rs = batch._fetch_allow_overflow(ctx)
-        cpu_contrib = sum(j["n_processed"] * j["metat"] for j, _ in cpu)
-        cpu_s = sum(dt for _, dt in cpu)
-        par = {}
-        for key in ("e2mp", "e2vp", "e2b"):
-            ref = np.sum([np.array(j[key]) for j, _ in cpu], axis=0)
-            cond = np.sum([np.array(j.get("cond_" + key, [0.0] * len(j[key]))) for j, _ in cpu], axis=0)
-            diff = np.abs(np.array(rs[key]) - ref)
-            par[key] = {"max_abs_diff": float(diff.max()), "tolerance": float((1e-10 + cond).max()),
-                        "ok": bool(np.all(diff <= 1e-10 + cond))}
-        par["n_processed_equal"] = rs["n_processed"] == sum(j["n_processed"] for j, _ in cpu)
-        line["cpu_baseline"] = {"value": cpu_contrib / cpu_s, "unit": UNIT, "cores": 1, "kind": "port",
-                                "sample": f"generators {picks} of S (one process each), {cpu_s:.0f} core-s; "
-                                          "rate per core, extrapolated to the whole step linearly in "
-                                          "contributions"}
-        line["parity_sample"] = par
-    ctx.close()
-    inp.close()
-    shutil.rmtree(base, ignore_errors=True)
-    if rank == 0:
-        print(json.dumps(line), flush=True)
-
-
 # ------------------------------------------------------------ adjoint form
 def run_adjoint_form(args, rank: int, world: int, local_rank: int):
     """The medium system plus a seeded symmetric dipole matrix mu ~ N(0, 0.5):
@@ -385,7 +328,7 @@ def run_adjoint_form(args, rank: int, world: int, local_rank: int):
     from cipsi_gb300 import adjoint, build, synth
     torch.cuda.set_device(local_rank)
     build.build()
-    cfg = synth.CONFIGS[CONFIG]
+    cfg = synth.CONFIGS["medium"]
     base = tempfile.mkdtemp(prefix="cipsi_adj_")
     wd = os.path.join(base, "sys")
     synth.generate(cfg, wd)
@@ -478,6 +421,27 @@ def run_adjoint_form(args, rank: int, world: int, local_rank: int):
 
 
 # ------------------------------------------------------------ GPU arm
+KERNEL_SOURCES = ["pt2_kernel.cuh", "pt2_common.cuh", "pt2_w1.cu", "pt2_w2.cu"]
+
+
+def kernel_sha() -> str:
+    h = hashlib.sha256()
+    for f in KERNEL_SOURCES:
+        with open(os.path.join(ROOT, "cipsi_gb300", "csrc", f), "rb") as fh:
+            h.update(fh.read())
+    return h.hexdigest()[:16]
+
+
+def kernel_profile(workload: str):
+    """The ncu figures of k_pt2 on this workload (profiles/k_pt2_<workload>.json)
+    when they were captured on the current kernel sources, else None."""
+    path = os.path.join(ROOT, "profiles", f"k_pt2_{workload}.json")
+    if not os.path.exists(path):
+        return None
+    d = json.load(open(path))
+    return d if d.get("kernel_sha") == kernel_sha() else None
+
+
 def run_gpu(args, rank: int, world: int, local_rank: int):
     import numpy as np
     import torch
@@ -488,9 +452,12 @@ def run_gpu(args, rank: int, world: int, local_rank: int):
     torch.cuda.set_device(local_rank)
     build.build()
     base = tempfile.mkdtemp(prefix=f"cipsi_bench_r{rank}_")
-    wd = make_workload(rank, base)
-    info = write_info(wd)
+    t0 = time.perf_counter()
+    wd, info = make_workload(args.workload, rank, base)
+    t_gen = time.perf_counter() - t0
     inp = engine.Inputs(wd)
+    mt = inp.dims.metat
+    W = 1 if inp.dims.norb <= 64 else 2
     ctx = engine.Context(inp.dims, device=local_rank)
     stream = torch.cuda.Stream()
     ctx.set_stream(stream.cuda_stream)
@@ -505,15 +472,16 @@ def run_gpu(args, rank: int, world: int, local_rank: int):
     if args.gen_every > 1:
         gmask = np.zeros(inp.dims.ncf, dtype=np.uint8)
         gmask[::args.gen_every] = 1
+    chunk = args.chunk_records
     for _ in range(args.warmup):
-        res = ctx.run(inp.opts, gen_mask=gmask)  # grows the selection buffer as needed
-    contrib_per_step = res["n_processed"] * inp.dims.metat
+        res = ctx.run_stream(inp.opts, chunk_records=chunk, gen_mask=gmask)
+    contrib_per_step = res["n_processed"] * mt
     clocks = Clocks(local_rank)
     clocks.start()
-    # ---- device-resident timing
+    # ---- device-resident timing: the streamed run, records kept on the device
     barrier()
     torch.cuda.synchronize()
-    step_ms, kern_ms = [], []
+    step_ms, pt2_ms = [], []
     launches = 0
     for _ in range(args.steps):
         with torch.cuda.stream(stream):
@@ -521,99 +489,111 @@ def run_gpu(args, rank: int, world: int, local_rank: int):
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        ctx.run_async(inp.opts, gen_mask=gmask)
+        r = ctx.run_stream(inp.opts, chunk_records=chunk, gen_mask=gmask)
         e1.record(stream)
-        r = ctx.fetch()
-        assert r["n_processed"] * inp.dims.metat == contrib_per_step
+        stream.synchronize()
+        assert r["n_processed"] * mt == contrib_per_step and r["n_selected"] == res["n_selected"]
         step_ms.append(e0.elapsed_time(e1))
-        kern_ms.append(r["kernel_ms"])
-        launches += 2  # k_pt2 + k_reduce
+        pt2_ms.append(r["pt2_ms"])
+        launches += r["launches"]
     torch.cuda.synchronize()
     barrier()
-    # ---- end-to-end through the C ABI from host buffers
+    # ---- end to end through the C ABI: upload from host buffers, stream,
+    # every record delivered to host memory and folded into a digest
     e2e_ms = []
-    nsel = r["n_selected"]
-    W = 1 if inp.dims.norb <= 64 else 2
-    pinned = {"bits": torch.empty((nsel, 2 * W), dtype=torch.int64, pin_memory=True).numpy().view(np.uint64),
-              "owner": torch.empty(nsel, dtype=torch.int32, pin_memory=True).numpy(),
-              "xam": torch.empty(nsel, dtype=torch.float64, pin_memory=True).numpy(),
-              "evp": torch.empty((nsel, inp.dims.metat), dtype=torch.float64, pin_memory=True).numpy()}
-    # the kernel writes the unit-60 records straight into these pinned host
-    # arrays (cipsi_set_selection_sink) while it computes
-    ctx.set_selection_sink(pinned)
-    for _ in range(args.steps):
+    digests = []
+    n_e2e = max(1, min(args.steps, args.e2e_steps))
+    for _ in range(n_e2e):
         with torch.cuda.stream(stream):
             flush.zero_()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         ctx.upload(inp)
-        ctx.run_async(inp.opts, gen_mask=gmask)
-        r2 = ctx.fetch()
-        ctx.selection_raw(r2["n_selected"], out=pinned)  # in place: nothing left to copy
+        d = engine.Digest()
+        d.threads = max(1, (os.cpu_count() or 2) - 1)
+        r2 = ctx.run_stream(inp.opts, chunk_records=chunk, consumer=d, gen_mask=gmask)
         e2e_ms.append(1e3 * (time.perf_counter() - t0))
-    ctx.set_selection_sink(None)
+        assert d.records == r2["n_selected"] == res["n_selected"]
+        digests.append(d.value())
+    assert all(x == digests[0] for x in digests), "streamed records differ between runs"
     clk = clocks.stop()
     tot_ms = sum(step_ms)
     tot_e2e = sum(e2e_ms)
     if world > 1:
-        t = torch.tensor([tot_ms, tot_e2e, float(contrib_per_step)], dtype=torch.float64, device="cuda")
+        t = torch.tensor([tot_ms, tot_e2e / n_e2e * args.steps, float(contrib_per_step)], dtype=torch.float64,
+                         device="cuda")
         mx = t.clone()
         torch.distributed.all_reduce(mx[:2], op=torch.distributed.ReduceOp.MAX)
         sm = t.clone()
         torch.distributed.all_reduce(sm[2:], op=torch.distributed.ReduceOp.SUM)
-        tot_ms, tot_e2e, all_contrib = float(mx[0]), float(mx[1]), float(sm[2])
+        tot_ms, tot_e2e_k, all_contrib = float(mx[0]), float(mx[1]), float(sm[2])
     else:
+        tot_e2e_k = tot_e2e / n_e2e * args.steps
         all_contrib = float(contrib_per_step)
     value = all_contrib * args.steps / (tot_ms / 1e3)
-    e2e_value = all_contrib * args.steps / (tot_e2e / 1e3)
-    # bytes copied per e2e step
-    n, nint = inp.dims.norb, None
-    ninte = os.path.getsize(os.path.join(wd, "ijkl"))  # upper bound source; exact below
-    from cipsi_gb300 import synth
-    recs = synth.read_records(os.path.join(wd, "ijkl"))
+    e2e_value = all_contrib * args.steps / (tot_e2e_k / 1e3)
+    # bytes copied per e2e step: the inputs up, the results and records down
+    synth = _synth()
     import struct
-    nint = struct.unpack_from("<i", recs[7], 0)[0]
-    ncf, mt = inp.dims.ncf, inp.dims.metat
+    recs = synth.read_records(os.path.join(wd, "ijkl"))
+    ninte = struct.unpack_from("<i", recs[7], 0)[0]
+    n, ncf = inp.dims.norb, inp.dims.ncf
     nter = n * (n + 1) // 2
-    h2d = (nint * 4 + 3 * nter * 8 + n * n * 4 + (nsym := inp.dims.nsym) * 4 + n + ncf * 2 * W * 8
+    h2d = (ninte * 4 + 3 * nter * 8 + n * n * 4 + inp.dims.nsym * 4 + n + ncf * 2 * W * 8
            + ncf * (1 + 1 + 4) + ncf * mt * 8 + 2 * n * 8)
-    d2h = (5 * mt * 8 + 8 * (10 + 1 + 10 + 10 * 8) + 2 * 10 * 8 * 8
-           + nsel * (2 * W * 8 + 4 + 8 + mt * 8))  # results + the records (kernel writes to pinned host)
+    nsel = res["n_selected"]
+    rec_bytes = 2 * W * 8 + 4 + 8 + mt * 8
+    d2h = 5 * mt * 8 + 8 * (10 + 1 + 10 + 10 * 8) + 2 * 10 * 8 * 8 + nsel * rec_bytes
     peak, peak_kind = measured_peaks()
-    kms = statistics.mean(kern_ms)
+    kms = statistics.mean(pt2_ms)
+    nl = max(1, (r["launches"] - 1) // 3)  # k_pt2 launches per step (one per chunk)
     achieved = r["alg_bytes"] / (kms / 1e3) / 1e9
+    prof = kernel_profile(args.workload) if args.gen_every == 1 else None
+    traffic = prof["dram_bytes_per_candidate"] * r["n_candidates"] / nl if prof else None
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": tot_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded integrals and reference space)",
-            "config": dict(workload_desc(), parallelism=f"replicas x{world}" if world > 1 else "single GPU",
+            "config": dict(workload_desc(args.workload),
                            **({"generator_sample": f"1/{args.gen_every} (profiling run)"}
                               if args.gen_every > 1 else {})),
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
-                    "d2h_bytes_per_step": int(d2h), "ms_per_step": tot_e2e / args.steps},
+                    "d2h_bytes_per_step": int(d2h), "ms_per_step": tot_e2e / n_e2e, "steps": n_e2e,
+                    "records_delivered_per_step": int(nsel), "record_bytes": rec_bytes,
+                    "digest": [format(x, "016x") for x in digests[0]]},
             "gpu_launches": launches,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak,
-                         "traffic": NCU_DRAM_BYTES_PER_LAUNCH if args.gen_every == 1 else None,
-                         "kernel": "k_pt2", "peak_source": peak_kind,
-                         "algorithmic_bytes_per_launch": r["alg_bytes"],
+                         "frac": achieved / peak, "traffic": traffic,
+                         "kernel": "k_pt2", "peak_source": peak_kind, "launches_per_step": nl,
+                         "algorithmic_bytes_per_launch": r["alg_bytes"] / nl,
+                         "kernel_ms_per_launch": kms / nl,
                          "note": "achieved = algorithmic bytes of the E2 loop (integral, coefficient and "
-                                 "diagonal-term reads) per launch / mean k_pt2+k_reduce time, against the "
-                                 "measured HBM copy bandwidth; the kernel is bound by the FP64 pipe (~55 % "
-                                 "busy) and L1/L2/shared-memory latency, not HBM; traffic (ncu) is mostly "
-                                 "unit-60 records and local-memory write-backs"},
+                                 "diagonal-term reads) / k_pt2 time (CUDA events around each chunk's launch on "
+                                 "its stream), against the measured HBM copy bandwidth; traffic: DRAM bytes per "
+                                 "launch scaled from an ncu capture of this kernel build on a generator sample "
+                                 "(null when the kernel changed since); the kernel is bound by FP64 issue and "
+                                 "latency, not HBM"},
             "clocks": clk,
             "work": {"perturbers": r["n_processed"], "candidates": r["n_candidates"],
                      "compares": r["n_compares"], "pairs_1": r["n_pairs_1"], "pairs_2": r["n_pairs_2"],
-                     "selected": r["n_selected"], "ietat": r["ietat"], "e2vp": r["e2vp"]}}
+                     "selected": r["n_selected"], "ietat": r["ietat"], "e2vp": r["e2vp"], "e2mp": r["e2mp"],
+                     "device_ms_per_step_incl_records": tot_ms / args.steps,
+                     "k_pt2_ms_per_step": kms, "generation_s": t_gen}}
+    if prof:
+        line["roofline"]["issue_slots"] = {"frac": prof.get("issue_active_frac"),
+                                           "fp64_pipe_frac": prof.get("fp64_pipe_frac"),
+                                           "source": prof.get("command")}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         from oracle import build as ob
         ob.build()
-        every = 400
-        contrib, dt = oracle_sample(wd, every, 0, False, base)
-        line["cpu_baseline"] = {"value": contrib / dt, "unit": UNIT, "cores": 1, "kind": "port",
-                                "sample": f"generators k = 0 mod {every} of S (1/{every} of the "
-                                          f"generators), {dt:.1f} s on one core"}
+        sample = CPU_SAMPLE[args.workload]
+        plan = sample_plan(inp.dims.ncf, inp.array("ysaut"), 1, 1, sample, seed=11)[0]
+        res_c, metat = oracle_plan(wd, plan, sample, base)
+        nproc, secs = res_c[0]
+        line["cpu_baseline"] = {"value": nproc * metat / secs, "unit": UNIT, "cores": 1, "kind": "port",
+                                "sample": f"generator {plan[0][1]} of S, 1 candidate in {sample} (systematic "
+                                          f"sample), {secs:.1f} s loop time on one core, inputs read once; "
+                                          "extrapolated linearly in contributions"}
     ctx.close()
     shutil.rmtree(base, ignore_errors=True)
     if rank == 0:
@@ -632,9 +612,11 @@ def main():
     ap.add_argument("--form", choices=["plain", "batched", "adjoint"], default="plain",
                     help="batched: the potential-curve batch (geometries/s, batched vs plain); "
                          "adjoint: dE2/d integrals on the medium system with checks")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="large")
+    ap.add_argument("--chunk-records", type=int, default=0,
+                    help="records per streamed chunk (0 = sized from free device memory)")
+    ap.add_argument("--e2e-steps", type=int, default=3, help="end-to-end steps (at most --steps)")
     ap.add_argument("--fd-elements", type=int, default=200)
-    ap.add_argument("--workload", choices=["medium", "large"], default="medium",
-                    help="large: the 120-orbital S = 20,000 system (plain form, records counted only)")
     ap.add_argument("--geometries", type=int, default=256)
     ap.add_argument("--batch-steps", type=int, default=2)
     ap.add_argument("--batch-warmup", type=int, default=1)
@@ -654,9 +636,6 @@ def main():
         return
     if args.form == "adjoint":
         run_adjoint_form(args, rank, world, local_rank)
-        return
-    if args.workload == "large":
-        run_large(args, rank, world, local_rank)
         return
     run_gpu(args, rank, world, local_rank)
 

@@ -1115,6 +1115,74 @@ void write_pie_records(std::FILE* f, const std::vector<int32_t>& nec, const std:
   }
 }
 
+// Record consumer of cipsi_run_pt2_stream that writes the selected
+// perturbers to unit 60 as pie.f does (cip/pie.f, cipsym/pie.f): records of
+// lungo = 1000 determinants, each with its excitation list relative to the
+// reference (holes and particles as 1-based spin orbitals, beta ones offset
+// by norb), v = xam and, in cipsym, ENvp per root.  Pieces arrive in record
+// order; a partial record waits for the next piece.
+struct Unit60Writer {
+  std::FILE* f;
+  int norb, noca, metat;
+  bool sym_variant;
+  std::vector<int32_t> nec, h, p;
+  std::vector<double> v, ev;
+  int64_t written = 0;
+  void add(int words, const uint64_t* bits, double xam, const double* evp) {
+    const int W = words / 2;
+    int nh = 0, np = 0;
+    int32_t hh[8] = {0}, pp[8] = {0};
+    for (int s = 0; s < 2; ++s)
+      for (int w = 0; w < W; ++w) {
+        const uint64_t word = bits[s * W + w];
+        const int lo = w * 64;
+        const int nref = std::min(std::max(noca - lo, 0), 64);
+        const uint64_t ref = nref >= 64 ? ~0ull : ((1ull << nref) - 1ull);
+        uint64_t hm = ref & ~word, pm = word & ~ref;
+        while (hm) {
+          const int b = __builtin_ctzll(hm);
+          hm &= hm - 1;
+          if (nh < 8) hh[nh] = lo + b + 1 + s * norb;
+          ++nh;
+        }
+        while (pm) {
+          const int b = __builtin_ctzll(pm);
+          pm &= pm - 1;
+          if (np < 8) pp[np] = lo + b + 1 + s * norb;
+          ++np;
+        }
+      }
+    if (nh > 8) throw Error("selected determinant with excitation degree > 8 (pie.f)");
+    nec.push_back(nh);
+    for (int l = 0; l < 8; ++l) {
+      h.push_back(hh[l]);
+      p.push_back(pp[l]);
+    }
+    v.push_back(xam);
+    for (int m = 0; m < metat; ++m) ev.push_back(evp[m]);
+    if (nec.size() == 1000) flush();
+  }
+  void flush() {
+    if (nec.empty()) return;
+    write_pie_records(f, nec, h, p, v, ev, metat, sym_variant, 8);
+    written += (int64_t)nec.size();
+    nec.clear(); h.clear(); p.clear(); v.clear(); ev.clear();
+  }
+};
+
+int unit60_consumer(void* user, int64_t first, int64_t count, int32_t words, int32_t metat, const uint64_t* bits,
+                    const int32_t* owner, const double* xam, const double* evp) {
+  (void)first;
+  (void)owner;
+  Unit60Writer* w = static_cast<Unit60Writer*>(user);
+  try {
+    for (int64_t i = 0; i < count; ++i) w->add(words, bits + (size_t)i * words, xam[i], evp + (size_t)i * metat);
+  } catch (const std::exception&) {
+    return 1;
+  }
+  return 0;
+}
+
 std::string json_array(const double* x, int n) {
   std::ostringstream s;
   s.precision(17);
@@ -1293,35 +1361,40 @@ extern "C" int cipsi_cip_main(const char* workdir, const char* stdin_path, int32
     };
     const std::vector<int> itm = root_flip_signs(R);
     cipsi_result res{};
-    if (R.o.ityper != 0) {  // ityper = 0: no perturbation (deter.f:231), no device work
-      chk(cipsi_ctx_create(&ctx, &d, device), "cipsi_ctx_create");
-      chk(cipsi_inputs_upload(in, ctx), "cipsi_inputs_upload");
-      chk(cipsi_run_pt2(ctx, &op, &res), "cipsi_run_pt2");
-    }
-    const auto t1 = std::chrono::steady_clock::now();
-    // unit 60 when ymoyen: S (v = 1) then the selected perturbers; without
-    // ymoyen the reference writes nothing to it (cip.f:222, pert1.f:264)
+    // unit 60 when ymoyen: S (v = 1) then the selected perturbers, streamed
+    // from the GPU chunk by chunk and written while the next chunk computes;
+    // without ymoyen the reference writes nothing to it (cip.f:222,
+    // pert1.f:264)
     long long ntot = 0;
+    std::FILE* f60 = nullptr;
     if (R.o.ymoyen) {
-      std::FILE* f60 = std::fopen(R.o.f60.c_str(), "wb");
+      f60 = std::fopen(R.o.f60.c_str(), "wb");
       if (!f60) throw Error("cannot rewrite " + R.o.f60);
       std::vector<int> identity(R.ncf);
       for (int k = 0; k < R.ncf; ++k) identity[k] = k;
       ntot += write_space_unit60(f60, R, identity, sym_variant != 0);
-      const int64_t ns = res.n_selected;
-      const int64_t chunk = 1 << 20;  // records converted per call (a multiple of lungo)
-      for (int64_t first = 0; first < ns; first += chunk) {
-        const int64_t cnt = std::min(chunk, ns - first);
-        std::vector<int32_t> snec(cnt), sh((size_t)cnt * 8), sp((size_t)cnt * 8), own(cnt);
-        std::vector<double> sx(cnt), sev((size_t)cnt * R.metat);
-        chk(cipsi_selection_get(ctx, first, cnt, snec.data(), sh.data(), sp.data(), sx.data(), sev.data(),
-                                own.data()),
-            "cipsi_selection_get");
-        write_pie_records(f60, snec, sh, sp, sx, sev, R.metat, sym_variant != 0, 8);
-      }
-      ntot += ns;
-      std::fclose(f60);
     }
+    struct CloseFile {
+      std::FILE*& f;
+      ~CloseFile() { if (f) std::fclose(f); }
+    } close60{f60};
+    if (R.o.ityper != 0) {  // ityper = 0: no perturbation (deter.f:231), no device work
+      chk(cipsi_ctx_create(&ctx, &d, device), "cipsi_ctx_create");
+      chk(cipsi_inputs_upload(in, ctx), "cipsi_inputs_upload");
+      if (f60) {
+        Unit60Writer w{f60, R.norb, R.noc, R.metat, sym_variant != 0, {}, {}, {}, {}, {}, 0};
+        chk(cipsi_run_pt2_stream(ctx, &op, 0, unit60_consumer, &w, &res), "cipsi_run_pt2_stream");
+        w.flush();
+        ntot += w.written;
+      } else {
+        chk(cipsi_run_pt2(ctx, &op, &res), "cipsi_run_pt2");
+      }
+    }
+    if (f60) {
+      std::fclose(f60);
+      f60 = nullptr;
+    }
+    const auto t1 = std::chrono::steady_clock::now();
     write_unit4_results(R, res.e2mp, res.e2vp, res.e2b, itm);
     // listing lines the Autocip driver reads (cipsym/cip.f:253-254, cip.f:243-247)
     std::printf("0 ont ete generes:    %10lld  etats efficaces\n", (long long)res.ietat);

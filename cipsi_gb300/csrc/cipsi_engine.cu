@@ -10,6 +10,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "pt2_common.cuh"
@@ -82,6 +83,85 @@ __global__ void k_slice_reduce(const double* sl, int nblocks, int stride, int nt
   else gf[i - 3 * nt] = s;
 }
 
+// Output offsets of the unit segments: unit_out[u] = base + the records of
+// units u0..u-1 (exclusive scan of unit_nsel over [u0, u1), one block);
+// *total = the records of [u0, u1).
+constexpr int kScanThreads = 1024;
+__global__ void __launch_bounds__(kScanThreads) k_scan_units(const int32_t* nsel, long long* out, int u0, int u1,
+                                                             long long base, unsigned long long* total) {
+  __shared__ long long wsum[kScanThreads / 32];
+  __shared__ long long carry;
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  if (tid == 0) carry = base;
+  __syncthreads();
+  for (int c0 = u0; c0 < u1; c0 += kScanThreads) {
+    const int u = c0 + tid;
+    const long long v = u < u1 ? nsel[u] : 0;
+    long long incl = v;
+    for (int o = 1; o < 32; o <<= 1) {
+      const long long y = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += y;
+    }
+    if (lane == 31) wsum[wid] = incl;
+    __syncthreads();
+    if (wid == 0) {
+      long long w = wsum[lane];
+      for (int o = 1; o < 32; o <<= 1) {
+        const long long y = __shfl_up_sync(0xffffffffu, w, o);
+        if (lane >= o) w += y;
+      }
+      wsum[lane] = w;  // inclusive over warps
+    }
+    __syncthreads();
+    const long long before = carry + (wid ? wsum[wid - 1] : 0) + (incl - v);
+    if (u < u1) out[u] = before;
+    __syncthreads();
+    if (tid == 0) carry += wsum[kScanThreads / 32 - 1];
+    __syncthreads();
+  }
+  if (tid == 0 && total) *total = (unsigned long long)(carry - base);
+}
+
+// Records of units [u0, u1) from their pool segments to the output arrays
+// at unit_out[u] - out_base (unit order), with the owner (1-based generator
+// index, 0 for pertu's candidates) taken from the unit; records beyond
+// out_cap are dropped (the run reports an overflow).
+struct GatherArgs {
+  const uint64_t* pool_bits;
+  const double* pool_xam;
+  const double* pool_evp;
+  long long pool_cap;
+  const long long* unit_pool;
+  const int32_t* unit_nsel;
+  const long long* unit_out;
+  const int32_t* unit_g;
+  const int32_t* gens;
+  int u0, u1, words, metat;
+  long long out_base, out_cap;
+  uint64_t* out_bits;
+  int32_t* out_owner;
+  double* out_xam;
+  double* out_evp;
+};
+__global__ void __launch_bounds__(256) k_gather(GatherArgs a) {
+  for (int u = a.u0 + blockIdx.x; u < a.u1; u += gridDim.x) {
+    const int n = a.unit_nsel[u];
+    if (n == 0) continue;
+    const long long src = a.unit_pool[u];
+    const long long dst = a.unit_out[u] - a.out_base;
+    const int k = a.gens[a.unit_g[u]];
+    const int owner = k < 0 ? 0 : k + 1;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+      const long long d = dst + i, q = src + i;
+      if (d >= a.out_cap || q >= a.pool_cap) break;
+      for (int w = 0; w < a.words; ++w) a.out_bits[d * a.words + w] = a.pool_bits[q * a.words + w];
+      a.out_owner[d] = owner;
+      a.out_xam[d] = a.pool_xam[q];
+      for (int m = 0; m < a.metat; ++m) a.out_evp[d * a.metat + m] = a.pool_evp[q * a.metat + m];
+    }
+  }
+}
+
 // zero what every geometry of a batch accumulates into (block b: geometry b)
 __global__ void k_batch_clear(const Params* geo) {
   const Params& p = geo[blockIdx.x];
@@ -90,6 +170,7 @@ __global__ void k_batch_clear(const Params* geo) {
   for (int i = threadIdx.x; i < 2 * kNClass * kMaxRoots; i += blockDim.x) p.hist_tab[i] = 0.0;
   const long long npart = (long long)max(p.nunits, 1) * 5 * p.metat;
   for (long long i = threadIdx.x; i < npart; i += blockDim.x) p.gen_part[i] = 0.0;
+  if (threadIdx.x == 0 && p.pool_count) *p.pool_count = 0ull;
 }
 
 }  // namespace
@@ -148,7 +229,39 @@ struct cipsi_ctx {
   int32_t* dsel_owner = nullptr;
   double *dsel_xam = nullptr, *dsel_evp = nullptr;
   long long sel_cap = 0;
-  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  // record path: per-CTA staging (slot-indexed), the pool of unit segments,
+  // the unit table (segment, records, output offset)
+  uint64_t* dst_bits = nullptr;
+  double *dst_xam = nullptr, *dst_evp = nullptr;
+  uint32_t* dst_mask = nullptr;
+  size_t st_slots = 0;  // allocated grid x st_cap slots
+  uint64_t* dpool_bits = nullptr;
+  double *dpool_xam = nullptr, *dpool_evp = nullptr;
+  long long pool_cap = 0;
+  unsigned long long* dpool_count = nullptr;
+  long long* dunit_pool = nullptr;
+  int32_t* dunit_nsel = nullptr;
+  long long* dunit_out = nullptr;
+  unsigned long long* dscan_total = nullptr;
+  int unit_tab_cap = 0;
+  // streamed runs (cipsi_run_pt2_stream): two device record buffers, a copy
+  // stream, a ring of pinned host buffers; per-unit record counts of the
+  // last run, reused to size the chunks of a run with the same plan
+  uint64_t* dout_bits[2] = {nullptr, nullptr};
+  int32_t* dout_owner[2] = {nullptr, nullptr};
+  double* dout_xam[2] = {nullptr, nullptr};
+  double* dout_evp[2] = {nullptr, nullptr};
+  long long out_cap = 0;
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t ev_gathered[2] = {nullptr, nullptr}, ev_copied[2] = {nullptr, nullptr};
+  cudaEvent_t ev_host[2] = {nullptr, nullptr};
+  void* hbuf[2] = {nullptr, nullptr};
+  long long hbuf_cap = 0;
+  int stream_chunks = 0;  // chunks of the last streamed run
+  std::vector<int32_t> last_unit_nsel;
+  unsigned long long last_plan_sig = 0;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr, evk = nullptr;  // evk: end of k_pt2
+  long long last_launches = 0;
   // launch tuning (cipsi_set_tuning): R blocks per work unit for generators
   // of excitation rank >= 2 (rank 0/1 generators get one block per unit),
   // and CTAs per SM (0 = as many as the shared-memory L_R size allows)
@@ -260,6 +373,7 @@ int cipsi_ctx_create(cipsi_ctx** out, const cipsi_dims* dims, int32_t device) {
   ctx->stream = ctx->own_stream;
   CK(cudaEventCreate(&ctx->ev0));
   CK(cudaEventCreate(&ctx->ev1));
+  CK(cudaEventCreate(&ctx->evk));
   return CIPSI_OK;
 }
 
@@ -276,8 +390,19 @@ void cipsi_ctx_destroy(cipsi_ctx* ctx) {
   dfree(ctx->dnb_j); dfree(ctx->dnb_em); dfree(ctx->dlr_ent); dfree(ctx->dgen_part);
   dfree(ctx->dcounters); dfree(ctx->dhist_tab); dfree(ctx->dred); dfree(ctx->dwork);
   dfree(ctx->dsel_bits); dfree(ctx->dsel_owner); dfree(ctx->dsel_xam); dfree(ctx->dsel_evp);
+  dfree(ctx->dst_bits); dfree(ctx->dst_xam); dfree(ctx->dst_evp); dfree(ctx->dst_mask);
+  dfree(ctx->dpool_bits); dfree(ctx->dpool_xam); dfree(ctx->dpool_evp); dfree(ctx->dpool_count);
+  dfree(ctx->dunit_pool); dfree(ctx->dunit_nsel); dfree(ctx->dunit_out); dfree(ctx->dscan_total);
+  for (int i = 0; i < 2; ++i) {
+    dfree(ctx->dout_bits[i]); dfree(ctx->dout_owner[i]); dfree(ctx->dout_xam[i]); dfree(ctx->dout_evp[i]);
+    if (ctx->hbuf[i]) cudaFreeHost(ctx->hbuf[i]);
+    for (cudaEvent_t e : {ctx->ev_gathered[i], ctx->ev_copied[i], ctx->ev_host[i]})
+      if (e) cudaEventDestroy(e);
+  }
+  if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
   if (ctx->ev0) cudaEventDestroy(ctx->ev0);
   if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+  if (ctx->evk) cudaEventDestroy(ctx->evk);
   if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
   delete ctx;
 }
@@ -533,6 +658,8 @@ struct RunPlan {
   std::vector<int32_t> gens;   // generator indices (0-based); -1 = pertu block
   std::vector<uint8_t> gmask;  // allowed rank changes, bit (D + 2)
   std::vector<int32_t> ug, ur0, ur1;
+  std::vector<long long> uslots;  // candidate slots per unit (block_candidates over its allowed blocks)
+  long long max_slots = 0;
   bool pertu_ref = false, pertu_mono = false;
 };
 
@@ -597,60 +724,72 @@ void plan_run(const cipsi_ctx* ctx, const cipsi_opts* o, int r_chunk, RunPlan& p
     const int rb = gens[b] < 0 ? -1 : ctx->rank[gens[b]];
     return ra < rb;
   });
-  std::vector<int> hfe(nel);
+  std::vector<int> hfe(nel), spe(nel);
+  auto push = [&](int g, int a, int b, long long slots) {
+    ug.push_back(g);
+    ur0.push_back(a);
+    ur1.push_back(b);
+    pl.uslots.push_back(slots);
+    pl.max_slots = std::max(pl.max_slots, slots);
+  };
   for (int g : order) {
     const int k = gens[g];
     if (k < 0) {
       const int ntot = (pertu_ref ? 1 : 0) + (pertu_mono ? 2 * noca * (n - noca) : 0);
-      for (int t = 0; t < ntot; t += kPertuChunk) {
-        ug.push_back(g);
-        ur0.push_back(t);
-        ur1.push_back(std::min(ntot, t + kPertuChunk));
-      }
+      for (int t = 0; t < ntot; t += kPertuChunk) push(g, t, std::min(ntot, t + kPertuChunk), std::min(ntot, t + kPertuChunk) - t);
       continue;
     }
     // electrons of k: alpha orbitals ascending, then beta; HF-occupied?
-    int ne = 0;
+    int ne = 0, nes[2] = {0, 0};
     for (int sp = 0; sp < 2; ++sp)
       for (int orb = 0; orb < n; ++orb)
-        if ((ctx->Sbits[(size_t)k * 2 * W + sp * W + (orb >> 6)] >> (orb & 63)) & 1ull) hfe[ne++] = orb < noca;
+        if ((ctx->Sbits[(size_t)k * 2 * W + sp * W + (orb >> 6)] >> (orb & 63)) & 1ull) {
+          spe[ne] = sp;
+          hfe[ne++] = orb < noca;
+          ++nes[sp];
+        }
+    const int nv[2] = {n - nes[0], n - nes[1]};
     const uint8_t m = gmask[g];
-    auto allowed = [&](int r) {
-      int hfR, nRr;
+    // rank-change class allowed for block r?  Its candidates (slots).
+    auto block = [&](int r, long long& cands) {
+      int hfR, nRr, e1, e2 = -1;
       if (r < nel) {
+        e1 = r;
         hfR = hfe[r];
         nRr = 1;
       } else {
-        int t = r - nel, e1 = 0;
+        int t = r - nel;
+        e1 = 0;
         while (t >= nel - 1 - e1) {
           t -= nel - 1 - e1;
           ++e1;
         }
-        hfR = hfe[e1] + hfe[e1 + 1 + t];
+        e2 = e1 + 1 + t;
+        hfR = hfe[e1] + hfe[e2];
         nRr = 2;
       }
+      cands = block_candidates(nRr, e2 >= 0 && spe[e1] == spe[e2], nv[spe[e1]], nv[0], nv[1]);
       for (int aV = 0; aV <= nRr; ++aV)
         if (m & (1u << (hfR + aV - nRr + 2))) return true;
       return false;
     };
     const int kRChunk = ctx->rank[k] <= 1 ? 1 : kRChunkHigh;
-    int cnt = 0, start = -1;
+    int cnt = 0, start = -1, last = -1;
+    long long slots = 0;
     for (int r = 0; r < nR; ++r) {
-      if (!allowed(r)) continue;
+      long long c;
+      if (!block(r, c)) continue;
       if (start < 0) start = r;
+      last = r;
+      slots += c;
       if (++cnt == kRChunk) {
-        ug.push_back(g);
-        ur0.push_back(start);
-        ur1.push_back(r + 1);
+        push(g, start, r + 1, slots);
         cnt = 0;
         start = -1;
+        slots = 0;
       }
     }
-    if (start >= 0) {
-      ug.push_back(g);
-      ur0.push_back(start);
-      ur1.push_back(nR);
-    }
+    if (start >= 0) push(g, start, last + 1, slots);
   }
 }
 
@@ -676,6 +815,33 @@ LaunchShape launch_shape(int W, int R, int ncf_max, int ctas) {
   ls.smem = (((size_t)ls.lr_cap * per_entry + 15) & ~(size_t)15) + qbytes + 16;
   ls.blocks_per_sm = ctas == 1 ? 1 : ls.smem <= 95 * 1024 ? 2 : 1;
   return ls;
+}
+
+// The record pool (unit segments), for `cap` records.
+int grow_pool(cipsi_ctx* ctx, long long cap) {
+  const int W = ctx->W, mt = ctx->d.metat;
+  ++ctx->buf_gen;
+  dfree(ctx->dpool_bits); dfree(ctx->dpool_xam); dfree(ctx->dpool_evp);
+  ctx->pool_cap = 0;
+  CK(cudaMalloc(&ctx->dpool_bits, (size_t)cap * 2 * W * sizeof(uint64_t)));
+  CK(cudaMalloc(&ctx->dpool_xam, (size_t)cap * sizeof(double)));
+  CK(cudaMalloc(&ctx->dpool_evp, (size_t)cap * mt * sizeof(double)));
+  ctx->pool_cap = cap;
+  return CIPSI_OK;
+}
+
+// The device record arrays (cipsi_selection_get / raw), for `cap` records.
+int grow_sel(cipsi_ctx* ctx, long long cap) {
+  const int W = ctx->W, mt = ctx->d.metat;
+  ++ctx->buf_gen;
+  dfree(ctx->dsel_bits); dfree(ctx->dsel_owner); dfree(ctx->dsel_xam); dfree(ctx->dsel_evp);
+  ctx->sel_cap = 0;
+  CK(cudaMalloc(&ctx->dsel_bits, (size_t)cap * 2 * W * sizeof(uint64_t)));
+  CK(cudaMalloc(&ctx->dsel_owner, (size_t)cap * sizeof(int32_t)));
+  CK(cudaMalloc(&ctx->dsel_xam, (size_t)cap * sizeof(double)));
+  CK(cudaMalloc(&ctx->dsel_evp, (size_t)cap * mt * sizeof(double)));
+  ctx->sel_cap = cap;
+  return CIPSI_OK;
 }
 
 // Device buffers of one run on ctx (generator and unit lists, per-unit
@@ -727,16 +893,48 @@ int prepare_run(cipsi_ctx* ctx, const RunPlan& pl, cudaStream_t st) {
     CK(cudaMalloc(&ctx->dred, 5 * kMaxRoots * sizeof(double)));
     CK(cudaMalloc(&ctx->dwork, sizeof(int)));
   }
+  if (ctx->pool_cap == 0) {
+    const int rc = grow_pool(ctx, 1 << 20);
+    if (rc) return rc;
+  }
   if (ctx->sel_cap == 0) {
+    const int rc = grow_sel(ctx, 1 << 20);
+    if (rc) return rc;
+  }
+  if (nunits > ctx->unit_tab_cap) {
     ++ctx->buf_gen;
-    ctx->sel_cap = 1 << 20;
-    CK(cudaMalloc(&ctx->dsel_bits, (size_t)ctx->sel_cap * 2 * W * sizeof(uint64_t)));
-    CK(cudaMalloc(&ctx->dsel_owner, (size_t)ctx->sel_cap * sizeof(int32_t)));
-    CK(cudaMalloc(&ctx->dsel_xam, (size_t)ctx->sel_cap * sizeof(double)));
-    CK(cudaMalloc(&ctx->dsel_evp, (size_t)ctx->sel_cap * mt * sizeof(double)));
+    dfree(ctx->dunit_pool); dfree(ctx->dunit_nsel); dfree(ctx->dunit_out);
+    CK(cudaMalloc(&ctx->dunit_pool, (size_t)nunits * sizeof(long long)));
+    CK(cudaMalloc(&ctx->dunit_nsel, (size_t)nunits * sizeof(int32_t)));
+    CK(cudaMalloc(&ctx->dunit_out, (size_t)nunits * sizeof(long long)));
+    ctx->unit_tab_cap = nunits;
+  }
+  if (!ctx->dpool_count) {
+    ++ctx->buf_gen;
+    CK(cudaMalloc(&ctx->dpool_count, sizeof(unsigned long long)));
+    CK(cudaMalloc(&ctx->dscan_total, sizeof(unsigned long long)));
   }
   return CIPSI_OK;
 }
+
+// Per-CTA record staging for `grid` CTAs of st_cap slots each.
+int ensure_staging(cipsi_ctx* ctx, int grid, long long st_cap) {
+  const size_t slots = (size_t)grid * (size_t)st_cap;
+  if (slots <= ctx->st_slots && ctx->dst_mask) return CIPSI_OK;
+  ++ctx->buf_gen;
+  dfree(ctx->dst_bits); dfree(ctx->dst_xam); dfree(ctx->dst_evp); dfree(ctx->dst_mask);
+  const int W = ctx->W, mt = ctx->d.metat;
+  CK(cudaMalloc(&ctx->dst_bits, slots * 2 * W * sizeof(uint64_t)));
+  CK(cudaMalloc(&ctx->dst_xam, slots * sizeof(double)));
+  CK(cudaMalloc(&ctx->dst_evp, slots * mt * sizeof(double)));
+  CK(cudaMalloc(&ctx->dst_mask, slots / 32 * sizeof(uint32_t)));
+  CK(cudaMemset(ctx->dst_mask, 0, slots / 32 * sizeof(uint32_t)));
+  ctx->st_slots = slots;
+  return CIPSI_OK;
+}
+
+// Staging slots per CTA for a plan: its largest unit, in whole mask words.
+long long staging_cap(const RunPlan& pl) { return std::max<long long>(32, (pl.max_slots + 31) / 32 * 32); }
 
 // Kernel parameters of one run on ctx (everything but the neighbour scratch
 // and the L_R capacity).
@@ -800,19 +998,89 @@ void fill_params(const cipsi_ctx* ctx, const cipsi_opts* o, const RunPlan& pl, P
   p.hist_nam = ctx->dcounters + C_NCOUNTERS + 1 + kNClass;
   p.hist_tab = ctx->dhist_tab;
   p.red = ctx->dred;
-  p.sel_bits = ctx->dsel_bits;
-  p.sel_owner = ctx->dsel_owner;
-  p.sel_xam = ctx->dsel_xam;
-  p.sel_evp = ctx->dsel_evp;
-  p.sel_cap = ctx->sel_cap;
-  if (ctx->sink) {
-    p.sel_bits = ctx->sink_bits;
-    p.sel_owner = ctx->sink_owner;
-    p.sel_xam = ctx->sink_xam;
-    p.sel_evp = ctx->sink_evp;
-    p.sel_cap = ctx->sink_cap;
-  }
+  p.rec_mode = 1;
+  p.st_cap = (int)staging_cap(pl);
+  p.st_bits = ctx->dst_bits;
+  p.st_xam = ctx->dst_xam;
+  p.st_evp = ctx->dst_evp;
+  p.st_mask = ctx->dst_mask;
+  p.pool_bits = ctx->dpool_bits;
+  p.pool_xam = ctx->dpool_xam;
+  p.pool_evp = ctx->dpool_evp;
+  p.pool_cap = ctx->pool_cap;
+  p.pool_count = ctx->dpool_count;
+  p.unit_pool = ctx->dunit_pool;
+  p.unit_nsel = ctx->dunit_nsel;
   p.work = ctx->dwork;
+}
+
+// Output arrays of a run's records: the caller's pinned sink or the
+// context's device arrays.
+void record_target(const cipsi_ctx* ctx, GatherArgs& a) {
+  if (ctx->sink) {
+    a.out_bits = ctx->sink_bits;
+    a.out_owner = ctx->sink_owner;
+    a.out_xam = ctx->sink_xam;
+    a.out_evp = ctx->sink_evp;
+    a.out_cap = ctx->sink_cap;
+  } else {
+    a.out_bits = ctx->dsel_bits;
+    a.out_owner = ctx->dsel_owner;
+    a.out_xam = ctx->dsel_xam;
+    a.out_evp = ctx->dsel_evp;
+    a.out_cap = ctx->sel_cap;
+  }
+}
+
+// Scan + gather of units [u0, u1) of run `p` (records at output offset
+// out_base.. of the target in `a`), enqueued on st.
+cudaError_t enqueue_gather(const cipsi_ctx* ctx, const Params& p, int u0, int u1, long long out_base, GatherArgs a,
+                           cudaStream_t st, int dev_sms) {
+  if (u1 <= u0) return cudaSuccess;
+  k_scan_units<<<1, kScanThreads, 0, st>>>(p.unit_nsel, ctx->dunit_out, u0, u1, out_base, ctx->dscan_total);
+  a.pool_bits = p.pool_bits;
+  a.pool_xam = p.pool_xam;
+  a.pool_evp = p.pool_evp;
+  a.pool_cap = p.pool_cap;
+  a.unit_pool = p.unit_pool;
+  a.unit_nsel = p.unit_nsel;
+  a.unit_out = ctx->dunit_out;
+  a.unit_g = p.unit_g;
+  a.gens = p.gens;
+  a.u0 = u0;
+  a.u1 = u1;
+  a.words = 2 * ctx->W;
+  a.metat = ctx->d.metat;
+  a.out_base = out_base;
+  const int grid = std::max(1, std::min(u1 - u0, 4 * dev_sms));
+  k_gather<<<grid, 256, 0, st>>>(a);
+  return cudaGetLastError();
+}
+
+// Per-CTA neighbour scratch (nb_j, nb_emask, lr_ent) for `grid` CTAs.
+int ensure_neighbour_scratch(cipsi_ctx* ctx, int grid) {
+  if ((size_t)grid <= ctx->scratch_blocks && ctx->dnb_j) return CIPSI_OK;
+  const int ncf = ctx->d.ncf;
+  ++ctx->buf_gen;
+  dfree(ctx->dnb_j); dfree(ctx->dnb_em); dfree(ctx->dlr_ent);
+  CK(cudaMalloc(&ctx->dnb_j, (size_t)grid * ncf * sizeof(int32_t)));
+  CK(cudaMalloc(&ctx->dnb_em, (size_t)grid * ncf * sizeof(uint64_t)));
+  CK(cudaMalloc(&ctx->dlr_ent, (size_t)grid * ncf * sizeof(uint64_t)));
+  ctx->scratch_blocks = grid;
+  return CIPSI_OK;
+}
+
+// the plain (one geometry) forward launch of k_pt2<W, R>
+cudaError_t launch_plain(const Params& p, int W, int R, int grid, size_t smem, cudaStream_t st) {
+  if (W == 1)
+    return R == 1 ? launch_pt2<1, 1, false>(p, BatchArgs{}, grid, smem, st)
+         : R == 2 ? launch_pt2<1, 2, false>(p, BatchArgs{}, grid, smem, st)
+         : R == 4 ? launch_pt2<1, 4, false>(p, BatchArgs{}, grid, smem, st)
+                  : launch_pt2<1, 8, false>(p, BatchArgs{}, grid, smem, st);
+  return R == 1 ? launch_pt2<2, 1, false>(p, BatchArgs{}, grid, smem, st)
+       : R == 2 ? launch_pt2<2, 2, false>(p, BatchArgs{}, grid, smem, st)
+       : R == 4 ? launch_pt2<2, 4, false>(p, BatchArgs{}, grid, smem, st)
+                : launch_pt2<2, 8, false>(p, BatchArgs{}, grid, smem, st);
 }
 
 }  // namespace
@@ -878,21 +1146,18 @@ int cipsi_run_pt2_async(cipsi_ctx* ctx, const cipsi_opts* o) {
   CK(cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, ctx->device));
   const LaunchShape ls = launch_shape(W, roots_pad(mt), ncf, ctx->tune_ctas);
   const int grid = std::max(1, std::min(nunits, dev_sms * ls.blocks_per_sm));
-  // per-block neighbour scratch
-  if ((size_t)grid > ctx->scratch_blocks || !ctx->dnb_j) {
-    dfree(ctx->dnb_j); dfree(ctx->dnb_em); dfree(ctx->dlr_ent);
-    CK(cudaMalloc(&ctx->dnb_j, (size_t)grid * ncf * sizeof(int32_t)));
-    CK(cudaMalloc(&ctx->dnb_em, (size_t)grid * ncf * sizeof(uint64_t)));
-    CK(cudaMalloc(&ctx->dlr_ent, (size_t)grid * ncf * sizeof(uint64_t)));
-    ctx->scratch_blocks = grid;
-  }
+  rc = ensure_neighbour_scratch(ctx, grid);
+  if (rc) return rc;
   rc = prepare_run(ctx, pl, ctx->stream);
+  if (rc) return rc;
+  rc = ensure_staging(ctx, grid, staging_cap(pl));
   if (rc) return rc;
   const size_t nq = (size_t)5 * mt;
   const size_t ncount = C_NCOUNTERS + 1 + kNClass + kNClass * kMaxRoots;
   CK(cudaMemsetAsync(ctx->dcounters, 0, ncount * sizeof(unsigned long long), ctx->stream));
   CK(cudaMemsetAsync(ctx->dhist_tab, 0, 2 * kNClass * kMaxRoots * sizeof(double), ctx->stream));
   CK(cudaMemsetAsync(ctx->dwork, 0, sizeof(int), ctx->stream));
+  CK(cudaMemsetAsync(ctx->dpool_count, 0, sizeof(unsigned long long), ctx->stream));
   CK(cudaMemsetAsync(ctx->dgen_part, 0, (size_t)std::max(nunits, 1) * nq * sizeof(double), ctx->stream));
 
   Params p{};
@@ -905,23 +1170,19 @@ int cipsi_run_pt2_async(cipsi_ctx* ctx, const cipsi_opts* o) {
 
   CK(cudaEventRecord(ctx->ev0, ctx->stream));
   if (nunits > 0) {
-    cudaError_t e;
-    const int R = roots_pad(mt);
-    if (W == 1) {
-      e = R == 1 ? launch_pt2<1, 1, false>(p, BatchArgs{}, grid, ls.smem, ctx->stream)
-        : R == 2 ? launch_pt2<1, 2, false>(p, BatchArgs{}, grid, ls.smem, ctx->stream)
-        : R == 4 ? launch_pt2<1, 4, false>(p, BatchArgs{}, grid, ls.smem, ctx->stream)
-                 : launch_pt2<1, 8, false>(p, BatchArgs{}, grid, ls.smem, ctx->stream);
-    } else {
-      e = R == 1 ? launch_pt2<2, 1, false>(p, BatchArgs{}, grid, ls.smem, ctx->stream)
-        : R == 2 ? launch_pt2<2, 2, false>(p, BatchArgs{}, grid, ls.smem, ctx->stream)
-        : R == 4 ? launch_pt2<2, 4, false>(p, BatchArgs{}, grid, ls.smem, ctx->stream)
-                 : launch_pt2<2, 8, false>(p, BatchArgs{}, grid, ls.smem, ctx->stream);
-    }
+    cudaError_t e = launch_plain(p, W, roots_pad(mt), grid, ls.smem, ctx->stream);
     if (e != cudaSuccess) return fail(ctx, CIPSI_ERR_CUDA, std::string("k_pt2 launch: ") + cudaGetErrorString(e));
+    CK(cudaEventRecord(ctx->evk, ctx->stream));
+    ctx->last_launches = 4;
+    GatherArgs ga{};
+    record_target(ctx, ga);
+    e = enqueue_gather(ctx, p, 0, nunits, 0, ga, ctx->stream, dev_sms);
+    if (e != cudaSuccess) return fail(ctx, CIPSI_ERR_CUDA, std::string("record gather: ") + cudaGetErrorString(e));
     k_reduce<<<(unsigned)nq, kReduceThreads, 0, ctx->stream>>>(ctx->dgen_part, nunits, (int)nq, ctx->dred);
     CK(cudaGetLastError());
   } else {
+    CK(cudaEventRecord(ctx->evk, ctx->stream));
+    ctx->last_launches = 0;
     CK(cudaMemsetAsync(ctx->dred, 0, nq * sizeof(double), ctx->stream));
   }
   CK(cudaEventRecord(ctx->ev1, ctx->stream));
@@ -984,21 +1245,31 @@ int cipsi_fetch_result(cipsi_ctx* ctx, cipsi_result* r) {
   r->alg_bytes = (int64_t)(cnt[C_NP2] * (8.0 * mt + 2 * 4.0 + 8.0) +
                            cnt[C_NP1] * (8.0 * mt + 8.0 + 2.0 * avg_rank * 2 * 4.0) +
                            cnt[C_NPROC] * (8.0 * avg_rank + 8.0 * (avg_rank + avg_rank * avg_rank) + 8.0 * mt));
-  float ms = -1.f;  // batched runs: the batch's time is reported by the batch
-  if (ctx->ev_valid) CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+  float ms = -1.f, mk = -1.f;  // batched runs: the batch's time is reported by the batch
+  if (ctx->ev_valid) {
+    CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+    CK(cudaEventElapsedTime(&mk, ctx->ev0, ctx->evk));
+  }
   r->kernel_ms = ms;
+  r->pt2_ms = mk;
+  r->launches = ctx->ev_valid ? ctx->last_launches : 0;
   // selection: records stay on the device (or in the sink) until
   // cipsi_selection_get/raw
   const long long nsel = (long long)cnt[C_NSEL];
   r->n_selected = nsel;
-  const long long cap = ctx->sink ? ctx->sink_cap : ctx->sel_cap;
-  ctx->nsel = std::min(nsel, cap);
-  if (nsel > cap)
+  if (cnt[C_STAGE_OVF])
+    return fail(ctx, CIPSI_ERR_CUDA, "internal error: a selected candidate's slot lay outside its staging region");
+  // the records are valid when every unit segment found room in the pool;
+  // the output arrays then hold the first out_cap of them, in unit order
+  const long long out_cap = ctx->sink ? ctx->sink_cap : ctx->sel_cap;
+  ctx->nsel = nsel > ctx->pool_cap ? 0 : std::min(nsel, out_cap);
+  if (nsel > ctx->pool_cap || nsel > out_cap)
     return fail(ctx, CIPSI_ERR_OVERFLOW,
                 "selection buffer overflow: " + std::to_string(nsel) + " records > capacity " +
-                    std::to_string(cap) +
-                    (ctx->sink ? " (the sink holds the first records; the rest were counted only)"
-                               : " (cipsi_run_pt2 grows the buffer and reruns)"));
+                    std::to_string(std::min(out_cap, ctx->pool_cap)) +
+                    (nsel > ctx->pool_cap ? " (counted only; cipsi_run_pt2 grows the buffers and reruns)"
+                     : ctx->sink         ? " (the sink holds the first records; the rest were counted only)"
+                                         : " (cipsi_run_pt2 grows the buffer and reruns)"));
   return CIPSI_OK;
 }
 
@@ -1007,20 +1278,368 @@ int cipsi_run_pt2(cipsi_ctx* ctx, const cipsi_opts* opts, cipsi_result* res) {
     int rc = cipsi_run_pt2_async(ctx, opts);
     if (rc) return rc;
     rc = cipsi_fetch_result(ctx, res);
-    if (rc != CIPSI_ERR_OVERFLOW || ctx->sink) return rc;
-    // grow the selection buffer to what the run needed and redo
-    unsigned long long nsel = 0;
-    CK(cudaMemcpy(&nsel, ctx->dcounters + C_NSEL, 8, cudaMemcpyDeviceToHost));
-    dfree(ctx->dsel_bits); dfree(ctx->dsel_owner); dfree(ctx->dsel_xam); dfree(ctx->dsel_evp);
-    ++ctx->buf_gen;
-    ctx->sel_cap = (long long)(nsel + nsel / 8 + 1024);
-    const int W = ctx->W, mt = ctx->d.metat;
-    CK(cudaMalloc(&ctx->dsel_bits, (size_t)ctx->sel_cap * 2 * W * sizeof(uint64_t)));
-    CK(cudaMalloc(&ctx->dsel_owner, (size_t)ctx->sel_cap * sizeof(int32_t)));
-    CK(cudaMalloc(&ctx->dsel_xam, (size_t)ctx->sel_cap * sizeof(double)));
-    CK(cudaMalloc(&ctx->dsel_evp, (size_t)ctx->sel_cap * mt * sizeof(double)));
+    if (rc != CIPSI_ERR_OVERFLOW) return rc;
+    // grow the pool (and the device record arrays) to what the run needed
+    // and redo; a caller's sink that is too small stays the caller's
+    const long long nsel = res->n_selected;
+    const long long cap = nsel + nsel / 8 + 1024;
+    if (nsel <= ctx->pool_cap && ctx->sink) return rc;
+    if (nsel > ctx->pool_cap && (rc = grow_pool(ctx, cap))) return rc;
+    if (!ctx->sink && nsel > ctx->sel_cap && (rc = grow_sel(ctx, cap))) return rc;
   }
   return fail(ctx, CIPSI_ERR_OVERFLOW, "selection buffer could not be grown");
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------- streamed records
+// cipsi_run_pt2_stream: the run in chunks of consecutive work units whose
+// candidate slots fit the record pool (a unit never selects more records
+// than it has slots), so any selection size runs in bounded device memory.
+// Per chunk, on the context stream: k_pt2 over the chunk's units, the unit
+// scan and the gather into one of two device record buffers; the copy
+// stream then brings the chunk to a ring of two pinned host buffers piece
+// by piece, and the caller's consumer gets each piece, in record order,
+// while the GPU computes the next chunk.
+
+namespace {
+
+int ensure_stream_buffers(cipsi_ctx* ctx, long long cap, bool host, long long hb_cap) {
+  const int W = ctx->W, mt = ctx->d.metat;
+  if (cap > ctx->out_cap) {
+    ++ctx->buf_gen;
+    for (int i = 0; i < 2; ++i) {
+      dfree(ctx->dout_bits[i]); dfree(ctx->dout_owner[i]); dfree(ctx->dout_xam[i]); dfree(ctx->dout_evp[i]);
+    }
+    ctx->out_cap = 0;
+    for (int i = 0; i < 2; ++i) {
+      CK(cudaMalloc(&ctx->dout_bits[i], (size_t)cap * 2 * W * sizeof(uint64_t)));
+      CK(cudaMalloc(&ctx->dout_owner[i], (size_t)cap * sizeof(int32_t)));
+      CK(cudaMalloc(&ctx->dout_xam[i], (size_t)cap * sizeof(double)));
+      CK(cudaMalloc(&ctx->dout_evp[i], (size_t)cap * mt * sizeof(double)));
+    }
+    ctx->out_cap = cap;
+  }
+  if (!ctx->copy_stream) {
+    CK(cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking));
+    for (int i = 0; i < 2; ++i) {
+      CK(cudaEventCreateWithFlags(&ctx->ev_gathered[i], cudaEventDisableTiming));
+      CK(cudaEventCreateWithFlags(&ctx->ev_copied[i], cudaEventDisableTiming));
+      CK(cudaEventCreateWithFlags(&ctx->ev_host[i], cudaEventDisableTiming));
+    }
+  }
+  if (host && hb_cap > ctx->hbuf_cap) {
+    for (int i = 0; i < 2; ++i)
+      if (ctx->hbuf[i]) {
+        cudaFreeHost(ctx->hbuf[i]);
+        ctx->hbuf[i] = nullptr;
+      }
+    ctx->hbuf_cap = 0;
+    const size_t bytes = (size_t)hb_cap * (2 * W * 8 + 8 + 8 + mt * 8);
+    for (int i = 0; i < 2; ++i) CK(cudaHostAlloc(&ctx->hbuf[i], bytes, cudaHostAllocDefault));
+    ctx->hbuf_cap = hb_cap;
+  }
+  return CIPSI_OK;
+}
+
+// the counters, histogram and sums of a finished run into *r (as
+// cipsi_fetch_result), reading on the context stream
+int read_results(cipsi_ctx* ctx, int nclass, cipsi_result* r) {
+  const int mt = ctx->d.metat;
+  const size_t ncount = C_NCOUNTERS + 1 + kNClass + kNClass * kMaxRoots;
+  std::vector<double> red(5 * mt), tab(2 * kNClass * kMaxRoots);
+  std::vector<unsigned long long> cnt(ncount);
+  CK(cudaMemcpyAsync(red.data(), ctx->dred, red.size() * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemcpyAsync(cnt.data(), ctx->dcounters, ncount * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                     ctx->stream));
+  CK(cudaMemcpyAsync(tab.data(), ctx->dhist_tab, tab.size() * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  memset(r, 0, sizeof(*r));
+  for (int m = 0; m < mt; ++m) {
+    r->e2mp[m] = red[0 * mt + m];
+    r->e2vp[m] = red[1 * mt + m];
+    r->e2b[m] = red[2 * mt + m];
+    r->psimp[m] = red[3 * mt + m];
+    r->psivp[m] = red[4 * mt + m];
+  }
+  r->ietat = (int64_t)cnt[C_IETAT];
+  r->n_processed = (int64_t)cnt[C_NPROC];
+  r->n_candidates = (int64_t)cnt[C_NCAND];
+  r->n_compares = (int64_t)cnt[C_NCMP];
+  r->n_pairs_1 = (int64_t)cnt[C_NP1];
+  r->n_pairs_2 = (int64_t)cnt[C_NP2];
+  r->n_selected = (int64_t)cnt[C_NSEL];
+  {
+    const unsigned long long b = cnt[C_NCOUNTERS];
+    memcpy(&r->dpivot, &b, 8);
+  }
+  for (int i = 0; i < nclass; ++i) r->nom[i] = (int64_t)cnt[C_NCOUNTERS + 1 + i];
+  for (int c = 0; c < nclass; ++c)
+    for (int m = 0; m < mt; ++m) {
+      r->nam[c * kMaxRoots + m] = (int64_t)cnt[C_NCOUNTERS + 1 + kNClass + c * mt + m];
+      r->tabmp[c * kMaxRoots + m] = tab[c * mt + m];
+      r->tabvp[c * kMaxRoots + m] = tab[nclass * mt + c * mt + m];
+    }
+  const double avg_rank = 4.0;
+  r->alg_bytes = (int64_t)(cnt[C_NP2] * (8.0 * mt + 2 * 4.0 + 8.0) +
+                           cnt[C_NP1] * (8.0 * mt + 8.0 + 2.0 * avg_rank * 2 * 4.0) +
+                           cnt[C_NPROC] * (8.0 * avg_rank + 8.0 * (avg_rank + avg_rank * avg_rank) + 8.0 * mt));
+  if (cnt[C_STAGE_OVF])
+    return fail(ctx, CIPSI_ERR_CUDA, "internal error: a selected candidate's slot lay outside its staging region");
+  return CIPSI_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int cipsi_run_pt2_stream(cipsi_ctx* ctx, const cipsi_opts* o, int64_t chunk_records, cipsi_record_fn fn,
+                         void* user, cipsi_result* r) {
+  int rc = check_run_args(ctx, o);
+  if (rc) return rc;
+  if (!r) return fail(ctx, CIPSI_ERR_ARG, "run_pt2_stream: null result");
+  if (ctx->pending) return fail(ctx, CIPSI_ERR_STATE, "an asynchronous run is pending: fetch its result first");
+  CK(cudaSetDevice(ctx->device));
+  const int ncf = ctx->d.ncf, W = ctx->W, mt = ctx->d.metat;
+  RunPlan pl;
+  plan_run(ctx, o, ctx->tune_r_chunk, pl);
+  const int nunits = (int)pl.ug.size();
+  int dev_sms = 0;
+  CK(cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, ctx->device));
+  const LaunchShape ls = launch_shape(W, roots_pad(mt), ncf, ctx->tune_ctas);
+  const int grid = std::max(1, std::min(nunits, dev_sms * ls.blocks_per_sm));
+  if ((rc = ensure_neighbour_scratch(ctx, grid))) return rc;
+  if ((rc = prepare_run(ctx, pl, ctx->stream))) return rc;
+  if ((rc = ensure_staging(ctx, grid, staging_cap(pl)))) return rc;
+  // chunk capacity: what was asked, else what about half the free device
+  // memory holds (pool + two record buffers), at most 2^29 records; at
+  // least the largest unit's slots
+  const long long rec_bytes = 2 * W * 8 + 8 + 8 * mt;
+  long long cap = chunk_records;
+  if (cap <= 0) {
+    size_t fr = 0, tot = 0;
+    CK(cudaMemGetInfo(&fr, &tot));
+    const double have = (double)fr + (double)(ctx->pool_cap + 2 * ctx->out_cap) * (rec_bytes + 4);
+    cap = std::min<long long>(1ll << 29, (long long)(0.45 * have / (3.0 * (rec_bytes + 4))));
+  }
+  cap = std::max(cap, std::max<long long>(pl.max_slots, 1024));
+  if (ctx->pool_cap < cap && (rc = grow_pool(ctx, cap))) return rc;
+  const long long hb_cap = std::min<long long>(cap, 1ll << 24);
+  if ((rc = ensure_stream_buffers(ctx, cap, fn != nullptr, hb_cap))) return rc;
+  // chunks: consecutive units whose slots add up to at most cap
+  std::vector<int> cut{0};
+  {
+    long long acc = 0;
+    for (int u = 0; u < nunits; ++u) {
+      if (acc + pl.uslots[u] > cap && u > cut.back()) {
+        cut.push_back(u);
+        acc = 0;
+      }
+      acc += pl.uslots[u];
+    }
+    if (cut.back() != nunits) cut.push_back(nunits);
+  }
+  const int nchunks = (int)cut.size() - 1;
+  // per chunk: records gathered and records placed in the pool (pinned)
+  unsigned long long* hcnt = nullptr;
+  CK(cudaHostAlloc((void**)&hcnt, (size_t)std::max(1, 2 * nchunks) * sizeof(unsigned long long),
+                   cudaHostAllocDefault));
+  struct HostFree {
+    unsigned long long* p;
+    ~HostFree() { if (p) cudaFreeHost(p); }
+  } hold{hcnt};
+
+  const size_t nq = (size_t)5 * mt;
+  const size_t ncount = C_NCOUNTERS + 1 + kNClass + kNClass * kMaxRoots;
+  CK(cudaMemsetAsync(ctx->dcounters, 0, ncount * sizeof(unsigned long long), ctx->stream));
+  CK(cudaMemsetAsync(ctx->dhist_tab, 0, 2 * kNClass * kMaxRoots * sizeof(double), ctx->stream));
+  CK(cudaMemsetAsync(ctx->dgen_part, 0, (size_t)std::max(nunits, 1) * nq * sizeof(double), ctx->stream));
+  Params p{};
+  fill_params(ctx, o, pl, p);
+  p.nb_j = ctx->dnb_j;
+  p.nb_emask = ctx->dnb_em;
+  p.lr_ent = ctx->dlr_ent;
+  p.lr_cap = ls.lr_cap;
+  p.nb_stride = ncf;
+  const size_t words = 2 * (size_t)W;
+
+  long long delivered = 0;  // records handed to the consumer so far
+  long long piece_no = 0;
+  auto deliver = [&](int c) -> int {
+    const int b = c & 1;
+    CK(cudaEventSynchronize(ctx->ev_gathered[b]));
+    const long long n = (long long)hcnt[2 * c];
+    if ((long long)hcnt[2 * c + 1] > ctx->pool_cap)
+      return fail(ctx, CIPSI_ERR_OVERFLOW, "internal error: a chunk's records overflowed the pool");
+    CK(cudaStreamWaitEvent(ctx->copy_stream, ctx->ev_gathered[b], 0));
+    const long long npieces = (n + hb_cap - 1) / hb_cap;
+    for (long long j = 0; j <= npieces; ++j) {
+      if (j < npieces) {
+        const long long off = j * hb_cap, cnt = std::min(hb_cap, n - off);
+        unsigned char* hb = static_cast<unsigned char*>(ctx->hbuf[(piece_no + j) & 1]);
+        CK(cudaMemcpyAsync(hb, ctx->dout_bits[b] + off * words, (size_t)cnt * words * 8, cudaMemcpyDeviceToHost,
+                           ctx->copy_stream));
+        hb += (size_t)hb_cap * words * 8;
+        CK(cudaMemcpyAsync(hb, ctx->dout_owner[b] + off, (size_t)cnt * 4, cudaMemcpyDeviceToHost, ctx->copy_stream));
+        hb += (size_t)hb_cap * 8;
+        CK(cudaMemcpyAsync(hb, ctx->dout_xam[b] + off, (size_t)cnt * 8, cudaMemcpyDeviceToHost, ctx->copy_stream));
+        hb += (size_t)hb_cap * 8;
+        CK(cudaMemcpyAsync(hb, ctx->dout_evp[b] + off * mt, (size_t)cnt * mt * 8, cudaMemcpyDeviceToHost,
+                           ctx->copy_stream));
+        CK(cudaEventRecord(ctx->ev_host[(piece_no + j) & 1], ctx->copy_stream));
+      }
+      if (j >= 1) {
+        const long long off = (j - 1) * hb_cap, cnt = std::min(hb_cap, n - off);
+        const int hbi = (int)((piece_no + j - 1) & 1);
+        CK(cudaEventSynchronize(ctx->ev_host[hbi]));
+        const unsigned char* hb = static_cast<const unsigned char*>(ctx->hbuf[hbi]);
+        const uint64_t* hbits = reinterpret_cast<const uint64_t*>(hb);
+        const int32_t* hown = reinterpret_cast<const int32_t*>(hb + (size_t)hb_cap * words * 8);
+        const double* hxam = reinterpret_cast<const double*>(hb + (size_t)hb_cap * (words * 8 + 8));
+        const double* hevp = reinterpret_cast<const double*>(hb + (size_t)hb_cap * (words * 8 + 16));
+        if (fn(user, delivered, cnt, (int32_t)words, mt, hbits, hown, hxam, hevp) != 0) {
+          cudaStreamSynchronize(ctx->copy_stream);
+          return fail(ctx, CIPSI_ERR_ARG, "run_pt2_stream: the record consumer returned an error");
+        }
+        delivered += cnt;
+      }
+    }
+    piece_no += npieces;
+    CK(cudaEventRecord(ctx->ev_copied[b], ctx->copy_stream));
+    return CIPSI_OK;
+  };
+
+  // k_pt2 of each chunk timed by a pair of events
+  std::vector<cudaEvent_t> kev(2 * (size_t)nchunks, nullptr);
+  struct EvFree {
+    std::vector<cudaEvent_t>& v;
+    ~EvFree() {
+      for (cudaEvent_t e : v)
+        if (e) cudaEventDestroy(e);
+    }
+  } evhold{kev};
+  for (auto& e : kev) CK(cudaEventCreate(&e));
+  CK(cudaEventRecord(ctx->ev0, ctx->stream));
+  for (int c = 0; c < nchunks; ++c) {
+    const int u0 = cut[c], u1 = cut[c + 1], b = c & 1;
+    // the record buffer of this chunk was last read by chunk c - 2's copies
+    if (c >= 2 && fn) CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_copied[b], 0));
+    CK(cudaMemsetAsync(ctx->dwork, 0, sizeof(int), ctx->stream));
+    CK(cudaMemsetAsync(ctx->dpool_count, 0, sizeof(unsigned long long), ctx->stream));
+    Params pc = p;
+    pc.nunits = u1 - u0;
+    pc.unit_g = p.unit_g + u0;
+    pc.unit_r0 = p.unit_r0 + u0;
+    pc.unit_r1 = p.unit_r1 + u0;
+    pc.gen_part = p.gen_part + (size_t)u0 * nq;
+    pc.unit_pool = p.unit_pool + u0;
+    pc.unit_nsel = p.unit_nsel + u0;
+    const int cgrid = std::max(1, std::min(u1 - u0, grid));
+    CK(cudaEventRecord(kev[2 * c], ctx->stream));
+    cudaError_t e = launch_plain(pc, W, roots_pad(mt), cgrid, ls.smem, ctx->stream);
+    if (e != cudaSuccess) return fail(ctx, CIPSI_ERR_CUDA, std::string("k_pt2 launch: ") + cudaGetErrorString(e));
+    CK(cudaEventRecord(kev[2 * c + 1], ctx->stream));
+    GatherArgs ga{};
+    ga.out_bits = ctx->dout_bits[b];
+    ga.out_owner = ctx->dout_owner[b];
+    ga.out_xam = ctx->dout_xam[b];
+    ga.out_evp = ctx->dout_evp[b];
+    ga.out_cap = ctx->out_cap;
+    e = enqueue_gather(ctx, p, u0, u1, 0, ga, ctx->stream, dev_sms);
+    if (e != cudaSuccess) return fail(ctx, CIPSI_ERR_CUDA, std::string("record gather: ") + cudaGetErrorString(e));
+    CK(cudaMemcpyAsync(&hcnt[2 * c], ctx->dscan_total, 8, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaMemcpyAsync(&hcnt[2 * c + 1], ctx->dpool_count, 8, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaEventRecord(ctx->ev_gathered[b], ctx->stream));
+    if (fn && c >= 1 && (rc = deliver(c - 1))) return rc;
+  }
+  if (fn && nchunks >= 1 && (rc = deliver(nchunks - 1))) return rc;
+  if (nunits > 0) {
+    k_reduce<<<(unsigned)nq, kReduceThreads, 0, ctx->stream>>>(ctx->dgen_part, nunits, (int)nq, ctx->dred);
+    CK(cudaGetLastError());
+  } else {
+    CK(cudaMemsetAsync(ctx->dred, 0, nq * sizeof(double), ctx->stream));
+  }
+  CK(cudaEventRecord(ctx->ev1, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  if (fn) CK(cudaStreamSynchronize(ctx->copy_stream));
+  if ((rc = read_results(ctx, o->nclass, r))) return rc;
+  float ms = 0.f;
+  CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+  r->kernel_ms = ms;
+  double pt2 = 0.0;
+  for (int c = 0; c < nchunks; ++c) {
+    float t = 0.f;
+    CK(cudaEventElapsedTime(&t, kev[2 * c], kev[2 * c + 1]));
+    pt2 += t;
+  }
+  r->pt2_ms = pt2;
+  r->launches = 3ll * nchunks + (nunits > 0 ? 1 : 0);
+  for (int c = 0; c < nchunks; ++c)
+    if ((long long)hcnt[2 * c + 1] > ctx->pool_cap)
+      return fail(ctx, CIPSI_ERR_OVERFLOW, "internal error: a chunk's records overflowed the pool");
+  if (fn && delivered != r->n_selected)
+    return fail(ctx, CIPSI_ERR_CUDA, "internal error: " + std::to_string(delivered) + " records delivered of " +
+                                         std::to_string(r->n_selected) + " selected");
+  ctx->nsel = 0;  // the streamed records are the consumer's; none stay readable
+  ctx->stream_chunks = nchunks;
+  return CIPSI_OK;
+}
+
+// Order-sensitive digest of streamed records (a record consumer): per
+// field array (bits, owner, xam, evp) a Fletcher-style pair of 64-bit sums
+// over its words in record order, s1 = sum w_i and s2 = sum of the running
+// s1, continued across calls; big pieces are split over host threads and
+// the per-slice pairs combined in order.
+int cipsi_record_digest(void* user, int64_t first, int64_t count, int32_t words, int32_t metat,
+                        const uint64_t* bits, const int32_t* owner, const double* xam, const double* evp) {
+  cipsi_digest* d = static_cast<cipsi_digest*>(user);
+  if (!d || first != d->records) return -1;
+  struct Pair {
+    uint64_t s1 = 0, s2 = 0, n = 0;
+  };
+  auto fold = [](Pair& acc, const Pair& x) {
+    acc.s2 += x.s2 + acc.s1 * x.n;
+    acc.s1 += x.s1;
+    acc.n += x.n;
+  };
+  // word i of a field array as a 64-bit integer
+  auto run = [&](int field, uint64_t n) {
+    auto word = [&](uint64_t i) -> uint64_t {
+      if (field == 0) return bits[i];
+      if (field == 1) return (uint64_t)(uint32_t)owner[i];
+      uint64_t v;
+      memcpy(&v, field == 2 ? &xam[i] : &evp[i], 8);
+      return v;
+    };
+    auto slice = [&](uint64_t a, uint64_t b_) {
+      Pair x;
+      for (uint64_t i = a; i < b_; ++i) {
+        x.s1 += word(i);
+        x.s2 += x.s1;
+      }
+      x.n = b_ - a;
+      return x;
+    };
+    const int nt = std::max(1, std::min<int>(d->threads > 0 ? d->threads : 1, (int)(n / 65536 + 1)));
+    std::vector<Pair> part(nt);
+    std::vector<std::thread> th;
+    for (int t = 1; t < nt; ++t)
+      th.emplace_back([&, t]() { part[t] = slice(n * t / nt, n * (t + 1) / nt); });
+    part[0] = slice(0, n / nt);
+    for (auto& x : th) x.join();
+    Pair acc{d->s1[field], d->s2[field], 0};
+    for (const Pair& x : part) fold(acc, x);
+    d->s1[field] = acc.s1;
+    d->s2[field] = acc.s2;
+  };
+  if (count > 0) {
+    run(0, (uint64_t)count * (uint64_t)words);
+    run(1, (uint64_t)count);
+    run(2, (uint64_t)count);
+    run(3, (uint64_t)count * (uint64_t)metat);
+  }
+  d->records += count;
+  return 0;
 }
 
 int cipsi_run_pt2_adjoint(cipsi_ctx* ctx, const cipsi_opts* o, const double* seed, double* gF,
@@ -1041,13 +1660,8 @@ int cipsi_run_pt2_adjoint(cipsi_ctx* ctx, const cipsi_opts* o, const double* see
   const int R = roots_pad(mt);
   const LaunchShape ls = launch_shape(W, R, ncf, ctx->tune_ctas);
   const int grid = std::max(1, std::min(nunits, dev_sms * ls.blocks_per_sm));
-  if ((size_t)grid > ctx->scratch_blocks || !ctx->dnb_j) {
-    dfree(ctx->dnb_j); dfree(ctx->dnb_em); dfree(ctx->dlr_ent);
-    CK(cudaMalloc(&ctx->dnb_j, (size_t)grid * ncf * sizeof(int32_t)));
-    CK(cudaMalloc(&ctx->dnb_em, (size_t)grid * ncf * sizeof(uint64_t)));
-    CK(cudaMalloc(&ctx->dlr_ent, (size_t)grid * ncf * sizeof(uint64_t)));
-    ctx->scratch_blocks = grid;
-  }
+  rc = ensure_neighbour_scratch(ctx, grid);
+  if (rc) return rc;
   rc = prepare_run(ctx, pl, ctx->stream);
   if (rc) return rc;
   const size_t nq = (size_t)5 * mt;
@@ -1087,7 +1701,7 @@ int cipsi_run_pt2_adjoint(cipsi_ctx* ctx, const cipsi_opts* o, const double* see
   p.lr_ent = ctx->dlr_ent;
   p.lr_cap = ls.lr_cap;
   p.nb_stride = ncf;
-  p.sel_cap = 0;  // no records from an adjoint launch
+  p.rec_mode = 0;  // no records from an adjoint launch
   for (int m = 0; m < mt; ++m) {
     p.seed_mp[m] = seed[m];
     p.seed_vp[m] = seed[mt + m];
@@ -1232,6 +1846,11 @@ struct cipsi_batch {
     int32_t* dnb_j = nullptr;
     uint64_t* dnb_em = nullptr;
     uint64_t* dlr_ent = nullptr;
+    // record staging shared by the class's geometries (per CTA)
+    long long st_cap = 32;
+    uint64_t* dst_bits = nullptr;
+    double *dst_xam = nullptr, *dst_evp = nullptr;
+    uint32_t* dst_mask = nullptr;
     cudaStream_t st = nullptr;
     cudaEvent_t ev_join = nullptr;
   };
@@ -1274,6 +1893,7 @@ void batch_free(cipsi_batch* b) {
   for (auto& c : b->classes) {
     dfree(c.dunit_geo); dfree(c.dunit_local); dfree(c.dwork);
     dfree(c.dnb_j); dfree(c.dnb_em); dfree(c.dlr_ent);
+    dfree(c.dst_bits); dfree(c.dst_xam); dfree(c.dst_evp); dfree(c.dst_mask);
     if (c.st) cudaStreamDestroy(c.st);
     if (c.ev_join) cudaEventDestroy(c.ev_join);
   }
@@ -1318,7 +1938,7 @@ int cipsi_batch_create(cipsi_batch** out, cipsi_ctx* const* ctxs, int32_t n, con
 
   // plan every geometry; per-context buffers as for a plain run
   std::vector<Params> P(n);
-  std::vector<long long> work(n);
+  std::vector<long long> work(n), stcap(n);
   b->ctxs.assign(ctxs, ctxs + n);
   b->opts.assign(opts, opts + n);
   for (int i = 0; i < n; ++i) {
@@ -1328,6 +1948,7 @@ int cipsi_batch_create(cipsi_batch** out, cipsi_ctx* const* ctxs, int32_t n, con
     plan_run(ctx, &opts[i], r_chunk, pl);
     if (prepare_run(ctx, pl, b->stream)) return bfail(b, CIPSI_ERR_CUDA, "context " + std::to_string(i) + ": " + ctx->err);
     fill_params(ctx, &opts[i], pl, P[i]);
+    stcap[i] = staging_cap(pl);
     work[i] = (long long)pl.ug.size() * ctx->d.ncf;
     const int W = ctx->W, R = roots_pad(ctx->d.metat);
     // contexts whose shared-memory list needs a whole SM go to their own
@@ -1352,8 +1973,11 @@ int cipsi_batch_create(cipsi_batch** out, cipsi_ctx* const* ctxs, int32_t n, con
   for (auto& c : b->classes) {
     std::stable_sort(c.geos.begin(), c.geos.end(), [&](int x, int y) { return work[x] > work[y]; });
     std::vector<int32_t> ugeo, ulocal;
+    int mt_max = 1;
     for (int i : c.geos) {
       c.ncf_max = std::max(c.ncf_max, ctxs[i]->d.ncf);
+      c.st_cap = std::max(c.st_cap, stcap[i]);
+      mt_max = std::max(mt_max, ctxs[i]->d.metat);
       for (int u = 0; u < P[i].nunits; ++u) {
         ugeo.push_back(i);
         ulocal.push_back(u);
@@ -1368,6 +1992,14 @@ int cipsi_batch_create(cipsi_batch** out, cipsi_ctx* const* ctxs, int32_t n, con
     BCK(cudaMalloc(&c.dnb_j, (size_t)c.grid * c.ncf_max * sizeof(int32_t)));
     BCK(cudaMalloc(&c.dnb_em, (size_t)c.grid * c.ncf_max * sizeof(uint64_t)));
     BCK(cudaMalloc(&c.dlr_ent, (size_t)c.grid * c.ncf_max * sizeof(uint64_t)));
+    {
+      const size_t slots = (size_t)c.grid * (size_t)c.st_cap;
+      BCK(cudaMalloc(&c.dst_bits, slots * 2 * c.W * sizeof(uint64_t)));
+      BCK(cudaMalloc(&c.dst_xam, slots * sizeof(double)));
+      BCK(cudaMalloc(&c.dst_evp, slots * mt_max * sizeof(double)));
+      BCK(cudaMalloc(&c.dst_mask, slots / 32 * sizeof(uint32_t)));
+      BCK(cudaMemset(c.dst_mask, 0, slots / 32 * sizeof(uint32_t)));
+    }
     if (c.nunits) {
       BCK(cudaMemcpy(c.dunit_geo, ugeo.data(), (size_t)c.nunits * sizeof(int32_t), cudaMemcpyHostToDevice));
       BCK(cudaMemcpy(c.dunit_local, ulocal.data(), (size_t)c.nunits * sizeof(int32_t), cudaMemcpyHostToDevice));
@@ -1378,6 +2010,11 @@ int cipsi_batch_create(cipsi_batch** out, cipsi_ctx* const* ctxs, int32_t n, con
       P[i].lr_ent = c.dlr_ent;
       P[i].nb_stride = c.ncf_max;
       P[i].lr_cap = c.ls.lr_cap;
+      P[i].st_cap = (int)c.st_cap;
+      P[i].st_bits = c.dst_bits;
+      P[i].st_xam = c.dst_xam;
+      P[i].st_evp = c.dst_evp;
+      P[i].st_mask = c.dst_mask;
     }
     BCK(cudaStreamCreateWithFlags(&c.st, cudaStreamNonBlocking));
     BCK(cudaEventCreateWithFlags(&c.ev_join, cudaEventDisableTiming));
@@ -1409,6 +2046,18 @@ int cipsi_batch_create(cipsi_batch** out, cipsi_ctx* const* ctxs, int32_t n, con
     BCK(cudaStreamWaitEvent(b->stream, c.ev_join, 0));
   }
   k_reduce_batch<<<dim3((unsigned)b->max_nq, (unsigned)n), kReduceThreads, 0, b->stream>>>(b->dgeo);
+  // every geometry's records, in its unit order
+  for (int i = 0; i < n; ++i) {
+    GatherArgs ga{};
+    record_target(ctxs[i], ga);
+    const cudaError_t e = enqueue_gather(ctxs[i], P[i], 0, P[i].nunits, 0, ga, b->stream, dev_sms);
+    if (e != cudaSuccess) {
+      cudaGraph_t g = nullptr;
+      cudaStreamEndCapture(b->stream, &g);
+      if (g) cudaGraphDestroy(g);
+      return bfail(b, CIPSI_ERR_CUDA, std::string("batched record gather: ") + cudaGetErrorString(e));
+    }
+  }
   BCK(cudaStreamEndCapture(b->stream, &b->graph));
   BCK(cudaGraphInstantiate(&b->exec, b->graph, 0));
   return CIPSI_OK;
@@ -1753,11 +2402,7 @@ int cipsi_run_pt2_static(cipsi_ctx* ctx, const cipsi_opts* o, cipsi_result* r) {
   p.hist_nam = dcounters + C_NCOUNTERS + 1 + kNClass;
   p.hist_tab = reinterpret_cast<double*>(base + off_tab);
   // no record storage: selected perturbers are counted only
-  p.sel_bits = nullptr;
-  p.sel_owner = nullptr;
-  p.sel_xam = nullptr;
-  p.sel_evp = nullptr;
-  p.sel_cap = 0;
+  p.rec_mode = 0;
   p.work = reinterpret_cast<int*>(base + off_work);
   double* dred = reinterpret_cast<double*>(base + off_red);
 
@@ -1827,6 +2472,8 @@ int cipsi_run_pt2_static(cipsi_ctx* ctx, const cipsi_opts* o, cipsi_result* r) {
   float ms = 0.f;
   CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
   r->kernel_ms = ms;
+  r->pt2_ms = ms;
+  r->launches = nunits > 0 ? 2 : 0;
   r->n_selected = (int64_t)cnt[C_NSEL];
   return CIPSI_OK;
 }

@@ -30,6 +30,7 @@ enum {
   C_NP2,
   C_ALGB,
   C_LRFALLBACK,
+  C_STAGE_OVF,  // selected candidates whose slot lay outside the staging region (must stay 0)
   C_NCOUNTERS
 };
 
@@ -76,11 +77,26 @@ struct Params {
   unsigned long long* hist_nam;      // nclass x metat
   double* hist_tab;                  // 2 x nclass x metat (tabmp, tabvp)
   double* red;                       // 5 x metat reduced sums (k_reduce output)
-  uint64_t* sel_bits;                // cap x 2W
-  int32_t* sel_owner;
-  double* sel_xam;
-  double* sel_evp;                   // cap x metat
-  long long sel_cap;
+  // unit-60 records.  A selected candidate is staged in its CTA's region at
+  // its slot (its position in the work unit's candidate order) and flagged
+  // in the region's slot mask; when the unit is done the CTA compacts the
+  // flagged slots, in slot order, into one segment of the record pool and
+  // notes the segment in the unit table.  k_gather then lays the segments
+  // out in unit order, so the records come out in (unit, candidate) order
+  // whatever the scheduling.
+  int rec_mode;                      // 0: selection counted only; 1: records kept
+  int st_cap;                        // slots per CTA region (multiple of 32)
+  uint64_t* st_bits;                 // grid x st_cap x 2W
+  double* st_xam;                    // grid x st_cap
+  double* st_evp;                    // grid x st_cap x metat
+  uint32_t* st_mask;                 // grid x st_cap / 32
+  uint64_t* pool_bits;               // pool_cap x 2W
+  double* pool_xam;                  // pool_cap
+  double* pool_evp;                  // pool_cap x metat
+  long long pool_cap;
+  unsigned long long* pool_count;    // records placed in the pool (may exceed pool_cap: then not stored)
+  long long* unit_pool;              // per unit: first pool record of its segment
+  int32_t* unit_nsel;                // per unit: records of its segment
   int* work;                         // work counter
   // (pq|rs) as doubles: the caller's FP64 integrals (derivative checks) or
   // the real*4 ones widened on the device; null = read the real*4 `eri`
@@ -125,9 +141,20 @@ struct WarpQueue {
   uint64_t u[2 * W][kQCap];
   double bc[R][kQCap];
   double hmp[kQCap], hvp[kQCap], fmul[kQCap];
-  int nmul[kQCap], owner[kQCap];
+  int nmul[kQCap], slot[kQCap];  // slot: the candidate's position in its work unit
   unsigned char flags[kQCap];  // bit 0 ybis, bit 1 is_pert1
 };
+
+// Candidates of one block of removed electrons R: nv added orbitals for
+// |R| = 1, nv(nv-1)/2 same-spin pairs, nva * nvb opposite-spin pairs (nv:
+// empty orbitals of the generator in the spin(s) of R).  A work unit's
+// candidate slots are numbered block after block (blocks with no allowed
+// rank-change class take none), then by the candidate's index in its block:
+// the added orbital, or the pair (a1 < a2) in row-major order.
+__host__ __device__ inline long long block_candidates(int nR, bool same_spin, int nv1, int nva, int nvb) {
+  if (nR == 1) return nv1;
+  return same_spin ? (long long)nv1 * (nv1 - 1) / 2 : (long long)nva * nvb;
+}
 
 // k_pt2<W, R, B, ADJ> launched with `smem` bytes of dynamic shared memory
 // (pt2_w1.cu / pt2_w2.cu: forward, plain and batched; pt2_adj.cu: adjoint).

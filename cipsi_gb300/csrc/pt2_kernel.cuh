@@ -598,7 +598,7 @@ __device__ __forceinline__ int hist_class(const Params& p, double val) {
 // all 32 lanes of a warp; `live` marks the lanes holding a perturber.
 template <int W, int R>
 __device__ void finish_candidate(const Params& p, bool live, const uint64_t* u, double hmpi,
-                                 double hvpi, const double* bc, int owner1 /*1-based, 0 = pertu*/,
+                                 double hvpi, const double* bc, int slot /*in the work unit*/,
                                  double fmul, int nmul, bool ybis, bool is_pert1, Acc<R>& acc,
                                  HistPriv<R>& hp) {
   constexpr unsigned kFull = 0xffffffffu;
@@ -693,27 +693,85 @@ __device__ void finish_candidate(const Params& p, bool live, const uint64_t* u, 
     }
   }
   if (ydeg) xam = 1.0;
-  // unit-60 record (pie.f): one slot reservation per warp
+  // unit-60 record (pie.f): counted per warp; kept, when asked, at the
+  // candidate's slot of this CTA's staging region (compacted in slot order
+  // when the work unit is done, unit_compact)
   const bool sel = live && xam > p.tau && p.ymoyen;
   const unsigned sm = __ballot_sync(kFull, sel);
-  if (sm) {
-    unsigned long long base = 0;
-    if (lane == 0) base = atomicAdd(&p.counters[C_NSEL], (unsigned long long)__popc(sm));
-    base = __shfl_sync(kFull, base, 0);
-    if (sel) {
-      const unsigned long long slot = base + __popc(sm & ((1u << lane) - 1u));
-      if ((long long)slot < p.sel_cap) {
+  if (sm && lane == 0) atomicAdd(&p.counters[C_NSEL], (unsigned long long)__popc(sm));
+  if (sel && p.rec_mode && slot >= p.st_cap) atomicAdd(&p.counters[C_STAGE_OVF], 1ull);  // host sizing error
+  if (sel && p.rec_mode && slot < p.st_cap) {
+    const size_t s = (size_t)blockIdx.x * p.st_cap + slot;
 #pragma unroll
-        for (int q = 0; q < 2 * W; ++q) p.sel_bits[slot * 2 * W + q] = u[q];
-        p.sel_owner[slot] = owner1;
-        p.sel_xam[slot] = xam;
-        // ENvp per root written by cipsym (cipsym/pert1.f:244): eivp*(fmul+1)
+    for (int q = 0; q < 2 * W; ++q) p.st_bits[s * 2 * W + q] = u[q];
+    p.st_xam[s] = xam;
+    // ENvp per root written by cipsym (cipsym/pert1.f:244): eivp*(fmul+1)
 #pragma unroll
-        for (int m = 0; m < R; ++m)
-          if (m < p.metat) p.sel_evp[slot * p.metat + m] = p.symvar ? sevp[m] : 0.0;
+    for (int m = 0; m < R; ++m)
+      if (m < p.metat) p.st_evp[s * p.metat + m] = p.symvar ? sevp[m] : 0.0;
+    atomicOr(&p.st_mask[(size_t)blockIdx.x * (p.st_cap >> 5) + (slot >> 5)], 1u << (slot & 31));
+  }
+}
+
+// End of a work unit (whole block): the staged records of its flagged
+// slots go, in slot order, to one segment of the record pool, reserved with
+// a single atomic; the unit table notes the segment.  The slot mask is
+// cleared for the next unit.  Records beyond the pool's capacity are
+// counted but not stored (the host sees pool_count > pool_cap).
+template <int W>
+__device__ __noinline__ void unit_compact(const Params& p, int unit, int nslots, int* tmp /* >= 32 ints */,
+                             long long& sbase /* shared */) {
+  constexpr unsigned kFull = 0xffffffffu;
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5, nw = blockDim.x >> 5;
+  __syncthreads();  // every warp's staging stores and mask bits are done
+  const int nwords = (min(nslots, p.st_cap) + 31) >> 5;
+  uint32_t* mask = p.st_mask + (size_t)blockIdx.x * (p.st_cap >> 5);
+  const size_t st0 = (size_t)blockIdx.x * p.st_cap;
+  // each thread owns a contiguous range of mask words
+  const int per = (nwords + (int)blockDim.x - 1) / (int)blockDim.x;
+  const int w0 = min(nwords, tid * per), w1 = min(nwords, w0 + per);
+  int cnt = 0;
+  for (int w = w0; w < w1; ++w) cnt += __popc(__ldcg(&mask[w]));
+  // block exclusive scan of cnt (thread order = slot order)
+  int incl = cnt;
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(kFull, incl, o);
+    if (lane >= o) incl += y;
+  }
+  if (lane == 31) tmp[wid] = incl;
+  __syncthreads();
+  if (tid == 0) {
+    int acc = 0;
+    for (int w = 0; w < nw; ++w) {
+      const int v = tmp[w];
+      tmp[w] = acc;
+      acc += v;
+    }
+    long long base = 0;
+    if (acc) base = (long long)atomicAdd(p.pool_count, (unsigned long long)acc);
+    p.unit_pool[unit] = base;
+    p.unit_nsel[unit] = acc;
+    sbase = base;
+  }
+  __syncthreads();
+  long long pos = sbase + tmp[wid] + (incl - cnt);
+  for (int w = w0; w < w1; ++w) {
+    uint32_t m = __ldcg(&mask[w]);
+    if (m) mask[w] = 0u;
+    while (m) {
+      const int b = __ffs(m) - 1;
+      m &= m - 1u;
+      if (pos < p.pool_cap) {
+        const size_t s = st0 + (size_t)(w * 32 + b);
+#pragma unroll
+        for (int q = 0; q < 2 * W; ++q) p.pool_bits[(size_t)pos * 2 * W + q] = __ldcg(&p.st_bits[s * 2 * W + q]);
+        p.pool_xam[pos] = __ldcg(&p.st_xam[s]);
+        for (int mm = 0; mm < p.metat; ++mm) p.pool_evp[(size_t)pos * p.metat + mm] = __ldcg(&p.st_evp[s * p.metat + mm]);
       }
+      ++pos;
     }
   }
+  __syncthreads();
 }
 
 template <int R>
@@ -757,7 +815,7 @@ __device__ void block_flush(const Params& p, Acc<R>& acc, int gslot, double* red
 template <int W, int R>
 __device__ void enqueue_candidate(const Params& p, WarpQueue<W, R>& q, int& qn, bool live,
                                   const uint64_t* u, double hmpi, double hvpi, const double* bc,
-                                  int owner1, double fmul, int nmul, bool ybis, bool is_pert1,
+                                  int slot, double fmul, int nmul, bool ybis, bool is_pert1,
                                   Acc<R>& acc, HistPriv<R>& hp);
 
 template <int W, int R>
@@ -776,7 +834,7 @@ __device__ __noinline__ void drain_queue(const Params& p, WarpQueue<W, R>& q, in
 #pragma unroll
     for (int m = 0; m < R; ++m) bc[m] = q.bc[m][e];
     const unsigned char f = q.flags[e];
-    finish_candidate<W, R>(p, live, u, q.hmp[e], q.hvp[e], bc, q.owner[e], q.fmul[e], q.nmul[e],
+    finish_candidate<W, R>(p, live, u, q.hmp[e], q.hvp[e], bc, q.slot[e], q.fmul[e], q.nmul[e],
                            (f & 1) != 0, (f & 2) != 0, acc, hp);
     __syncwarp();
     qn = base;
@@ -786,7 +844,7 @@ __device__ __noinline__ void drain_queue(const Params& p, WarpQueue<W, R>& q, in
 template <int W, int R>
 __device__ void enqueue_candidate(const Params& p, WarpQueue<W, R>& q, int& qn, bool live,
                                   const uint64_t* u, double hmpi, double hvpi, const double* bc,
-                                  int owner1, double fmul, int nmul, bool ybis, bool is_pert1,
+                                  int slot, double fmul, int nmul, bool ybis, bool is_pert1,
                                   Acc<R>& acc, HistPriv<R>& hp) {
   const int lane = threadIdx.x & 31;
   const unsigned lm = __ballot_sync(0xffffffffu, live);
@@ -800,7 +858,7 @@ __device__ void enqueue_candidate(const Params& p, WarpQueue<W, R>& q, int& qn, 
     q.hvp[e] = hvpi;
     q.fmul[e] = fmul;
     q.nmul[e] = nmul;
-    q.owner[e] = owner1;
+    q.slot[e] = slot;
     q.flags[e] = (unsigned char)((ybis ? 1 : 0) | (is_pert1 ? 2 : 0));
   }
   qn += __popc(lm);
@@ -881,6 +939,7 @@ struct BlockShared {
   int gen;
   int kidx;
   int rank_k;
+  long long unit_base;    // pool segment of the unit being compacted
 };
 
 template <int W, int R, bool B, bool ADJ>
@@ -1073,10 +1132,11 @@ __global__ void __launch_bounds__(kThreads, 2) k_pt2(Params p0, BatchArgs ba) {
             diag_terms_adj<W>(p, u, hf, p.yen ? gh : 0.0, gm, adj_sl);
           }
         } else {
-          enqueue_candidate<W, R>(p, wq, qn, live, u, hmpi, hvpi, bc, 0, 0.0, 0, false, true, acc, hp);
+          enqueue_candidate<W, R>(p, wq, qn, live, u, hmpi, hvpi, bc, t - ur0, 0.0, 0, false, true, acc, hp);
         }
       }
       drain_queue<W, R>(p, wq, qn, true, acc, hp);
+      if (!ADJ && p.rec_mode) unit_compact<W>(p, unit, ur1 - ur0, ctmp, sh.unit_base);
       block_flush<R>(p, acc, unit, red);
       continue;
     }
@@ -1145,9 +1205,9 @@ __global__ void __launch_bounds__(kThreads, 2) k_pt2(Params p0, BatchArgs ba) {
         ctmp).x;
     const int rank_k = sh.rank_k;
     const uint8_t dmask = p.gen_dmask[g];
-    const int k1 = k + 1;  // 1-based owner index
     const int nespk = p.nesp[k];
     const bool yefk = p.yef[k] != 0;
+    int slot0 = 0;  // first candidate slot of the current block in the unit
 
     // ---------------- blocks of removed electrons R (this unit's range)
     for (int r = ur0; r < ur1; ++r) {
@@ -1177,6 +1237,8 @@ __global__ void __launch_bounds__(kThreads, 2) k_pt2(Params p0, BatchArgs ba) {
         if (dmask & (1u << (D + 2))) any = true;
       }
       if (!any) continue;
+      const int bslot = slot0;
+      slot0 += (int)block_candidates(nRr, sp1 == sp2, sh.nvir[sp1], sh.nvir[0], sh.nvir[1]);
       const uint64_t rmask = (1ull << e1) | (e2 >= 0 ? (1ull << e2) : 0ull);
       // K' = k - R
       uint64_t kp[2 * W];
@@ -1315,7 +1377,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_pt2(Params p0, BatchArgs ba) {
       // listed entries rb[0..nrb) (owner test, already in S, <I|H|j>), then
       // the E2 / selection epilogue.  Called by whole warps.
       auto candidate = [&](bool live, int a1, int a2, int sa1, int sa2, int nscan, const int16_t* rb,
-                           int nrb) {
+                           int nrb, int slot) {
         int D = 0;
         bool ysyspi = true;
         if (live) {
@@ -1376,17 +1438,21 @@ __global__ void __launch_bounds__(kThreads, 2) k_pt2(Params p0, BatchArgs ba) {
             return false;
           };
           for (int i0 = 0; i0 < nscan && !drop; i0 += 4) {
-            // four independent compares per step (latency of the loads overlaps)
-            int xs[4];
-#pragma unroll
-            for (int g4 = 0; g4 < 4; ++g4) {
-              const int i = i0 + g4;
-              xs[g4] = i < nscan ? lr_diff(ent_at(i), c1x4, c2x4, two) : 99;
+            // four independent compares per step (latency of the loads
+            // overlaps); the hits are walked as a bit mask and each one's
+            // difference picked by selects, so nothing here is indexed at run
+            // time (a run-time index into a local array puts it on the stack)
+            const int x0 = lr_diff(ent_at(i0), c1x4, c2x4, two);
+            const int x1 = i0 + 1 < nscan ? lr_diff(ent_at(i0 + 1), c1x4, c2x4, two) : 99;
+            const int x2 = i0 + 2 < nscan ? lr_diff(ent_at(i0 + 2), c1x4, c2x4, two) : 99;
+            const int x3 = i0 + 3 < nscan ? lr_diff(ent_at(i0 + 3), c1x4, c2x4, two) : 99;
+            unsigned hits = (x0 <= 4 ? 1u : 0u) | (x1 <= 4 ? 2u : 0u) | (x2 <= 4 ? 4u : 0u) | (x3 <= 4 ? 8u : 0u);
+            while (hits && !drop) {
+              const int g4 = __ffs(hits) - 1;
+              hits &= hits - 1u;
+              const int x = g4 == 0 ? x0 : g4 == 1 ? x1 : g4 == 2 ? x2 : x3;
+              drop = visit(i0 + g4, x);
             }
-            if (xs[0] > 4 && xs[1] > 4 && xs[2] > 4 && xs[3] > 4) continue;
-#pragma unroll 1
-            for (int g4 = 0; g4 < 4 && !drop; ++g4)
-              if (xs[g4] <= 4) drop = visit(i0 + g4, xs[g4]);
           }
           for (int q2 = 0; q2 < nrb && !drop; ++q2) {
             const int i = rb[q2];
@@ -1478,7 +1544,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_pt2(Params p0, BatchArgs ba) {
           }
           return;
         }
-        enqueue_candidate<W, R>(p, wq, qn, live, u, hmpi, hvpi, bc, k1, fmul, nmul, ybis, is_pert1, acc, hp);
+        enqueue_candidate<W, R>(p, wq, qn, live, u, hmpi, hvpi, bc, slot, fmul, nmul, ybis, is_pert1, acc, hp);
       };
       if (nRr == 1 || !fast) {
         // flat: threads take candidates, every candidate scans all of L_R
@@ -1505,7 +1571,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_pt2(Params p0, BatchArgs ba) {
               sa2 = 1;
             }
           }
-          candidate(live, a1, a2, sa1, sa2, nlr, nullptr, 0);
+          candidate(live, a1, a2, sa1, sa2, nlr, nullptr, 0, bslot + t);
         }
       } else {
         // rows: one warp per first added orbital a1; an entry with
@@ -1542,10 +1608,12 @@ __global__ void __launch_bounds__(kThreads, 2) k_pt2(Params p0, BatchArgs ba) {
             const int c = c0 + lane;
             const bool live = c < ncols;
             const int a2 = live ? (same ? sh.vir[sc][row + 1 + c] : sh.vir[sc][c]) : 0;
-            if (!overflow)
-              candidate(live, a1, a2, sr, sc, n01, rowbuf, nrb);
-            else
-              candidate(live, a1, a2, sr, sc, nlr, nullptr, 0);
+            // a row list that overflowed falls back to the whole of L_R (one
+            // call site: the candidate code is instantiated once for rows)
+            // slot: the pair's index in the flat enumeration (row-major
+            // over a1 < a2 for one spin, a1 x a2 for opposite spins)
+            const int tflat = same ? row * (nv1 - 1) - row * (row - 1) / 2 + c : row * sh.nvir[1] + c;
+            candidate(live, a1, a2, sr, sc, overflow ? nlr : n01, rowbuf, overflow ? 0 : nrb, bslot + tflat);
           }
           __syncwarp();
         }
@@ -1611,6 +1679,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_pt2(Params p0, BatchArgs ba) {
       }
     }
     drain_queue<W, R>(p, wq, qn, true, acc, hp);
+    if (!ADJ && p.rec_mode) unit_compact<W>(p, unit, slot0, ctmp, sh.unit_base);
     block_flush<R>(p, acc, unit, red);
   }
 

@@ -46,7 +46,40 @@ class Result(ctypes.Structure):
                 ("tabvp", ctypes.c_double * (NCLASS * MAX_ROOTS)),
                 ("n_candidates", ctypes.c_int64), ("n_compares", ctypes.c_int64),
                 ("n_pairs_1", ctypes.c_int64), ("n_pairs_2", ctypes.c_int64),
-                ("alg_bytes", ctypes.c_int64), ("kernel_ms", ctypes.c_double)]
+                ("alg_bytes", ctypes.c_int64), ("kernel_ms", ctypes.c_double), ("pt2_ms", ctypes.c_double),
+                ("launches", ctypes.c_int64)]
+
+
+class Digest(ctypes.Structure):
+    """cipsi_digest: order-sensitive digest of streamed records."""
+    _fields_ = [("s1", ctypes.c_uint64 * 4), ("s2", ctypes.c_uint64 * 4), ("records", ctypes.c_int64),
+                ("threads", ctypes.c_int32)]
+
+    def value(self) -> tuple:
+        return tuple(self.s1) + tuple(self.s2)
+
+
+# cipsi_record_fn
+RECORD_FN = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_int32,
+                             ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p)
+
+
+def digest_arrays(bits, owner, xam, evp, state=None) -> tuple:
+    """The cipsi_digest pair sums of record arrays (numpy restatement of
+    cipsi_record_digest, for checks): per field array, s1 = sum of its 64-bit
+    words and s2 = sum of the running s1, modulo 2^64, continuing `state`."""
+    s1 = list(state[:4]) if state else [0] * 4
+    s2 = list(state[4:]) if state else [0] * 4
+    arrays = [np.ascontiguousarray(bits, np.uint64).ravel(),
+              np.ascontiguousarray(owner, np.int32).ravel().view(np.uint32).astype(np.uint64),
+              np.ascontiguousarray(xam, np.float64).ravel().view(np.uint64),
+              np.ascontiguousarray(evp, np.float64).ravel().view(np.uint64)]
+    for f, w in enumerate(arrays):
+        with np.errstate(over="ignore"):
+            run = np.cumsum(w, dtype=np.uint64) + np.uint64(s1[f])
+            s2[f] = (s2[f] + int(run.sum(dtype=np.uint64))) % (1 << 64) if len(w) else s2[f]
+            s1[f] = int(run[-1]) if len(w) else s1[f]
+    return tuple(s1) + tuple(s2)
 
 
 _bound = False
@@ -86,6 +119,8 @@ def _lib():
         "cipsi_set_integrals_f64store": ([P, P, P, P, P, P, P, P, P, ctypes.c_int64], ctypes.c_int),
         "cipsi_set_roots": ([P, P, P, P, P, P, P, P], ctypes.c_int),
         "cipsi_run_pt2_adjoint": ([P, ctypes.POINTER(Opts), P, P, P, P, P, P, P], ctypes.c_int),
+        "cipsi_run_pt2_stream": ([P, ctypes.POINTER(Opts), ctypes.c_int64, P, P, ctypes.POINTER(Result)],
+                                 ctypes.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)
@@ -98,7 +133,7 @@ def _lib():
 def result_dict(r: Result, metat: int, nclass: int = NCLASS) -> dict:
     d = {k: list(getattr(r, k))[:metat] for k in ("e2mp", "e2vp", "e2b", "psimp", "psivp")}
     for k in ("dpivot", "ietat", "n_processed", "n_selected", "n_candidates", "n_compares",
-              "n_pairs_1", "n_pairs_2", "alg_bytes", "kernel_ms"):
+              "n_pairs_1", "n_pairs_2", "alg_bytes", "kernel_ms", "pt2_ms", "launches"):
         d[k] = getattr(r, k)
     d["nom"] = list(r.nom)[:nclass]
     d["nam"] = [[r.nam[c * MAX_ROOTS + m] for c in range(nclass)] for m in range(metat)]
@@ -254,6 +289,39 @@ class Context:
         o = self._opts(opts, gen_mask, run_pertu)
         self._last_nclass = o.nclass
         self._check(self.lib.cipsi_run_pt2_async(self._c, ctypes.byref(o)), "run_pt2_async")
+
+    def run_stream(self, opts: Opts, chunk_records: int = 0, consumer=None, gen_mask: Optional[np.ndarray] = None,
+                   run_pertu: Optional[bool] = None) -> dict:
+        """cipsi_run_pt2_stream.  consumer: None (records stay on the device),
+        a Digest (the library's native digest consumer), or a Python callable
+        f(first, bits, owner, xam, evp) given numpy copies of each piece."""
+        o = self._opts(opts, gen_mask, run_pertu)
+        r = Result()
+        mt = self.dims.metat
+        keep = None
+        if consumer is None:
+            fn, user = None, None
+        elif isinstance(consumer, Digest):
+            fn = ctypes.cast(self.lib.cipsi_record_digest, ctypes.c_void_p).value
+            user = ctypes.addressof(consumer)
+        else:
+            def _cb(user_, first, count, words, metat, bits, owner, xam, evp):
+                try:
+                    def arr(ptr, ctype, n):
+                        return np.ctypeslib.as_array(ctypes.cast(ptr, ctypes.POINTER(ctype)), shape=(n,)).copy()
+                    consumer(first, arr(bits, ctypes.c_uint64, count * words).reshape(count, words),
+                             arr(owner, ctypes.c_int32, count), arr(xam, ctypes.c_double, count),
+                             arr(evp, ctypes.c_double, count * metat).reshape(count, metat))
+                    return 0
+                except Exception:  # noqa: BLE001 -- any failure stops the run
+                    return 1
+            keep = RECORD_FN(_cb)
+            fn, user = ctypes.cast(keep, ctypes.c_void_p).value, None
+        self._last_nclass = o.nclass
+        self._check(self.lib.cipsi_run_pt2_stream(self._c, ctypes.byref(o), chunk_records, fn, user,
+                                                  ctypes.byref(r)), "run_pt2_stream")
+        del keep
+        return result_dict(r, mt, o.nclass)
 
     def fetch(self) -> dict:
         r = Result()

@@ -93,6 +93,17 @@ class SynthConfig:
                                      # L(R) = L0 + exp(-R/3) L1, eps(R) = eps0 + 0.1 exp(-R/2) eps1
     energy: str = "rayleigh"  # root energies: "rayleigh" (<Psi|H|Psi>) or "diagonal"
                               # (sum_k c_k^2 H_kk: no O(ncf^2) pass, for many large geometries)
+    # space = "cas": S is the complete active space of the cas_occ highest
+    # occupied and cas_virt lowest virtual orbitals (every Ms = 0 placement
+    # of their 2*cas_occ electrons, ncf is then C(cas_occ+cas_virt,
+    # cas_occ)^2); core_shift lowers the other occupied orbitals and
+    # virt_shift raises only the other virtuals, so every perturber (it has
+    # an electron outside the active space) lies several Eh above every root
+    # energy: E2 without small denominators, for any roots within S
+    space: str = "random"
+    cas_occ: int = 2
+    cas_virt: int = 8
+    core_shift: float = 0.0
 
 
 CONFIGS: Dict[str, SynthConfig] = {
@@ -131,7 +142,11 @@ def make_integrals(cfg: SynthConfig, rng: np.random.Generator):
     if cfg.virt_shift:
         # a gap between occupied and virtual orbital energies keeps every
         # perturbation denominator away from zero (well-conditioned E2)
-        h[np.arange(cfg.nocc, n), np.arange(cfg.nocc, n)] += cfg.virt_shift
+        v0 = cfg.nocc + (cfg.cas_virt if cfg.space == "cas" else 0)
+        h[np.arange(v0, n), np.arange(v0, n)] += cfg.virt_shift
+    if cfg.core_shift:
+        c1 = cfg.nocc - (cfg.cas_occ if cfg.space == "cas" else 0)
+        h[np.arange(0, c1), np.arange(0, c1)] -= cfg.core_shift
     def cholesky_vectors():
         out = np.zeros((cfg.ncholesky, n, n))
         for K in range(cfg.ncholesky):
@@ -376,8 +391,44 @@ def random_det(rng, rank: int, norb: int, nocc: int, irrep, isym: int):
     raise RuntimeError("could not draw a determinant of the requested symmetry")
 
 
+def build_cas_space(cfg: SynthConfig, irrep):
+    """S = the complete active space (space = "cas"), as (holes, parts)
+    lists closed under spin flip (partners adjacent) and orbit indices."""
+    import itertools
+    norb, nocc = cfg.norb, cfg.nocc
+    act = list(range(nocc - cfg.cas_occ + 1, nocc + cfg.cas_virt + 1))
+    occ_act = set(range(nocc - cfg.cas_occ + 1, nocc + 1))
+    strings = []
+    for sel in itertools.combinations(act, cfg.cas_occ):
+        hs = sorted(occ_act - set(sel))
+        ps = sorted(o for o in sel if o > nocc)
+        g = 0
+        for o in hs + ps:
+            g ^= int(irrep[o - 1])
+        strings.append((hs, ps, g))
+    dets, rep_of = [], []
+    nrep = 0
+    for a, (ha, pa, ga) in enumerate(strings):
+        for b in range(a, len(strings)):
+            hb, pb, gb = strings[b]
+            if ga ^ gb:
+                continue
+            key = (tuple(sorted(ha + [o + norb for o in hb])), tuple(sorted(pa + [o + norb for o in pb])))
+            dets.append(key)
+            rep_of.append(nrep)
+            if a != b:
+                fkey = (tuple(sorted(hb + [o + norb for o in ha])), tuple(sorted(pb + [o + norb for o in pa])))
+                dets.append(fkey)
+                rep_of.append(nrep)
+            nrep += 1
+    order = sorted(range(len(dets)), key=lambda i: (len(dets[i][0]), i))
+    return [dets[i] for i in order], [rep_of[i] for i in order]
+
+
 def build_space(cfg: SynthConfig, rng, irrep):
     """S as a list of (holes, parts, rep_index) closed under spin flip."""
+    if cfg.space == "cas":
+        return build_cas_space(cfg, irrep)
     norb, nocc = cfg.norb, cfg.nocc
     seen = set()
     dets: List[Tuple[Tuple[int, ...], Tuple[int, ...]]] = []

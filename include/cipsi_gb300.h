@@ -93,6 +93,10 @@ typedef struct {
   int64_t alg_bytes;      /* algorithmic bytes (integrals, coefficients,     */
                           /* diagonal terms) read by the E2 loop             */
   double kernel_ms;       /* device time of the perturbation kernels         */
+  double pt2_ms;          /* of which the perturbation kernel itself (k_pt2, */
+                          /* summed over its launches)                        */
+  int64_t launches;       /* kernel launches of the run (k_pt2, record scan  */
+                          /* and gather per chunk, final reduction)           */
 } cipsi_result;
 
 /* Create a context on CUDA device `device`.
@@ -174,14 +178,52 @@ int cipsi_set_tuning(cipsi_ctx* ctx, int32_t r_chunk, int32_t ctas_per_sm);
 int cipsi_set_selection_sink(cipsi_ctx* ctx, uint64_t* bits, int32_t* owner, double* xam, double* evp,
                              int64_t capacity);
 
+/* Streamed run (no counterpart in the reference; replaces pie.f's
+   buffered writes of lungo records to unit 60, CIPSI_sources/cip/pie.f:
+   20-36, for selections too large for device memory): the same work as
+   cipsi_run_pt2, in chunks of consecutive work units whose candidate slots
+   fit `chunk_records` records (0 = sized from the free device memory, at
+   most 2^29).  Each chunk's records are copied into pinned host buffers
+   while the next chunk computes, and `fn` receives them piece by piece, in
+   the order cipsi_selection_get gives, with `first` = the index of the
+   piece's first record in the run: bits[count*words] (words = 2W, as
+   cipsi_selection_raw), owner[count], xam[count], evp[count*metat].  The
+   pointers are valid during the call only.  A non-zero return from fn stops
+   the run (CIPSI_ERR_ARG).  fn = NULL keeps each chunk's records in device
+   memory only (timing of the device work).  Blocks until done; nothing is
+   left for cipsi_selection_get. */
+typedef int (*cipsi_record_fn)(void* user, int64_t first, int64_t count, int32_t words, int32_t metat,
+                               const uint64_t* bits, const int32_t* owner, const double* xam,
+                               const double* evp);
+int cipsi_run_pt2_stream(cipsi_ctx* ctx, const cipsi_opts* opts, int64_t chunk_records,
+                         cipsi_record_fn fn, void* user, cipsi_result* res);
+
+/* A record consumer for cipsi_run_pt2_stream (user = cipsi_digest*, zero it
+   and set `threads` first): an order-sensitive digest of the streamed
+   records, per field array (bits, owner, xam, evp) the pair s1 = sum of its
+   64-bit words, s2 = sum of the running s1, over the run's records in
+   order (unsigned arithmetic modulo 2^64; owner words zero-extended, doubles
+   as their bit patterns).  Pieces must arrive in order (first ==
+   records).  No counterpart in the reference. */
+typedef struct {
+  uint64_t s1[4], s2[4];
+  int64_t records;
+  int32_t threads;
+} cipsi_digest;
+int cipsi_record_digest(void* user, int64_t first, int64_t count, int32_t words, int32_t metat,
+                        const uint64_t* bits, const int32_t* owner, const double* xam, const double* evp);
+
 /* Enqueue the same work on the context stream without waiting; the result is
    collected by cipsi_fetch_result.  Used to time the kernels alone. */
 int cipsi_run_pt2_async(cipsi_ctx* ctx, const cipsi_opts* opts);
 int cipsi_fetch_result(cipsi_ctx* ctx, cipsi_result* res);
 
 /* Selected perturbers (what pie.f writes to unit 60), records
-   [first, first+count) of the last run in the engine's emission order (the
-   set of records is deterministic; their order is not).
+   [first, first+count) of the last run.  Their order is fixed whatever the
+   GPU's scheduling: work units in the run's order (generators by
+   excitation rank, then by index; pertu's candidates first), and within a
+   unit blocks of removed electrons, then added orbitals, in enumeration
+   order.  Two runs on the same inputs give identical arrays.
      nec[count]           excitation degree
      holes/parts[8*count] sorted spin orbitals (1-based), zero padded
      xam[count]           selection value written as v(n)

@@ -401,6 +401,10 @@ static int run_pertu_ref = 1;          /* include pertu's kk=0 candidates */
 static FILE* cand_log = NULL;
 static long long n_processed = 0;      /* perturbers reaching the E2 loop */
 static int cur_src = 0;                /* 0 pertu, 1 igene, 2 diexcit */
+/* systematic sample (CPU timing only, --sample M with --plan): one pert1
+   candidate in M, and one diexcit hole/particle quadruple in M, counted in
+   enumeration order from samp_seq; residue samp_m is kept */
+static long long samp_M = 0, samp_m = 0, samp_seq = 0;
 
 static int noc_[3], igels_[3], norbs_[3]; /* equivalence (noca,noc(1)) etc. */
 
@@ -703,6 +707,7 @@ static int* ikk_buf;
 static double* stok_buf;
 
 static void pert1(int kkmod, int nf) {
+  if (samp_M > 1 && (samp_seq++ % samp_M) != samp_m) return;
   int nts[16], nps[16];
   double vil[64] = {0}, him[64], dmp[64], dvp[64], db[64], venvp[64];
   if (kkmod < 0) kkmod = 0;
@@ -1262,6 +1267,7 @@ static void pertu(void) {
 static int* irapid;
 
 static void diexcit_one(int ii, int jj, int kk, int ll, int nspin, int yijkl, double* hijkl_p) {
+  if (samp_M > 1 && (samp_seq++ % samp_M) != samp_m) return;
   /* isp(4,3) data 0,1,0,1, 0,0,0,0, 0,1,1,0 (column-major isp(i,isa)) */
   static const int ISP[4][5] = {{0}, {0, 0, 1, 0, 1}, {0, 0, 0, 0, 0}, {0, 0, 1, 1, 0}};
   int nf = ncf + 1, ndf = nd[nf];
@@ -2093,7 +2099,9 @@ static double now_s(void) {
 static void usage(void) {
   fprintf(stderr,
           "usage: cipsi_ref [--sym] [--json out.json] [--candlog file] [--genmask file]\n"
-          "                 [--no-pertu-ref] < stdin-namelists\n");
+          "                 [--no-pertu-ref] [--sample M --plan file] < stdin-namelists\n"
+          "  --plan: lines 'm k1 k2 ...' (1-based generators); each line runs those\n"
+          "  generators on the sample residue m and reports [perturbers, seconds]\n");
   exit(2);
 }
 
@@ -2101,6 +2109,7 @@ int main(int argc, char** argv) {
   const char* json_path = "cipsi_ref.json";
   const char* cand_path = NULL;
   const char* mask_path = NULL;
+  const char* plan_path = NULL;
   for (int a = 1; a < argc; a++) {
     if (!strcmp(argv[a], "--sym"))
       g_sym_variant = 1;
@@ -2112,6 +2121,10 @@ int main(int argc, char** argv) {
       mask_path = argv[++a];
     else if (!strcmp(argv[a], "--no-pertu-ref"))
       run_pertu_ref = 0;
+    else if (!strcmp(argv[a], "--sample") && a + 1 < argc)
+      samp_M = atoll(argv[++a]);
+    else if (!strcmp(argv[a], "--plan") && a + 1 < argc)
+      plan_path = argv[++a];
     else
       usage();
   }
@@ -2646,10 +2659,45 @@ int main(int argc, char** argv) {
     free(r.b);
     return 0;
   }
+  /* --plan: timing of sampled generator sets on inputs read once (the
+     perturbation loop only, by this process's clock) */
+  long long plan_n[4096];
+  double plan_t[4096];
+  int nplan = 0;
+  if (plan_path) {
+    FILE* fp = fopen(plan_path, "r");
+    if (!fp) die("cannot open plan %s", plan_path);
+    if (!gen_mask) gen_mask = (unsigned char*)xcalloc((size_t)ncf + 4, 1);
+    run_pertu_ref = 0;
+    char line[65536];
+    while (fgets(line, sizeof line, fp) && nplan < 4096) {
+      char* q = line;
+      char* e;
+      long long m = strtoll(q, &e, 10);
+      if (e == q) continue;
+      q = e;
+      memset(gen_mask, 0, (size_t)ncf + 4);
+      for (;;) {
+        long k = strtol(q, &e, 10);
+        if (e == q) break;
+        q = e;
+        if (k >= 1 && k <= ncf) gen_mask[k] = 1;
+      }
+      samp_m = samp_M > 1 ? m % samp_M : 0;
+      samp_seq = 0;
+      const long long n0 = n_processed;
+      const double ta = now_s();
+      if (ypertu) pertu();
+      if (ypertu) diexcit();
+      plan_t[nplan] = now_s() - ta;
+      plan_n[nplan++] = n_processed - n0;
+    }
+    fclose(fp);
+  }
   double t0 = now_s();
-  if (ypertu) pertu();
+  if (ypertu && !plan_path) pertu();
   double t1 = now_s();
-  if (ypertu) diexcit();
+  if (ypertu && !plan_path) diexcit();
   double t2 = now_s();
   if (ymoyen) {
     fine();
@@ -2737,6 +2785,8 @@ int main(int argc, char** argv) {
       for (int i = 1; i <= nclass; i++) fprintf(fj, "%s%.17g", i > 1 ? ", " : "", tabvp[i][m]);
       fprintf(fj, "]");
     }
+    fprintf(fj, "],\n  \"plan\": [");
+    for (int i = 0; i < nplan; i++) fprintf(fj, "%s[%lld, %.6f]", i ? ", " : "", plan_n[i], plan_t[i]);
     fprintf(fj, "],\n  \"t_pertu_s\": %.6f, \"t_diexcit_s\": %.6f\n}\n", t1 - t0, t2 - t1);
     fclose(fj);
   }

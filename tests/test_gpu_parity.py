@@ -152,11 +152,9 @@ def test_deterministic(tmp_path, engine_lib):
         s2 = ctx.selection(r2["n_selected"])
     for k in ("e2mp", "e2vp", "e2b", "psimp", "psivp", "ietat", "n_processed", "dpivot", "nom", "nam"):
         assert r1[k] == r2[k], k
-    # the set of selected records is reproducible (their order is not)
-    def rows(s):
-        return sorted(zip(s["owner"].tolist(), map(tuple, s["holes"].tolist()), map(tuple, s["parts"].tolist()),
-                          s["xam"].tolist(), map(tuple, s["evp"].tolist())))
-    assert rows(s1) == rows(s2)
+    # the selected records and their order are reproducible
+    for k in ("owner", "nec", "holes", "parts", "xam", "evp"):
+        assert np.array_equal(s1[k], s2[k]), k
 
 
 def test_generator_shards_add_up(tmp_path, engine_lib):
@@ -177,3 +175,112 @@ def test_generator_shards_add_up(tmp_path, engine_lib):
     assert comb["nom"] == full["nom"]
     for k in ("e2mp", "e2vp", "e2b"):
         np.testing.assert_allclose(comb[k], full[k], rtol=1e-12, atol=1e-9)
+
+
+# ---------------------------------------------------------------- strict
+# E2 to 1e-10 Eh with no rounding-bound allowance, at the benchmark sizes.
+# The reference space is a complete active space (2 + 2 electrons in the 2
+# highest occupied and 8 lowest virtual orbitals, 2025 determinants) with
+# the other occupied orbitals lowered and the other virtuals raised by 6 Eh:
+# every perturber has an electron outside the active space, so it lies
+# several Eh above every root and no denominator comes near zero (the
+# oracle's first-order rounding bound is ~1e-12 Eh).  Measured |dE2| go to
+# $CIPSI_PARITY_LOG when set.
+
+def _cas(name, norb, nocc, nch, metat, tau, seed=1, **kw):
+    return synth.SynthConfig(name, norb=norb, nocc=nocc, ncholesky=nch, ncf=0, metat=metat, tau=tau,
+                             coef_mode="gauss005", seed=seed, space="cas", cas_occ=2, cas_virt=8,
+                             core_shift=6.0, virt_shift=6.0, **kw)
+
+
+def _log(name, jo, jg):
+    path = os.environ.get("CIPSI_PARITY_LOG")
+    if not path:
+        return
+    rec = {"case": name, "n_processed": jg["n_processed"]}
+    for k in ("e2mp", "e2vp", "e2b"):
+        rec[k] = jg[k]
+        rec["max_abs_diff_" + k] = float(np.max(np.abs(np.array(jo[k]) - np.array(jg[k]))))
+        rec["cond_" + k] = jo["cond_" + k]
+    with open(path, "a") as fh:
+        fh.write(json.dumps(rec) + "\n")
+
+
+def test_parity_strict_medium_size(tmp_path, oracle_exe, engine_lib):
+    """60 orbitals, 20 electrons, S = 2025, 3 roots, every 25th determinant
+    of S as generator (81 generators), E2 to 1e-10 Eh."""
+    cfg = _cas("cas60", 60, 10, 120, 3, 0.01)
+    jo, jg, wo, wg = run_both(tmp_path, cfg, mask_every=25)
+    assert max(max(jo["cond_" + k]) for k in ("e2mp", "e2vp", "e2b")) < 1e-11
+    _log("strict_medium_size", jo, jg)
+    check(jo, jg, wo, wg, "cipsym", strict=True)
+
+
+def test_parity_strict_large_size(tmp_path, oracle_exe, engine_lib):
+    """120 orbitals, 30 electrons (two 64-bit words per spin string),
+    S = 2025, 2 roots, tau 0.005, every 120th determinant of S as generator,
+    E2 to 1e-10 Eh."""
+    cfg = _cas("cas120", 120, 15, 240, 2, 0.005)
+    jo, jg, wo, wg = run_both(tmp_path, cfg, mask_every=120)
+    assert max(max(jo["cond_" + k]) for k in ("e2mp", "e2vp", "e2b")) < 1e-11
+    _log("strict_large_size", jo, jg)
+    check(jo, jg, wo, wg, "cipsym", strict=True)
+
+
+def _gap(seed, ranks, nsym, **kw):
+    return synth.SynthConfig("gap", norb=16, nocc=4, ncholesky=16, ncf=60, metat=2, tau=0.01, ranks=ranks,
+                             coef_mode="gauss005", seed=seed, nsym=nsym, virt_shift=3.0, **kw)
+
+
+@pytest.mark.parametrize("ityper,iselec", [(1, 1), (2, 2), (2, 3), (1, 3)])
+def test_parity_options_ityper_iselec(tmp_path, oracle_exe, engine_lib, ityper, iselec):
+    """MP only (ityper = 1: no EN sums, the MP coefficient selects),
+    iselec = 2 (teste = test, taum = 1) and 3 (selection on energy
+    contributions), strict, on the small and the medium-size CAS system."""
+    for seed, ranks, nsym in ((32, (1, 2, 3), 1), (33, (1, 2), 2)):
+        cfg = dataclasses.replace(_gap(seed, ranks, nsym), ityper=ityper, iselec=iselec)
+        jo, jg, wo, wg = run_both(tmp_path / f"s{seed}", cfg)
+        check(jo, jg, wo, wg, "cipsym", strict=True)
+    cfg = dataclasses.replace(_cas("cas60", 60, 10, 120, 3, 0.01), ityper=ityper, iselec=iselec)
+    jo, jg, wo, wg = run_both(tmp_path / "cas", cfg, mask_every=97)
+    _log(f"strict_medium_ityper{ityper}_iselec{iselec}", jo, jg)
+    check(jo, jg, wo, wg, "cipsym", strict=True)
+
+
+def test_parity_c1_mp_only(tmp_path, oracle_exe, engine_lib):
+    """The small system (20 orbitals, S = 50, 1 root, tau 0.02) with the MP
+    partition only (ityper = 1), as well as MP + EN (the default)."""
+    cfg = dataclasses.replace(synth.CONFIGS["small"], ityper=1)
+    jo, jg, wo, wg = run_both(tmp_path, cfg)
+    check(jo, jg, wo, wg, "cipsym")
+
+
+@pytest.mark.parametrize("coeff", [0.02, 0.1])
+def test_parity_cip_generators_by_coeff(tmp_path, oracle_exe, engine_lib, coeff):
+    """cip (not cipsym) runs as generators only the determinants with
+    |c| >= coeff in some root (ic001.f)."""
+    cfg = dataclasses.replace(_gap(32, (1, 2, 3), 1), variant="cip", extra_icinp=f"coeff={coeff}")
+    jo, jg, wo, wg = run_both(tmp_path, cfg, variant="cip")
+    check(jo, jg, wo, wg, "cip", strict=True)
+
+
+def test_parity_without_ywdeg(tmp_path, oracle_exe, engine_lib):
+    """ywdeg = .false.: near-degenerate perturbers are not forced into the
+    selection."""
+    for i, cfg in enumerate([dataclasses.replace(synth.CONFIGS["small"], extra_icinp="ywdeg=f"),
+                             dataclasses.replace(synth.CONFIGS["medium"], extra_icinp="ywdeg=f")]):
+        jo, jg, wo, wg = run_both(tmp_path / f"c{i}", cfg, mask_every=None if i == 0 else 199)
+        check(jo, jg, wo, wg, "cipsym")
+
+
+@pytest.mark.parametrize("metat", [5, 6, 8])
+def test_parity_five_to_eight_roots(tmp_path, oracle_exe, engine_lib, metat):
+    """5-8 roots: the kernel's R = 8 instantiation (roots padded to 8)."""
+    cfg = synth.SynthConfig("gap", norb=14, nocc=4, ncholesky=14, ncf=60, metat=metat, tau=0.01, ranks=(1, 2),
+                            coef_mode="decay09", seed=35, virt_shift=3.0)
+    jo, jg, wo, wg = run_both(tmp_path, cfg)
+    check(jo, jg, wo, wg, "cipsym")
+    cfg = _cas("cas8", 24, 6, 30, metat, 0.01, seed=7)
+    jo, jg, wo, wg = run_both(tmp_path / "cas", cfg)
+    _log(f"strict_cas_{metat}roots", jo, jg)
+    check(jo, jg, wo, wg, "cipsym", strict=True)

@@ -85,3 +85,37 @@ def test_no_gpu_means_error_not_fallback(tmp_path, engine_lib):
     wd = _golden(tmp_path)
     with pytest.raises(cg.CipsiError, match="cuda|CUDA"):
         cg.run_cip(wd)
+
+
+def test_record_digest_consumer_matches_its_restatement(engine_lib):
+    """cipsi_record_digest (host code, the streamed run's native consumer)
+    over pieces of records, with several host threads, against the numpy
+    restatement; a piece out of order is refused."""
+    import numpy as np
+    from cipsi_gb300 import engine
+    lib = engine._lib()
+    f = lib.cipsi_record_digest
+    f.argtypes = [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_int32, ctypes.c_int32,
+                  ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+    f.restype = ctypes.c_int
+    rng = np.random.default_rng(3)
+    n, words, mt = 300_000, 4, 3
+    bits = rng.integers(0, 2**63, size=(n, words), dtype=np.uint64)
+    owner = rng.integers(-5, 20000, size=n).astype(np.int32)
+    xam = rng.random(n)
+    evp = rng.normal(size=(n, mt))
+    d = engine.Digest()
+    d.threads = 6
+    for a, b in ((0, 70_001), (70_001, 70_001), (70_001, 250_000), (250_000, n)):
+        rc = f(ctypes.addressof(d), a, b - a, words, mt, bits[a:].ctypes.data, owner[a:].ctypes.data,
+               xam[a:].ctypes.data, evp[a:].ctypes.data)
+        assert rc == 0
+    assert d.records == n
+    assert d.value() == engine.digest_arrays(bits, owner, xam, evp)
+    # the digest depends on the order of the records
+    sw = [x.copy() for x in (bits, owner, xam, evp)]
+    for x in sw:
+        x[[5, 6]] = x[[6, 5]]
+    assert engine.digest_arrays(*sw) != d.value()
+    assert f(ctypes.addressof(d), 5, 1, words, mt, bits.ctypes.data, owner.ctypes.data, xam.ctypes.data,
+             evp.ctypes.data) != 0
