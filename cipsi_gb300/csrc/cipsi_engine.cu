@@ -808,12 +808,14 @@ LaunchShape launch_shape(int W, int R, int ncf_max, int ctas) {
   // two CTAs per SM unless one is asked for: the part of a long L_R list
   // beyond shared memory is read from the block's global scratch, 8 bytes
   // per entry, which costs less than halving the resident warps
-  const size_t smem_total = ctas == 1 ? (size_t)200 * 1024 : (size_t)90 * 1024;
+  // (the kernel's static shared memory, ~28 KB, comes on top: two CTAs of
+  // 82 + 28 KB, or one of 192 + 28 KB, fit the SM's 228 KB)
+  const size_t smem_total = ctas == 1 ? (size_t)192 * 1024 : (size_t)82 * 1024;
   const size_t smem_budget = smem_total > qbytes + 16 ? smem_total - qbytes - 16 : 0;
   LaunchShape ls;
   ls.lr_cap = (int)std::min<size_t>((size_t)ncf_max, smem_budget / per_entry);
   ls.smem = (((size_t)ls.lr_cap * per_entry + 15) & ~(size_t)15) + qbytes + 16;
-  ls.blocks_per_sm = ctas == 1 ? 1 : ls.smem <= 95 * 1024 ? 2 : 1;
+  ls.blocks_per_sm = ctas == 1 ? 1 : ls.smem <= 86 * 1024 ? 2 : 1;
   return ls;
 }
 

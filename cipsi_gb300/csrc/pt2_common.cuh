@@ -18,6 +18,7 @@ constexpr int kMaxSym = 8;
 constexpr int kMaxElec = 64;
 constexpr int kMaxOrb = 128;
 constexpr int kRowCap = 128;  // per-warp list of |K' \ j| = 2 entries holding a1
+constexpr int kHitCap = 8;    // per-thread list of scan hits awaiting their matrix elements
 
 // counters[] slots
 enum {

@@ -955,6 +955,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_pt2(Params p0, BatchArgs ba) {
   __shared__ double red[5 * kMaxRoots * 32];
   __shared__ int ctmp[33];
   __shared__ int16_t wrow[(kThreads / 32) * kRowCap];
+  __shared__ int hitl[kThreads * kHitCap];  // per-thread lists of scan hits
 
   const int tid = threadIdx.x;
   // shared L_R arrays (fast path)
@@ -1405,43 +1406,77 @@ __global__ void __launch_bounds__(kThreads, 2) k_pt2(Params p0, BatchArgs ba) {
 #pragma unroll
         for (int m = 0; m < R; ++m) bc[m] = 0.0;
         int nint = 0, nnz = 0, lesp = 0;
+        // The scan runs in two phases so that the expensive part (the
+        // Slater-Condon element and its integral gathers) runs with the warp
+        // converged: phase A compares I with every entry and applies the
+        // owner and already-in-S tests from the entry alone, keeping the
+        // lane's remaining hits in its list; phase B then takes the t-th hit
+        // of every lane at once.  Visiting each hit as it is found would run
+        // the element once per hitting lane (hits fall at different
+        // positions for different lanes), i.e. one lane at a time.  Both
+        // loops below are warp-uniform (nscan and nrb are the same for the
+        // whole warp); a lane's hits keep their scan order, so the sums are
+        // the same as with in-place visits.
+        bool drop = !live;
+        int nh = 0;
+        int* hl = hitl + threadIdx.x * kHitCap;
+        const int rankI = rank_k + D;
+        const bool two = a2 >= 0;
+        const uint32_t c1x4 = live ? (uint32_t)(a1 + sa1 * p.norb) * 0x01010101u : 0u;
+        const uint32_t c2x4 = live && two ? (uint32_t)(a2 + sa2 * p.norb) * 0x01010101u : 0u;
         if (live) {
           sc.ncand++;
           or_word<2 * W>(u, sa1 * W + (a1 >> 6), 1ull << (a1 & 63));
           if (a2 >= 0) or_word<2 * W>(u, sa2 * W + (a2 >> 6), 1ull << (a2 & 63));
-          const int rankI = rank_k + D;
-          bool drop = false;
-          const bool two = a2 >= 0;
-          const uint32_t c1x4 = (uint32_t)(a1 + sa1 * p.norb) * 0x01010101u;
-          const uint32_t c2x4 = two ? (uint32_t)(a2 + sa2 * p.norb) * 0x01010101u : 0u;
-          // one S determinant of L_R against I: owner test, already-in-S
-          // test, <I|H|j> accumulation; returns true when I is dropped
-          auto visit = [&](int i, int x) -> bool {
-            const int j = lr_entry_j(ent_at(i));
-            if (j < k) return p.ygen[j] != 0;
-            uint64_t vv[2 * W];
+        }
+        // phase A on one entry: j < k is the owner test (a generator below k
+        // within two excitations owns I), x == 0 means I is in S
+        auto hit = [&](int i, int x) {
+          const int j = lr_entry_j(ent_at(i));
+          if (j < k) {
+            if (p.ygen[j]) drop = true;
+            return;
+          }
+          if (x == 0) {
+            drop = true;
+            return;
+          }
+          hl[nh++] = i;
+        };
+        // phase B: <I|H|j> of the listed hits, lanes in step
+        auto flush = [&]() {
+          const int maxh = __reduce_max_sync(0xffffffffu, drop ? 0 : nh);
+          for (int t = 0; t < maxh; ++t) {
+            if (!drop && t < nh) {
+              const int j = lr_entry_j(ent_at(hl[t]));
+              uint64_t vv[2 * W];
 #pragma unroll
-            for (int q = 0; q < 2 * W; ++q) vv[q] = __ldg(&p.S[(size_t)j * 2 * W + q]);
-            if (x == 0) return true;
-            int rankJ = 0;
+              for (int q = 0; q < 2 * W; ++q) vv[q] = __ldg(&p.S[(size_t)j * 2 * W + q]);
+              int rankJ = 0;
 #pragma unroll
-            for (int q = 0; q < 2 * W; ++q) rankJ += __popcll(hf[q] & ~vv[q]);
-            int kind;
-            const double h = hmat<W>(p, u, vv, rankI, rankJ, hf, kind);
-            if (kind == 1) sc.np1++; else sc.np2++;
-            ++nint;
-            if (h != 0.0) ++nnz;
-            if (j > k && j <= k + nespk) ++lesp;
+              for (int q = 0; q < 2 * W; ++q) rankJ += __popcll(hf[q] & ~vv[q]);
+              int kind;
+              const double h = hmat<W>(p, u, vv, rankI, rankJ, hf, kind);
+              if (kind == 1) sc.np1++; else sc.np2++;
+              ++nint;
+              if (h != 0.0) ++nnz;
+              if (j > k && j <= k + nespk) ++lesp;
 #pragma unroll
-            for (int m = 0; m < R; ++m)
-              if (m < p.metat) bc[m] += h * __ldg(&p.c[(size_t)j * p.metat + m]);
-            return false;
-          };
-          for (int i0 = 0; i0 < nscan && !drop; i0 += 4) {
+              for (int m = 0; m < R; ++m)
+                if (m < p.metat) bc[m] += h * __ldg(&p.c[(size_t)j * p.metat + m]);
+            }
+          }
+          nh = 0;
+        };
+        for (int i0 = 0; i0 < nscan; i0 += 4) {
+          if (__all_sync(0xffffffffu, drop)) break;
+          if (__any_sync(0xffffffffu, !drop && nh > kHitCap - 4)) flush();
+          if (!drop) {
             // four independent compares per step (latency of the loads
             // overlaps); the hits are walked as a bit mask and each one's
-            // difference picked by selects, so nothing here is indexed at run
-            // time (a run-time index into a local array puts it on the stack)
+            // difference picked by selects, so nothing here is indexed at
+            // run time (a run-time index into a local array puts it on the
+            // stack)
             const int x0 = lr_diff(ent_at(i0), c1x4, c2x4, two);
             const int x1 = i0 + 1 < nscan ? lr_diff(ent_at(i0 + 1), c1x4, c2x4, two) : 99;
             const int x2 = i0 + 2 < nscan ? lr_diff(ent_at(i0 + 2), c1x4, c2x4, two) : 99;
@@ -1450,15 +1485,21 @@ __global__ void __launch_bounds__(kThreads, 2) k_pt2(Params p0, BatchArgs ba) {
             while (hits && !drop) {
               const int g4 = __ffs(hits) - 1;
               hits &= hits - 1u;
-              const int x = g4 == 0 ? x0 : g4 == 1 ? x1 : g4 == 2 ? x2 : x3;
-              drop = visit(i0 + g4, x);
+              hit(i0 + g4, g4 == 0 ? x0 : g4 == 1 ? x1 : g4 == 2 ? x2 : x3);
             }
           }
-          for (int q2 = 0; q2 < nrb && !drop; ++q2) {
+        }
+        for (int q2 = 0; q2 < nrb; ++q2) {
+          if (__all_sync(0xffffffffu, drop)) break;
+          if (__any_sync(0xffffffffu, !drop && nh >= kHitCap)) flush();
+          if (!drop) {
             const int i = rb[q2];
             const int x = lr_diff(ent_at(i), c1x4, c2x4, two);
-            if (x <= 4) drop = visit(i, x);
+            if (x <= 4) hit(i, x);
           }
+        }
+        flush();
+        if (live) {
           sc.ncmp += (unsigned long long)(nscan + nrb);
           if (drop || nint == 0) live = false;
           if (live && D == 2 && nnz == 0) live = false;  // diexcit drops zero couplings

@@ -373,6 +373,16 @@ static long long ietat;
    sum over perturbers of |term| * (2*kb + kd), kb = 16u*sum|H c|/|b|,
    kd = 16u*(|E0| + sum of |diagonal terms|)/|denominator| */
 static double cond_mp[64], cond_vp[64], cond_b[64];
+/* instrumentation (not in cip): the same E2 terms summed with an error-free
+   two-sum (value + accumulated rounding errors), to separate the serial
+   sum's own rounding from differences of the terms */
+static double ks_mp[64], kc_mp[64], ks_vp[64], kc_vp[64], ks_b[64], kc_b[64];
+static void comp_add(double* sum, double* err, double t) {
+  const double a = *sum + t;
+  const double bp = a - *sum;
+  *err += (*sum - (a - bp)) + (t - bp);
+  *sum = a;
+}
 #define U16 (16.0 * 1.1102230246251565e-16)
 static double* fmpb;
 /* /hist/ */
@@ -819,6 +829,7 @@ static void pert1(int kkmod, int nf) {
       eimp = bcalc * cimp;
       semp[m] = eimp;
       e2mp[m] = e2mp[m] + eimp;
+      comp_add(&ks_mp[m], &kc_mp[m], eimp);
       double xim = fabs(cimp);
       if (ysele) xim = fabs(eimp);
       double deno = dmp[m], eim = eimp;
@@ -830,6 +841,7 @@ static void pert1(int kkmod, int nf) {
         eivp = bcalc * civp;
         sevp[m] = eivp;
         e2vp[m] = e2vp[m] + eivp;
+        comp_add(&ks_vp[m], &kc_vp[m], eivp);
         xim = fabs(civp);
         if (ysele) xim = fabs(eivp);
         deno = dvp[m];
@@ -838,6 +850,7 @@ static void pert1(int kkmod, int nf) {
         double cib = bcalc / (db[m]);
         eib = bcalc * cib;
         e2b[m] = e2b[m] + eib;
+        comp_add(&ks_b[m], &kc_b[m], eib);
       }
       if (!(fabs(deno) > 0.05) && !(fabs(eim) < 1.0e-6)) {
         if (ywdeg) ydeg = 1;
@@ -855,10 +868,13 @@ static void pert1(int kkmod, int nf) {
       venvp[m] = eivp * (fmul + 1.0); /* cipsym/pert1.f:244 */
       if (ybis) {
         e2mp[m] = e2mp[m] + eimp * fmul;
+        comp_add(&ks_mp[m], &kc_mp[m], eimp * fmul);
         psimp[m] = psimp[m] + car * fmul;
         if (yen) {
           e2vp[m] = e2vp[m] + eivp * fmul;
+          comp_add(&ks_vp[m], &kc_vp[m], eivp * fmul);
           e2b[m] = e2b[m] + eib * fmul;
+          comp_add(&ks_b[m], &kc_b[m], eib * fmul);
           psivp[m] = psivp[m] + carvp * fmul;
         }
       }
@@ -1423,6 +1439,7 @@ static void diexcit_one(int ii, int jj, int kk, int ll, int nspin, int yijkl, do
           double eimp = bcalc * cimp;
           semp[m] = eimp;
           e2mp[m] = e2mp[m] + eimp;
+          comp_add(&ks_mp[m], &kc_mp[m], eimp);
           double xim = fabs(cimp);
           if (ysele) xim = fabs(eimp);
           double deno = dmpm, eim = eimp;
@@ -1435,6 +1452,7 @@ static void diexcit_one(int ii, int jj, int kk, int ll, int nspin, int yijkl, do
             eivp = bcalc * civp;
             sevp[m] = eivp;
             e2vp[m] = e2vp[m] + eivp;
+            comp_add(&ks_vp[m], &kc_vp[m], eivp);
             xim = fabs(civp);
             if (ysele) xim = fabs(eivp);
             deno = dvpm;
@@ -1443,6 +1461,7 @@ static void diexcit_one(int ii, int jj, int kk, int ll, int nspin, int yijkl, do
             double cib = bcalc / dbm;
             eib = bcalc * cib;
             e2b[m] = e2b[m] + eib;
+            comp_add(&ks_b[m], &kc_b[m], eib);
           }
           if (!(fabs(deno) > 0.05) && !(fabs(eim) < 1.0e-6)) {
             if (ywdeg) ydeg = 1;
@@ -1458,10 +1477,13 @@ static void diexcit_one(int ii, int jj, int kk, int ll, int nspin, int yijkl, do
           venvp[m] = eivp * (fmul + 1.0); /* cipsym/diexcit.f:446 */
           if (ybis) {
             e2mp[m] = e2mp[m] + eimp * fmul;
+            comp_add(&ks_mp[m], &kc_mp[m], eimp * fmul);
             psimp[m] = psimp[m] + car * fmul;
             if (yen) {
               e2vp[m] = e2vp[m] + eivp * fmul;
+              comp_add(&ks_vp[m], &kc_vp[m], eivp * fmul);
               e2b[m] = e2b[m] + eib * fmul;
+              comp_add(&ks_b[m], &kc_b[m], eib * fmul);
               psivp[m] = psivp[m] + carvp * fmul;
             }
           }
@@ -2752,9 +2774,16 @@ int main(int argc, char** argv) {
     fprintf(fj, "  \"ietat\": %lld, \"n_processed\": %lld, \"ntot60\": %lld,\n", ietat, n_processed,
             det_ntot);
     fprintf(fj, "  \"dpivot\": %.17g,\n", dpivot);
-    const char* nm[8] = {"e2mp", "e2vp", "e2b", "psimp", "psivp", "cond_e2mp", "cond_e2vp", "cond_e2b"};
-    double* ar[8] = {e2mp, e2vp, e2b, psimp, psivp, cond_mp, cond_vp, cond_b};
-    for (int q = 0; q < 8; q++) {
+    double cm[64], cv[64], cb[64];
+    for (int m = 1; m <= metat; m++) {
+      cm[m] = ks_mp[m] + kc_mp[m];
+      cv[m] = ks_vp[m] + kc_vp[m];
+      cb[m] = ks_b[m] + kc_b[m];
+    }
+    const char* nm[11] = {"e2mp", "e2vp", "e2b", "psimp", "psivp", "cond_e2mp", "cond_e2vp", "cond_e2b",
+                          "comp_e2mp", "comp_e2vp", "comp_e2b"};
+    double* ar[11] = {e2mp, e2vp, e2b, psimp, psivp, cond_mp, cond_vp, cond_b, cm, cv, cb};
+    for (int q = 0; q < 11; q++) {
       fprintf(fj, "  \"%s\": [", nm[q]);
       for (int m = 1; m <= metat; m++) fprintf(fj, "%s%.17g", m > 1 ? ", " : "", ar[q][m]);
       fprintf(fj, "],\n");

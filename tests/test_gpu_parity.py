@@ -3,7 +3,9 @@ on the same input files.
 
 Bit-exact: the processed perturber set (counts, ietat), the histogram counts,
 the set of determinants written to unit 60.  Floating point: E2 within
-1e-10 Eh on well-conditioned inputs; on inputs whose EN/MP denominators come
+1e-10 Eh of the oracle's terms (summed with an error-free two-sum; the
+oracle's serial sum, like the reference's, carries its own rounding) on
+well-conditioned inputs; on inputs whose EN/MP denominators come
 close to zero the tolerance adds the oracle's first-order rounding bound
 (cond_e2*), since there a 1-ulp change of a diagonal energy moves E2 by far
 more than 1e-10.  Selection values xam agree to 1e-9 relative, and cipsym's
@@ -65,9 +67,15 @@ def check(jo, jg, wo, wg, variant, strict=False):
         assert jo[k] == jg[k], k
     assert jo["dpivot"] == pytest.approx(jg["dpivot"], rel=1e-12, abs=1e-15)
     for k in ("e2mp", "e2vp", "e2b"):
-        a, b = np.array(jo[k]), np.array(jg[k])
+        # the oracle sums its terms serially, as the reference does; over
+        # millions of terms that sum's own rounding reaches ~1e-10 Eh when
+        # E2 is hundreds of Eh, so the GPU is held to 1e-10 Eh against the
+        # oracle's terms summed with an error-free two-sum (comp_), and to
+        # 1e-10 Eh plus that serial rounding against the serial sum
+        a, b, c = np.array(jo[k]), np.array(jg[k]), np.array(jo["comp_" + k])
         tol = 1e-10 + (0.0 if strict else np.array(jo["cond_" + k]))
-        assert np.all(np.abs(a - b) <= tol), (k, a, b, np.abs(a - b), tol)
+        assert np.all(np.abs(c - b) <= tol), (k, c, b, np.abs(c - b), tol)
+        assert np.all(np.abs(a - b) <= tol + np.abs(a - c)), (k, a, b, np.abs(a - b), tol)
     mt = jo["metat"]
     so = read60(os.path.join(wo, "det"), mt, variant == "cipsym")
     sg = read60(os.path.join(wg, "det"), mt, variant == "cipsym")
@@ -200,7 +208,8 @@ def _log(name, jo, jg):
     rec = {"case": name, "n_processed": jg["n_processed"]}
     for k in ("e2mp", "e2vp", "e2b"):
         rec[k] = jg[k]
-        rec["max_abs_diff_" + k] = float(np.max(np.abs(np.array(jo[k]) - np.array(jg[k]))))
+        rec["max_abs_diff_" + k] = float(np.max(np.abs(np.array(jo["comp_" + k]) - np.array(jg[k]))))
+        rec["oracle_serial_rounding_" + k] = float(np.max(np.abs(np.array(jo[k]) - np.array(jo["comp_" + k]))))
         rec["cond_" + k] = jo["cond_" + k]
     with open(path, "a") as fh:
         fh.write(json.dumps(rec) + "\n")
