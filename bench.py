@@ -315,6 +315,94 @@ def run_batched(args, rank: int, world: int, local_rank: int):
         print(json.dumps(line), flush=True)
 
 
+# ------------------------------------------------------------ moy form
+MOY_WORKLOAD = ("moy over S: 60 MOs, 20 e-, Ms=0, {n} determinants (ref + singles/doubles/triples, "
+                "spin-flip closed), the list of the run that only writes S (Autocip's moy input)")
+
+
+def _moy_workdir(base: str, ndet: int, seed: int) -> str:
+    """Synthetic inputs of the moy form: the medium system's integrals and a
+    list of `ndet` determinants; unit 4 and unit 60 from the run that only
+    writes S (ityper = -1, host only), as Autocip feeds moy."""
+    import dataclasses
+    synth = _synth()
+    cfg = dataclasses.replace(synth.CONFIGS["medium"], name="moy", ncf=ndet, metat=2, seed=seed,
+                              energy="diagonal")
+    wd = os.path.join(base, f"moy_{ndet}_{seed}")
+    synth.generate(cfg, wd)
+    txt = open(os.path.join(wd, "cip.in")).read().replace(f"ityper={cfg.ityper}", "ityper=-1")
+    open(os.path.join(wd, "cip.in"), "w").write(txt)
+    with open(os.path.join(wd, "moy.in"), "w") as fh:
+        fh.write(" &moyfil\n &end\n &moyen\n  tau=0d0, title='moy'\n &end\n")
+    return wd
+
+
+def run_moy_form(args, rank: int, world: int, local_rank: int):
+    """The moy drop-in (cipsi_moy_main): the Hamiltonian over a list of
+    --moy-dets determinants.  value: pair tests per second of the two GPU
+    passes (count + fill, device time of the library's events); e2e: the
+    whole drop-in (read the files, build the list, the GPU passes, write
+    units 1, 61, 64); cpu_baseline: the oracle's restatement of moy on a
+    smaller list of the same recipe, extrapolated by the number of pair
+    tests (they grow as n^2)."""
+    import torch
+    import cipsi_gb300 as cg
+    from cipsi_gb300 import build
+    torch.cuda.set_device(local_rank)
+    build.build()
+    base = tempfile.mkdtemp(prefix=f"cipsi_moy_r{rank}_")
+    t0 = time.perf_counter()
+    wd = _moy_workdir(base, args.moy_dets, 7 + rank)
+    cg.run_cip(wd)  # ityper = -1: S ordered and written back, unit 4 (host only)
+    t_gen = time.perf_counter() - t0
+    for _ in range(args.warmup):
+        j = cg.run_moy(wd)
+    n = j["ncf"]
+    tests = n * (n - 1) // 2
+    clocks = Clocks(local_rank)
+    clocks.start()
+    dev_ms, wall = [], []
+    for _ in range(args.steps):
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        j = cg.run_moy(wd)
+        wall.append(time.perf_counter() - t1)
+        dev_ms.append(j["hbuild_ms"])
+    clk = clocks.stop()
+    line = {"metric": "moy pair tests/s", "value": tests / (statistics.mean(dev_ms) / 1e3), "unit": "pair tests/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": statistics.mean(dev_ms),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded integrals and determinant list)",
+            "config": {"workload": MOY_WORKLOAD.format(n=n), "determinants": n,
+                       "l2": "the list (<= 3.2 MB) stays L2-resident by design; inputs re-read from files each step"},
+            "e2e": {"value": tests / statistics.mean(wall), "unit": "pair tests/s", "ms_per_step":
+                    1e3 * statistics.mean(wall), "h2d_bytes_per_step": int(n * 32),
+                    "d2h_bytes_per_step": int(j["pairs"] * 12 + 4 * n)},
+            "gpu_launches": 2 * args.steps,
+            "work": {"pairs_within_two": j["pairs"], "unit1_elements": j["nhij"], "unit1_records": j["unit1_records"],
+                     "generation_s": t_gen},
+            "clocks": clk}
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        import subprocess
+        from oracle import build as ob
+        exe = ob.build()
+        ws = _moy_workdir(base, args.moy_cpu_dets, 7)
+        cg.run_cip(ws)
+        with open(os.path.join(ws, "moy.in")) as fin:
+            subprocess.run([exe, "--moy", "--json", "moy_ref.json"], cwd=ws, stdin=fin, stdout=subprocess.DEVNULL,
+                           check=True)
+        jr = json.load(open(os.path.join(ws, "moy_ref.json")))
+        ns = jr["ncf"]
+        line["cpu_baseline"] = {"value": ns * (ns - 1) // 2 / jr["hloop_s"], "unit": "pair tests/s", "cores": 1,
+                                "kind": "port",
+                                "sample": f"the oracle's moy over {ns} determinants of the same recipe, its own "
+                                          f"clock around the matrix loop ({jr['hloop_s']:.1f} s, unit 1 written); "
+                                          "rate extrapolated to the full list (pair tests grow as n^2)"}
+    shutil.rmtree(base, ignore_errors=True)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 # ------------------------------------------------------------ adjoint form
 def run_adjoint_form(args, rank: int, world: int, local_rank: int):
     """The medium system plus a seeded symmetric dipole matrix mu ~ N(0, 0.5):
@@ -609,9 +697,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--form", choices=["plain", "batched", "adjoint"], default="plain",
+    ap.add_argument("--form", choices=["plain", "batched", "adjoint", "moy"], default="plain",
                     help="batched: the potential-curve batch (geometries/s, batched vs plain); "
-                         "adjoint: dE2/d integrals on the medium system with checks")
+                         "adjoint: dE2/d integrals on the medium system with checks; "
+                         "moy: the Hamiltonian over a determinant list (the moy drop-in)")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="large")
     ap.add_argument("--chunk-records", type=int, default=0,
                     help="records per streamed chunk (0 = sized from free device memory)")
@@ -620,6 +709,8 @@ def main():
     ap.add_argument("--geometries", type=int, default=256)
     ap.add_argument("--batch-steps", type=int, default=2)
     ap.add_argument("--batch-warmup", type=int, default=1)
+    ap.add_argument("--moy-dets", type=int, default=100000, help="moy form: determinants in the list")
+    ap.add_argument("--moy-cpu-dets", type=int, default=20000, help="moy form: list size of the CPU sample")
     ap.add_argument("--gen-every", type=int, default=1,
                     help="profiling aid: run only every n-th determinant of S as a generator")
     args = ap.parse_args()
@@ -636,6 +727,9 @@ def main():
         return
     if args.form == "adjoint":
         run_adjoint_form(args, rank, world, local_rank)
+        return
+    if args.form == "moy":
+        run_moy_form(args, rank, world, local_rank)
         return
     run_gpu(args, rank, world, local_rank)
 

@@ -2,7 +2,9 @@
 
 Python mirror of the reference's process-level interface: `run_cip` does what
 running cip.exe (variant="cip") or cipsym.exe (variant="cipsym") in a
-calculation directory does, with the perturbation loop on the GPU.  The
+calculation directory does, with the perturbation loop on the GPU; `run_moy`
+does what moy.exe does (the Hamiltonian over S + the selected perturbers),
+with the pair scan and matrix elements on the GPU.  The
 compiled library is built in-tree by `cipsi_gb300.build.build()`; when it is
 missing every entry point raises instead of falling back to a CPU path.
 """
@@ -18,6 +20,7 @@ import numpy as np
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "_build", "libcipsi_gb300.so")
 EXE_PATH = os.path.join(_HERE, "_build", "cip_gpu")
+MOY_EXE_PATH = os.path.join(_HERE, "_build", "moy_gpu")
 
 _lib = None
 
@@ -30,6 +33,7 @@ EXPORTED = [
     "cipsi_set_tuning", "cipsi_batch_create", "cipsi_batch_run", "cipsi_batch_wait",
     "cipsi_batch_last_error", "cipsi_batch_destroy", "cipsi_inputs_array", "cipsi_set_integrals_f64store",
     "cipsi_run_pt2_adjoint", "cipsi_set_selection_sink", "cipsi_run_pt2_stream", "cipsi_record_digest",
+    "cipsi_hamiltonian_build", "cipsi_hamiltonian_get", "cipsi_hamiltonian_ms", "cipsi_moy_main",
 ]
 
 
@@ -48,6 +52,9 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
     lib.cipsi_cip_main.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int32, ctypes.c_char_p,
                                    ctypes.c_void_p, ctypes.c_int32, ctypes.c_char_p, ctypes.c_int32]
     lib.cipsi_cip_main.restype = ctypes.c_int
+    lib.cipsi_moy_main.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int32,
+                                   ctypes.c_char_p, ctypes.c_int32]
+    lib.cipsi_moy_main.restype = ctypes.c_int
     _lib = lib
     return lib
 
@@ -68,6 +75,23 @@ def run_cip(workdir: str, variant: str = "cipsym", json_path: Optional[str] = No
     rc = lib.cipsi_cip_main(workdir.encode(), (stdin_path or os.path.join(workdir, "cip.in")).encode(),
                             1 if variant == "cipsym" else 0, json_path.encode(), mask_ptr, device,
                             err, len(err))
+    if rc != 0:
+        raise CipsiError(err.value.decode(errors="replace"))
+    with open(json_path) as fh:
+        return json.load(fh)
+
+
+def run_moy(workdir: str, json_path: Optional[str] = None, device: int = 0,
+            stdin_path: Optional[str] = None) -> dict:
+    """Run the moy drop-in in `workdir` (namelists &moyfil/&moyen from
+    `stdin_path`, default workdir/moy.in).  Returns the JSON summary (list
+    size, element counts, morue's second-order sums, device time)."""
+    lib = load_library()
+    if json_path is None:
+        json_path = os.path.join(workdir, "moy_gpu.json")
+    err = ctypes.create_string_buffer(2048)
+    rc = lib.cipsi_moy_main(workdir.encode(), (stdin_path or os.path.join(workdir, "moy.in")).encode(),
+                            json_path.encode(), device, err, len(err))
     if rc != 0:
         raise CipsiError(err.value.decode(errors="replace"))
     with open(json_path) as fh:

@@ -288,6 +288,18 @@ struct cipsi_ctx {
   double *sink_xam = nullptr, *sink_evp = nullptr;
   long long sink_cap = 0;
   void* sink_host[4] = {nullptr, nullptr, nullptr, nullptr};  // the caller's addresses
+  // the Hamiltonian over the space (cipsi_hamiltonian_build): phases of the
+  // determinants, the caller's Fock matrix when given, pairs by rows
+  int8_t* dsigma = nullptr;
+  double* dFraw = nullptr;
+  int32_t* dh_count = nullptr;
+  long long* dh_rowptr = nullptr;
+  int32_t* dh_col = nullptr;
+  double* dh_val = nullptr;
+  long long h_cap = 0;
+  std::vector<long long> h_rowptr;
+  bool have_h = false;
+  float h_ms = 0.f;
 };
 
 namespace {
@@ -393,6 +405,8 @@ void cipsi_ctx_destroy(cipsi_ctx* ctx) {
   dfree(ctx->dst_bits); dfree(ctx->dst_xam); dfree(ctx->dst_evp); dfree(ctx->dst_mask);
   dfree(ctx->dpool_bits); dfree(ctx->dpool_xam); dfree(ctx->dpool_evp); dfree(ctx->dpool_count);
   dfree(ctx->dunit_pool); dfree(ctx->dunit_nsel); dfree(ctx->dunit_out); dfree(ctx->dscan_total);
+  dfree(ctx->dsigma); dfree(ctx->dFraw); dfree(ctx->dh_count); dfree(ctx->dh_rowptr);
+  dfree(ctx->dh_col); dfree(ctx->dh_val);
   for (int i = 0; i < 2; ++i) {
     dfree(ctx->dout_bits[i]); dfree(ctx->dout_owner[i]); dfree(ctx->dout_xam[i]); dfree(ctx->dout_evp[i]);
     if (ctx->hbuf[i]) cudaFreeHost(ctx->hbuf[i]);
@@ -2479,5 +2493,114 @@ int cipsi_run_pt2_static(cipsi_ctx* ctx, const cipsi_opts* o, cipsi_result* r) {
   r->n_selected = (int64_t)cnt[C_NSEL];
   return CIPSI_OK;
 }
+
+}  // extern "C"
+
+// ================================================ Hamiltonian over the space
+// cipsi_hamiltonian_build / cipsi_hamiltonian_get: the lower triangle of H
+// over the determinants given to cipsi_set_space, by rows, as moy writes it
+// to its unit 1 (moy/moy.f:117-199) -- row i: the columns j < min(i, jmax)
+// within two excitations, in increasing j, with <i|H|j> in the phase of the
+// excitation lists.  The elements moy drops (|h| < 1e-10) are kept here;
+// the caller filters them when it writes the file.
+extern "C" {
+
+int cipsi_hamiltonian_build(cipsi_ctx* ctx, const double* fock, int32_t jmax, int64_t* npairs) {
+  if (!ctx || !npairs) return CIPSI_ERR_ARG;
+  if (!ctx->have_int || !ctx->have_space)
+    return fail(ctx, CIPSI_ERR_STATE, "hamiltonian_build needs set_integrals and set_space");
+  if (ctx->pending) return fail(ctx, CIPSI_ERR_STATE, "a run is pending: fetch its result first");
+  CK(cudaSetDevice(ctx->device));
+  const int n = ctx->d.ncf, W = ctx->W, norb = ctx->d.norb;
+  *npairs = 0;
+  ctx->have_h = false;
+  int rc;
+  {
+    std::vector<int8_t> sg(n);
+    for (int k = 0; k < n; ++k) sg[k] = ctx->sigma[k] < 0 ? -1 : 1;
+    if ((rc = upload(ctx, &ctx->dsigma, sg.data(), sg.size()))) return rc;
+  }
+  const double* dF = ctx->dF;
+  if (fock) {
+    if ((rc = upload(ctx, &ctx->dFraw, fock, (size_t)norb * (norb + 1) / 2))) return rc;
+    dF = ctx->dFraw;
+  }
+  dfree(ctx->dh_count);
+  ++ctx->buf_gen;
+  CK(cudaMalloc((void**)&ctx->dh_count, (size_t)n * sizeof(int32_t)));
+  HBuildArgs a{};
+  a.p.norb = norb;
+  a.p.noca = ctx->d.noca;
+  a.p.nsym = ctx->d.nsym;
+  a.p.eri = ctx->deri;
+  a.p.eri64 = ctx->deri64 ? ctx->deri64 : ctx->deri_w;
+  a.p.pairtab = ctx->dpairtab;
+  a.p.ntttt = ctx->dntttt;
+  a.p.F = dF;
+  a.S = ctx->dS;
+  a.sigma = ctx->dsigma;
+  a.n = n;
+  a.jmax = jmax < 0 ? n : std::min(jmax, n);
+  for (int q = 0; q < 4; ++q) a.hf[q] = 0ull;
+  for (int o = 0; o < ctx->d.noca; ++o) {
+    a.hf[o >> 6] |= 1ull << (o & 63);
+    a.hf[W + (o >> 6)] |= 1ull << (o & 63);
+  }
+  a.count = ctx->dh_count;
+  CK(cudaEventRecord(ctx->ev0, ctx->stream));
+  cudaError_t e = W == 1 ? launch_hpairs<1>(a, false, ctx->stream) : launch_hpairs<2>(a, false, ctx->stream);
+  if (e != cudaSuccess) return fail(ctx, CIPSI_ERR_CUDA, std::string("k_hpairs (count): ") + cudaGetErrorString(e));
+  std::vector<int32_t> cnt(n);
+  CK(cudaMemcpyAsync(cnt.data(), ctx->dh_count, (size_t)n * sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  ctx->h_rowptr.assign((size_t)n + 1, 0);
+  for (int i = 0; i < n; ++i) ctx->h_rowptr[i + 1] = ctx->h_rowptr[i] + cnt[i];
+  const long long total = ctx->h_rowptr[n];
+  if ((rc = upload(ctx, &ctx->dh_rowptr, ctx->h_rowptr.data(), ctx->h_rowptr.size()))) return rc;
+  if (total > ctx->h_cap || !ctx->dh_col) {
+    dfree(ctx->dh_col);
+    dfree(ctx->dh_val);
+    ++ctx->buf_gen;
+    CK(cudaMalloc((void**)&ctx->dh_col, (size_t)std::max(total, 1ll) * sizeof(int32_t)));
+    CK(cudaMalloc((void**)&ctx->dh_val, (size_t)std::max(total, 1ll) * sizeof(double)));
+    ctx->h_cap = std::max(total, 1ll);
+  }
+  a.rowptr = ctx->dh_rowptr;
+  a.col = ctx->dh_col;
+  a.val = ctx->dh_val;
+  e = W == 1 ? launch_hpairs<1>(a, true, ctx->stream) : launch_hpairs<2>(a, true, ctx->stream);
+  if (e != cudaSuccess) return fail(ctx, CIPSI_ERR_CUDA, std::string("k_hpairs (fill): ") + cudaGetErrorString(e));
+  CK(cudaEventRecord(ctx->ev1, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  CK(cudaEventElapsedTime(&ctx->h_ms, ctx->ev0, ctx->ev1));
+  ctx->have_h = true;
+  *npairs = total;
+  return CIPSI_OK;
+}
+
+int cipsi_hamiltonian_get(cipsi_ctx* ctx, int32_t row0, int32_t nrows, int64_t* rowptr, int32_t* col,
+                          double* val) {
+  if (!ctx) return CIPSI_ERR_ARG;
+  if (!ctx->have_h) return fail(ctx, CIPSI_ERR_STATE, "hamiltonian_get before hamiltonian_build");
+  const int n = ctx->d.ncf;
+  if (row0 < 0 || nrows < 0 || row0 + (long long)nrows > n)
+    return fail(ctx, CIPSI_ERR_ARG, "hamiltonian_get: rows out of range");
+  const long long a = ctx->h_rowptr[row0], b = ctx->h_rowptr[row0 + nrows];
+  if (rowptr)
+    for (int r = 0; r <= nrows; ++r) rowptr[r] = ctx->h_rowptr[row0 + r] - a;
+  CK(cudaSetDevice(ctx->device));
+  if (b > a && (col || val)) {
+    if (col)
+      CK(cudaMemcpyAsync(col, ctx->dh_col + a, (size_t)(b - a) * sizeof(int32_t), cudaMemcpyDeviceToHost,
+                         ctx->stream));
+    if (val)
+      CK(cudaMemcpyAsync(val, ctx->dh_val + a, (size_t)(b - a) * sizeof(double), cudaMemcpyDeviceToHost,
+                         ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+  }
+  return CIPSI_OK;
+}
+
+float cipsi_hamiltonian_ms(const cipsi_ctx* ctx) { return ctx ? ctx->h_ms : 0.f; }
 
 }  // extern "C"

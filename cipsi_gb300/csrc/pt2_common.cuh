@@ -162,4 +162,23 @@ __host__ __device__ inline long long block_candidates(int nR, bool same_spin, in
 template <int W, int R, bool B, bool ADJ = false>
 cudaError_t launch_pt2(const Params& p, const BatchArgs& ba, int grid, size_t smem, cudaStream_t st);
 
+// The Hamiltonian over a determinant list by rows (hbuild.cu): pass 1
+// counts, per row i, the columns j < min(i, jmax) within two excitations;
+// pass 2 writes them, in increasing j, from rowptr[i] on.
+struct HBuildArgs {
+  Params p;                 // integrals (pairtab, ntttt, eri / eri64, F) and norb
+  const uint64_t* S;        // n x 2W words
+  const int8_t* sigma;      // n: phase of each determinant's excitation list
+  int n;                    // determinants (rows)
+  int jmax;                 // columns j < min(i, jmax)
+  uint64_t hf[4];           // the reference determinant (2W words)
+  int32_t* count;           // pass 1 output: columns per row
+  const long long* rowptr;  // pass 2 input: first pair of each row
+  int32_t* col;             // pass 2 outputs
+  double* val;
+};
+
+template <int W>
+cudaError_t launch_hpairs(const HBuildArgs& a, bool fill, cudaStream_t st);
+
 }  // namespace cipsi_dev

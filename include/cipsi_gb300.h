@@ -365,6 +365,44 @@ void cipsi_batch_destroy(cipsi_batch* b);
    corrupt each other's results, so callers must serialise them. */
 int cipsi_run_pt2_static(cipsi_ctx* ctx, const cipsi_opts* opts, cipsi_result* res);
 
+/* The Hamiltonian over the determinants given to cipsi_set_space, lower
+   triangle by rows, as moy builds it over S + the selected perturbers
+   (CIPSI_sources/moy/moy.f:117-199, the double loop over i and j < i with
+   its degree test and hntd).  Row i holds every column j < min(i, jmax)
+   (jmax < 0: no limit; moy's y_secd sets jmax = |S|) within two
+   excitations of i, in increasing j, with <i|H|j> in the phase of the
+   reference's excitation lists (the value hntd returns; 0 for identical
+   determinants).  moy drops the elements with |h| < 1e-10 when it writes
+   unit 1: they are kept here, the caller filters.  The diagonal is not
+   included (moy/hdig.f, on the host).  `fock` (optional, packed like f) is
+   the Fock matrix the one-difference elements use; moy reads it from unit
+   40 as it stands (moy/ijkf.f), while cipsi_set_integrals zeroes
+   |F| < 1e-10 as cip/ijkf.f does.  Needs cipsi_set_integrals* and
+   cipsi_set_space; blocks until done; *npairs = pairs over all rows.
+   The pairs stay on the device until the next build or ctx_destroy. */
+int cipsi_hamiltonian_build(cipsi_ctx* ctx, const double* fock, int32_t jmax, int64_t* npairs);
+/* Rows row0 .. row0+nrows-1 of the last build: rowptr[nrows+1] (offsets
+   into col/val, from 0), col (0-based j) and val; any output may be NULL
+   (rowptr alone costs no device copy). */
+int cipsi_hamiltonian_get(cipsi_ctx* ctx, int32_t row0, int32_t nrows, int64_t* rowptr, int32_t* col,
+                          double* val);
+/* Device time of the last build's two kernels, in ms. */
+float cipsi_hamiltonian_ms(const cipsi_ctx* ctx);
+
+/* Process-level drop-in for moy.exe (CIPSI_sources/moy/moy.f): reads the
+   &moyfil/&moyen namelists from `stdin_path` and, in `workdir`, units 4
+   (first record), 40 and 60; builds the determinant list as moy/deter.f
+   does (unit-60 records with vs >= tau, by excitation degree, each followed
+   by its spin-flip partner, repeats dropped); writes units 64 and 61 (the
+   lists), unit 1 (H by rows, |h| >= 1e-10, in 8192-element records), unit
+   63 (MP diagonal, ystkmp) and, as moy/morue.f, the second-order energies
+   of the determinants beyond S (unit 33 records and the fourth unit-4
+   record).  The pairs come from cipsi_hamiltonian_build on `device`.
+   `json_path` (optional) receives counts and energies.  Not supported:
+   yspipro, yion, spatial degeneracy operations (ntrans > 0). */
+int cipsi_moy_main(const char* workdir, const char* stdin_path, const char* json_path, int32_t device,
+                   char* errbuf, int32_t errlen);
+
 #ifdef __cplusplus
 }
 #endif

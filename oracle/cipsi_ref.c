@@ -52,6 +52,7 @@
 #include <stdlib.h>
 #include <string.h>
 #include <time.h>
+#include <unistd.h>
 
 /* ---------------------------------------------------------------- utils */
 static void die(const char* fmt, ...) {
@@ -2118,10 +2119,597 @@ static double now_s(void) {
   return (double)ts.tv_sec + 1e-9 * (double)ts.tv_nsec;
 }
 
+/* ================================================================= moy
+ * CIPSI_sources/moy: the Hamiltonian over the determinants read from unit 60
+ * (S followed by the selected perturbers), lower triangle row by row, to
+ * unit 1 (moy.f:117-199); the determinant lists to units 64 and 61
+ * (moy.f:79-104); MP diagonal energies to unit 63 (ystkmp, moy.f:200-208);
+ * morue.f: second-order contributions of the determinants beyond the first
+ * ndims (the size of S written to unit 4) to unit 33 and a fourth unit-4
+ * record.
+ *
+ * Followed sources: moy/moy.f, moy/openf.f, moy/deter.f (ntrans = 0),
+ * moy/lec60.f, moy/transf.f, moy/pie.f, moy/ijkf.f, moy/reijkl.f,
+ * moy/hntd.f, moy/hdig.f, moy/hmp.f (the same algorithms as cip's, called
+ * here through hntd(), hdig(), hmp() on the moy list), moy/morue.f,
+ * moy/stkener.f.  Not restated: yspipro (spin-adapted lists, spipr.f and
+ * stk62.f), yion.
+ */
+#define MOY_LSIZE 8192
+#define MOY_NDIMH 10000000
+
+/* moy/lec60.f: the records of unit 60 with vs >= tau, grouped by excitation
+   degree (at most 6), the reference determinant counted once */
+static void moy_lec60(FILE* f, double tau_) {
+  rec_t r = {0};
+  rewind(f);
+  while (rec_read(f, &r)) {
+    int mw = rec_i4(&r), nw = rec_i4(&r);
+    int* idet = (int*)xcalloc((size_t)mw + 1, sizeof(int));
+    int* necst = (int*)xcalloc((size_t)nw + 1, sizeof(int));
+    double* v = (double*)xcalloc((size_t)nw + 1, sizeof(double));
+    for (int i = 1; i <= mw; i++) idet[i] = rec_i4(&r);
+    for (int i = 1; i <= nw; i++) necst[i] = rec_i4(&r);
+    for (int i = 1; i <= nw; i++) v[i] = rec_r8(&r);
+    int myy = 0;
+    for (int l = 1; l <= nw; l++) {
+      int nec = necst[l];
+      if (nec > 6) die("erreur degre d excitation %d depasse les possibilites du programme", nec);
+      if (v[l] < tau_) {
+        myy += 2 * nec;
+        continue;
+      }
+      int itab[20];
+      for (int s = 1; s <= nec; s++) {
+        itab[s - 1] = idet[++myy];
+        itab[s - 1 + nec] = idet[++myy];
+      }
+      if (nec == 0) {
+        if (isz != 0) continue;
+        kf_ref++;
+        if (kf_ref != 1) {
+          kf_ref--;
+          printf(" fondamental deja present\n");
+        }
+        continue;
+      }
+      kex_push(nec, itab);
+    }
+    free(idet);
+    free(necst);
+    free(v);
+  }
+  free(r.b);
+  rewind(f);
+}
+
+/* moy/transf.f + moy/pie.f: sort the holes and the particles, check the
+   spin orbitals, refuse a determinant of another symmetry, drop a repeat,
+   else append it (nd(ncf+1) = nd(ncf) + nec) */
+static void moy_transf(int nec) {
+  if (nec == 0) {
+    ncf++;
+    ne[ncf] = 0;
+    nd[ncf + 1] = nd[ncf];
+    if (isz != 0) ncf--;
+    isym = 1;
+    return;
+  }
+  if (nec > 1) {
+    for (int i = 1; i <= nec - 1; i++)
+      for (int j = i + 1; j <= nec; j++) {
+        if (!(tr_nt[j] > tr_nt[i])) { int n = tr_nt[j]; tr_nt[j] = tr_nt[i]; tr_nt[i] = n; }
+        if (!(tr_np[j] > tr_np[i])) { int n = tr_np[j]; tr_np[j] = tr_np[i]; tr_np[i] = n; }
+      }
+  }
+  int is = 1, ls = 0;
+  if (tr_nt[1] < igela) die("1 spin orbitale est hors de l espace de base");
+  if (tr_np[nec] > mnorb) die("1 spin orbitale est hors de l espace de base");
+  if (tr_nt[nec] > nocb) die("1 spin orbitale est hors de l espace de base");
+  if (tr_np[nec] <= noca) die("1 spin orbitale est hors de l espace de base");
+  for (int i = 1; i <= nec; i++) {
+    if (!(tr_nt[i] <= noca) && tr_nt[i] < igelb) die("1 spin orbitale est hors de l espace de base");
+    if (!(tr_np[i] > nocb)) {
+      if (tr_np[i] > norb) die("1 spin orbitale est hors de l espace de base");
+      if (tr_np[i] <= noca) die("1 spin orbitale est hors de l espace de base");
+    }
+    is = its[is][itsym[tr_nt[i]]];
+    is = its[is][itsym[tr_np[i]]];
+    ls = ls + ispin[tr_np[i]];
+    ls = ls - ispin[tr_nt[i]];
+  }
+  if (isym == 0) isym = is;
+  if (is != isym) { /* transf.f:90-95: refused, the run goes on */
+    printf(" determinant de mauvaise symetrie\n");
+    return;
+  }
+  if (ls != isz) die("mauvais spin");
+  for (int j = ncf; j >= 1; j--) {
+    if (ne[j] != nec) continue;
+    int d = nd[j], same = 1;
+    for (int k = 1; k <= nec; k++)
+      if (trou[d + k] != tr_nt[k] || part[d + k] != tr_np[k]) { same = 0; break; }
+    if (same) return;
+  }
+  ncf++;
+  if (ncf > g_ncf_cap) die("moy: list capacity exceeded");
+  ne[ncf] = nec;
+  int d = nd[ncf];
+  for (int k = 1; k <= nec; k++) {
+    trou[d + k] = tr_nt[k];
+    part[d + k] = tr_np[k];
+  }
+  nd[ncf + 1] = d + nec;
+}
+
+/* moy/stkener.f: one (char*40, real*8 x(n)) record appended to unit 33 */
+static void moy_stkener(const char* n33, const char* typener, const double* x, int n) {
+  FILE* f33 = fopen(n33, "ab");
+  if (!f33) die("cannot open unit 33 file %s", n33);
+  wbuf_t w = {0};
+  char typ[41];
+  snprintf(typ, sizeof typ, "%-40.40s", typener);
+  wb_put(&w, typ, 40);
+  for (int m = 1; m <= n; m++) wb_r8(&w, x[m]);
+  wb_flush(f33, &w);
+  free(w.b);
+  fclose(f33);
+  printf(" *************************************\n");
+  printf(" %s stockee sur la file 33", typ);
+  for (int m = 1; m <= n; m++) printf(" %24.16E", x[m]);
+  printf("\n *************************************\n");
+}
+
+static void moy_write_buffer(FILE* f1, const int* itab, const int* jtab, const double* vbuf) {
+  wbuf_t w = {0};
+  for (int k = 1; k <= MOY_LSIZE; k++) wb_i4(&w, itab[k]);
+  for (int k = 1; k <= MOY_LSIZE; k++) wb_i4(&w, jtab[k]);
+  for (int k = 1; k <= MOY_LSIZE; k++) wb_r8(&w, vbuf[k]);
+  wb_flush(f1, &w);
+  free(w.b);
+}
+
+static int moy_main(const char* json_path) {
+  rec_t r = {0};
+  /* openf.f */
+  nlgroup_t gf;
+  static const char* const moyfil_names[] = {"prefix", "det", "ijkl", "f04", "det1", "ijkl1", "f041",
+                                             "det_cl", "det_spin", "mat", "enmp", "csf", "det_cl1",
+                                             "mat1", "enmp1", "ener", "ener1", "csf1", "det_spin1", NULL};
+  nl_parse("moyfil", &gf, moyfil_names);
+  char prefix[256] = "";
+  {
+    const char* v = nl_scalar(&gf, "prefix");
+    if (v) snprintf(prefix, sizeof prefix, "%s", v);
+  }
+  char n01[512], n04[512], n33[512], n40[512], n60[512], n61[512], n63[512], n64[512];
+  unit_name(&gf, "mat", "mat1", "mat", prefix, n01, sizeof n01);
+  unit_name(&gf, "f04", "f041", "f04", prefix, n04, sizeof n04);
+  unit_name(&gf, "ener", "ener1", "ener", prefix, n33, sizeof n33);
+  unit_name(&gf, "ijkl", "ijkl1", "ijkl", prefix, n40, sizeof n40);
+  unit_name(&gf, "det", "det1", "det", prefix, n60, sizeof n60);
+  unit_name(&gf, "det_cl", "det_cl1", "det_cl", prefix, n61, sizeof n61);
+  unit_name(&gf, "enmp", "enmp1", "enmp", prefix, n63, sizeof n63);
+  unit_name(&gf, "det_spin", "det_spin1", "det_spin", prefix, n64, sizeof n64);
+
+  /* moy.f:50-58: the first record of unit 4 */
+  FILE* f4 = fopen(n04, "rb");
+  if (!f4) die("cannot open unit 4 file %s", n04);
+  if (!rec_read(f4, &r)) die("unit 4: empty");
+  norb = rec_i4(&r);
+  noca = rec_i4(&r);
+  nocb = rec_i4(&r);
+  metat = rec_i4(&r);
+  int ndet_s = rec_i4(&r);
+  isz = rec_i4(&r);
+  yion = rec_l1(&r);
+  int ii4 = rec_i4(&r), jj4 = rec_i4(&r);
+  for (int i = 0; i < 2 * ndet_s + 2 * ii4; i++) (void)rec_i4(&r);
+  double* c4 = (double*)xcalloc((size_t)jj4 + 4, sizeof(double)); /* morue.f:29 */
+  for (int i = 1; i <= jj4; i++) c4[i] = rec_r8(&r);
+  double e4[64], ebmp[64], eben[64];
+  if (metat > 60) die("moy: metat > 60");
+  for (int m = 1; m <= metat; m++) e4[m] = rec_r8(&r);
+  for (int m = 1; m <= metat; m++) ebmp[m] = rec_r8(&r);
+  for (int m = 1; m <= metat; m++) eben[m] = rec_r8(&r);
+  for (int m = 1; m <= metat; m++) (void)rec_i4(&r);
+  for (int i = 1; i <= ndet_s; i++) (void)rec_r8(&r);
+  mnorb = 2 * norb;
+  fmpb = (double*)xcalloc((size_t)mnorb + 4, sizeof(double));
+  for (int i = 1; i <= norb; i++) fmpb[i] = rec_r8(&r);
+  for (int i = 1; i <= norb; i++) fmpb[i + norb] = fmpb[i];
+  fmpb[mnorb + 1] = 0.0;
+  fclose(f4);
+  if (yion) die("yion is not restated");
+
+  /* &moyen (moy.f:29-47) */
+  int yecr = 0, ystkmp = 0, ymat = 0, yrcmp = 0, y_secd = 0, yspipro = 0;
+  double moy_tau = 0.0;
+  yprt = 0;
+  snprintf(title, sizeof title, "%-20.20s", "");
+  nlgroup_t gm;
+  static const char* const moyen_names[] = {"yprt", "tau", "yecr", "ystkmp", "ymat", "iord", "title",
+                                            "yrcmp", "y_secd", "yspipro", "ysymat", NULL};
+  if (!nl_parse("moyen", &gm, moyen_names)) die("erreur dans la namelist moyen");
+  nl_set_log(&gm, "yprt", &yprt);
+  nl_set_real(&gm, "tau", &moy_tau);
+  nl_set_log(&gm, "yecr", &yecr);
+  nl_set_log(&gm, "ystkmp", &ystkmp);
+  nl_set_log(&gm, "ymat", &ymat);
+  nl_set_log(&gm, "yrcmp", &yrcmp);
+  nl_set_log(&gm, "y_secd", &y_secd);
+  nl_set_log(&gm, "yspipro", &yspipro);
+  {
+    const char* t = nl_scalar(&gm, "title");
+    if (t) snprintf(title, sizeof title, "%-20.20s", t);
+  }
+  if (yspipro) die("yspipro (spin-adapted lists) is not restated");
+  printf(" seuil de selection %10.5f\n", moy_tau);
+
+  /* moy/deter.f: unit 40 header, spin-flip map, the list */
+  FILE* f40 = fopen(n40, "rb");
+  if (!f40) die("cannot open unit 40 file %s", n40);
+  if (!rec_read(f40, &r)) die("empty unit 40");
+  nsym = rec_i4(&r);
+  int norb40 = rec_i4(&r);
+  if (norb40 != norb) die("moy: unit 40 (norb=%d) and unit 4 (norb=%d) differ", norb40, norb);
+  (void)rec_i4(&r); /* noc */
+  int ntrans = rec_i4(&r);
+  itsym = (int*)xcalloc((size_t)mnorb + 4, sizeof(int));
+  for (int i = 1; i <= norb; i++) itsym[i] = itsym[i + norb] = rec_i4(&r);
+  (void)rec_i4(&r); /* noa */
+  ydp = rec_l1(&r);
+  if (ntrans != 0) die("spatial degeneracy operations (ntrans>0) are not restated");
+  if (!rec_read(f40, &r)) die("unit 40: missing its");
+  for (int j = 1; j <= nsym; j++)
+    for (int i = 1; i <= nsym; i++) its[i][j] = rec_i4(&r);
+  igela = 1;
+  igelb = igela + norb;
+  iorb = (int*)xcalloc((size_t)mnorb + 4, sizeof(int));
+  ispin = (int*)xcalloc((size_t)mnorb + 4, sizeof(int));
+  isytr1 = (int*)xcalloc((size_t)mnorb + 4, sizeof(int));
+  for (int i = 1; i <= norb; i++) {
+    iorb[i] = i;
+    iorb[i + norb] = i;
+    ispin[i] = 0;
+    ispin[i + norb] = 1;
+  }
+  for (int i = 1; i <= norb; i++) {
+    int k = i + norb, zero = 0;
+    if (k < igelb && i > igela) zero = 1;
+    if (k > igelb && i < igela) zero = 1;
+    if (k < nocb && i > noca) zero = 1;
+    if (k > nocb && i < noca) zero = 1;
+    isytr1[i] = zero ? 0 : k;
+    isytr1[k] = zero ? 0 : i;
+  }
+  FILE* fd60 = fopen(n60, "rb");
+  if (!fd60) die("cannot open unit 60 file %s", n60);
+  moy_lec60(fd60, moy_tau);
+  fclose(fd60);
+  {
+    long long tot = 2, ntp = 2;
+    for (int nec = 1; nec <= 6; nec++) {
+      tot += kex_cnt[nec];
+      ntp += (long long)kex_cnt[nec] * nec;
+    }
+    g_ncf_cap = (int)(2 * tot + 4);
+    ntp_cap = (int)(2 * ntp + 64);
+  }
+  ne = (int*)xcalloc((size_t)g_ncf_cap + 4, sizeof(int));
+  nd = (int*)xcalloc((size_t)g_ncf_cap + 4, sizeof(int));
+  trou = (int*)xcalloc((size_t)ntp_cap + 64, sizeof(int));
+  part = (int*)xcalloc((size_t)ntp_cap + 64, sizeof(int));
+  ncf = 0;
+  isym = 0;
+  if (kf_ref) moy_transf(0);
+  for (int nec = 1; nec <= 6; nec++) {
+    for (int d = 0; d < kex_cnt[nec]; d++) {
+      const int* itab = kex_lists[nec] + (size_t)d * 2 * nec;
+      int ncfo = ncf + 1;
+      for (int l = 1; l <= nec; l++) {
+        tr_nt[l] = itab[l - 1];
+        tr_np[l] = itab[l - 1 + nec];
+      }
+      moy_transf(nec);
+      if (ncf < ncfo) continue;
+      if (isz != 0) continue;
+      int ok = 1;
+      for (int l = 1; l <= nec; l++) {
+        int ntl = isytr1[tr_nt[l]], npl = isytr1[tr_np[l]];
+        if (ntl == 0 || npl == 0) { ok = 0; break; }
+        tr_nt[l] = ntl;
+        tr_np[l] = npl;
+      }
+      if (ok) moy_transf(nec);
+    }
+  }
+  printf(" determinants engendres\n%12d\n", ncf);
+  if (ncf > MOY_NDIMH) die("moy: stop 99 (more than %d determinants)", MOY_NDIMH);
+
+  /* moy.f:79-104: units 64 and 61 */
+  {
+    int ii = nd[ncf] + ne[ncf] + 1;
+    FILE* f64 = fopen(n64, "wb");
+    if (!f64) die("cannot open unit 64 file %s", n64);
+    wbuf_t w = {0};
+    wb_i4(&w, ncf);
+    wb_i4(&w, ii);
+    wb_i4(&w, mnorb);
+    unsigned char yb = 0;
+    wb_put(&w, &yb, 1);
+    for (int i = 1; i <= ncf; i++) { wb_i4(&w, ne[i]); wb_i4(&w, nd[i]); }
+    for (int i = 1; i <= ii; i++) { wb_i4(&w, trou[i]); wb_i4(&w, part[i]); }
+    for (int i = 1; i <= mnorb + 1; i++) wb_i4(&w, i <= mnorb ? iorb[i] : 0);
+    for (int i = 1; i <= mnorb + 1; i++) wb_i4(&w, i <= mnorb ? ispin[i] : 0);
+    wb_flush(f64, &w);
+    free(w.b);
+    fclose(f64);
+    FILE* f61 = fopen(n61, "wb");
+    if (!f61) die("cannot open unit 61 file %s", n61);
+    for (int i = 1; i <= ncf; i++) {
+      wbuf_t a = {0};
+      wb_i4(&a, ne[i]);
+      wb_flush(f61, &a);
+      free(a.b);
+      if (ne[i] != 0) {
+        wbuf_t b = {0};
+        for (int j = 1; j <= ne[i]; j++) wb_i4(&b, trou[nd[i] + j]);
+        for (int j = 1; j <= ne[i]; j++) wb_i4(&b, part[nd[i] + j]);
+        wb_flush(f61, &b);
+        free(b.b);
+      }
+    }
+    fclose(f61);
+  }
+  if (yrcmp) { /* moy.f:106-107: the lists only */
+    fclose(f40);
+    FILE* fj = fopen(json_path, "w");
+    if (fj) {
+      fprintf(fj, "{\"ncf\": %d, \"ndims\": %d, \"yrcmp\": true, \"variant\": \"moy\"}\n", ncf, ndet_s);
+      fclose(fj);
+    }
+    return 0;
+  }
+
+  /* moy/ijkf.f (no zeroing of small Fock elements) and moy/reijkl.f */
+  int nter = norb * (norb + 1) / 2;
+  f_ = (double*)xcalloc((size_t)nter + 4, sizeof(double));
+  aj = (double*)xcalloc((size_t)nter + 4, sizeof(double));
+  ak = (double*)xcalloc((size_t)nter + 4, sizeof(double));
+  fdiag = (double*)xcalloc((size_t)mnorb + 4, sizeof(double));
+  if (!rec_read(f40, &r)) die("unit 40: missing h");
+  if (!rec_read(f40, &r)) die("unit 40: missing J");
+  for (int l = 1; l <= nter; l++) aj[l] = rec_r8(&r);
+  if (!rec_read(f40, &r)) die("unit 40: missing K");
+  for (int l = 1; l <= nter; l++) ak[l] = rec_r8(&r);
+  if (!rec_read(f40, &r)) die("unit 40: missing F");
+  for (int l = 1; l <= nter; l++) f_[l] = rec_r8(&r);
+  {
+    int l = 0;
+    for (int ll = 1; ll <= norb; ll++) {
+      l += ll;
+      fdiag[ll] = f_[l];
+      fdiag[ll + norb] = f_[l];
+    }
+  }
+  ij0_ = (int16_t*)xcalloc((size_t)norb * (size_t)norb, sizeof(int16_t));
+  if (!rec_read(f40, &r)) die("unit 40: missing ij0");
+  for (int j = 1; j <= norb; j++)
+    for (int i = 1; i <= norb; i++) IJ0(i, j) = rec_i2(&r);
+  if (!rec_read(f40, &r)) die("unit 40: missing ninte");
+  ninte = rec_i4(&r);
+  for (int i = 1; i <= nsym; i++) ntttt[i] = rec_i4(&r);
+  {
+    long long lsize = 8192, nbuf = ninte / lsize + 1, mint = 0;
+    bijkl = (float*)xcalloc((size_t)(nbuf * lsize) + 4, sizeof(float));
+    for (long long k = 0; k < nbuf; k++) {
+      if (!rec_read(f40, &r)) die("unit 40: missing integral buffer %lld", k + 1);
+      for (long long i = 0; i < lsize; i++) {
+        ++mint;
+        bijkl[mint] = ydp ? (float)rec_r8(&r) : rec_r4(&r);
+      }
+    }
+  }
+  fclose(f40);
+
+  /* moy.f:117-199: the matrix, row by row, to unit 1 */
+  static int itab[MOY_LSIZE + 1], jtab[MOY_LSIZE + 1];
+  static double vbuf[MOY_LSIZE + 1];
+  double* stefen = (double*)xcalloc((size_t)ncf + 4, sizeof(double));
+  double* stefmp = (double*)xcalloc((size_t)ncf + 4, sizeof(double));
+  unsigned char* yocm = (unsigned char*)xcalloc((size_t)mnorb + 4, 1);
+  FILE* f1 = fopen(n01, "wb");
+  if (!f1) die("cannot open unit 1 file %s", n01);
+  long long nhntd = 0, nhij = 0, nrec1 = 0;
+  int nbuf = 0;
+  const double th0 = now_s();
+  for (int i = 1; i <= ncf; i++) {
+    int ne1 = ne[i];
+    for (int k = 1; k <= ne1; k++) {
+      yocm[trou[nd[i] + k]] = 1;
+      yocm[part[nd[i] + k]] = 1;
+    }
+    int im1 = i - 1;
+    if (y_secd && im1 > ndet_s) im1 = ndet_s;
+    for (int j = 1; j <= im1; j++) {
+      int ne2 = ne[j];
+      int ndif = ne1 - ne2;
+      if (ndif > 2) continue;
+      if (ne2 != 0) {
+        for (int k = 1; k <= ne2; k++) {
+          if (!yocm[trou[nd[j] + k]]) ndif++;
+          if (!yocm[part[nd[j] + k]]) ndif++;
+        }
+        if (ndif > 2) continue;
+      }
+      double hij = hntd(i, j);
+      nhntd++;
+      if (fabs(hij) < 1.0e-10) continue;
+      nhij++;
+      nbuf++;
+      itab[nbuf] = i;
+      jtab[nbuf] = j;
+      vbuf[nbuf] = hij;
+      if (nbuf < MOY_LSIZE) continue;
+      moy_write_buffer(f1, itab, jtab, vbuf);
+      nrec1++;
+      nbuf = 0;
+    }
+    double stfn = hdig(i);
+    nhntd++;
+    nhij++;
+    stefen[i] = stfn;
+    stefmp[i] = hmp(i);
+    nbuf++;
+    itab[nbuf] = i;
+    jtab[nbuf] = i;
+    vbuf[nbuf] = stfn * 0.5;
+    if (nbuf >= MOY_LSIZE) {
+      moy_write_buffer(f1, itab, jtab, vbuf);
+      nrec1++;
+      nbuf = 0;
+    }
+    for (int k = 1; k <= ne1; k++) {
+      yocm[trou[nd[i] + k]] = 0;
+      yocm[part[nd[i] + k]] = 0;
+    }
+  }
+  itab[MOY_LSIZE] = -1;
+  jtab[MOY_LSIZE] = nbuf;
+  moy_write_buffer(f1, itab, jtab, vbuf);
+  nrec1++;
+  fclose(f1);
+  const double hloop_s = now_s() - th0;
+  if (nbuf == 0) printf(" **** attention le dernier buffer sur 1 ne contient aucun element\n");
+  printf(" *** fin de la construction de h ***\n appels a hntd %10lld elements stockes sur 1 %10lld\n",
+         nhntd, nhij);
+  if (ystkmp) {
+    FILE* f63 = fopen(n63, "wb");
+    if (!f63) die("cannot open unit 63 file %s", n63);
+    wbuf_t w = {0};
+    for (int i = 1; i <= ncf; i++) wb_r8(&w, stefmp[i]);
+    wb_flush(f63, &w);
+    free(w.b);
+    fclose(f63);
+  }
+
+  /* morue.f: second order of the determinants k > ndims on the roots of S,
+     from the unit-1 elements (k, i <= ndims) of each row k */
+  int mmm = metat * (metat + 1) / 2;
+  double* hefmp = (double*)xcalloc((size_t)mmm + 2, sizeof(double));
+  double* hefen = (double*)xcalloc((size_t)mmm + 2, sizeof(double));
+  double* hefenb = (double*)xcalloc((size_t)mmm + 2, sizeof(double));
+  double cunt[64];
+  for (int m = 1; m <= metat; m++) cunt[m] = 0.0;
+  int ndims = ndet_s;
+  if (ndims != ncf) {
+    f1 = fopen(n01, "rb");
+    if (!f1) die("cannot reopen unit 1 file %s", n01);
+    static int rt[MOY_LSIZE + 1], rj[MOY_LSIZE + 1];
+    static double rv[MOY_LSIZE + 1];
+    int last = MOY_LSIZE, nb = MOY_LSIZE;
+    rt[MOY_LSIZE] = 0;
+    for (;;) {
+      nb++;
+      if (nb > last) {
+        if (rt[MOY_LSIZE] == -1) break;
+        if (!rec_read(f1, &r)) die("unit 1: missing record");
+        for (int k = 1; k <= MOY_LSIZE; k++) rt[k] = rec_i4(&r);
+        for (int k = 1; k <= MOY_LSIZE; k++) rj[k] = rec_i4(&r);
+        for (int k = 1; k <= MOY_LSIZE; k++) rv[k] = rec_r8(&r);
+        if (rt[MOY_LSIZE] == -1) last = rj[MOY_LSIZE];
+        nb = 1;
+      }
+      int k = rt[nb], i = rj[nb];
+      if (k == 1) continue;
+      if (k == i && k > ndims) {
+        double stenk = stefen[k], stmpk = stefmp[k];
+        double enk2 = stenk + stenk, empk2 = stmpk + stmpk;
+        int ii = 0;
+        for (int m = 1; m <= metat; m++)
+          for (int n = 1; n <= m; n++) {
+            ii++;
+            double denb = eben[m] + eben[n] - enk2;
+            double dmp = ebmp[m] + ebmp[n] - empk2;
+            double den = e4[m] + e4[n] - enk2;
+            double hmn = cunt[m] * cunt[n];
+            hmn = hmn + hmn;
+            hefmp[ii] = hefmp[ii] + hmn / dmp;
+            hefen[ii] = hefen[ii] + hmn / den;
+            hefenb[ii] = hefenb[ii] + hmn / denb;
+          }
+        for (int m = 1; m <= metat; m++) cunt[m] = 0.0;
+        continue;
+      }
+      if (k <= ndims || i > ndims) continue;
+      double hij = rv[nb];
+      int mi = i - ndims;
+      for (int m = 1; m <= metat; m++) {
+        mi = mi + ndims;
+        cunt[m] = cunt[m] + c4[mi] * hij;
+      }
+    }
+    fclose(f1);
+    char typener[96];
+    for (int m = 1; m <= metat; m++) cunt[m] = hefmp[m * (m + 1) / 2];
+    snprintf(typener, sizeof typener, "moyens mbp %s", title);
+    moy_stkener(n33, typener, cunt, metat);
+    for (int m = 1; m <= metat; m++) cunt[m] = hefen[m * (m + 1) / 2];
+    snprintf(typener, sizeof typener, "moyens envp%s", title);
+    moy_stkener(n33, typener, cunt, metat);
+    for (int m = 1; m <= metat; m++) cunt[m] = hefenb[m * (m + 1) / 2];
+    snprintf(typener, sizeof typener, "moyens enb %s", title);
+    moy_stkener(n33, typener, cunt, metat);
+  }
+  /* morue.f:8300: the fourth record of unit 4 replaces whatever follows the
+     third (ny, never set in morue, is written as 0) */
+  {
+    f4 = fopen(n04, "rb");
+    if (!f4) die("cannot reopen unit 4 file %s", n04);
+    long keep = 0;
+    for (int q = 0; q < 3; q++) {
+      if (!rec_read(f4, &r)) die("unit 4: fewer than three records");
+      keep = ftell(f4);
+    }
+    fclose(f4);
+    if (truncate(n04, keep) != 0) die("cannot truncate unit 4 file %s", n04);
+    f4 = fopen(n04, "ab");
+    if (!f4) die("cannot append to unit 4 file %s", n04);
+    wbuf_t w = {0};
+    for (int i = 1; i <= mmm; i++) wb_r8(&w, hefmp[i]);
+    for (int i = 1; i <= mmm; i++) wb_r8(&w, hefen[i]);
+    for (int i = 1; i <= mmm; i++) wb_r8(&w, hefenb[i]);
+    wb_i4(&w, 0);
+    wb_flush(f4, &w);
+    free(w.b);
+    fclose(f4);
+  }
+
+  FILE* fj = fopen(json_path, "w");
+  if (fj) {
+    fprintf(fj, "{\n  \"ncf\": %d, \"ndims\": %d, \"metat\": %d, \"norb\": %d,\n", ncf, ndims, metat, norb);
+    fprintf(fj, "  \"nhntd\": %lld, \"nhij\": %lld, \"unit1_records\": %lld,\n", nhntd, nhij, nrec1);
+    fprintf(fj, "  \"hloop_s\": %.6f,\n", hloop_s);
+    const char* nm[3] = {"hefmp", "hefen", "hefenb"};
+    double* ar[3] = {hefmp, hefen, hefenb};
+    for (int q = 0; q < 3; q++) {
+      fprintf(fj, "  \"%s\": [", nm[q]);
+      for (int i = 1; i <= mmm; i++) fprintf(fj, "%s%.17g", i > 1 ? ", " : "", ar[q][i]);
+      fprintf(fj, "],\n");
+    }
+    fprintf(fj, "  \"variant\": \"moy\"\n}\n");
+    fclose(fj);
+  }
+  free(r.b);
+  return 0;
+}
+
 static void usage(void) {
   fprintf(stderr,
           "usage: cipsi_ref [--sym] [--json out.json] [--candlog file] [--genmask file]\n"
           "                 [--no-pertu-ref] [--sample M --plan file] < stdin-namelists\n"
+          "       cipsi_ref --moy [--json out.json] < stdin-namelists   (moy: H over unit 60)\n"
           "  --plan: lines 'm k1 k2 ...' (1-based generators); each line runs those\n"
           "  generators on the sample residue m and reports [perturbers, seconds]\n");
   exit(2);
@@ -2132,6 +2720,7 @@ int main(int argc, char** argv) {
   const char* cand_path = NULL;
   const char* mask_path = NULL;
   const char* plan_path = NULL;
+  int run_moy = 0;
   for (int a = 1; a < argc; a++) {
     if (!strcmp(argv[a], "--sym"))
       g_sym_variant = 1;
@@ -2147,10 +2736,13 @@ int main(int argc, char** argv) {
       samp_M = atoll(argv[++a]);
     else if (!strcmp(argv[a], "--plan") && a + 1 < argc)
       plan_path = argv[++a];
+    else if (!strcmp(argv[a], "--moy"))
+      run_moy = 1;
     else
       usage();
   }
   g_stdin_text = read_all(stdin);
+  if (run_moy) return moy_main(json_path);
 
   /* openf.f */
   nlgroup_t gf;
