@@ -29,7 +29,9 @@ def _compare(wo, wg, jo, jg):
     for k in ("ncf", "ndims", "nhntd", "nhij", "unit1_records"):
         assert jo[k] == jg[k], k
     for f in ("det_spin", "det_cl", "enmp"):
-        assert open(os.path.join(wo, f), "rb").read() == open(os.path.join(wg, f), "rb").read(), f
+        assert os.path.exists(os.path.join(wo, f)) == os.path.exists(os.path.join(wg, f)), f
+        if os.path.exists(os.path.join(wo, f)):
+            assert open(os.path.join(wo, f), "rb").read() == open(os.path.join(wg, f), "rb").read(), f
     ro, Io, Jo, Vo = mf.read_unit1(os.path.join(wo, "mat"))
     rg, Ig, Jg, Vg = mf.read_unit1(os.path.join(wg, "mat"))
     assert len(ro) == len(rg)
@@ -42,9 +44,13 @@ def _compare(wo, wg, jo, jg):
     e33o = synth.read_records(os.path.join(wo, "ener"))
     e33g = synth.read_records(os.path.join(wg, "ener"))
     assert len(e33o) == len(e33g)
-    for a, b in zip(e33o, e33g):
-        assert a[:40] == b[:40]
-        np.testing.assert_allclose(np.frombuffer(b[40:], "<f8"), np.frombuffer(a[40:], "<f8"), rtol=1e-9, atol=1e-12)
+    for a, b in zip(e33o, e33g):  # the records cip wrote, then morue's (char*40, real*8 x metat)
+        assert len(a) == len(b) and a[:40] == b[:40]
+        if a[:6] == b"moyens":
+            np.testing.assert_allclose(np.frombuffer(b[40:], "<f8"), np.frombuffer(a[40:], "<f8"), rtol=1e-9,
+                                       atol=1e-12)
+        else:
+            assert a == b
     r4o = synth.read_records(os.path.join(wo, "f04"))
     r4g = synth.read_records(os.path.join(wg, "f04"))
     assert len(r4o) == len(r4g) == 4
