@@ -1536,39 +1536,60 @@ __global__ void __launch_bounds__(kThreads, 2) k_pt2(Params p0, BatchArgs ba) {
           }
         }
         if (ADJ) {
-          if (!live) return;
-          double gb[R], gh, gm;
-          adj_factors<R>(p, bc, hmpi, hvpi, ybis ? 1.0 + fmul : 1.0, gb, gh, gm, adjr);
-          if (!p.yen) gh = 0.0;
-          // second pass over the same entries: dE/dH_Ij = sum_m gb[m] c_jm
+          double gb[R], gh = 0.0, gm = 0.0;
+#pragma unroll
+          for (int m = 0; m < R; ++m) gb[m] = 0.0;
+          if (live) {
+            adj_factors<R>(p, bc, hmpi, hvpi, ybis ? 1.0 + fmul : 1.0, gb, gh, gm, adjr);
+            if (!p.yen) gh = 0.0;
+          }
+          // second pass over the same entries: dE/dH_Ij = sum_m gb[m] c_jm,
+          // spread over the integrals of <I|H|j>.  Two phases as in the first
+          // pass: each lane lists the entries that interact with its I, then
+          // the warp takes the t-th listed entry of every lane at once, so
+          // hmat_adj runs with the warp in step instead of once per hitting
+          // lane.  The loops are warp-uniform (nscan, nrb); dead lanes list
+          // nothing.
           const int rankI = rank_k + D;
           const bool two = a2 >= 0;
-          const uint32_t c1x4 = (uint32_t)(a1 + sa1 * p.norb) * 0x01010101u;
-          const uint32_t c2x4 = two ? (uint32_t)(a2 + sa2 * p.norb) * 0x01010101u : 0u;
-          auto visit_adj = [&](int i, int x) {
-            const int j = lr_entry_j(ent_at(i));
-            if (j < k || x == 0) return;
-            uint64_t vv[2 * W];
+          const uint32_t c1x4 = live ? (uint32_t)(a1 + sa1 * p.norb) * 0x01010101u : 0u;
+          const uint32_t c2x4 = live && two ? (uint32_t)(a2 + sa2 * p.norb) * 0x01010101u : 0u;
+          int nh = 0;
+          int* hl = hitl + threadIdx.x * kHitCap;
+          auto note = [&](int i) {
+            const int x = lr_diff(ent_at(i), c1x4, c2x4, two);
+            if (x <= 4 && x != 0 && lr_entry_j(ent_at(i)) >= k) hl[nh++] = i;
+          };
+          auto flush_adj = [&]() {
+            const int maxh = __reduce_max_sync(0xffffffffu, nh);
+            for (int t = 0; t < maxh; ++t) {
+              if (t < nh) {
+                const int j = lr_entry_j(ent_at(hl[t]));
+                uint64_t vv[2 * W];
 #pragma unroll
-            for (int q = 0; q < 2 * W; ++q) vv[q] = __ldg(&p.S[(size_t)j * 2 * W + q]);
-            int rankJ = 0;
+                for (int q = 0; q < 2 * W; ++q) vv[q] = __ldg(&p.S[(size_t)j * 2 * W + q]);
+                int rankJ = 0;
 #pragma unroll
-            for (int q = 0; q < 2 * W; ++q) rankJ += __popcll(hf[q] & ~vv[q]);
-            double w = 0.0;
+                for (int q = 0; q < 2 * W; ++q) rankJ += __popcll(hf[q] & ~vv[q]);
+                double w = 0.0;
 #pragma unroll
-            for (int m = 0; m < R; ++m)
-              if (m < p.metat) w += gb[m] * __ldg(&p.c[(size_t)j * p.metat + m]);
-            hmat_adj<W>(p, u, vv, rankI, rankJ, hf, w);
+                for (int m = 0; m < R; ++m)
+                  if (m < p.metat) w += gb[m] * __ldg(&p.c[(size_t)j * p.metat + m]);
+                hmat_adj<W>(p, u, vv, rankI, rankJ, hf, w);
+              }
+            }
+            nh = 0;
           };
           for (int i = 0; i < nscan; ++i) {
-            const int x = lr_diff(ent_at(i), c1x4, c2x4, two);
-            if (x <= 4) visit_adj(i, x);
+            if (__any_sync(0xffffffffu, nh == kHitCap)) flush_adj();
+            if (live) note(i);
           }
           for (int q2 = 0; q2 < nrb; ++q2) {
-            const int i = rb[q2];
-            const int x = lr_diff(ent_at(i), c1x4, c2x4, two);
-            if (x <= 4) visit_adj(i, x);
+            if (__any_sync(0xffffffffu, nh == kHitCap)) flush_adj();
+            if (live) note(rb[q2]);
           }
+          flush_adj();
+          if (!live) return;
           // diagonal terms: hdig(I) = hdig(K') + vdg[a1] + vdg[a2] + G(a1,a2),
           // hmp(I) = hmp(K') + fmpb[a1] + fmpb[a2]
           adj_gK += gh;
