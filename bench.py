@@ -559,7 +559,7 @@ def run_gpu(args, rank: int, world: int, local_rank: int):
     gmask = None
     if args.gen_every > 1:
         gmask = np.zeros(inp.dims.ncf, dtype=np.uint8)
-        gmask[::args.gen_every] = 1
+        gmask[args.gen_offset::args.gen_every] = 1
     chunk = args.chunk_records
     for _ in range(args.warmup):
         res = ctx.run_stream(inp.opts, chunk_records=chunk, gen_mask=gmask)
@@ -637,7 +637,7 @@ def run_gpu(args, rank: int, world: int, local_rank: int):
     nl = max(1, (r["launches"] - 1) // 3)  # k_pt2 launches per step (one per chunk)
     achieved = r["alg_bytes"] / (kms / 1e3) / 1e9
     prof = kernel_profile(args.workload) if args.gen_every == 1 else None
-    traffic = prof["dram_bytes_per_candidate"] * r["n_candidates"] / nl if prof else None
+    traffic = prof.get("dram_bytes_per_launch") if prof else None
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": tot_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64",
@@ -658,9 +658,9 @@ def run_gpu(args, rank: int, world: int, local_rank: int):
                          "note": "achieved = algorithmic bytes of the E2 loop (integral, coefficient and "
                                  "diagonal-term reads) / k_pt2 time (CUDA events around each chunk's launch on "
                                  "its stream), against the measured HBM copy bandwidth; traffic: DRAM bytes per "
-                                 "launch scaled from an ncu capture of this kernel build on a generator sample "
-                                 "(null when the kernel changed since); the kernel is bound by FP64 issue and "
-                                 "latency, not HBM"},
+                                 "k_pt2 launch, the mean over every launch of one step of this workload in a "
+                                 "single-pass ncu capture of this kernel build (null when the kernel changed "
+                                 "since); the kernel is bound by integer issue and latency, not HBM"},
             "clocks": clk,
             "work": {"perturbers": r["n_processed"], "candidates": r["n_candidates"],
                      "compares": r["n_compares"], "pairs_1": r["n_pairs_1"], "pairs_2": r["n_pairs_2"],
@@ -713,6 +713,7 @@ def main():
     ap.add_argument("--moy-cpu-dets", type=int, default=20000, help="moy form: list size of the CPU sample")
     ap.add_argument("--gen-every", type=int, default=1,
                     help="profiling aid: run only every n-th determinant of S as a generator")
+    ap.add_argument("--gen-offset", type=int, default=0, help="profiling aid: first generator of --gen-every")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -4,7 +4,9 @@ Python mirror of the reference's process-level interface: `run_cip` does what
 running cip.exe (variant="cip") or cipsym.exe (variant="cipsym") in a
 calculation directory does, with the perturbation loop on the GPU; `run_moy`
 does what moy.exe does (the Hamiltonian over S + the selected perturbers),
-with the pair scan and matrix elements on the GPU.  The
+with the pair scan and matrix elements on the GPU; `run_bd` does what bd.exe
+does (the lowest eigenpairs of that matrix), with a Davidson iteration on
+the GPU.  The
 compiled library is built in-tree by `cipsi_gb300.build.build()`; when it is
 missing every entry point raises instead of falling back to a CPU path.
 """
@@ -21,6 +23,7 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "_build", "libcipsi_gb300.so")
 EXE_PATH = os.path.join(_HERE, "_build", "cip_gpu")
 MOY_EXE_PATH = os.path.join(_HERE, "_build", "moy_gpu")
+BD_EXE_PATH = os.path.join(_HERE, "_build", "bd_gpu")
 
 _lib = None
 
@@ -34,6 +37,7 @@ EXPORTED = [
     "cipsi_batch_last_error", "cipsi_batch_destroy", "cipsi_inputs_array", "cipsi_set_integrals_f64store",
     "cipsi_run_pt2_adjoint", "cipsi_set_selection_sink", "cipsi_run_pt2_stream", "cipsi_record_digest",
     "cipsi_hamiltonian_build", "cipsi_hamiltonian_get", "cipsi_hamiltonian_ms", "cipsi_moy_main",
+    "cipsi_davidson", "cipsi_bd_main",
 ]
 
 
@@ -55,6 +59,8 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
     lib.cipsi_moy_main.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int32,
                                    ctypes.c_char_p, ctypes.c_int32]
     lib.cipsi_moy_main.restype = ctypes.c_int
+    lib.cipsi_bd_main.argtypes = lib.cipsi_moy_main.argtypes
+    lib.cipsi_bd_main.restype = ctypes.c_int
     _lib = lib
     return lib
 
@@ -92,6 +98,23 @@ def run_moy(workdir: str, json_path: Optional[str] = None, device: int = 0,
     err = ctypes.create_string_buffer(2048)
     rc = lib.cipsi_moy_main(workdir.encode(), (stdin_path or os.path.join(workdir, "moy.in")).encode(),
                             json_path.encode(), device, err, len(err))
+    if rc != 0:
+        raise CipsiError(err.value.decode(errors="replace"))
+    with open(json_path) as fh:
+        return json.load(fh)
+
+
+def run_bd(workdir: str, json_path: Optional[str] = None, device: int = 0,
+           stdin_path: Optional[str] = None) -> dict:
+    """Run the bd drop-in in `workdir` (namelists &bdfil/&option from
+    `stdin_path`, default workdir/bd.in).  Returns the JSON summary
+    (eigenvalues, residual norms, iterations)."""
+    lib = load_library()
+    if json_path is None:
+        json_path = os.path.join(workdir, "bd_gpu.json")
+    err = ctypes.create_string_buffer(2048)
+    rc = lib.cipsi_bd_main(workdir.encode(), (stdin_path or os.path.join(workdir, "bd.in")).encode(),
+                           json_path.encode(), device, err, len(err))
     if rc != 0:
         raise CipsiError(err.value.decode(errors="replace"))
     with open(json_path) as fh:

@@ -1,5 +1,5 @@
-"""Build the GB300 engine in-tree: libcipsi_gb300.so and the cip_gpu and
-moy_gpu drop-ins.
+"""Build the GB300 engine in-tree: libcipsi_gb300.so and the cip_gpu,
+moy_gpu and bd_gpu drop-ins.
 
 Sources are compiled for sm_103a only, in parallel, and skipped when the
 sources and flags have not changed since the last build.
@@ -19,15 +19,18 @@ OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libcipsi_gb300.so")
 EXE = os.path.join(OUT, "cip_gpu")
 MOY_EXE = os.path.join(OUT, "moy_gpu")
+BD_EXE = os.path.join(OUT, "bd_gpu")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
 # no fused multiply-add contraction in host code: the same results on x86 and Arm
 CXXFLAGS = ["-O2", "-ffp-contract=off", "-std=c++17", "-fPIC", "-Wall"]
 
-CU_SOURCES = ["cipsi_engine.cu", "pt2_w1.cu", "pt2_w2.cu", "pt2_adj.cu", "hbuild.cu"]
-SOURCES = CU_SOURCES + ["pt2_common.cuh", "pt2_kernel.cuh", "host_io.h", "cip_host.cpp", "moy_host.cpp",
-                        "cip_gpu_main.cpp", "moy_gpu_main.cpp"]
+CU_SOURCES = ["cipsi_engine.cu", "pt2_w1.cu", "pt2_w2.cu", "pt2_adj.cu", "hbuild.cu", "davidson.cu"]
+HOST_SOURCES = ["cip_host.cpp", "moy_host.cpp", "bd_host.cpp"]
+MAINS = {"cip_gpu": "cip_gpu_main.cpp", "moy_gpu": "moy_gpu_main.cpp", "bd_gpu": "bd_gpu_main.cpp"}
+SOURCES = CU_SOURCES + HOST_SOURCES + list(MAINS.values()) + ["pt2_common.cuh", "pt2_kernel.cuh", "host_io.h",
+                                                              "symeig.h"]
 HEADERS = [os.path.join(ROOT, "include", "cipsi_gb300.h")]
 
 
@@ -57,23 +60,17 @@ def build(force: bool = False, verbose: bool = False) -> str:
     nvcc = _nvcc()
     stamp = os.path.join(OUT, ".stamp")
     dig = _digest(" ".join(ARCH + NVFLAGS + CXXFLAGS))
-    if (not force and os.path.exists(LIB) and os.path.exists(EXE) and os.path.exists(MOY_EXE)
+    if (not force and os.path.exists(LIB) and all(os.path.exists(os.path.join(OUT, e)) for e in MAINS)
             and os.path.exists(stamp)):
         if open(stamp).read().strip() == dig:
             return LIB
     objs = {c: os.path.join(OUT, c.replace(".cu", ".o")) for c in CU_SOURCES}
-    objs["host"] = os.path.join(OUT, "cip_host.o")
-    objs["main"] = os.path.join(OUT, "cip_gpu_main.o")
-    objs["moy"] = os.path.join(OUT, "moy_host.o")
-    objs["moy_main"] = os.path.join(OUT, "moy_gpu_main.o")
+    for c in HOST_SOURCES + list(MAINS.values()):
+        objs[c] = os.path.join(OUT, c.replace(".cpp", ".o"))
     jobs = [[nvcc] + ARCH + NVFLAGS + ["-Xptxas", "-v", "-c", os.path.join(CSRC, c), "-o", objs[c]]
             for c in CU_SOURCES]
-    jobs += [
-        ["g++"] + CXXFLAGS + ["-c", os.path.join(CSRC, "cip_host.cpp"), "-o", objs["host"]],
-        ["g++"] + CXXFLAGS + ["-c", os.path.join(CSRC, "cip_gpu_main.cpp"), "-o", objs["main"]],
-        ["g++"] + CXXFLAGS + ["-c", os.path.join(CSRC, "moy_host.cpp"), "-o", objs["moy"]],
-        ["g++"] + CXXFLAGS + ["-c", os.path.join(CSRC, "moy_gpu_main.cpp"), "-o", objs["moy_main"]],
-    ]
+    jobs += [["g++"] + CXXFLAGS + ["-c", os.path.join(CSRC, c), "-o", objs[c]]
+             for c in HOST_SOURCES + list(MAINS.values())]
     with ThreadPoolExecutor(max_workers=len(jobs)) as ex:
         outs = list(ex.map(_run, jobs))
     ptxas = "".join(outs[:len(CU_SOURCES)])
@@ -81,10 +78,9 @@ def build(force: bool = False, verbose: bool = False) -> str:
         sys.stdout.write(ptxas)
     with open(os.path.join(OUT, "ptxas_info.txt"), "w") as fh:
         fh.write(ptxas)
-    _run([nvcc] + ARCH + ["-shared", "-o", LIB] + [objs[c] for c in CU_SOURCES] + [objs["host"], objs["moy"],
-                                                                        "-lcudart"])
-    for exe, main in ((EXE, objs["main"]), (MOY_EXE, objs["moy_main"])):
-        _run(["g++", "-o", exe, main, "-L" + OUT, "-lcipsi_gb300", "-Wl,-rpath,$ORIGIN",
+    _run([nvcc] + ARCH + ["-shared", "-o", LIB] + [objs[c] for c in CU_SOURCES + HOST_SOURCES] + ["-lcudart"])
+    for exe, main in MAINS.items():
+        _run(["g++", "-o", os.path.join(OUT, exe), objs[main], "-L" + OUT, "-lcipsi_gb300", "-Wl,-rpath,$ORIGIN",
               "-L" + os.path.join(os.path.dirname(os.path.dirname(nvcc)), "lib64"), "-lcudart"])
     with open(stamp, "w") as fh:
         fh.write(dig)

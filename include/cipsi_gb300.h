@@ -403,6 +403,33 @@ float cipsi_hamiltonian_ms(const cipsi_ctx* ctx);
 int cipsi_moy_main(const char* workdir, const char* stdin_path, const char* json_path, int32_t device,
                    char* errbuf, int32_t errlen);
 
+/* The lowest eigenpairs of the CI matrix that moy writes to unit 1 (the
+   work of CIPSI_sources/bd/bigdia.f): the n x n symmetric H = L + L^T, L
+   given as nel elements (itab[t], jtab[t], val[t]), 1-based, jtab <= itab,
+   each diagonal element stored as half its value (moy/moy.f:150-190,
+   bd/getmat.f).  A block Davidson iteration on `device` (davidson.cu),
+   converged when every root's residual norm |H x - e x| is at most `tol`:
+   evals[nroots] ascending, evecs[n * nroots] (root-major, unit norm, each
+   vector's largest component positive), *iters, resid[nroots] (optional).
+   nroots <= 8.  Returns CIPSI_ERR_OVERFLOW (results of the last iteration
+   filled in) if not converged within maxiter iterations.  Allocates its
+   device buffers for the call. */
+int cipsi_davidson(int32_t n, int64_t nel, const int32_t* itab, const int32_t* jtab, const double* val,
+                   int32_t nroots, double tol, int32_t maxiter, int32_t device, double* evals, double* evecs,
+                   int32_t* iters, double* resid, char* errbuf, int32_t errlen);
+
+/* Process-level drop-in for bd.exe (CIPSI_sources/bd/bd.f): reads the
+   &bdfil/&option namelists from `stdin_path` and, in `workdir`, unit 1 (the
+   matrix moy wrote) and the first two records of unit 4 (metat, ncper,
+   escf); computes the lowest metat eigenpairs with cipsi_davidson; writes
+   the 'energies var.' record of unit 33, unit 59 (qwvec: ncf, netat, the
+   vectors, the total energies), unit 55 (qws) and the listing lines
+   ' ncf,netat,ncper,iget' that the Autocip driver reads.  Not supported:
+   qnorm, qrvec, qhef, qdcple, and ind, cold, netat or ites given in
+   &option. */
+int cipsi_bd_main(const char* workdir, const char* stdin_path, const char* json_path, int32_t device,
+                  char* errbuf, int32_t errlen);
+
 #ifdef __cplusplus
 }
 #endif
