@@ -1,0 +1,79 @@
+"""The in-process CIPSI loop of the Autocip driver (cipsi_gb300.autocip,
+Autocip_13/calcul.f90:255-480) on the GPU drop-ins: a complete active space
+as the first S, CIPSI iterations that grow S until it holds det_bounds[0]
+determinants, then the final space chosen by the ENvp of the selected
+records and its moy/bd.  Checks: the steps come in calcul_cip's order, each
+S-only run writes S grown by the previous selection, the namelist edits are
+sed's, E2 and the vectors feed the next step, and the final space is S plus
+the records down to the chosen threshold."""
+import os
+import struct
+
+import numpy as np
+import pytest
+
+from cipsi_gb300 import autocip, synth
+
+COMMON = (" &MOYFIL\n &end\n &moyen\n TAU=0d0,\n &end\n &bdfil\n &end\n &option\n QGIV =T,\n NCPER=800,\n"
+          " test=0.3d-3,\n qws=t,\n qwb=t,\n qwvec=t,\n &end\n")
+
+
+def _icinp(extra):
+    return (" &cipfil\n &end\n &icinp\n twdet=0.5\n ISZ=0,\n METAT=2,\n YMOYEN=T,\n YBRD=F,\n YION=F,\n"
+            " ISELEC=  1,\n TEST=0d0,\n TAU=0d0,\n ITYPER=-1,\n" + extra + " &end\n")
+
+
+def _files(wd):
+    f_bd = os.path.join(wd, "chain.bd")
+    cas = " NUMAC=3,4,5,6,7,8,9,10,\n NUSYM=1,\n NOAC=8,\n NELAC=2,\n NEMAX=2,\n LECDET=4,\n"
+    with open(f_bd, "w") as fh:
+        fh.write(_icinp(cas) + COMMON)
+    for suffix in ("_loop", "_end"):
+        with open(f_bd + suffix, "w") as fh:
+            fh.write(_icinp(" LECDET=5,\n") + COMMON)
+    return f_bd
+
+
+def test_sed_item_is_seds_substitution():
+    t = " &icinp\n ITYPER=2, LECDET=5,\n TAU=0.01,\n XITYPER=3,\n &end"
+    out = autocip.sed_item(t, "ITYPER", "-1")
+    assert out.split("\n")[1] == " ITYPER=-1,"  # the rest of the line goes, as with sed
+    assert out.split("\n")[3] == " XITYPER=3,"  # ' ITYPER=' with its blank only
+    assert autocip.sed_item(t, "TAU", "0d0").split("\n")[2] == " TAU=0d0,"
+
+
+@pytest.mark.gpu
+def test_cipsi_loop_on_the_drop_ins(tmp_path, engine_lib):
+    cfg = synth.SynthConfig("chain", norb=12, nocc=3, ncholesky=12, ncf=10, metat=2, tau=0.02,
+                            ranks=(1, 2), coef_mode="gauss005", seed=41, virt_shift=3.0)
+    wd = str(tmp_path / "geo")
+    synth.generate(cfg, wd)
+    for u in ("det", "bdvec", "f04"):
+        os.remove(os.path.join(wd, u))
+    f_bd = _files(wd)
+    log = []
+    out = autocip.calcul_cip(wd, f_bd, metat=2, netat_pertu=1, envp_max=1e-3, det_bounds=(400, 100000, 10, 10 ** 6),
+                             imax_s=4, tau_init=0.05, tau_step=0.5, ncf=0, log=log)
+    kinds = [s["step"] for s in log]
+    # per iteration: cip (S), moy, bd, cip (E2); then the final moy, bd
+    n_it = (len(kinds) - 2) // 4
+    assert kinds == ["cip", "moy", "bd", "cip"] * n_it + ["moy", "bd"]
+    assert 2 <= n_it <= 4
+    s_sizes = [log[4 * i + 2]["result"]["ncf"] for i in range(n_it)]  # bd over S in iteration i
+    assert s_sizes[0] == 64  # the CAS of 2 electrons in 8 orbitals
+    assert all(b > a for a, b in zip(s_sizes, s_sizes[1:]))
+    for i in range(n_it):
+        pert = log[4 * i + 3]["result"]
+        assert pert["ncf"] == s_sizes[i] and pert["ntot60"] >= pert["ncf"]
+        if i + 1 < n_it:  # the next S is this S plus the selection (and partners)
+            assert s_sizes[i + 1] >= pert["ntot60"]
+    # the variational energy of the lowest root does not rise as S grows
+    e0 = [log[4 * i + 2]["result"]["eigenvalues"][0] for i in range(n_it)]
+    assert all(b <= a + 1e-10 for a, b in zip(e0, e0[1:]))
+    # the final space: S and the records whose xam reaches the chosen tau
+    last = log[4 * (n_it - 1) + 3]["result"]
+    xam, _ = autocip._unit60_xam_envp(os.path.join(wd, "det"), last["metat"])
+    assert out["ncf"] >= out["nbase"] == s_sizes[-1]
+    assert out["ncf"] >= int(np.sum(xam >= out["tau"]))
+    assert len(out["e_corr"]) == 2 and all(np.isfinite(out["e_corr"]))
+    assert out["e_corr"][0] < abs(last["e2vp"][0]) + 1e-12
