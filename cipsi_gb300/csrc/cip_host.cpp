@@ -14,13 +14,14 @@
 // cip/hmp.f, cip/hdig.f, cip/pie.f, cip/stkener.f and the cipsym variants
 // (cipsym/cip.f:226-254, cipsym/pie.f, cipsym/ic001.f:179).
 //
-// Supported: the perturbation run, lecdet 5 (S from unit 60, vectors from
-// unit 59) with ityper >= 0; and the run that only writes S (ityper < 0,
+// Supported: the perturbation run with lecdet 5 (S from unit 60, vectors
+// from unit 59) or with lecdet 2, 3, 4 (S from unit 60 or a complete active
+// space, diagonalised here on the GPU as cip/ic001.f:81-131 does); and the
+// run that only writes S (ityper < 0,
 // cip/cip.f:200-236), with S from unit 60 (lecdet 2, 3, 5) or generated as
 // a complete active space (lecdet 4, cip/cas.f) -- the two ways the Autocip
 // driver calls cipsym (Autocip_13/calcul.f90:318-353).  isz = 0.  Other
-// inputs are rejected with a message (cip stops on them, or they need the S
-// diagonalisation).
+// inputs are rejected with a message.
 
 #include <algorithm>
 #include <cctype>
@@ -150,6 +151,7 @@ struct Run {
   std::vector<double> tocom, empdet;  // faifoc.f occupations (after cip.f:75-84), hmp of S
   std::vector<double> hdiag;          // hdig of S
   std::vector<double> tocom21;        // occupations read from unit 21 (ytocom)
+  int device = -1;  // the GPU of the S diagonalisation (lecdet != 5); -1: none allowed
 };
 
 // transf.f: sort, validate, dedup and append one determinant
@@ -399,6 +401,8 @@ double hdig_list(const Run& R, int k) {
 }
 
 void read_vectors(Run& R, bool sym_variant);
+void vectors_of_s(Run& R, bool sym_variant);
+void s_space_ci(Run& R, bool sym_variant);
 void zero_order(Run& R);
 
 void read_inputs(Run& R, bool sym_variant) {
@@ -408,8 +412,8 @@ void read_inputs(Run& R, bool sym_variant) {
   if (o.ybrd && o.metat > 1) throw Error("ybrd (QDPT effective Hamiltonian) is not supported");
   if (o.ninact > 0) throw Error("ninact > 0 (restricted perturbation space) is not supported");
   if (o.lecdet < 2 || o.lecdet > 5) throw Error("lecdet 1 (determinants on cards) is not supported");
-  if (o.ityper >= 0 && o.lecdet != 5)
-    throw Error("a perturbation run needs lecdet = 5 (vectors of S read from unit 59)");
+  if (o.ityper >= 0 && o.lecdet != 5 && R.device < 0)
+    throw Error("a perturbation run with lecdet != 5 diagonalises S on the GPU: run it through cipsi_cip_main");
   if (o.metat < 1 || o.metat > 60) throw Error("trop d etats demandes en perturbation");
   auto recs = read_records(o.f40);
   if (recs.size() < 9) throw Error("unit 40 too short");
@@ -476,6 +480,8 @@ void read_inputs(Run& R, bool sym_variant) {
     R.metat = o.metat;
     R.c.assign((size_t)R.ncf * R.metat, 0.0);
     R.e.assign(R.metat, 0.0);
+  } else if (o.lecdet != 5) {
+    s_space_ci(R, sym_variant);
   } else {
     read_vectors(R, sym_variant);
   }
@@ -555,15 +561,112 @@ void read_vectors(Run& R, bool sym_variant) {
       for (int k = 0; k < R.ncf; ++k) R.c[(size_t)m * R.ncf + k] = tmp[k];
     }
   }
+  vectors_of_s(R, sym_variant);
+}
+
+// after the vectors of S are known (ic001.f): degen, then the generators --
+// every determinant for cipsym (cipsym/ic001.f:179), those with |c| >= coeff
+// on some root for cip (cip/ic001.f:751)
+void vectors_of_s(Run& R, bool sym_variant) {
   rotate_degenerate_roots(R);
   for (int k = 0; k < R.ncf; ++k) {
     if (sym_variant) {
       R.S.ygen[k] = 1;
     } else {
       for (int m = 0; m < R.metat; ++m)
-        if (std::fabs(R.c[(size_t)m * R.ncf + k]) >= o.coeff) R.S.ygen[k] = 1;
+        if (std::fabs(R.c[(size_t)m * R.ncf + k]) >= R.o.coeff) R.S.ygen[k] = 1;
     }
   }
+}
+
+// ic001.f:81-131 (lecdet != 5, ityper >= 0): H over S -- hdig on the
+// diagonal, hntd within two excitations -- and its lowest metat eigenpairs.
+// The pairs come from cipsi_hamiltonian_build on the run's GPU, the
+// eigenpairs from cipsi_davidson (residuals converged to 1e-13 of H's
+// largest diagonal element)
+// instead of the reference's LAPACK call (diagonaliser.f90).  Each
+// vector's first component of magnitude above 1e-8 of its largest is made
+// positive (LAPACK's signs are its own; E2 and the selection use
+// <I|H|Psi>^2).
+void s_space_ci(Run& R, bool sym_variant) {
+  const int n = R.ncf;
+  R.metat = std::min(R.o.metat, n);
+  if (R.metat > CIPSI_MAX_ROOTS) throw Error("the S diagonalisation takes at most 8 roots");
+  cipsi_dims d{};
+  d.norb = R.norb;
+  d.noca = R.noc;
+  d.nsym = R.nsym;
+  d.isym = R.isym > 0 ? R.isym : 1;
+  d.isz = 0;
+  d.metat = 1;
+  d.ncf = n;
+  cipsi_ctx* ctx = nullptr;
+  struct Guard {
+    cipsi_ctx*& c;
+    ~Guard() { if (c) cipsi_ctx_destroy(c); }
+  } guard{ctx};
+  auto chk = [&](int code, const char* what) {
+    if (code) throw Error(std::string(what) + ": " + cipsi_last_error(ctx));
+  };
+  chk(cipsi_ctx_create(&ctx, &d, R.device), "cipsi_ctx_create");
+  chk(cipsi_set_integrals(ctx, R.itsym.data(), R.its.data(), R.F.data(), R.J.data(), R.K.data(), R.ij0.data(),
+                          R.ntttt.data(), R.eri.data(), (int64_t)R.eri.size()),
+      "cipsi_set_integrals");
+  chk(cipsi_set_space(ctx, R.S.ne.data(), R.S.nd.data(), R.S.trou.data(), R.S.part.data(), (int64_t)R.S.trou.size(),
+                      R.S.ygen.data(), R.S.ysaut.data(), R.S.nesp.data(), R.S.yef1.data()),
+      "cipsi_set_space");
+  int64_t npairs = 0;
+  chk(cipsi_hamiltonian_build(ctx, nullptr, -1, &npairs), "cipsi_hamiltonian_build");
+  std::vector<int64_t> rowptr((size_t)n + 1);
+  std::vector<int32_t> col((size_t)std::max<int64_t>(npairs, 1));
+  std::vector<double> val((size_t)std::max<int64_t>(npairs, 1));
+  chk(cipsi_hamiltonian_get(ctx, 0, n, rowptr.data(), col.data(), val.data()), "cipsi_hamiltonian_get");
+  cipsi_ctx_destroy(ctx);
+  ctx = nullptr;
+  std::vector<int32_t> I, J;
+  std::vector<double> V;
+  I.reserve((size_t)npairs + n);
+  J.reserve((size_t)npairs + n);
+  V.reserve((size_t)npairs + n);
+  for (int i = 0; i < n; ++i) {
+    for (int64_t t = rowptr[i]; t < rowptr[i + 1]; ++t) {
+      I.push_back(i + 1);
+      J.push_back(col[t] + 1);
+      V.push_back(val[t]);
+    }
+    I.push_back(i + 1);
+    J.push_back(i + 1);
+    V.push_back(0.5 * hdig_list(R, i));  // cipsi_davidson takes the diagonal halved
+  }
+  // residuals converged to 1e-13 of the largest diagonal element (about
+  // what double precision resolves), so the vectors agree with a dense
+  // solver's to ~1e-13 and E2 to ~1e-12 of itself
+  double hmax = 1.0;
+  for (int i = 0; i < n; ++i) hmax = std::max(hmax, std::fabs(hdig_list(R, i)));
+  std::vector<double> ev(R.metat), vec((size_t)n * R.metat);
+  char derr[512] = {0};
+  int iters = 0;
+  if (cipsi_davidson(n, (int64_t)V.size(), I.data(), J.data(), V.data(), R.metat, 1.0e-13 * hmax, 5000, R.device,
+                     ev.data(), vec.data(), &iters, nullptr, derr, (int32_t)sizeof derr))
+    throw Error(derr);
+  R.e = ev;
+  R.c = vec;
+  for (int m = 0; m < R.metat; ++m) {
+    double* x = R.c.data() + (size_t)m * n;
+    double big = 0.0;
+    for (int i = 0; i < n; ++i) big = std::max(big, std::fabs(x[i]));
+    double sg = 1.0;
+    for (int i = 0; i < n; ++i)
+      if (std::fabs(x[i]) > 1e-8 * big) {
+        sg = x[i] < 0.0 ? -1.0 : 1.0;
+        break;
+      }
+    for (int i = 0; i < n; ++i) x[i] *= sg;
+  }
+  std::printf(" nombre de determinants   ncf=%9d\n valeurs propres\n", n);
+  for (double x : R.e) std::printf(" %12.8f", x);
+  std::printf("\n");
+  vectors_of_s(R, sym_variant);
 }
 
 // faifoc.f and the zero-order quantities of cip.f:75-135
@@ -988,8 +1091,19 @@ void seterr(char* errbuf, int32_t errlen, const std::string& m) {
 
 }  // namespace
 
+namespace {
+int inputs_read(cipsi_inputs** out, const char* workdir, const char* stdin_path, int32_t sym_variant, int device,
+                char* errbuf, int32_t errlen);
+}
+
 extern "C" int cipsi_inputs_read(cipsi_inputs** out, const char* workdir, const char* stdin_path,
                                  int32_t sym_variant, char* errbuf, int32_t errlen) {
+  return inputs_read(out, workdir, stdin_path, sym_variant, -1, errbuf, errlen);
+}
+
+namespace {
+int inputs_read(cipsi_inputs** out, const char* workdir, const char* stdin_path, int32_t sym_variant, int device,
+                char* errbuf, int32_t errlen) {
   if (!out) return CIPSI_ERR_ARG;
   *out = nullptr;
   try {
@@ -1003,6 +1117,7 @@ extern "C" int cipsi_inputs_read(cipsi_inputs** out, const char* workdir, const 
     try {
       h->R.o = read_options(ss.str(), dir, sym_variant != 0);
       if (h->R.o.teseff < 0.0) h->R.o.teseff = 0.05 * h->R.o.tau;
+      h->R.device = device;
       read_inputs(h->R, sym_variant != 0);
     } catch (...) {
       delete h;
@@ -1015,6 +1130,7 @@ extern "C" int cipsi_inputs_read(cipsi_inputs** out, const char* workdir, const 
     return CIPSI_ERR_ARG;
   }
 }
+}  // namespace
 
 extern "C" void cipsi_inputs_free(cipsi_inputs* in) { delete in; }
 
@@ -1090,7 +1206,7 @@ extern "C" int cipsi_cip_main(const char* workdir, const char* stdin_path, int32
   cipsi_ctx* ctx = nullptr;
   cipsi_inputs* in = nullptr;
   try {
-    int rc = cipsi_inputs_read(&in, workdir, stdin_path, sym_variant, errbuf, errlen);
+    int rc = inputs_read(&in, workdir, stdin_path, sym_variant, device, errbuf, errlen);
     if (rc) return rc;
     const Run& R = in->R;
     const auto t0 = std::chrono::steady_clock::now();

@@ -238,6 +238,12 @@ extern "C" int cipsi_davidson(int32_t n, int64_t nel, const int32_t* itab, const
   // the columns orthonormal through their Gram matrix, dropping directions
   // with no weight left; returns the columns kept (written back into T)
   auto orthonormalise = [&](int k, int nt) -> int {
+    // the scale of the corrections before projection: a direction is
+    // dropped when projecting leaves less than 1e-10 of that scale
+    std::vector<double> G0;
+    gram(T, nt, T, nt, G0);
+    double scale2 = 0.0;
+    for (int q = 0; q < nt; ++q) scale2 = std::max(scale2, G0[(size_t)q * nt + q]);
     for (int pass = 0; pass < 2 && k > 0; ++pass) {
       std::vector<double> C;
       gram(V, k, T, nt, C);  // k x nt
@@ -248,10 +254,9 @@ extern "C" int cipsi_davidson(int32_t n, int64_t nel, const int32_t* itab, const
     gram(T, nt, T, nt, G);
     if (!d.ok) return 0;
     sym_eig(nt, G, w, U);
-    const double wmax = w.empty() ? 0.0 : w.back();
     std::vector<int> keep;
     for (int q = nt - 1; q >= 0; --q)
-      if (w[q] > 1e-20 * std::max(wmax, 1e-300) && w[q] > 1e-26) keep.push_back(q);
+      if (w[q] > 1e-20 * scale2 && w[q] > 0.0) keep.push_back(q);
     const int nk = (int)keep.size();
     if (nk == 0) return 0;
     std::vector<double> Sx((size_t)nt * nk);

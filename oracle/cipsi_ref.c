@@ -34,14 +34,16 @@
  *   CIPSI_sources/cip/isto.f, pie.f, stkener.f
  *   CIPSI_sources/cipsym/pie.f, pert1.f:244, diexcit.f:446, cip.f:226-254,
  *   CIPSI_sources/cipsym/ic001.f:179 (all determinants are generators)
+ *   CIPSI_sources/cip/ic001.f:81-131 (lecdet != 5: H over S and its lowest
+ *                                roots, here by Jacobi rotations)
+ *   CIPSI_sources/moy/*.f        the Hamiltonian over unit 60 (--moy)
  *
  * Arrays are 1-based (index 0 unused) to keep the restatement checkable
  * against the Fortran line by line.
  *
- * Not restated (rejected with an error): lecdet=1 (card input),
- * S diagonalisation (ityper>=0 with lecdet!=5), ybrd (QDPT effective
- * Hamiltonian), yion (excitation to infinity), iord or ygen given in the
- * namelist.
+ * Not restated (rejected with an error): lecdet=1 (card input), ybrd (QDPT
+ * effective Hamiltonian), yion (excitation to infinity), iord or ygen given
+ * in the namelist.
  */
 #define _GNU_SOURCE
 #include <ctype.h>
@@ -1924,6 +1926,96 @@ static void build_space(void) {
   if (ncf == 0) die("aucun determinant dans le sous espace variationnel");
 }
 
+/* ---------------------------------------------- S-space CI (ic001.f:81-131)
+   lecdet != 5 with ityper >= 0: H over S (hdig on the diagonal, hntd
+   within two excitations, every value kept), its lowest metat eigenpairs
+   (the reference calls LAPACK through diagonaliser.f90; restated here by
+   cyclic Jacobi rotations).  Each vector's sign: its first component of
+   magnitude above 1e-8 of its largest is positive (the reference's signs
+   come from LAPACK; E2 and the selection use <I|H|Psi>^2 and do not
+   depend on them). */
+static void s_space_ci(void) {
+  if (metat > ncf) metat = ncf;
+  int n = ncf;
+  double* a = (double*)xcalloc((size_t)n * n + 4, sizeof(double));
+  double* v = (double*)xcalloc((size_t)n * n + 4, sizeof(double));
+#define A_(i, j) a[(size_t)((i)-1) * n + ((j)-1)]
+#define V_(i, j) v[(size_t)((i)-1) * n + ((j)-1)]
+  for (int i = 1; i <= n; i++) {
+    hdiag[i] = hdig(i);
+    A_(i, i) = hdiag[i];
+    V_(i, i) = 1.0;
+    for (int j = i + 1; j <= n; j++) {
+      int ndif = ne[i] - ne[j];
+      for (int k = nd[j] + 1; k <= nd[j] + ne[j]; k++) {
+        if (!YOCD(trou[k], i)) ndif++;
+        if (!YOCD(part[k], i)) ndif++;
+      }
+      double h = ndif <= 2 ? hntd(i, j) : 0.0;
+      A_(i, j) = A_(j, i) = h;
+    }
+  }
+  double norm = 0.0;
+  for (size_t q = 0; q < (size_t)n * n; q++) norm += a[q] * a[q];
+  for (int sweep = 0; sweep < 100; sweep++) {
+    double off = 0.0;
+    for (int p = 1; p <= n; p++)
+      for (int q = p + 1; q <= n; q++) off += A_(p, q) * A_(p, q);
+    if (off <= 1e-30 * norm || off == 0.0) break;
+    for (int p = 1; p <= n; p++)
+      for (int q = p + 1; q <= n; q++) {
+        double apq = A_(p, q);
+        if (apq == 0.0) continue;
+        double theta = (A_(q, q) - A_(p, p)) / (2.0 * apq);
+        double t = (theta >= 0.0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
+        double cs = 1.0 / sqrt(t * t + 1.0), sn = t * cs;
+        for (int k = 1; k <= n; k++) {
+          double akp = A_(k, p), akq = A_(k, q);
+          A_(k, p) = cs * akp - sn * akq;
+          A_(k, q) = sn * akp + cs * akq;
+        }
+        for (int k = 1; k <= n; k++) {
+          double apk = A_(p, k), aqk = A_(q, k);
+          A_(p, k) = cs * apk - sn * aqk;
+          A_(q, k) = sn * apk + cs * aqk;
+        }
+        A_(p, q) = A_(q, p) = 0.0;
+        for (int k = 1; k <= n; k++) {
+          double vkp = V_(k, p), vkq = V_(k, q);
+          V_(k, p) = cs * vkp - sn * vkq;
+          V_(k, q) = sn * vkp + cs * vkq;
+        }
+      }
+  }
+  /* the metat lowest, ascending (ties keep their column order) */
+  int* ord = (int*)xcalloc((size_t)n + 4, sizeof(int));
+  for (int i = 1; i <= n; i++) ord[i] = i;
+  for (int i = 2; i <= n; i++) { /* insertion sort: stable */
+    int x = ord[i], j = i - 1;
+    while (j >= 1 && A_(ord[j], ord[j]) > A_(x, x)) { ord[j + 1] = ord[j]; j--; }
+    ord[j + 1] = x;
+  }
+  c = (double*)xcalloc((size_t)metat * (size_t)ncf + 4, sizeof(double));
+  for (int m = 1; m <= metat; m++) {
+    int col = ord[m];
+    e[m] = A_(col, col);
+    double big = 0.0;
+    for (int i = 1; i <= n; i++) if (fabs(V_(i, col)) > big) big = fabs(V_(i, col));
+    double sg = 1.0;
+    for (int i = 1; i <= n; i++)
+      if (fabs(V_(i, col)) > 1e-8 * big) { sg = V_(i, col) < 0.0 ? -1.0 : 1.0; break; }
+    for (int i = 1; i <= n; i++) c[(m - 1) * ncf + i] = sg * V_(i, col);
+  }
+#undef A_
+#undef V_
+  free(ord);
+  free(a);
+  free(v);
+  printf(" nombre de determinants   ncf=%9d\n valeurs propres\n", ncf);
+  for (int m = 1; m <= metat; m++) printf(" %12.8f", e[m]);
+  printf("\n");
+}
+
 /* ------------------------------------------------------------- unit 4 */
 /* brdnee.f:38-135 for ntrsy == 1, isz == 0: the signed index itk(k) of the
    spin-flip image of every determinant of S (0 = none) and the sign itm(m)
@@ -2892,7 +2984,6 @@ int main(int argc, char** argv) {
   if (yion) die("yion is not restated");
   if (ybrd && metat > 1) die("ybrd (QDPT heff) is not restated");
   if (lecdet < 2 || lecdet > 5) die("lecdet=%d is not restated", lecdet);
-  if (ityper >= 0 && lecdet != 5) die("ityper>=0 requires lecdet=5 here (no S diagonalisation)");
   if (metat > 60) die("trop d etats demandes en perturbation");
 
   noca = 0; nocb = 0; igela = 0; igelb = 0;
@@ -3033,6 +3124,8 @@ int main(int argc, char** argv) {
      (cip.f:71), which leaves c and e at zero */
   if (ityper < 0) {
     c = (double*)xcalloc((size_t)metat * (size_t)ncf + 4, sizeof(double));
+  } else if (lecdet != 5) {
+    s_space_ci();
   } else {
     FILE* f4 = fopen(n04, "rb");
     if (!f4) die("cannot open unit 4 file %s", n04);
@@ -3070,6 +3163,8 @@ int main(int argc, char** argv) {
     }
     for (int i = 1; i <= ncf; i++) hdiag[i] = hdig(i);
     free(iord60);
+  }
+  if (ityper >= 0) {
     /* degen (brdnee.f:299): rotation of degenerate roots */
     if (metat > 1) {
       int jj = 0;

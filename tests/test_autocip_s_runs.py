@@ -249,7 +249,6 @@ def test_lecdet5_ignores_tdet(tmp_path, engine_lib, oracle_exe):
     ("metat=1, ityper=-1, lecdet=4, numac=2,3,99, noac=3, nelac=2, nusym=1", "numac"),
     ("metat=1, ityper=-1, lecdet=4, numac=2, noac=1, nelac=4, nusym=1", "active"),
     ("metat=1, ityper=-1, lecdet=1", "lecdet"),
-    ("metat=1, ityper=2, lecdet=4, numac=2,3,4,5, noac=4, nelac=2, nusym=1", "lecdet"),
     ("metat=1, ityper=-1, lecdet=5, iord=2,1", "iord"),
 ])
 def test_s_run_rejects_what_it_does_not_support(tmp_path, engine_lib, oracle_exe, body, msg):

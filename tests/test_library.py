@@ -57,14 +57,26 @@ def _golden(tmp_path):
 def test_unsupported_inputs_are_rejected(tmp_path, engine_lib):
     wd = _golden(tmp_path)
     txt = open(os.path.join(wd, "cip.in")).read()
-    for extra, word in [("isz=2", "isz"), ("ninact=1, nonact=3", "ninact"), ("lecdet=2", "lecdet"),
-                        ("ybrd=t, metat=2", None)]:
+    for extra, word in [("isz=2", "isz"), ("ninact=1, nonact=3", "ninact"), ("ybrd=t, metat=2", None)]:
         with open(os.path.join(wd, "cip_bad.in"), "w") as fh:
             fh.write(txt.replace("ymoyen=t", "ymoyen=t, " + extra))
         if word is None:
             continue
         with pytest.raises(cg.CipsiError, match=word):
             cg.run_cip(wd, stdin_path=os.path.join(wd, "cip_bad.in"))
+
+
+def test_s_diagonalisation_needs_the_drop_in(tmp_path, engine_lib):
+    """A perturbation run with lecdet != 5 diagonalises S (ic001.f:81-131)
+    on the GPU inside cipsi_cip_main; the host-only input reader refuses it
+    with that reason instead of running without vectors."""
+    from cipsi_gb300 import engine
+    wd = _golden(tmp_path)
+    txt = open(os.path.join(wd, "cip.in")).read()
+    with open(os.path.join(wd, "cip.in"), "w") as fh:
+        fh.write(txt.replace("lecdet=5", "lecdet=2"))
+    with pytest.raises(cg.CipsiError, match="lecdet != 5"):
+        engine.Inputs(wd)
 
 
 def test_missing_and_corrupt_files_fail_cleanly(tmp_path, engine_lib):
