@@ -406,7 +406,8 @@ def run_moy_form(args, rank: int, world: int, local_rank: int):
 # ------------------------------------------------------------ adjoint form
 def run_adjoint_form(args, rank: int, world: int, local_rank: int):
     """The medium system plus a seeded symmetric dipole matrix mu ~ N(0, 0.5):
-    dE2/dh and dE2/d(pq|rs) from one backward pass, checked against central
+    dE2/dh and dE2/d(pq|rs) from one backward pass (and E2 with dE2/dh from
+    one one-electron adjoint pass), checked against central
     differences (step 1e-5) on `--fd-elements` random integrals and the
     dipole sum mu_pq dE2/dh_pq against finite-field runs at F = +-1e-4
     (integrals in FP64 on the device)."""
@@ -435,7 +436,8 @@ def run_adjoint_form(args, rank: int, world: int, local_rank: int):
     args_e = [x.numpy().copy() for x in S.engine_inputs(torch.as_tensor(h_tri), torch.as_tensor(eri))]
     eng = [args_e[0], args_e[1], args_e[2], eri.copy(), args_e[3], args_e[4], args_e[5], args_e[6]]
     S.run_engine(*[torch.as_tensor(x) for x in eng])  # warm-up (sizes the buffers)
-    fwd_ms, adj_ms = [], []
+    fwd_ms, adj_ms, one_ms = [], [], []
+    e2_fwd = S.run_engine(*[torch.as_tensor(x) for x in eng])
     for _ in range(args.steps):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
@@ -444,6 +446,12 @@ def run_adjoint_form(args, rank: int, world: int, local_rank: int):
         t0 = time.perf_counter()
         g = S.ctx.adjoint(S.opts, seed)  # at the inputs the forward above loaded
         adj_ms.append(1e3 * (time.perf_counter() - t0))
+        t0 = time.perf_counter()
+        e2_1e, g1 = S.ctx.adjoint_1e(S.opts, seed)
+        one_ms.append(1e3 * (time.perf_counter() - t0))
+    # the one-electron pass against the full adjoint and the forward sums
+    one_check = {"max_rel_diff_e2": float(np.max(np.abs(e2_1e - e2_fwd)) / np.max(np.abs(e2_fwd))),
+                 "max_rel_diff_gF": float(np.max(np.abs(g1["F"] - g["F"])) / np.max(np.abs(g["F"])))}
     # finite differences on random integrals the sums depend on
     nz = np.nonzero(g["eri"])[0]
     picks = rng.choice(nz, min(args.fd_elements, len(nz)), replace=False)
@@ -459,7 +467,10 @@ def run_adjoint_form(args, rank: int, world: int, local_rank: int):
     # dipole: one backward pass against two finite-field runs
     def dipole_check(system, h_t, eri_t):
         t0 = time.perf_counter()
-        d_adj = adjoint.dipole(system, h_t, eri_t, mu, seed)
+        d_full = adjoint.dipole(system, h_t, eri_t, mu, seed, one_electron=False)
+        t_full = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        d_adj = adjoint.dipole(system, h_t, eri_t, mu, seed)  # one-electron adjoint pass
         t_dip = time.perf_counter() - t0
         mu_tri = np.zeros_like(h_t)
         mu_tri[adjoint._tri(ti, tj)] = mu[ti, tj]
@@ -473,8 +484,9 @@ def run_adjoint_form(args, rank: int, world: int, local_rank: int):
                 e.append(float((E.numpy() * seed).sum()))
             ff[f"{field:g}"] = (e[0] - e[1]) / (2 * field)
         t_ff = (time.perf_counter() - t0) / 2
-        return {"adjoint": d_adj, "finite_field": ff, "abs_diff_1e-4": abs(d_adj - ff["0.0001"]),
-                "adjoint_s": t_dip, "finite_field_s": t_ff}
+        return {"adjoint": d_adj, "forward_plus_full_backward": d_full, "finite_field": ff,
+                "abs_diff_1e-4": abs(d_adj - ff["0.0001"]), "adjoint_s": t_dip,
+                "forward_plus_full_backward_s": t_full, "finite_field_s": t_ff}
 
     dip = dipole_check(S, h_tri, eri)
     S.close()
@@ -499,6 +511,14 @@ def run_adjoint_form(args, rank: int, world: int, local_rank: int):
             "higher_is_better": False, "dtype": "f64", "data": "synthetic (seeded medium system + dipole)",
             "config": {"workload": "medium (60 MOs, S = 2000, 3 roots), integrals in FP64, seed on e2vp[0]"},
             "forward_ms": statistics.mean(fwd_ms), "adjoint_ms": statistics.mean(adj_ms),
+            "adjoint_1e_ms": statistics.mean(one_ms), "adjoint_1e_check": one_check,
+            # cost of dE2/dh for a field direction, in forward runs: the
+            # one-electron pass (E2 included), a forward plus the full
+            # backward, a central finite difference, ffield.f90's 3-point fit
+            "dipole_cost_in_forward_runs": {
+                "one_electron_adjoint": statistics.mean(one_ms) / statistics.mean(fwd_ms),
+                "forward_plus_full_backward": 1.0 + statistics.mean(adj_ms) / statistics.mean(fwd_ms),
+                "finite_field_central": 2.0, "finite_field_three_point_fit": 3.0},
             "fd_check": {"elements": len(picks), "step": step, "max_rel_err": worst},
             "dipole_medium": dip, "dipole_medium_near_ground_state": dip_w,
             "note": "the medium recipe (random decay-0.9 roots) has EN denominators near zero, so its "

@@ -35,7 +35,7 @@ EXPORTED = [
     "cipsi_inputs_free", "cipsi_selection_raw", "cipsi_run_pt2_static",
     "cipsi_set_tuning", "cipsi_batch_create", "cipsi_batch_run", "cipsi_batch_wait",
     "cipsi_batch_last_error", "cipsi_batch_destroy", "cipsi_inputs_array", "cipsi_set_integrals_f64store",
-    "cipsi_run_pt2_adjoint", "cipsi_set_selection_sink", "cipsi_run_pt2_stream", "cipsi_record_digest",
+    "cipsi_run_pt2_adjoint", "cipsi_run_pt2_adjoint_1e", "cipsi_set_selection_sink", "cipsi_run_pt2_stream", "cipsi_record_digest",
     "cipsi_hamiltonian_build", "cipsi_hamiltonian_get", "cipsi_hamiltonian_ms", "cipsi_moy_main",
     "cipsi_davidson", "cipsi_bd_main",
 ]

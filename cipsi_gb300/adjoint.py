@@ -20,8 +20,11 @@ and (pq|rs):
 with i over the doubly occupied orbitals.  The S coefficients and the
 absolute root energies (file 59) are held fixed, as a finite-field cip run
 that reuses the bd vectors does.  A dipole-like property
-sum_pq mu_pq dE2/dh_pq is then one backward pass instead of two cip runs at
-h +- F mu.
+sum_pq mu_pq dE2/dh_pq is then one pass of the one-electron adjoint
+(`System.grad_h`: E2 and dE2/dh together, about the cost of one forward
+run) instead of the cip runs at h +- F mu (two for a central difference,
+three or more for the quadratic fit of Autocip_13/ffield.f90:66-127), and
+gives every field direction at once.
 """
 from __future__ import annotations
 
@@ -182,6 +185,22 @@ class System:
         self.load(F, J, K, eri, fmpb, e, eb, emp)
         return self.ctx.adjoint(self.opts, seed)
 
+    def grad_h(self, h_tri, eri, seed) -> tuple:
+        """E2 sums [3, metat] and dL/dh (packed lower triangle) with
+        L = sum(seed * E2), from one one-electron adjoint pass
+        (cipsi_run_pt2_adjoint_1e): the (pq|rs) are held fixed, so their
+        gradient is not formed, and the pass costs about one forward run."""
+        h = torch.tensor(np.asarray(h_tri, np.float64), requires_grad=True)
+        eri_t = torch.as_tensor(eri, dtype=torch.float64)
+        outs = self.engine_inputs(h, eri_t)  # F, J, K, fmpb, e, eb, emp
+        self.load(outs[0], outs[1], outs[2], eri_t, *outs[3:])
+        e2, g = self.ctx.adjoint_1e(self.opts, seed)
+        grads = [torch.as_tensor(g[k], dtype=torch.float64) for k in ("F", "J", "K", "fmpb", "e", "eb", "emp")]
+        # J and K come from (pq|rs) alone: they do not depend on h
+        pairs = [(o, gr) for o, gr in zip(outs, grads) if o.requires_grad]
+        torch.autograd.backward([o for o, _ in pairs], [gr for _, gr in pairs])
+        return e2, h.grad.numpy().copy()
+
     def close(self):
         if self._ctx is not None:
             self._ctx.close()
@@ -208,17 +227,23 @@ class E2Function(torch.autograd.Function):
 
 
 def dipole(system: System, h_tri: np.ndarray, eri: np.ndarray, mu: np.ndarray,
-           seed: Optional[np.ndarray] = None) -> float:
+           seed: Optional[np.ndarray] = None, one_electron: bool = True) -> float:
     """sum_pq mu_pq dL/dh_pq with L = sum seed * [e2mp; e2vp; e2b] (default:
-    e2vp of root 1), one forward and one backward pass; mu full symmetric."""
+    e2vp of root 1); mu full symmetric.  one_electron: one pass of the
+    one-electron adjoint (System.grad_h); otherwise a forward and a full
+    backward pass through E2Function (which also forms dL/d(pq|rs))."""
     mt = system.dims.metat
     if seed is None:
         seed = np.zeros((3, mt))
         seed[1, 0] = 1.0
-    h = torch.tensor(h_tri, dtype=torch.float64, requires_grad=True)
-    E = system.e2(h, torch.as_tensor(eri, dtype=torch.float64))
-    (E * torch.as_tensor(seed)).sum().backward()
+    if one_electron:
+        _, gh = system.grad_h(h_tri, eri, seed)
+    else:
+        h = torch.tensor(h_tri, dtype=torch.float64, requires_grad=True)
+        E = system.e2(h, torch.as_tensor(eri, dtype=torch.float64))
+        (E * torch.as_tensor(seed)).sum().backward()
+        gh = h.grad.numpy()
     n = system.dims.norb
     ti, tj = np.tril_indices(n)
     # the field h -> h + F mu moves the packed element of (i >= j) by F mu_ij
-    return float((h.grad.numpy()[_tri(ti, tj)] * mu[ti, tj]).sum())
+    return float((gh[_tri(ti, tj)] * mu[ti, tj]).sum())

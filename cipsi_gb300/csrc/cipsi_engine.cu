@@ -1658,12 +1658,16 @@ int cipsi_record_digest(void* user, int64_t first, int64_t count, int32_t words,
   return 0;
 }
 
-int cipsi_run_pt2_adjoint(cipsi_ctx* ctx, const cipsi_opts* o, const double* seed, double* gF,
-                          double* gJ, double* gK, double* geri, double* gfmpb, double* groots) {
-  int rc = check_run_args(ctx, o);
-  if (rc) return rc;
-  if (!seed || !gF || !gJ || !gK || !geri || !gfmpb || !groots)
-    return fail(ctx, CIPSI_ERR_ARG, "run_pt2_adjoint: null seed or gradient array");
+}  // extern "C"
+
+namespace {
+
+// The adjoint launch behind cipsi_run_pt2_adjoint (geri given) and
+// cipsi_run_pt2_adjoint_1e (geri null: no (pq|rs) gradient, the second pass
+// over singles only).  e2, when given, receives the E2 sums of the same pass.
+int run_adjoint(cipsi_ctx* ctx, const cipsi_opts* o, const double* seed, double* e2, double* gF, double* gJ,
+                double* gK, double* geri, double* gfmpb, double* groots) {
+  int rc = 0;
   if (ctx->pending) return fail(ctx, CIPSI_ERR_STATE, "an asynchronous run is pending: fetch its result first");
   CK(cudaSetDevice(ctx->device));
   const int ncf = ctx->d.ncf, W = ctx->W, mt = ctx->d.metat, n = ctx->d.norb;
@@ -1698,14 +1702,16 @@ int cipsi_run_pt2_adjoint(cipsi_ctx* ctx, const cipsi_opts* o, const double* see
     release();
     return fail(ctx, CIPSI_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
   };
-  if ((rc = ck(cudaMalloc(&d_eri, (size_t)ctx->ninte * sizeof(double)), "cudaMalloc"))) return rc;
+  const bool one_e = geri == nullptr;
+  if (!one_e && (rc = ck(cudaMalloc(&d_eri, (size_t)ctx->ninte * sizeof(double)), "cudaMalloc"))) return rc;
   if ((rc = ck(cudaMalloc(&d_F, (size_t)nt * sizeof(double)), "cudaMalloc"))) return rc;
   if ((rc = ck(cudaMalloc(&d_J, (size_t)nt * sizeof(double)), "cudaMalloc"))) return rc;
   if ((rc = ck(cudaMalloc(&d_K, (size_t)nt * sizeof(double)), "cudaMalloc"))) return rc;
   if ((rc = ck(cudaMalloc(&d_f, (size_t)2 * n * sizeof(double)), "cudaMalloc"))) return rc;
   if ((rc = ck(cudaMalloc(&d_sl, (size_t)grid * stride * sizeof(double)), "cudaMalloc"))) return rc;
   if ((rc = ck(cudaMalloc(&d_roots, (size_t)3 * mt * sizeof(double)), "cudaMalloc"))) return rc;
-  if ((rc = ck(cudaMemsetAsync(d_eri, 0, (size_t)ctx->ninte * sizeof(double), ctx->stream), "memset"))) return rc;
+  if (!one_e && (rc = ck(cudaMemsetAsync(d_eri, 0, (size_t)ctx->ninte * sizeof(double), ctx->stream), "memset")))
+    return rc;
   if ((rc = ck(cudaMemsetAsync(d_F, 0, (size_t)nt * sizeof(double), ctx->stream), "memset"))) return rc;
   if ((rc = ck(cudaMemsetAsync(d_sl, 0, (size_t)grid * stride * sizeof(double), ctx->stream), "memset"))) return rc;
   if ((rc = ck(cudaMemsetAsync(d_roots, 0, (size_t)3 * mt * sizeof(double), ctx->stream), "memset"))) return rc;
@@ -1728,6 +1734,7 @@ int cipsi_run_pt2_adjoint(cipsi_ctx* ctx, const cipsi_opts* o, const double* see
   p.g_slice = d_sl;
   p.slice_stride = stride;
   p.g_roots = d_roots;
+  p.adj_1e = one_e ? 1 : 0;
   if (nunits > 0) {
     cudaError_t e;
     if (W == 1) {
@@ -1742,6 +1749,9 @@ int cipsi_run_pt2_adjoint(cipsi_ctx* ctx, const cipsi_opts* o, const double* see
                  : launch_pt2<2, 8, false, true>(p, BatchArgs{}, grid, ls.smem, ctx->stream);
     }
     if ((rc = ck(e, "adjoint k_pt2 launch"))) return rc;
+    k_reduce<<<(unsigned)nq, kReduceThreads, 0, ctx->stream>>>(ctx->dgen_part, nunits, (int)nq, ctx->dred);
+  } else {
+    if ((rc = ck(cudaMemsetAsync(ctx->dred, 0, nq * sizeof(double), ctx->stream), "memset"))) return rc;
   }
   k_slice_reduce<<<(stride + 255) / 256, 256, 0, ctx->stream>>>(d_sl, grid, stride, nt, d_F, d_J, d_K, d_f);
   if ((rc = ck(cudaGetLastError(), "k_slice_reduce"))) return rc;
@@ -1750,14 +1760,37 @@ int cipsi_run_pt2_adjoint(cipsi_ctx* ctx, const cipsi_opts* o, const double* see
     const double* dev;
     size_t n;
   } outs[] = {{geri, d_eri, (size_t)ctx->ninte}, {gF, d_F, (size_t)nt}, {gJ, d_J, (size_t)nt},
-              {gK, d_K, (size_t)nt}, {gfmpb, d_f, (size_t)2 * n}, {groots, d_roots, (size_t)3 * mt}};
+              {gK, d_K, (size_t)nt}, {gfmpb, d_f, (size_t)2 * n}, {groots, d_roots, (size_t)3 * mt},
+              {e2, ctx->dred, (size_t)3 * mt}};
   for (const Out& x : outs)
-    if ((rc = ck(cudaMemcpyAsync(x.host, x.dev, x.n * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream),
-                 "copy gradients")))
+    if (x.host && (rc = ck(cudaMemcpyAsync(x.host, x.dev, x.n * sizeof(double), cudaMemcpyDeviceToHost,
+                                           ctx->stream), "copy gradients")))
       return rc;
   if ((rc = ck(cudaStreamSynchronize(ctx->stream), "adjoint run"))) return rc;
   release();
   return CIPSI_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int cipsi_run_pt2_adjoint(cipsi_ctx* ctx, const cipsi_opts* o, const double* seed, double* gF,
+                          double* gJ, double* gK, double* geri, double* gfmpb, double* groots) {
+  const int rc = check_run_args(ctx, o);
+  if (rc) return rc;
+  if (!seed || !gF || !gJ || !gK || !geri || !gfmpb || !groots)
+    return fail(ctx, CIPSI_ERR_ARG, "run_pt2_adjoint: null seed or gradient array");
+  return run_adjoint(ctx, o, seed, nullptr, gF, gJ, gK, geri, gfmpb, groots);
+}
+
+int cipsi_run_pt2_adjoint_1e(cipsi_ctx* ctx, const cipsi_opts* o, const double* seed, double* e2, double* gF,
+                             double* gJ, double* gK, double* gfmpb, double* groots) {
+  const int rc = check_run_args(ctx, o);
+  if (rc) return rc;
+  if (!seed || !e2 || !gF || !gJ || !gK || !gfmpb || !groots)
+    return fail(ctx, CIPSI_ERR_ARG, "run_pt2_adjoint_1e: null seed, energy or gradient array");
+  return run_adjoint(ctx, o, seed, e2, gF, gJ, gK, nullptr, gfmpb, groots);
 }
 
 int cipsi_selection_raw(cipsi_ctx* ctx, int64_t first, int64_t count, uint64_t* bits,

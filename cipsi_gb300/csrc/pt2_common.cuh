@@ -110,6 +110,9 @@ struct Params {
   double* g_slice;  // per block: [F | J | K] packed triangles, then fmpb[2n]
   int slice_stride; // doubles per block slice (3 n(n+1)/2 + 2n)
   double* g_roots;  // 3 x metat: dE/d e, d eb, d emp
+  // one-electron adjoint: no (pq|rs) gradient (g_eri unused), so only the
+  // single-excitation elements (their F term) take part in the second pass
+  int adj_1e;
 };
 
 static_assert(sizeof(Params) % sizeof(int) == 0, "Params is copied as ints");

@@ -241,9 +241,11 @@ __device__ __forceinline__ double hmat(const Params& p, const uint64_t* u, const
 
 // Adjoint of hmat: adds w * d<I|H|J>/d(integral) to the gradients (F
 // off-diagonal terms to g_F, (pq|rs) to g_eri), same cases and phases.
+// with_eri false: the F term only (one-electron adjoint; two-difference
+// elements then add nothing).
 template <int W>
 __device__ void hmat_adj(const Params& p, const uint64_t* u, const uint64_t* v, int rankI, int rankJ,
-                         const uint64_t* hf, double w) {
+                         const uint64_t* hf, double w, bool with_eri) {
   if (w == 0.0) return;
   uint64_t remv[2 * W], addv[2 * W];
   int nrem[2] = {0, 0};
@@ -265,6 +267,7 @@ __device__ void hmat_adj(const Params& p, const uint64_t* u, const uint64_t* v, 
     const int lo = pp < qq ? pp : qq, hi = pp < qq ? qq : pp;
     const double sw = (popc_between<W>(vs, lo, hi) & 1) ? -w : w;
     atomicAdd(&p.g_F[tri(pp, qq)], sw);
+    if (!with_eri) return;
     const bool dI = rankI > rankJ;
     uint64_t D[2 * W];
 #pragma unroll
@@ -291,6 +294,7 @@ __device__ void hmat_adj(const Params& p, const uint64_t* u, const uint64_t* v, 
     }
     return;
   }
+  if (!with_eri) return;
   if (nrem[0] == 1 && nrem[1] == 1) {
     const int pa = first_bit<W>(remv), qa = first_bit<W>(addv);
     const int pb = first_bit<W>(remv + W), qb = first_bit<W>(addv + W);
@@ -315,14 +319,32 @@ __device__ void hmat_adj(const Params& p, const uint64_t* u, const uint64_t* v, 
   ai_adj(p, p1, q2, p2, q1, -sw);
 }
 
+// E2 sums of one thread, Kahan-compensated, and its counters
+template <int R>
+struct Acc {
+  double e2mp[R], cmp[R], e2vp[R], cvp[R], e2b[R], cb[R], psimp[R], psivp[R];
+  unsigned long long ietat, nproc;
+  double dpivot;
+  __device__ void zero() {
+#pragma unroll
+    for (int m = 0; m < R; ++m) {
+      e2mp[m] = cmp[m] = e2vp[m] = cvp[m] = e2b[m] = cb[m] = psimp[m] = psivp[m] = 0.0;
+    }
+    ietat = nproc = 0ull;
+    dpivot = 0.0;
+  }
+};
+
 // Per-perturber derivative factors of the E2 sums (pert1.f:151-191):
 //   t_mp = b^2/(emp - hmp), t_vp = b^2/(e - hdig), t_b = b^2/(eb - hdig),
 // each weighted by wgt; gb[m] = dE/db_m, gh = dE/dhdig, gm = dE/dhmp, and
-// the root-energy gradients accumulated into gr[3][R] (e, eb, emp).
+// the root-energy gradients accumulated into gr[3][R] (e, eb, emp).  The
+// terms themselves go to acc (the forward's E2 sums and norms, from the same
+// quotients b/d).
 template <int R>
 __device__ __forceinline__ void adj_factors(const Params& p, const double* bc, double hmpi, double hvpi,
                                             double wgt, double* gb, double& gh, double& gm,
-                                            double (*gr)[R]) {
+                                            double (*gr)[R], Acc<R>& acc) {
   gh = 0.0;
   gm = 0.0;
 #pragma unroll
@@ -330,19 +352,24 @@ __device__ __forceinline__ void adj_factors(const Params& p, const double* bc, d
     gb[m] = 0.0;
     if (m >= p.metat) continue;
     const double b = bc[m];
-    const double dmp = p.emp[m] - hmpi;
-    const double tmp = wgt * p.seed_mp[m] * (b / dmp) * (b / dmp);
-    gb[m] = wgt * p.seed_mp[m] * 2.0 * b / dmp;
+    const double qmp = b / (p.emp[m] - hmpi);
+    const double tmp = wgt * p.seed_mp[m] * qmp * qmp;
+    gb[m] = wgt * p.seed_mp[m] * (2.0 * qmp);
     gm += tmp;
     gr[2][m] -= tmp;
+    kahan_add(acc.e2mp[m], acc.cmp[m], (b * qmp) * wgt);
+    acc.psimp[m] = fma(qmp * qmp, wgt, acc.psimp[m]);
     if (p.yen) {
-      const double dvp = p.e[m] - hvpi, db = p.eb[m] - hvpi;
-      const double tv = wgt * p.seed_vp[m] * (b / dvp) * (b / dvp);
-      const double tb = wgt * p.seed_b[m] * (b / db) * (b / db);
-      gb[m] += wgt * (p.seed_vp[m] * 2.0 * b / dvp + p.seed_b[m] * 2.0 * b / db);
+      const double qvp = b / (p.e[m] - hvpi), qb = b / (p.eb[m] - hvpi);
+      const double tv = wgt * p.seed_vp[m] * qvp * qvp;
+      const double tb = wgt * p.seed_b[m] * qb * qb;
+      gb[m] += wgt * (p.seed_vp[m] * (2.0 * qvp) + p.seed_b[m] * (2.0 * qb));
       gh += tv + tb;
       gr[0][m] -= tv;
       gr[1][m] -= tb;
+      kahan_add(acc.e2vp[m], acc.cvp[m], (b * qvp) * wgt);
+      kahan_add(acc.e2b[m], acc.cb[m], (b * qb) * wgt);
+      acc.psivp[m] = fma(qvp * qvp, wgt, acc.psivp[m]);
     }
   }
 }
@@ -533,21 +560,6 @@ __device__ int2 ordered_partition2(int n, Part part, Emit emit, int* warp_tmp /*
   __syncthreads();
   return make_int2(n0, n1);
 }
-
-template <int R>
-struct Acc {
-  double e2mp[R], cmp[R], e2vp[R], cvp[R], e2b[R], cb[R], psimp[R], psivp[R];
-  unsigned long long ietat, nproc;
-  double dpivot;
-  __device__ void zero() {
-#pragma unroll
-    for (int m = 0; m < R; ++m) {
-      e2mp[m] = cmp[m] = e2vp[m] = cvp[m] = e2b[m] = cb[m] = psimp[m] = psivp[m] = 0.0;
-    }
-    ietat = nproc = 0ull;
-    dpivot = 0.0;
-  }
-};
 
 // Counters of the candidate scan.  Kept apart from Acc: Acc is passed by
 // reference to the out-of-line queue drain, so it lives in local memory,
@@ -1107,7 +1119,9 @@ __global__ void __launch_bounds__(kThreads, 2) k_pt2(Params p0, BatchArgs ba) {
         if (ADJ) {
           if (live) {
             double gb[R], gh, gm;
-            adj_factors<R>(p, bc, hmpi, hvpi, 1.0, gb, gh, gm, adjr);
+            adj_factors<R>(p, bc, hmpi, hvpi, 1.0, gb, gh, gm, adjr, acc);
+            acc.ietat += 1;
+            acc.nproc += 1;
             int rankI = 0;
 #pragma unroll
             for (int q = 0; q < 2 * W; ++q) rankI += __popcll(hf[q] & ~u[q]);
@@ -1120,7 +1134,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_pt2(Params p0, BatchArgs ba) {
                 vv[q] = __ldg(&v[q]);
                 x += __popcll(u[q] ^ vv[q]);
               }
-              if (x > 4 || x == 0) continue;
+              if (x > 4 || x == 0 || (p.adj_1e && x == 4)) continue;
               int rankJ = 0;
 #pragma unroll
               for (int q = 0; q < 2 * W; ++q) rankJ += __popcll(hf[q] & ~vv[q]);
@@ -1128,7 +1142,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_pt2(Params p0, BatchArgs ba) {
 #pragma unroll
               for (int m = 0; m < R; ++m)
                 if (m < p.metat) w += gb[m] * __ldg(&p.c[(size_t)j * p.metat + m]);
-              hmat_adj<W>(p, u, vv, rankI, rankJ, hf, w);
+              hmat_adj<W>(p, u, vv, rankI, rankJ, hf, w, !p.adj_1e);
             }
             diag_terms_adj<W>(p, u, hf, p.yen ? gh : 0.0, gm, adj_sl);
           }
@@ -1420,6 +1434,9 @@ __global__ void __launch_bounds__(kThreads, 2) k_pt2(Params p0, BatchArgs ba) {
         bool drop = !live;
         int nh = 0;
         int* hl = hitl + threadIdx.x * kHitCap;
+        // adjoint: the first two one-difference partners j (and their count),
+        // for the one-electron second pass
+        int s1n = 0, s1j0 = 0, s1j1 = 0;
         const int rankI = rank_k + D;
         const bool two = a2 >= 0;
         const uint32_t c1x4 = live ? (uint32_t)(a1 + sa1 * p.norb) * 0x01010101u : 0u;
@@ -1458,6 +1475,11 @@ __global__ void __launch_bounds__(kThreads, 2) k_pt2(Params p0, BatchArgs ba) {
               int kind;
               const double h = hmat<W>(p, u, vv, rankI, rankJ, hf, kind);
               if (kind == 1) sc.np1++; else sc.np2++;
+              if (ADJ && kind == 1) {
+                s1j1 = s1n == 1 ? j : s1j1;
+                s1j0 = s1n == 0 ? j : s1j0;
+                ++s1n;
+              }
               ++nint;
               if (h != 0.0) ++nnz;
               if (j > k && j <= k + nespk) ++lesp;
@@ -1540,7 +1562,9 @@ __global__ void __launch_bounds__(kThreads, 2) k_pt2(Params p0, BatchArgs ba) {
 #pragma unroll
           for (int m = 0; m < R; ++m) gb[m] = 0.0;
           if (live) {
-            adj_factors<R>(p, bc, hmpi, hvpi, ybis ? 1.0 + fmul : 1.0, gb, gh, gm, adjr);
+            adj_factors<R>(p, bc, hmpi, hvpi, ybis ? 1.0 + fmul : 1.0, gb, gh, gm, adjr, acc);
+            acc.ietat += (unsigned long long)(long long)(nmul + 1);
+            acc.nproc += 1;
             if (!p.yen) gh = 0.0;
           }
           // second pass over the same entries: dE/dH_Ij = sum_m gb[m] c_jm,
@@ -1549,46 +1573,55 @@ __global__ void __launch_bounds__(kThreads, 2) k_pt2(Params p0, BatchArgs ba) {
           // the warp takes the t-th listed entry of every lane at once, so
           // hmat_adj runs with the warp in step instead of once per hitting
           // lane.  The loops are warp-uniform (nscan, nrb); dead lanes list
-          // nothing.
-          const int rankI = rank_k + D;
+          // nothing.  One-electron adjoint: only the one-difference partners
+          // matter; those the first pass noted (up to two) are done here,
+          // and the scan runs only for lanes with more.
+          const bool with_eri = !p.adj_1e;
+          const bool rescan = live && (with_eri || s1n > 2);
+          const auto adj_one = [&](int j) {
+            uint64_t vv[2 * W];
+#pragma unroll
+            for (int q = 0; q < 2 * W; ++q) vv[q] = __ldg(&p.S[(size_t)j * 2 * W + q]);
+            int rankJ = 0;
+#pragma unroll
+            for (int q = 0; q < 2 * W; ++q) rankJ += __popcll(hf[q] & ~vv[q]);
+            double w = 0.0;
+#pragma unroll
+            for (int m = 0; m < R; ++m)
+              if (m < p.metat) w += gb[m] * __ldg(&p.c[(size_t)j * p.metat + m]);
+            hmat_adj<W>(p, u, vv, rank_k + D, rankJ, hf, w, with_eri);
+          };
+          if (!with_eri && live && s1n <= 2) {
+            if (s1n > 0) adj_one(s1j0);
+            if (s1n > 1) adj_one(s1j1);
+          }
           const bool two = a2 >= 0;
-          const uint32_t c1x4 = live ? (uint32_t)(a1 + sa1 * p.norb) * 0x01010101u : 0u;
-          const uint32_t c2x4 = live && two ? (uint32_t)(a2 + sa2 * p.norb) * 0x01010101u : 0u;
+          const uint32_t c1x4 = rescan ? (uint32_t)(a1 + sa1 * p.norb) * 0x01010101u : 0u;
+          const uint32_t c2x4 = rescan && two ? (uint32_t)(a2 + sa2 * p.norb) * 0x01010101u : 0u;
+          const int xmax = with_eri ? 4 : 2;
           int nh = 0;
           int* hl = hitl + threadIdx.x * kHitCap;
           auto note = [&](int i) {
             const int x = lr_diff(ent_at(i), c1x4, c2x4, two);
-            if (x <= 4 && x != 0 && lr_entry_j(ent_at(i)) >= k) hl[nh++] = i;
+            if (x <= xmax && x != 0 && lr_entry_j(ent_at(i)) >= k) hl[nh++] = i;
           };
           auto flush_adj = [&]() {
             const int maxh = __reduce_max_sync(0xffffffffu, nh);
-            for (int t = 0; t < maxh; ++t) {
-              if (t < nh) {
-                const int j = lr_entry_j(ent_at(hl[t]));
-                uint64_t vv[2 * W];
-#pragma unroll
-                for (int q = 0; q < 2 * W; ++q) vv[q] = __ldg(&p.S[(size_t)j * 2 * W + q]);
-                int rankJ = 0;
-#pragma unroll
-                for (int q = 0; q < 2 * W; ++q) rankJ += __popcll(hf[q] & ~vv[q]);
-                double w = 0.0;
-#pragma unroll
-                for (int m = 0; m < R; ++m)
-                  if (m < p.metat) w += gb[m] * __ldg(&p.c[(size_t)j * p.metat + m]);
-                hmat_adj<W>(p, u, vv, rankI, rankJ, hf, w);
-              }
-            }
+            for (int t = 0; t < maxh; ++t)
+              if (t < nh) adj_one(lr_entry_j(ent_at(hl[t])));
             nh = 0;
           };
-          for (int i = 0; i < nscan; ++i) {
-            if (__any_sync(0xffffffffu, nh == kHitCap)) flush_adj();
-            if (live) note(i);
+          if (__any_sync(0xffffffffu, rescan)) {
+            for (int i = 0; i < nscan; ++i) {
+              if (__any_sync(0xffffffffu, nh == kHitCap)) flush_adj();
+              if (rescan) note(i);
+            }
+            for (int q2 = 0; q2 < nrb; ++q2) {
+              if (__any_sync(0xffffffffu, nh == kHitCap)) flush_adj();
+              if (rescan) note(rb[q2]);
+            }
+            flush_adj();
           }
-          for (int q2 = 0; q2 < nrb; ++q2) {
-            if (__any_sync(0xffffffffu, nh == kHitCap)) flush_adj();
-            if (live) note(rb[q2]);
-          }
-          flush_adj();
           if (!live) return;
           // diagonal terms: hdig(I) = hdig(K') + vdg[a1] + vdg[a2] + G(a1,a2),
           // hmp(I) = hmp(K') + fmpb[a1] + fmpb[a2]

@@ -119,6 +119,7 @@ def _lib():
         "cipsi_set_integrals_f64store": ([P, P, P, P, P, P, P, P, P, ctypes.c_int64], ctypes.c_int),
         "cipsi_set_roots": ([P, P, P, P, P, P, P, P], ctypes.c_int),
         "cipsi_run_pt2_adjoint": ([P, ctypes.POINTER(Opts), P, P, P, P, P, P, P], ctypes.c_int),
+        "cipsi_run_pt2_adjoint_1e": ([P, ctypes.POINTER(Opts), P, P, P, P, P, P, P], ctypes.c_int),
         "cipsi_run_pt2_stream": ([P, ctypes.POINTER(Opts), ctypes.c_int64, P, P, ctypes.POINTER(Result)],
                                  ctypes.c_int),
     }
@@ -263,6 +264,24 @@ class Context:
         r = out.pop("roots")
         out["e"], out["eb"], out["emp"] = r[:mt], r[mt:2 * mt], r[2 * mt:]
         return out
+
+    def adjoint_1e(self, opts: Opts, seed) -> tuple:
+        """E2 sums [3, metat] and the gradients of sum(seed * E2) except the
+        (pq|rs) one, from one pass (cipsi_run_pt2_adjoint_1e)."""
+        n, mt = self.dims.norb, self.dims.metat
+        nt = n * (n + 1) // 2
+        seed = np.ascontiguousarray(np.asarray(seed, np.float64).reshape(3 * mt))
+        e2 = np.zeros(3 * mt)
+        out = {"F": np.zeros(nt), "J": np.zeros(nt), "K": np.zeros(nt), "fmpb": np.zeros(2 * n),
+               "roots": np.zeros(3 * mt)}
+        o = Opts.from_buffer_copy(opts)
+        self._check(self.lib.cipsi_run_pt2_adjoint_1e(
+            self._c, ctypes.byref(o), seed.ctypes.data, e2.ctypes.data, out["F"].ctypes.data,
+            out["J"].ctypes.data, out["K"].ctypes.data, out["fmpb"].ctypes.data, out["roots"].ctypes.data),
+            "run_pt2_adjoint_1e")
+        r = out.pop("roots")
+        out["e"], out["eb"], out["emp"] = r[:mt], r[mt:2 * mt], r[2 * mt:]
+        return e2.reshape(3, mt), out
 
     def upload(self, inp: Inputs):
         self._check(self.lib.cipsi_inputs_upload(inp._h, self._c), "inputs_upload")

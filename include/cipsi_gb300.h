@@ -299,6 +299,19 @@ int cipsi_set_integrals_f64store(cipsi_ctx* ctx, const int32_t* itsym, const int
 int cipsi_run_pt2_adjoint(cipsi_ctx* ctx, const cipsi_opts* opts, const double* seed, double* gF,
                           double* gJ, double* gK, double* geri, double* gfmpb, double* groots);
 
+/* One-electron adjoint (no counterpart in the reference): the E2 sums and
+   the gradients of cipsi_run_pt2_adjoint except the (pq|rs) one, from one
+   pass.  e2 [3 metat] receives [e2mp; e2vp; e2b] as cipsi_run_pt2 computes
+   them (the same terms; the rounding of a sum may differ in the last bits);
+   gF, gJ, gK, gfmpb, groots are complete (J and K enter only hdig, F the
+   diagonal terms and the one-difference elements).  Without the (pq|rs)
+   gradient the second pass visits only the pairs one excitation apart, so
+   the call costs about one forward run: a perturbation h -> h + F mu of the
+   one-electron operator (the finite-field runs of Autocip_13/ffield.f90:66-127)
+   needs gF, the fmpb gradient and the root-energy gradients only. */
+int cipsi_run_pt2_adjoint_1e(cipsi_ctx* ctx, const cipsi_opts* opts, const double* seed, double* e2,
+                             double* gF, double* gJ, double* gK, double* gfmpb, double* groots);
+
 /* Batched form: the runs of many contexts (the geometries of an Autocip
    grid, of different sizes) in one persistent launch per class of contexts
    with the same string width (norb <= 64 or not) and padded root count,

@@ -90,8 +90,32 @@ def test_adjoint_matches_finite_differences(tmp_path, engine_lib, cfg):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("cfg", [SMALL_WELL, MIX_SYM], ids=["small", "sym2"])
+def test_one_electron_adjoint_matches_full(tmp_path, engine_lib, cfg):
+    """cipsi_run_pt2_adjoint_1e: its E2 sums are the forward run's and its
+    F, J, K, fmpb and root-energy gradients the full adjoint's (FP64 atomics
+    add in a run-dependent order: equal to rounding)."""
+    S, h_tri, eri, _ = make_system(tmp_path, cfg)
+    vals = [x.numpy().copy() for x in S.engine_inputs(torch.as_tensor(h_tri), torch.as_tensor(eri))]
+    F, J, K, fmpb, e, eb, emp = vals
+    args = [F, J, K, eri.copy(), fmpb, e, eb, emp]
+    fwd = S.run_engine(*[torch.as_tensor(x) for x in args])
+    mt = S.dims.metat
+    seed = np.random.default_rng(5).normal(size=(3, mt))
+    full = S.adjoint_at(*args, seed)
+    S.load(*args)
+    e2, one = S.ctx.adjoint_1e(S.opts, seed)
+    np.testing.assert_allclose(e2, fwd, rtol=1e-12, atol=1e-16)
+    for k in ("F", "J", "K", "fmpb", "e", "eb", "emp"):
+        scale = max(np.abs(full[k]).max(), 1e-300)
+        np.testing.assert_allclose(one[k], full[k], rtol=0, atol=1e-12 * scale, err_msg=k)
+    S.close()
+
+
+@pytest.mark.gpu
 def test_dipole_matches_finite_field(tmp_path, engine_lib):
-    """sum mu_pq dE2/dh_pq (one backward pass) against cip-style runs at
+    """sum mu_pq dE2/dh_pq (one one-electron adjoint pass, and a forward plus
+    a full backward pass) against cip-style runs at
     h +- F mu with F, J, K, E_HF and the zero-order sums regenerated."""
     S, h_tri, eri, _ = make_system(tmp_path, SMALL_WELL)
     n = S.dims.norb
@@ -100,7 +124,9 @@ def test_dipole_matches_finite_field(tmp_path, engine_lib):
     mu = 0.5 * (mu + mu.T)
     seed = np.zeros((3, S.dims.metat))
     seed[1, 0] = 1.0  # e2vp of the first root
-    d_adj = adjoint.dipole(S, h_tri, eri, mu, seed)
+    d_adj = adjoint.dipole(S, h_tri, eri, mu, seed)  # one-electron adjoint pass
+    d_full = adjoint.dipole(S, h_tri, eri, mu, seed, one_electron=False)
+    assert abs(d_adj - d_full) <= 1e-11 * max(1.0, abs(d_full)), (d_adj, d_full)
     ti, tj = np.tril_indices(n)
     mu_tri = np.zeros_like(h_tri)
     mu_tri[adjoint._tri(ti, tj)] = mu[ti, tj]
