@@ -28,12 +28,16 @@ Steps, as calcul.f90 orders them (imax_s > 0, the CIPSI method):
   moy with TAU = tau and bd on the end namelist: the final S + M space.
 With imax_s <= 0 (the FCI method): cipsym once on the first namelist, then
 moy and bd on the end namelist.
+
+run_grid runs calcul_cip over the points of a grid on a pool of threads, as
+the reference's OpenMP loop over grid points does (autocip13.f90:525-640).
 """
 from __future__ import annotations
 
 import os
 import re
 import struct
+from concurrent.futures import ThreadPoolExecutor
 from typing import Dict, List, Optional, Sequence
 
 import numpy as np
@@ -151,3 +155,45 @@ def calcul_cip(workdir: str, f_bd: str, metat: int, netat_pertu: int, envp_max: 
         bd = call("bd", text)
     return {"e_corr": [abs(float(x)) for x in energ2[:metat]] + [0.0] * max(0, metat - len(energ2)),
             "nbase": nbase, "ncf": bd["ncf"], "tau": tau, "steps": len(steps)}
+
+
+def run_grid(points: Sequence[Dict], workers: int = 4, device: int = 0,
+             logs: Optional[List] = None) -> List[Dict]:
+    """The loop over the points of an Autocip grid for the CIPSI step
+    (Autocip_13/autocip13.f90:525-640: an OpenMP loop with
+    SCHEDULE(DYNAMIC), one work directory per thread, calcul_cip per point).
+
+    points: one dict of calcul_cip keyword arguments per point (workdir,
+    f_bd, metat, netat_pertu, envp_max, det_bounds, imax_s, tau_init,
+    tau_step[, ncf, device]); each point needs its own work directory.
+    `workers` threads take the points in order as they become free.  The
+    engine library releases the interpreter lock during its calls, and each
+    call's context runs on its own stream.  One point's host steps
+    (namelists, unit files, the S build, moy's lists) therefore overlap
+    other points' GPU work.
+
+    Returns one result per point, in point order: calcul_cip's dict, or
+    {"error": message} for a point whose chain stopped (the reference marks
+    such a point as not accepted and carries on with the others).  `logs`,
+    if given, is filled with each point's step log."""
+    dirs = [os.path.abspath(pt["workdir"]) for pt in points]
+    if len(set(dirs)) != len(dirs):
+        raise ValueError("run_grid: every point needs its own work directory")
+    results: List[Optional[Dict]] = [None] * len(points)
+    if logs is not None:
+        logs[:] = [None] * len(points)
+
+    def one(i: int) -> None:
+        kw = dict(points[i])
+        kw.setdefault("device", device)
+        log: List[Dict] = []
+        try:
+            results[i] = calcul_cip(log=log, **kw)
+        except CipsiError as e:
+            results[i] = {"error": str(e)}
+        if logs is not None:
+            logs[i] = log
+
+    with ThreadPoolExecutor(max_workers=max(1, int(workers))) as ex:
+        list(ex.map(one, range(len(points))))
+    return results

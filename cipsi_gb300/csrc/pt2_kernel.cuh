@@ -352,7 +352,25 @@ __device__ __forceinline__ void adj_factors(const Params& p, const double* bc, d
     gb[m] = 0.0;
     if (m >= p.metat) continue;
     const double b = bc[m];
-    const double qmp = b / (p.emp[m] - hmpi);
+    const double dmp = p.emp[m] - hmpi;
+    double qmp, qvp = 0.0, qb = 0.0;
+    if (p.yen) {
+      // one division for the three quotients, as in the forward epilogue
+      const double dvp = p.e[m] - hvpi, db = p.eb[m] - hvpi;
+      const double pvb = dvp * db, prod = dmp * pvb;
+      if (((unsigned)(__double_as_longlong(prod) >> 52) & 0x7FFu) - 93u < 1860u) {
+        const double br = b / prod;
+        qmp = br * pvb;
+        qvp = br * (dmp * db);
+        qb = br * (dmp * dvp);
+      } else {
+        qmp = b / dmp;
+        qvp = b / dvp;
+        qb = b / db;
+      }
+    } else {
+      qmp = b / dmp;
+    }
     const double tmp = wgt * p.seed_mp[m] * qmp * qmp;
     gb[m] = wgt * p.seed_mp[m] * (2.0 * qmp);
     gm += tmp;
@@ -360,7 +378,6 @@ __device__ __forceinline__ void adj_factors(const Params& p, const double* bc, d
     kahan_add(acc.e2mp[m], acc.cmp[m], (b * qmp) * wgt);
     acc.psimp[m] = fma(qmp * qmp, wgt, acc.psimp[m]);
     if (p.yen) {
-      const double qvp = b / (p.e[m] - hvpi), qb = b / (p.eb[m] - hvpi);
       const double tv = wgt * p.seed_vp[m] * qvp * qvp;
       const double tb = wgt * p.seed_b[m] * qb * qb;
       gb[m] += wgt * (p.seed_vp[m] * (2.0 * qvp) + p.seed_b[m] * (2.0 * qb));

@@ -7,6 +7,7 @@ S-only run writes S grown by the previous selection, the namelist edits are
 sed's, E2 and the vectors feed the next step, and the final space is S plus
 the records down to the chosen threshold."""
 import os
+import shutil
 import struct
 
 import numpy as np
@@ -80,3 +81,51 @@ def test_cipsi_loop_on_the_drop_ins(tmp_path, engine_lib):
     assert out["ncf"] >= int(np.sum(xam >= out["tau"]))
     assert len(out["e_corr"]) == 2 and all(np.isfinite(out["e_corr"]))
     assert out["e_corr"][0] < abs(last["e2vp"][0]) + 1e-12
+
+
+def _grid_point(base, k, seed, det_max=100000):
+    cfg = synth.SynthConfig("chain", norb=12, nocc=3, ncholesky=12, ncf=10, metat=2, tau=0.02,
+                            ranks=(1, 2), coef_mode="gauss005", seed=seed, virt_shift=3.0)
+    wd = os.path.join(base, f"point{k}")
+    synth.generate(cfg, wd)
+    for u in ("det", "bdvec", "f04"):
+        os.remove(os.path.join(wd, u))
+    return dict(workdir=wd, f_bd=_files(wd), metat=2, netat_pertu=1, envp_max=1e-3,
+                det_bounds=(400, det_max, 10, 10 ** 6), imax_s=4, tau_init=0.05, tau_step=0.5)
+
+
+def test_grid_needs_one_directory_per_point(tmp_path):
+    pt = dict(workdir=str(tmp_path), f_bd="x")
+    with pytest.raises(ValueError):
+        autocip.run_grid([pt, dict(pt)])
+
+
+def test_grid_records_a_failed_point_and_goes_on(tmp_path):
+    """A point whose chain stops (here S outgrows det_bounds[1] = 10 after
+    its first S-only run; on a machine without a GPU, its first GPU step)
+    gets an error entry; the driver returns one entry per point."""
+    pts = [_grid_point(str(tmp_path), 0, 41, det_max=10), _grid_point(str(tmp_path), 1, 42, det_max=10)]
+    logs = []
+    out = autocip.run_grid(pts, workers=2, logs=logs)
+    assert len(out) == 2 and all("error" in r for r in out)
+    assert len(logs) == 2 and all(log and log[0]["step"] == "cip" for log in logs)
+
+
+@pytest.mark.gpu
+def test_grid_matches_points_run_one_by_one(tmp_path, engine_lib):
+    """Three points on three threads (and one that stops) give the results
+    of calcul_cip run on each point alone."""
+    pts = [_grid_point(str(tmp_path / "grid"), k, 41 + k) for k in range(3)]
+    pts.append(_grid_point(str(tmp_path / "grid"), 3, 44, det_max=10))
+    alone = []
+    for k, pt in enumerate(pts[:3]):
+        wd = str(tmp_path / "alone" / f"point{k}")
+        shutil.copytree(pt["workdir"], wd)
+        kw = dict(pt, workdir=wd, f_bd=os.path.join(wd, os.path.basename(pt["f_bd"])))
+        alone.append(autocip.calcul_cip(**kw))
+    out = autocip.run_grid(pts, workers=3)
+    assert "S size too big" in out[3]["error"]
+    for a, g in zip(alone, out[:3]):
+        assert "error" not in g
+        assert a["e_corr"] == g["e_corr"] and a["ncf"] == g["ncf"] and a["nbase"] == g["nbase"]
+        assert a["tau"] == g["tau"]
