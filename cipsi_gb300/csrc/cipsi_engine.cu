@@ -816,20 +816,24 @@ struct LaunchShape {
   int blocks_per_sm;
 };
 
-LaunchShape launch_shape(int W, int R, int ncf_max, int ctas) {
+// adj: the adjoint launch.  Its static shared memory exceeds the forward's
+// by ~4 KB (the per-block dE/dhdig and dE/dhmp sums), which its L_R list
+// gives back so that two CTAs still fit per SM; it never fills the
+// epilogue queues (its drains find them empty), so they take no space.
+LaunchShape launch_shape(int W, int R, int ncf_max, int ctas, bool adj = false) {
   const size_t per_entry = 8;  // compact L_R entry
-  const size_t qbytes = (size_t)(kThreads / 32) * queue_bytes(W, R);
+  const size_t qbytes = adj ? 0 : (size_t)(kThreads / 32) * queue_bytes(W, R);
   // two CTAs per SM unless one is asked for: the part of a long L_R list
   // beyond shared memory is read from the block's global scratch, 8 bytes
   // per entry, which costs less than halving the resident warps
   // (the kernel's static shared memory, ~28 KB, comes on top: two CTAs of
   // 82 + 28 KB, or one of 192 + 28 KB, fit the SM's 228 KB)
-  const size_t smem_total = ctas == 1 ? (size_t)192 * 1024 : (size_t)82 * 1024;
+  const size_t smem_total = (ctas == 1 ? (size_t)192 * 1024 : (size_t)82 * 1024) - (adj ? 4096 : 0);
   const size_t smem_budget = smem_total > qbytes + 16 ? smem_total - qbytes - 16 : 0;
   LaunchShape ls;
   ls.lr_cap = (int)std::min<size_t>((size_t)ncf_max, smem_budget / per_entry);
   ls.smem = (((size_t)ls.lr_cap * per_entry + 15) & ~(size_t)15) + qbytes + 16;
-  ls.blocks_per_sm = ctas == 1 ? 1 : ls.smem <= 86 * 1024 ? 2 : 1;
+  ls.blocks_per_sm = ctas == 1 ? 1 : ls.smem <= (adj ? 82 : 86) * 1024 ? 2 : 1;
   return ls;
 }
 
@@ -1678,7 +1682,7 @@ int run_adjoint(cipsi_ctx* ctx, const cipsi_opts* o, const double* seed, double*
   int dev_sms = 0;
   CK(cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, ctx->device));
   const int R = roots_pad(mt);
-  const LaunchShape ls = launch_shape(W, R, ncf, ctx->tune_ctas);
+  const LaunchShape ls = launch_shape(W, R, ncf, ctx->tune_ctas, true);
   const int grid = std::max(1, std::min(nunits, dev_sms * ls.blocks_per_sm));
   rc = ensure_neighbour_scratch(ctx, grid);
   if (rc) return rc;
