@@ -609,6 +609,7 @@ def run_gpu(args, rank: int, world: int, local_rank: int):
     # ---- end to end through the C ABI: upload from host buffers, stream,
     # every record delivered to host memory and folded into a digest
     e2e_ms = []
+    upload_ms = []
     digests = []
     n_e2e = max(1, min(args.steps, args.e2e_steps))
     for _ in range(n_e2e):
@@ -617,6 +618,7 @@ def run_gpu(args, rank: int, world: int, local_rank: int):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         ctx.upload(inp)
+        upload_ms.append(1e3 * (time.perf_counter() - t0))
         d = engine.Digest()
         d.threads = max(1, (os.cpu_count() or 2) - 1)
         r2 = ctx.run_stream(inp.opts, chunk_records=chunk, consumer=d, gen_mask=gmask)
@@ -667,6 +669,7 @@ def run_gpu(args, rank: int, world: int, local_rank: int):
                               if args.gen_every > 1 else {})),
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h), "ms_per_step": tot_e2e / n_e2e, "steps": n_e2e,
+                    "upload_ms_per_step": statistics.mean(upload_ms),
                     "records_delivered_per_step": int(nsel), "record_bytes": rec_bytes,
                     "digest": [format(x, "016x") for x in digests[0]]},
             "gpu_launches": launches,

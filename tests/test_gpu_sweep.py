@@ -1,0 +1,53 @@
+"""A seeded sweep of small random systems against the oracle: sizes, point
+groups, excitation ranks of S, root counts, thresholds, the partitions
+(ityper), the selection rules (iselec), ywdeg, the reference determinant in
+S or not, the cip and cipsym variants, and cip's coeff-restricted
+generators, drawn together so that combinations the targeted tests do not
+pair up are run too.  Each case is checked as the other parity tests are:
+integers, counts and the selected set exactly, E2 to 1e-10 Eh plus the
+oracle's condition bound."""
+import numpy as np
+import pytest
+
+from cipsi_gb300 import synth
+from test_gpu_parity import check, run_both
+
+pytestmark = pytest.mark.gpu
+
+
+def sweep_cases(n=20, seed=20261204):
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n):
+        norb = int(rng.integers(10, 21))
+        nocc = int(rng.integers(3, 6))
+        nsym = int(rng.choice([1, 2, 4]))
+        nr = int(rng.integers(1, 4))
+        ranks = tuple(sorted(int(x) for x in rng.choice([1, 2, 3, 4], size=nr, replace=False)))
+        metat = int(rng.integers(1, 5))
+        ncf = int(rng.integers(20, 80))
+        tau = float(rng.choice([0.005, 0.02, 0.05]))
+        ityper = int(rng.choice([1, 2]))
+        iselec = int(rng.choice([1, 2, 3]))
+        coef = str(rng.choice(["decay09", "gauss005"]))
+        hf = bool(rng.random() < 0.7)
+        variant = str(rng.choice(["cipsym", "cip"]))
+        extra = []
+        if rng.random() < 0.3:
+            extra.append("ywdeg=f")
+        if variant == "cip" and rng.random() < 0.5:
+            extra.append(f"coeff={float(rng.choice([0.02, 0.1]))}")
+        shift = float(rng.choice([0.0, 3.0]))
+        name = f"sweep{i:02d}"
+        cfg = synth.SynthConfig(name, norb=norb, nocc=nocc, ncholesky=norb, ncf=ncf, metat=metat, tau=tau,
+                                ityper=ityper, iselec=iselec, ranks=ranks, coef_mode=coef, seed=1000 + i,
+                                nsym=nsym, include_hf=hf, variant=variant, extra_icinp=", ".join(extra),
+                                virt_shift=shift)
+        out.append((name, cfg, variant))
+    return out
+
+
+@pytest.mark.parametrize("name,cfg,variant", sweep_cases(), ids=[c[0] for c in sweep_cases()])
+def test_parity_sweep(tmp_path, oracle_exe, engine_lib, name, cfg, variant):
+    jo, jg, wo, wg = run_both(tmp_path, cfg, variant=variant)
+    check(jo, jg, wo, wg, variant)
