@@ -403,6 +403,96 @@ def run_moy_form(args, rank: int, world: int, local_rank: int):
         print(json.dumps(line), flush=True)
 
 
+# ------------------------------------------------------------ bd form
+def _unit1_csr(path: str, n: int):
+    """moy's unit 1 (8192-element records of row, column, value; the last
+    record holds its count in jtab(8192)) as the full symmetric matrix
+    L + L^T in scipy CSR form (the diagonal is stored halved)."""
+    import numpy as np
+    import scipy.sparse as sp
+    lsize = 8192
+    synth = _synth()
+    rows, cols, vals = [], [], []
+    recs = synth.read_records(path)
+    for k, r in enumerate(recs):
+        it = np.frombuffer(r, dtype="<i4", count=lsize, offset=0)
+        jt = np.frombuffer(r, dtype="<i4", count=lsize, offset=4 * lsize)
+        vb = np.frombuffer(r, dtype="<f8", count=lsize, offset=8 * lsize)
+        m = int(jt[lsize - 1]) if k == len(recs) - 1 else lsize
+        rows.append(it[:m] - 1)
+        cols.append(jt[:m] - 1)
+        vals.append(vb[:m])
+    L = sp.csr_matrix((np.concatenate(vals), (np.concatenate(rows), np.concatenate(cols))), shape=(n, n))
+    return (L + L.T).tocsr()
+
+
+def run_bd_form(args, rank: int, world: int, local_rank: int):
+    """The bd drop-in (cipsi_bd_main): the lowest roots of moy's matrix over
+    --moy-dets determinants by the block Davidson iteration on the GPU.
+    value: seconds of the Davidson solve (the library's clock around it);
+    e2e: the whole drop-in (read unit 1 and unit 4, the solve, write units
+    59 and 33).  cpu_baseline: scipy's Lanczos (ARPACK eigsh) on the host
+    cores for the same roots of the same matrix to the same residual, the
+    reference's own bd being Fortran that cannot be built here."""
+    import numpy as np
+    import torch
+    import cipsi_gb300 as cg
+    from cipsi_gb300 import build
+    torch.cuda.set_device(local_rank)
+    build.build()
+    base = tempfile.mkdtemp(prefix=f"cipsi_bd_r{rank}_")
+    t0 = time.perf_counter()
+    wd = _moy_workdir(base, args.moy_dets, 7 + rank)
+    cg.run_cip(wd)
+    jm = cg.run_moy(wd)
+    with open(os.path.join(wd, "bd.in"), "w") as fh:
+        fh.write(" &bdfil\n &end\n &option\n  ncper=800, test=0.3d-3, qwvec=t\n &end\n")
+    t_gen = time.perf_counter() - t0
+    for _ in range(args.warmup):
+        j = cg.run_bd(wd)
+    clocks = Clocks(local_rank)
+    clocks.start()
+    solve, wall = [], []
+    for _ in range(args.steps):
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        j = cg.run_bd(wd)
+        wall.append(time.perf_counter() - t1)
+        solve.append(j["davidson_s"])
+    clk = clocks.stop()
+    n, netat = j["ncf"], len(j["eigenvalues"])
+    H = _unit1_csr(os.path.join(wd, "mat"), n)
+    ev = np.array(j["eigenvalues"])
+    line = {"metric": "bd lowest roots: solve time", "value": statistics.mean(solve), "unit": "s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * statistics.mean(solve), "higher_is_better": False, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded integrals and determinant list)",
+            "config": {"workload": f"bd over moy's matrix of {n} determinants ({MOY_WORKLOAD.format(n=n)}), "
+                                   f"{netat} roots, every residual norm below 1e-8 Eh",
+                       "determinants": n, "roots": netat, "matrix_elements": int(H.nnz)},
+            "e2e": {"value": statistics.mean(wall), "unit": "s", "ms_per_step": 1e3 * statistics.mean(wall),
+                    "h2d_bytes_per_step": int(jm["nhij"] * 16), "d2h_bytes_per_step": int(8 * n * netat)},
+            "gpu_launches": None,
+            "work": {"iterations": j["iterations"], "eigenvalues": j["eigenvalues"], "residuals": j["residuals"],
+                     "generation_s": t_gen},
+            "clocks": clk}
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        import scipy.sparse.linalg as spl
+        t1 = time.perf_counter()
+        w, v = spl.eigsh(H, k=netat, which="SA", tol=1e-10)
+        t_cpu = time.perf_counter() - t1
+        order = np.argsort(w)
+        w, v = w[order], v[:, order]
+        res = [float(np.linalg.norm(H @ v[:, m] - w[m] * v[:, m])) for m in range(netat)]
+        line["cpu_baseline"] = {"value": t_cpu, "unit": "s", "cores": os.cpu_count(), "kind": "library",
+                                "sample": "scipy.sparse.linalg.eigsh (ARPACK Lanczos, tol 1e-10) on the same "
+                                          f"matrix, the same {netat} roots; residual norms {res}",
+                                "max_abs_eigenvalue_diff": float(np.max(np.abs(w - ev)))}
+    shutil.rmtree(base, ignore_errors=True)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 # ------------------------------------------------------------ adjoint form
 def run_adjoint_form(args, rank: int, world: int, local_rank: int):
     """The medium system plus a seeded symmetric dipole matrix mu ~ N(0, 0.5):
@@ -720,7 +810,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--form", choices=["plain", "batched", "adjoint", "moy"], default="plain",
+    ap.add_argument("--form", choices=["plain", "batched", "adjoint", "moy", "bd"], default="plain",
                     help="batched: the potential-curve batch (geometries/s, batched vs plain); "
                          "adjoint: dE2/d integrals on the medium system with checks; "
                          "moy: the Hamiltonian over a determinant list (the moy drop-in)")
@@ -754,6 +844,9 @@ def main():
         return
     if args.form == "moy":
         run_moy_form(args, rank, world, local_rank)
+        return
+    if args.form == "bd":
+        run_bd_form(args, rank, world, local_rank)
         return
     run_gpu(args, rank, world, local_rank)
 

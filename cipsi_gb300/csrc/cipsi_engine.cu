@@ -1441,6 +1441,14 @@ int cipsi_run_pt2_stream(cipsi_ctx* ctx, const cipsi_opts* o, int64_t chunk_reco
     CK(cudaMemGetInfo(&fr, &tot));
     const double have = (double)fr + (double)(ctx->pool_cap + 2 * ctx->out_cap) * (rec_bytes + 4);
     cap = std::min<long long>(1ll << 29, (long long)(0.45 * have / (3.0 * (rec_bytes + 4))));
+    // with a consumer, about eight chunks once the run has more than 8M
+    // slots: each chunk's records are delivered while the next computes,
+    // so only the last chunk's delivery follows the kernels
+    if (fn) {
+      long long total = 0;
+      for (long long x : pl.uslots) total += x;
+      cap = std::min(cap, std::max<long long>(total / 8 + 1, 1ll << 20));
+    }
   }
   cap = std::max(cap, std::max<long long>(pl.max_slots, 1024));
   if (ctx->pool_cap < cap && (rc = grow_pool(ctx, cap))) return rc;

@@ -183,7 +183,8 @@ int cipsi_set_selection_sink(cipsi_ctx* ctx, uint64_t* bits, int32_t* owner, dou
    20-36, for selections too large for device memory): the same work as
    cipsi_run_pt2, in chunks of consecutive work units whose candidate slots
    fit `chunk_records` records (0 = sized from the free device memory, at
-   most 2^29).  Each chunk's records are copied into pinned host buffers
+   most 2^29, and with fn given at most an eighth of the run's slots, at
+   least 2^20, so that delivery overlaps the kernels).  Each chunk's records are copied into pinned host buffers
    while the next chunk computes, and `fn` receives them piece by piece, in
    the order cipsi_selection_get gives, with `first` = the index of the
    piece's first record in the run: bits[count*words] (words = 2W, as
