@@ -129,3 +129,40 @@ def test_grid_matches_points_run_one_by_one(tmp_path, engine_lib):
         assert "error" not in g
         assert a["e_corr"] == g["e_corr"] and a["ncf"] == g["ncf"] and a["nbase"] == g["nbase"]
         assert a["tau"] == g["tau"]
+
+
+def test_grid_takes_points_on_its_threads_in_order(monkeypatch):
+    """run_grid with a stand-in for calcul_cip: every point runs once, on at
+    most `workers` threads at a time, the results come back in point order,
+    and a point that raises CipsiError gets an error entry while the others
+    finish."""
+    import threading
+    import time
+    from cipsi_gb300 import CipsiError
+    lock = threading.Lock()
+    state = {"now": 0, "peak": 0, "seen": []}
+
+    def fake(workdir, log=None, **kw):
+        with lock:
+            state["now"] += 1
+            state["peak"] = max(state["peak"], state["now"])
+            state["seen"].append(workdir)
+        time.sleep(0.02)
+        with lock:
+            state["now"] -= 1
+        log.append({"step": "cip", "result": {}})
+        if workdir.endswith("bad"):
+            raise CipsiError("S size too big for calculation")
+        return {"e_corr": [float(len(workdir))], "device": kw["device"]}
+
+    monkeypatch.setattr(autocip, "calcul_cip", fake)
+    pts = [dict(workdir=f"/tmp/grid/p{k}" + ("bad" if k == 5 else ""), f_bd="x") for k in range(12)]
+    logs = []
+    out = autocip.run_grid(pts, workers=3, device=1, logs=logs)
+    assert sorted(state["seen"]) == sorted(p["workdir"] for p in pts)
+    assert 1 < state["peak"] <= 3
+    assert "S size too big" in out[5]["error"]
+    for k, r in enumerate(out):
+        if k != 5:
+            assert r == {"e_corr": [float(len(pts[k]["workdir"]))], "device": 1}
+    assert all(len(log) == 1 for log in logs)
