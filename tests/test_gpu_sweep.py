@@ -1,8 +1,8 @@
 """A seeded sweep of small random systems against the oracle: sizes, point
 groups, excitation ranks of S, root counts, thresholds, the partitions
 (ityper), the selection rules (iselec), ywdeg, the reference determinant in
-S or not, the cip and cipsym variants, and cip's coeff-restricted
-generators, drawn together so that combinations the targeted tests do not
+S or not, the cip and cipsym variants, cip's coeff-restricted generators,
+and one- and two-word spin strings, drawn together so that combinations the targeted tests do not
 pair up are run too.  Each case is checked as the other parity tests are:
 integers, counts and the selected set exactly, E2 to 1e-10 Eh plus the
 oracle's condition bound."""
@@ -15,7 +15,7 @@ from test_gpu_parity import check, run_both
 pytestmark = pytest.mark.gpu
 
 
-def sweep_cases(n=20, seed=20261204):
+def sweep_cases(n=20, n_wide=4, seed=20261204):
     rng = np.random.default_rng(seed)
     out = []
     for i in range(n):
@@ -43,6 +43,19 @@ def sweep_cases(n=20, seed=20261204):
                                 ityper=ityper, iselec=iselec, ranks=ranks, coef_mode=coef, seed=1000 + i,
                                 nsym=nsym, include_hf=hf, variant=variant, extra_icinp=", ".join(extra),
                                 virt_shift=shift)
+        out.append((name, cfg, variant))
+    # two 64-bit words per spin string (65-90 orbitals), S of singles and
+    # doubles, either variant
+    for i in range(n_wide):
+        norb = int(rng.integers(65, 91))
+        nocc = int(rng.integers(3, 6))
+        variant = str(rng.choice(["cipsym", "cip"]))
+        name = f"wide{i}"
+        cfg = synth.SynthConfig(name, norb=norb, nocc=nocc, ncholesky=24, ncf=int(rng.integers(20, 60)),
+                                metat=int(rng.integers(1, 4)), tau=float(rng.choice([0.005, 0.02])),
+                                ityper=int(rng.choice([1, 2])), iselec=int(rng.choice([1, 2, 3])),
+                                ranks=(1, 2), coef_mode=str(rng.choice(["decay09", "gauss005"])), seed=2000 + i,
+                                nsym=int(rng.choice([1, 2])), variant=variant)
         out.append((name, cfg, variant))
     return out
 
