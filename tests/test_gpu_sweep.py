@@ -64,3 +64,37 @@ def sweep_cases(n=20, n_wide=4, seed=20261204):
 def test_parity_sweep(tmp_path, oracle_exe, engine_lib, name, cfg, variant):
     jo, jg, wo, wg = run_both(tmp_path, cfg, variant=variant)
     check(jo, jg, wo, wg, variant)
+
+
+def moy_sweep_cases(seed=20261205):
+    """The one-word cipsym systems of the sweep (their unit 60 holds at most
+    a few tens of thousands of records: moy's pair scan is O(n^2) in the
+    oracle), each with a moy threshold and options drawn for it."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for name, cfg, variant in sweep_cases(n_wide=0):
+        if variant != "cipsym":
+            continue
+        tau = float(rng.choice([0.0, 0.0, 0.01, 0.05]))
+        extra = "y_secd=t" if rng.random() < 0.3 else ""
+        out.append((name, cfg, tau, extra))
+    return out
+
+
+@pytest.mark.parametrize("name,cfg,tau,extra", moy_sweep_cases(), ids=[c[0] for c in moy_sweep_cases()])
+def test_moy_sweep(tmp_path, oracle_exe, engine_lib, name, cfg, tau, extra):
+    """moy_gpu against the oracle's moy on the unit 60 of the oracle's
+    cipsym run of each sweep system: lists, unit 1 and morue's sums, as
+    tests/test_gpu_moy.py compares them."""
+    import shutil
+
+    import cipsi_gb300 as cg
+    import moy_files as mf
+    from test_gpu_moy import _compare
+    wo = str(tmp_path / "ora")
+    mf.prepare(wo, cfg, moy_tau=tau, extra=extra)
+    wg = str(tmp_path / "gpu")
+    shutil.copytree(wo, wg)
+    jo = mf.run_oracle_moy(wo)
+    jg = cg.run_moy(wg)
+    _compare(wo, wg, jo, jg)
