@@ -26,7 +26,7 @@ NVFLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-rela
 # no fused multiply-add contraction in host code: the same results on x86 and Arm
 CXXFLAGS = ["-O2", "-ffp-contract=off", "-std=c++17", "-fPIC", "-Wall"]
 
-CU_SOURCES = ["cipsi_engine.cu", "pt2_w1.cu", "pt2_w2.cu", "pt2_adj.cu", "hbuild.cu", "davidson.cu"]
+CU_SOURCES = ["cipsi_engine.cu", "pt2_w1.cu", "pt2_w2.cu", "pt2_adj.cu", "pt2_adj_w2.cu", "hbuild.cu", "davidson.cu"]
 HOST_SOURCES = ["cip_host.cpp", "moy_host.cpp", "bd_host.cpp"]
 MAINS = {"cip_gpu": "cip_gpu_main.cpp", "moy_gpu": "moy_gpu_main.cpp", "bd_gpu": "bd_gpu_main.cpp"}
 SOURCES = CU_SOURCES + HOST_SOURCES + list(MAINS.values()) + ["pt2_common.cuh", "pt2_kernel.cuh", "host_io.h",
