@@ -868,7 +868,7 @@ int grow_sel(cipsi_ctx* ctx, long long cap) {
 // partial sums, counters, histogram, records), sized for the plan; the lists
 // are uploaded on stream st.
 int prepare_run(cipsi_ctx* ctx, const RunPlan& pl, cudaStream_t st) {
-  const int W = ctx->W, mt = ctx->d.metat;
+  const int mt = ctx->d.metat;
   const int ngen = (int)pl.gens.size(), nunits = (int)pl.ug.size();
   ctx->ngen = ngen;
   ctx->nunits = nunits;
